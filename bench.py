@@ -1,0 +1,372 @@
+"""Benchmark: electron particle-steps/s of the hybrid PIC-MCC step on GB300.
+
+Workload (default): the 1 Torr argon CCP scale-up with 1024 cells, 2e7 electron
+macroparticles, 5-bin ES-WPNC (edges 2, 6, 11.5, 15.76 eV) every 50 steps, analytic
+cross sections, float32 particle state, dt = tau/400. A step is one pass of the hot
+path (push + collide + deposit + compaction, plus binning and resampling when due,
+plus the device grid update, ion fluid and Poisson solve) over all particles.
+
+Prints one JSON line. ``--impl reference`` times the reference's algorithm on the
+host cores instead (the C restatement of the reference path, OpenMP, float64, the
+reference's array-of-structures layout) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "electron particle-steps/s"
+UNIT = "particle-steps/s"
+BYTES_PER_PARTICLE = 40  # float32 SoA x, vx, vy, vz, w read + written by the push
+BYTES_PER_CHILD = 20
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (read-only)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"),
+                               parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl"
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, v, device):
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(pg, v, device):
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+# --------------------------------------------------------------------------------------
+# CPU baseline: the reference algorithm (oracle port) on the host cores
+# --------------------------------------------------------------------------------------
+def cpu_reference_rate(sample_particles, steps, cells, seed=0, threads=None, time_budget=20.0):
+    import numpy as np
+    from oracle import oracle as O
+    from boltzmann_gb300 import xsec
+    from boltzmann_gb300.config import gas_sigma_reference
+    threads = threads or os.cpu_count() or 1
+    N = cells
+    L = 2.54
+    rng = np.random.default_rng(seed)
+    n = int(sample_particles)
+    x = rng.uniform(0, L, n)
+    sig = math.sqrt(1.0 * 1.5 * 1.17255e11)
+    v = rng.normal(0, sig, (n, 3))
+    w = np.full(n, 1e9 * (N + 1) / n)
+    tab = xsec.analytic_argon(2000)
+    nn = 3.22e22
+    dt = 1.0 / 13.56e6 / 400
+    E = rng.uniform(-500, 500, N)
+    p = O.make_params(N, L=L, bnf=4, dt=dt, nn=nn, xs_mode=0, rng_mode=1, precision=64, seed=seed,
+                      gas_sigma=gas_sigma_reference(), xs_table=tab.nsigma(nn), xs_emin=tab.emin, xs_emax=tab.emax,
+                      e_exc=tab.e_exc)
+    n0 = n
+    cap = 3 * n
+    data0, tosum0 = O.soa_to_aos(x, v[:, 0], v[:, 1], v[:, 2], w, cap=cap)
+    data, tosum = data0.copy(), tosum0.copy()
+    dtmp = np.zeros((2 * cap, 6))
+    ttmp = np.zeros((2 * cap, 4))
+    mom = np.zeros((4, N + 1))
+    E = np.ascontiguousarray(E)
+    import ctypes
+    lib = O.lib()
+    done = 0
+    t0 = time.perf_counter()
+    k = 0
+    while k < steps:
+        if 2 * n > cap:  # the sample has no resampling: restart it before it outgrows its buffers
+            data[:], tosum[:] = data0, tosum0
+            n = n0
+        p.step = k
+        nn_ = lib.orc_step_omp(ctypes.byref(p), n, cap, data, tosum, dtmp, ttmp, E, mom, threads)
+        if nn_ < 0:
+            raise RuntimeError("oracle step refused: sample outgrew its buffers")
+        done += n
+        n = int(nn_)
+        k += 1
+        if time.perf_counter() - t0 > time_budget:
+            break
+    el = time.perf_counter() - t0
+    return done / el, threads, k, int(sample_particles)
+
+
+def run_reference_arm(args, world, rank, pg):
+    if rank != 0:
+        return
+    sample = int(args.ref_sample)
+    rate, threads, k, n = cpu_reference_rate(sample, args.steps + args.warmup, args.cells, time_budget=args.ref_budget)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": k, "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(args),
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{n} particles x {k} steps of the {args.cells}-cell CCP step "
+                                   "(push+collide+deposit+compaction), float64 AoS, OpenMP"},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args):
+    return {"workload": f"argon CCP 1 Torr, {args.cells} cells, {args.particles:.3g} electrons, 5-bin ES-WPNC",
+            "cells": args.cells, "particles": int(args.particles), "bins": 5, "resample_every": args.rsf,
+            "dt": "tau/400", "state": "float32 SoA", "l2": "inputs larger than L2 (particle state 400 MB)",
+            "parallelism": "replicas" if args.gpus > 1 else "1 GPU"}
+
+
+# --------------------------------------------------------------------------------------
+# our arm
+# --------------------------------------------------------------------------------------
+def run_ours(args, world, rank, local, pg):
+    import numpy as np
+    import torch
+    from boltzmann_gb300 import config, kernels as K
+    from boltzmann_gb300.solver import BoltzmannGB300
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    cfg = config.ccp_1024(num_particles=int(args.particles), gridpts=args.cells + 1, resample_freq=args.rsf,
+                          seed=1 + rank)
+    sol = BoltzmannGB300(cfg, device=dev)
+    n_start = sol.n()
+    for _ in range(args.warmup):
+        sol.step()
+    torch.cuda.synchronize()
+    ps0 = int(sol.particle_steps.item())
+    n_resample = sum(1 for s in range(sol.bigstep, sol.bigstep + args.steps) if s % cfg.resample_freq == 0)
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(pg)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        e0.record(st)
+        for _ in range(args.steps):
+            sol.step()
+        e1.record(st)
+        torch.cuda.synchronize()
+    barrier(pg)
+    ms = e0.elapsed_time(e1)
+    ps = int(sol.particle_steps.item()) - ps0
+    t_max = max_over_ranks(pg, ms / 1e3, dev)
+    ps_all = sum_over_ranks(pg, ps, dev)
+    value = ps_all / t_max
+    status = sol.device_status()
+
+    # dominant kernel alone: the fused push (ping-pong on the solver's buffers)
+    A, B = sol.A, sol.B
+    mom = sol.moments
+    prm = sol.params(step_on_device=False)
+    M = 20
+    cnts = []
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    for i in range(3):
+        mom.zero_()
+        K.electron_kernel(prm, A, B, sol.E_push, sol.status, sol.ws, moments=mom)
+        A, B = B, A
+    torch.cuda.synchronize()
+    n_in = torch.zeros(M, dtype=torch.int64, device=dev)
+    n_out = torch.zeros(M, dtype=torch.int64, device=dev)
+    n_ch = torch.zeros(M, dtype=torch.int64, device=dev)
+    ev[0].record(st)
+    for i in range(M):
+        mom.zero_()
+        K.electron_kernel(prm, A, B, sol.E_push, sol.status, sol.ws, moments=mom)
+        A, B = B, A
+    ev[1].record(st)
+    torch.cuda.synchronize()
+    push_ms = ev[0].elapsed_time(ev[1]) / M
+    # algorithmic bytes: read the particles pushed, write survivors and children
+    n_now = A.n()
+    bytes_per_launch = BYTES_PER_PARTICLE * n_now
+    achieved = bytes_per_launch / (push_ms * 1e-3) / 1e9
+    peak, kind = peaks()
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "push_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            tj = json.load(f)
+        traffic = tj["dram_bytes_per_particle"] * n_now
+
+    # e2e through the solver API with the reference's per-step host traffic
+    e2e = None
+    if not args.no_e2e:
+        grid_h = torch.zeros(5 * sol.N + 4, dtype=torch.float64, pin_memory=True)
+        grid_d = torch.zeros_like(grid_h, device=dev)
+        back_h = torch.zeros(4 * sol.nnodes + sol.N + sol.nnodes, dtype=torch.float64, pin_memory=True)
+        N = sol.N
+        grid_h[:N] = sol.E.cpu()
+        grid_h[2 * N + 1: 3 * N + 2] = sol.ni.cpu()
+        K2 = max(10, args.steps // 2)
+        torch.cuda.synchronize()
+        ps_e0 = int(sol.particle_steps.item())
+        t0 = time.perf_counter()
+        for _ in range(K2):
+            grid_d.copy_(grid_h, non_blocking=True)        # _copy_to_GPU (boltzmann.py:719-741)
+            sol.E.copy_(grid_d[:N])
+            sol.ni.copy_(grid_d[2 * N + 1: 3 * N + 2])
+            sol.step()
+            back = torch.cat([sol.moments.reshape(-1), sol.E, sol.ni])
+            back_h.copy_(back, non_blocking=True)           # back_to_cpu (post_processing_1D.py:6-24)
+            torch.cuda.synchronize()
+            grid_h[:N] = back_h[4 * sol.nnodes: 4 * sol.nnodes + N]
+            grid_h[2 * N + 1: 3 * N + 2] = back_h[4 * sol.nnodes + N:]
+        el = time.perf_counter() - t0
+        ps_e = int(sol.particle_steps.item()) - ps_e0
+        el = max_over_ranks(pg, el, dev)
+        ps_e = sum_over_ranks(pg, ps_e, dev)
+        e2e = {"value": ps_e / el, "unit": UNIT, "h2d_bytes_per_step": int(grid_h.numel() * 8),
+               "d2h_bytes_per_step": int(back_h.numel() * 8), "steps": K2}
+
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu:
+        rate, threads, k, n = cpu_reference_rate(args.cpu_sample, 1000, args.cells, time_budget=args.cpu_budget)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{n} particles x {k} steps of the same CCP step, float64 AoS (reference layout), "
+                         f"OpenMP {threads} threads"}
+    launches_per_step = 6
+    launches_resample = 10
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic", "config": workload_config(args),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "kernel": "k_push (fused push+collide+deposit+compaction)",
+                     "launch_ms": push_ms, "particles_per_launch": n_now, "peak_kind": kind},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": launches_per_step * args.steps + launches_resample * n_resample,
+        "clocks": clk.summary(),
+        "particles_start": n_start, "particles_end": n_now, "device_status": status,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--particles", type=float, default=2e7)
+    ap.add_argument("--cells", type=int, default=1024)
+    ap.add_argument("--rsf", type=int, default=50)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-sample", type=float, default=1e6)
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--ref-sample", type=float, default=2e6)
+    ap.add_argument("--ref-budget", type=float, default=60.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local, pg = dist_setup()
+    args.gpus = max(args.gpus, world)
+    if args.impl == "reference":
+        run_reference_arm(args, world, rank, pg)
+    else:
+        run_ours(args, world, rank, local, pg)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

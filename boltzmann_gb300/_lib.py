@@ -1,0 +1,118 @@
+"""ctypes binding of libbz.so, the sm_103a kernels behind include/bz.h.
+
+There is no fallback: if the library is missing or cannot be loaded, every call
+raises ``BzLibraryError``. Build it with ``python -m boltzmann_gb300.build``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libbz.so")
+
+BZ_OK, BZ_ERR_ARG, BZ_ERR_CUDA, BZ_ERR_WORKSPACE, BZ_ERR_UNSUPPORTED = 0, 1, 2, 3, 4
+DEV_CAPACITY, DEV_LOOKBACK, DEV_NONFINITE, DEV_BINRANGE = 0x1, 0x2, 0x4, 0x8
+QUIRK_SPLIT_WRAP, QUIRK_DEAD_IONFLAG, QUIRK_TRIGGER_LAST, FIX_MERGE_ENERGY = 0x1, 0x2, 0x4, 0x8
+XS_TABLE, XS_REF_FITS = 0, 1
+COLL_DIRECT, COLL_NULL = 0, 1
+
+_ERRNAMES = {1: "invalid argument", 2: "CUDA error", 3: "workspace too small", 4: "unsupported configuration"}
+
+
+class BzLibraryError(RuntimeError):
+    pass
+
+
+class BzError(RuntimeError):
+    def __init__(self, fn, code):
+        super().__init__(f"{fn} failed: {_ERRNAMES.get(code, code)} (status {code})")
+        self.code = code
+
+
+class BzParams(ctypes.Structure):
+    _fields_ = [
+        ("n_faces", ctypes.c_int32), ("n_nodes", ctypes.c_int32), ("bnf", ctypes.c_int32),
+        ("advect", ctypes.c_int32), ("L", ctypes.c_double), ("dx", ctypes.c_double),
+        ("dt", ctypes.c_double), ("nn", ctypes.c_double), ("gas_sigma", ctypes.c_double),
+        ("e_exc", ctypes.c_double), ("nu_max", ctypes.c_double),
+        ("xs_mode", ctypes.c_int32), ("coll_model", ctypes.c_int32), ("xs_n", ctypes.c_int32),
+        ("flags", ctypes.c_int32), ("xs_emin", ctypes.c_double), ("xs_emax", ctypes.c_double),
+        ("xs_table", ctypes.c_void_p), ("seed", ctypes.c_uint64), ("step", ctypes.c_uint64),
+        ("step_ptr", ctypes.c_void_p),
+    ]
+
+
+class Particles(ctypes.Structure):
+    """bz_particles_f32 / bz_particles_f64: five device pointers."""
+    _fields_ = [("x", ctypes.c_void_p), ("vx", ctypes.c_void_p), ("vy", ctypes.c_void_p),
+                ("vz", ctypes.c_void_p), ("w", ctypes.c_void_p)]
+
+
+_lib = None
+
+_vp = ctypes.c_void_p
+_i32 = ctypes.c_int32
+_i64 = ctypes.c_int64
+_f64 = ctypes.c_double
+_sz = ctypes.c_size_t
+_P = ctypes.POINTER(BzParams)
+
+_PROTOS = {
+    "bz_version": (ctypes.c_char_p, []),
+    "bz_push_workspace": (_sz, [_i64]),
+    "bz_push_collide_f32": (ctypes.c_int, [_P, Particles, _vp, _i64, Particles, _i64, _vp, _vp, _vp, _vp, _vp, _vp,
+                                           _sz, _vp, _vp]),
+    "bz_push_collide_f64": (ctypes.c_int, [_P, Particles, _vp, _i64, Particles, _i64, _vp, _vp, _vp, _vp, _vp, _vp,
+                                           _sz, _vp, _vp]),
+    "bz_deposit_f32": (ctypes.c_int, [_P, Particles, _vp, _i64, _vp, _vp, _vp]),
+    "bz_deposit_f64": (ctypes.c_int, [_P, Particles, _vp, _i64, _vp, _vp, _vp]),
+    "bz_bin_workspace": (_sz, [_i64, _i32]),
+    "bz_bin_f32": (ctypes.c_int, [_P, Particles, _vp, _i64, _i32, _vp, _f64, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp]),
+    "bz_bin_f64": (ctypes.c_int, [_P, Particles, _vp, _i64, _i32, _vp, _f64, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp]),
+    "bz_resample_workspace": (_sz, [_i64, _i32]),
+    "bz_resample_f32": (ctypes.c_int, [_P, Particles, _vp, _i64, Particles, _vp, _i32, _vp, _vp, _f64, _f64, _f64,
+                                       _f64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp]),
+    "bz_resample_f64": (ctypes.c_int, [_P, Particles, _vp, _i64, Particles, _vp, _i32, _vp, _vp, _f64, _f64, _f64,
+                                       _f64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp]),
+    "bz_compact_workspace": (_sz, [_i64]),
+    "bz_compact_f32": (ctypes.c_int, [Particles, _vp, _i64, Particles, _i64, _vp, _vp, _sz, _vp, _vp]),
+    "bz_compact_f64": (ctypes.c_int, [Particles, _vp, _i64, Particles, _i64, _vp, _vp, _sz, _vp, _vp]),
+    "bz_grid_update": (ctypes.c_int, [_i32, _vp, _vp, _vp, _vp, _vp]),
+    "bz_ion_fluid": (ctypes.c_int, [_i32, _f64, _f64, _f64, _f64, _vp, _vp, _vp, _vp, _vp]),
+    "bz_poisson_factor": (ctypes.c_int, [_i32, _f64, _vp, _vp]),
+    "bz_poisson": (ctypes.c_int, [_i32, _f64, _f64, _f64, _f64, _f64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "bz_advance_clock": (ctypes.c_int, [_vp, _vp, _f64, _vp]),
+}
+
+
+def exported_symbols():
+    return sorted(_PROTOS)
+
+
+def load():
+    """Load libbz.so (once). Raises BzLibraryError if it is missing or broken."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise BzLibraryError(f"{LIB_PATH} is missing; build it with `python -m boltzmann_gb300.build` "
+                             "(there is no CPU fallback)")
+    try:
+        lib = ctypes.CDLL(LIB_PATH)
+    except OSError as e:
+        raise BzLibraryError(f"cannot load {LIB_PATH}: {e}") from e
+    for name, (res, args) in _PROTOS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def call(name, *args):
+    """Call an entry point and raise BzError on a non-zero status."""
+    rc = getattr(load(), name)(*args)
+    if rc != BZ_OK:
+        raise BzError(name, rc)
+    return rc

@@ -1,0 +1,304 @@
+// Cell x energy-bin binning as a stable counting sort.
+//
+// Replaces define_particle_bins (bin_particles.py:7-22; 3bin/5bin :7-49), whose atomic
+// appends give a nondeterministic order, with a deterministic one: particles sorted by
+// key = cell*nbins + ebin, ascending particle index within a key (the order the
+// reference's serial semantics would give). Keys are 16-bit; the sort is an LSD radix
+// sort with 8-bit digits (one or two passes). Each pass: per-tile digit histograms,
+// a scan in (digit, tile) order, and a stable scatter in which every warp ranks its
+// own contiguous segment with __match_any_sync. Per-key counts and split-candidate
+// counts are formed in the key pass with shared-memory histograms.
+#include <algorithm>
+
+#include "bz_common.cuh"
+
+namespace bz {
+
+constexpr int RB_T = 512;               // threads per tile CTA
+constexpr int RB_I = 32;                // items per thread
+constexpr int RB_TILE = RB_T * RB_I;    // 16384 items per tile
+constexpr int RB_W = RB_T / 32;         // warps
+constexpr int RB_SEG = RB_TILE / RB_W;  // items per warp segment (1024)
+constexpr int RADIX = 256;
+
+// energy as the reference holds it when binning: tosum[:,3] = ((e*w)/w) after
+// post_processing (post_processing_1D.py:53,62), e = 0.5 m_e j_ev (vx^2+vy^2+vz^2)
+template <typename T>
+__device__ __forceinline__ int energy_bin(T vx, T vy, T vz, T w, int nb, const double *edges_s, float efac_f,
+                                          double efac_d) {
+    if (nb == 1) return 0;
+    if (sizeof(T) == 4) {
+        float e = efac_f * (float(vx) * float(vx) + float(vy) * float(vy) + float(vz) * float(vz));
+        bool safe = true;
+        int b = nb - 1;
+        for (int k = nb - 2; k >= 0; --k) {
+            float ed = float(edges_s[k]);
+            if (fabsf(e - ed) <= 1e-5f * fabsf(ed) + 1e-30f) safe = false;
+            if (e < ed) b = k;
+        }
+        if (safe && isfinite(e)) return b;
+    }
+    double dvx = double(vx), dvy = double(vy), dvz = double(vz), dw = double(w);
+    double e = efac_d * (dvx * dvx + dvy * dvy + dvz * dvz);
+    if (dw > 0) e = (e * dw) / dw;
+    for (int k = 0; k < nb - 1; ++k)
+        if (e < edges_s[k]) return k;
+    if (e >= edges_s[nb - 2]) return nb - 1;
+    return -1;  // NaN energy: in no bin (every comparison of the reference fails)
+}
+
+template <typename T>
+__global__ void __launch_bounds__(RB_T) k_bin_keys(bz_params p, const T *x, const T *vx, const T *vy, const T *vz,
+                                                   const T *w, const int32_t *n_ptr, int64_t cap, int nb,
+                                                   const double *edges,
+                                                   double min_wt, uint16_t *keys, uint32_t *hist, int32_t *counts,
+                                                   int32_t *hw_counts, int nkeys, uint32_t *status) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint32_t *c_s = reinterpret_cast<uint32_t *>(smem);  // [nkeys] counts
+    uint32_t *h_s = c_s + nkeys;                          // [nkeys] hw counts
+    uint32_t *d_s = h_s + nkeys;                          // [RADIX] low-digit histogram
+    __shared__ double edges_s[16];
+    const int n = int(min(int64_t(max(*n_ptr, 0)), cap));
+    const int ntiles = int(ceil_div(n, RB_TILE));
+    if (int(blockIdx.x) >= ntiles) return;
+    for (int i = threadIdx.x; i < 2 * nkeys + RADIX; i += RB_T) c_s[i] = 0;
+    if (threadIdx.x < 16) edges_s[threadIdx.x] = threadIdx.x < nb - 1 ? edges[threadIdx.x] : 0.0;
+    __syncthreads();
+    const float inv_dx_f = float(1.0 / p.dx);
+    const float efac_f = float(0.5 * m_e() * j_ev());
+    const double efac_d = 0.5 * m_e() * j_ev();
+    uint32_t err = 0;
+    const int64_t t0 = int64_t(blockIdx.x) * RB_TILE;
+    for (int j = threadIdx.x; j < RB_TILE; j += RB_T) {
+        int64_t i = t0 + j;
+        if (i >= n) break;
+        T wi = w[i];
+        int key = nkeys;  // invalid: sorted past every bin
+        if (wi > T(0)) {
+            int cell = p.advect ? cell_index(x[i], p.dx, inv_dx_f) : 0;
+            int b = energy_bin(vx[i], vy[i], vz[i], wi, nb, edges_s, efac_f, efac_d);
+            if (cell >= 0 && cell < p.n_nodes && b >= 0) {
+                key = cell * nb + b;
+                atomicAdd(&c_s[key], 1u);
+                if (double(wi) > min_wt) atomicAdd(&h_s[key], 1u);
+            } else {
+                err |= BZ_DEV_BINRANGE;
+            }
+        }
+        keys[i] = uint16_t(key);
+        atomicAdd(&d_s[key & 0xff], 1u);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < nkeys; k += RB_T) {
+        if (c_s[k]) atomicAdd(reinterpret_cast<unsigned int *>(&counts[k]), c_s[k]);
+        if (h_s[k]) atomicAdd(reinterpret_cast<unsigned int *>(&hw_counts[k]), h_s[k]);
+    }
+    for (int d = threadIdx.x; d < RADIX; d += RB_T) hist[size_t(blockIdx.x) * RADIX + d] = d_s[d];
+    if (err) atomicOr(status, err);
+}
+
+__global__ void __launch_bounds__(RB_T) k_radix_hist(const uint16_t *keys, const int32_t *n_ptr, int64_t cap,
+                                                     int shift, uint32_t *hist) {
+    __shared__ uint32_t d_s[RADIX];
+    const int n = int(min(int64_t(max(*n_ptr, 0)), cap));
+    const int ntiles = int(ceil_div(n, RB_TILE));
+    if (int(blockIdx.x) >= ntiles) return;
+    for (int i = threadIdx.x; i < RADIX; i += RB_T) d_s[i] = 0;
+    __syncthreads();
+    const int64_t t0 = int64_t(blockIdx.x) * RB_TILE;
+    for (int j = threadIdx.x; j < RB_TILE; j += RB_T) {
+        int64_t i = t0 + j;
+        if (i >= n) break;
+        atomicAdd(&d_s[(keys[i] >> shift) & 0xff], 1u);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < RADIX; d += RB_T) hist[size_t(blockIdx.x) * RADIX + d] = d_s[d];
+}
+
+// hist[t][d] -> global exclusive offset of (digit d, tile t) in (digit, tile) order.
+// One CTA of 1024 threads: 4 threads per digit, each owning a quarter of the tiles.
+__global__ void __launch_bounds__(1024) k_radix_scan(uint32_t *hist, const int32_t *n_ptr, int64_t cap) {
+    __shared__ uint32_t part[4][RADIX];
+    __shared__ uint32_t dig_base[RADIX];
+    const int n = int(min(int64_t(max(*n_ptr, 0)), cap));
+    const int ntiles = int(ceil_div(n, RB_TILE));
+    const int d = threadIdx.x & (RADIX - 1), q = threadIdx.x >> 8;
+    const int per = (ntiles + 3) / 4;
+    const int lo = q * per, hi = min(ntiles, lo + per);
+    uint32_t s = 0;
+    for (int t = lo; t < hi; ++t) s += hist[size_t(t) * RADIX + d];
+    part[q][d] = s;
+    __syncthreads();
+    if (threadIdx.x < RADIX) {
+        uint32_t tot = part[0][d] + part[1][d] + part[2][d] + part[3][d];
+        dig_base[d] = tot;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (int k = 0; k < RADIX; ++k) { uint32_t v = dig_base[k]; dig_base[k] = run; run += v; }
+    }
+    __syncthreads();
+    uint32_t run = dig_base[d];
+    for (int k = 0; k < q; ++k) run += part[k][d];
+    for (int t = lo; t < hi; ++t) {
+        uint32_t v = hist[size_t(t) * RADIX + d];
+        hist[size_t(t) * RADIX + d] = run;
+        run += v;
+    }
+}
+
+// Stable scatter by the digit at ``shift``. vals_in == nullptr means identity values.
+__global__ void __launch_bounds__(RB_T) k_radix_scatter(const uint16_t *keys_in, const uint32_t *vals_in,
+                                                        const int32_t *n_ptr, int64_t cap, int shift,
+                                                        const uint32_t *offsets, uint16_t *keys_out,
+                                                        uint32_t *vals_out) {
+    __shared__ uint32_t cnt[RB_W][RADIX];
+    const int n = int(min(int64_t(max(*n_ptr, 0)), cap));
+    const int ntiles = int(ceil_div(n, RB_TILE));
+    if (int(blockIdx.x) >= ntiles) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < RB_W * RADIX; i += RB_T) (&cnt[0][0])[i] = 0;
+    __syncthreads();
+    const int64_t seg0 = int64_t(blockIdx.x) * RB_TILE + int64_t(warp) * RB_SEG;
+    uint16_t k[RB_I];
+    uint32_t v[RB_I];
+    const unsigned lt_mask = (1u << lane) - 1u;
+#pragma unroll
+    for (int r = 0; r < RB_I; ++r) {
+        int64_t i = seg0 + r * 32 + lane;
+        bool ok = i < n;
+        k[r] = ok ? keys_in[i] : uint16_t(0);
+        v[r] = ok ? (vals_in ? vals_in[i] : uint32_t(i)) : 0u;
+        unsigned act = __ballot_sync(0xffffffffu, ok);
+        if (ok) {
+            int dg = (k[r] >> shift) & 0xff;
+            unsigned peers = __match_any_sync(act, dg);
+            if (lane == __ffs(peers) - 1) cnt[warp][dg] += __popc(peers);
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    // exclusive over warps per digit, plus the tile's global offset
+    for (int dg = threadIdx.x; dg < RADIX; dg += RB_T) {
+        uint32_t run = offsets[size_t(blockIdx.x) * RADIX + dg];
+        for (int ww = 0; ww < RB_W; ++ww) {
+            uint32_t t = cnt[ww][dg];
+            cnt[ww][dg] = run;
+            run += t;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < RB_I; ++r) {
+        int64_t i = seg0 + r * 32 + lane;
+        bool ok = i < n;
+        unsigned act = __ballot_sync(0xffffffffu, ok);
+        if (ok) {
+            int dg = (k[r] >> shift) & 0xff;
+            unsigned peers = __match_any_sync(act, dg);
+            uint32_t pos = cnt[warp][dg] + __popc(peers & lt_mask);
+            keys_out[pos] = k[r];
+            vals_out[pos] = v[r];
+            __syncwarp(act);
+            if (lane == __ffs(peers) - 1) cnt[warp][dg] += __popc(peers);
+        }
+        __syncwarp();
+    }
+}
+
+// offsets[k] = exclusive scan of counts[0..nkeys), offsets[nkeys] = live total.
+__global__ void __launch_bounds__(1024) k_key_offsets(const int32_t *counts, int nkeys, int32_t *offsets) {
+    __shared__ int32_t part[1024];
+    const int per = (nkeys + 1023) / 1024;
+    const int lo = threadIdx.x * per, hi = min(nkeys, lo + per);
+    int32_t s = 0;
+    for (int k = lo; k < hi; ++k) s += counts[k];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        int32_t t = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+        __syncthreads();
+        part[threadIdx.x] += t;
+        __syncthreads();
+    }
+    int32_t run = part[threadIdx.x] - s;
+    for (int k = lo; k < hi; ++k) { offsets[k] = run; run += counts[k]; }
+    if (threadIdx.x == 1023) offsets[nkeys] = part[1023];
+}
+
+struct BinWs {
+    size_t keys_a, keys_b, vals_a, hist, total;
+    BinWs(int64_t cap) {
+        size_t c = size_t(std::max<int64_t>(cap, 1));
+        size_t nt = size_t(ceil_div(int64_t(c), RB_TILE));
+        keys_a = 0;
+        keys_b = keys_a + ((c * 2 + 255) & ~size_t(255));
+        vals_a = keys_b + ((c * 2 + 255) & ~size_t(255));
+        hist = vals_a + ((c * 4 + 255) & ~size_t(255));
+        total = hist + nt * RADIX * 4;
+    }
+};
+
+template <typename T, typename P>
+static int bin_entry(const bz_params *pp, P s, const int32_t *n, int64_t cap, int nb, const double *edges,
+                     double min_wt, int32_t *perm, int32_t *offsets, int32_t *counts, int32_t *hw_counts, void *ws,
+                     size_t ws_bytes, uint32_t *status, void *stream) {
+    if (!pp || !n || cap <= 0 || !perm || !offsets || !counts || !hw_counts || !ws || !status) return BZ_ERR_ARG;
+    if (!s.x || !s.vx || !s.vy || !s.vz || !s.w) return BZ_ERR_ARG;
+    const bz_params &p = *pp;
+    if (nb < 1 || nb > 16 || (nb > 1 && !edges) || p.n_nodes < 1 || (p.advect && p.dx <= 0)) return BZ_ERR_ARG;
+    const int nkeys = p.n_nodes * nb;
+    if (nkeys >= 65535) return BZ_ERR_UNSUPPORTED;
+    BinWs L(cap);
+    if (ws_bytes < L.total) return BZ_ERR_WORKSPACE;
+    unsigned char *b = static_cast<unsigned char *>(ws);
+    uint16_t *keys_a = reinterpret_cast<uint16_t *>(b + L.keys_a);
+    uint16_t *keys_b = reinterpret_cast<uint16_t *>(b + L.keys_b);
+    uint32_t *vals_a = reinterpret_cast<uint32_t *>(b + L.vals_a);
+    uint32_t *hist = reinterpret_cast<uint32_t *>(b + L.hist);
+    cudaStream_t st = as_stream(stream);
+    const int grid = int(ceil_div(cap, RB_TILE));
+    if (cudaMemsetAsync(counts, 0, sizeof(int32_t) * nkeys, st) != cudaSuccess) return BZ_ERR_CUDA;
+    if (cudaMemsetAsync(hw_counts, 0, sizeof(int32_t) * nkeys, st) != cudaSuccess) return BZ_ERR_CUDA;
+    size_t smem = sizeof(uint32_t) * (2 * size_t(nkeys) + RADIX);
+    auto kk = k_bin_keys<T>;
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(kk, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess)
+        return BZ_ERR_UNSUPPORTED;
+    kk<<<grid, RB_T, smem, st>>>(p, s.x, s.vx, s.vy, s.vz, s.w, n, cap, nb, edges, min_wt, keys_a, hist, counts, hw_counts,
+                                 nkeys, status);
+    const bool two = nkeys >= RADIX;  // invalid key = nkeys must be ordered too
+    k_radix_scan<<<1, 1024, 0, st>>>(hist, n, cap);
+    k_radix_scatter<<<grid, RB_T, 0, st>>>(keys_a, nullptr, n, cap, 0, hist, keys_b,
+                                           two ? vals_a : reinterpret_cast<uint32_t *>(perm));
+    if (two) {
+        k_radix_hist<<<grid, RB_T, 0, st>>>(keys_b, n, cap, 8, hist);
+        k_radix_scan<<<1, 1024, 0, st>>>(hist, n, cap);
+        k_radix_scatter<<<grid, RB_T, 0, st>>>(keys_b, vals_a, n, cap, 8, hist, keys_a,
+                                               reinterpret_cast<uint32_t *>(perm));
+    }
+    k_key_offsets<<<1, 1024, 0, st>>>(counts, nkeys, offsets);
+    return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+}
+
+}  // namespace bz
+
+extern "C" {
+size_t bz_bin_workspace(int64_t capacity, int32_t nkeys) {
+    (void)nkeys;
+    return bz::BinWs(capacity).total;
+}
+int bz_bin_f32(const bz_params *p, bz_particles_f32 s, const int32_t *n, int64_t capacity, int32_t nbins,
+               const double *edges, double min_wt, int32_t *perm, int32_t *offsets, int32_t *counts,
+               int32_t *hw_counts, void *workspace, size_t workspace_bytes, uint32_t *status, void *stream) {
+    return bz::bin_entry<float>(p, s, n, capacity, nbins, edges, min_wt, perm, offsets, counts, hw_counts, workspace,
+                                workspace_bytes, status, stream);
+}
+int bz_bin_f64(const bz_params *p, bz_particles_f64 s, const int32_t *n, int64_t capacity, int32_t nbins,
+               const double *edges, double min_wt, int32_t *perm, int32_t *offsets, int32_t *counts,
+               int32_t *hw_counts, void *workspace, size_t workspace_bytes, uint32_t *status, void *stream) {
+    return bz::bin_entry<double>(p, s, n, capacity, nbins, edges, min_wt, perm, offsets, counts, hw_counts, workspace,
+                                 workspace_bytes, status, stream);
+}
+}

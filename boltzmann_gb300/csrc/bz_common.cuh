@@ -1,0 +1,224 @@
+// Shared device helpers for libbz (sm_103a): constants, Philox4x32-10, uniform and
+// normal conventions, exact reference index arithmetic, decoupled look-back.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "bz.h"
+
+namespace bz {
+
+// electron_kernel_numba.py:13-24 (same expressions, so the float64 values match).
+__host__ __device__ inline double q_e() { return 1.602 * 1e-19; }
+__host__ __device__ inline double m_e() { return 9.10938 * 1e-31; }
+__host__ __device__ inline double m_n() { return 6.6 * 1e-26; }
+__host__ __device__ inline double j_ev() { return 6.241509 * 1e18; }
+constexpr double E_ION = 15.76;
+constexpr double EPS_DEAD = 0.01;  // velocity given to w<=0 particles inside the kernel
+constexpr double X_DEAD = 0.00000001;  // where the reference parks absorbed particles
+
+// --------------------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as
+// 1, 2, 3", SC'11): 10 rounds of two 32x32->64 multiplies, Weyl key schedule.
+// --------------------------------------------------------------------------------------
+struct u32x4 { uint32_t x, y, z, w; };
+
+__device__ __forceinline__ u32x4 philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0,
+                                        uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+        uint32_t n0 = hi1 ^ c1 ^ k0;
+        uint32_t n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return {c0, c1, c2, c3};
+}
+
+// A uniform and its complement, both exact: float path u = ((r>>9)+0.5)*2^-23;
+// double path u = ((hi26<<26 | lo26) + 0.5)*2^-52. Keeping 1-u exact lets sin(chi)
+// = 2 sqrt(u(1-u)) keep full relative accuracy near the poles.
+template <typename T> struct Uni { T u, c; };
+
+__device__ __forceinline__ Uni<float> uni_f(uint32_t r) {
+    uint32_t k = r >> 9;
+    return {(float(k) + 0.5f) * 0x1p-23f, (float(0x800000u - k) - 0.5f) * 0x1p-23f};
+}
+__device__ __forceinline__ Uni<double> uni_d(uint32_t a, uint32_t b) {
+    uint64_t k = (uint64_t(a >> 6) << 26) | uint64_t(b >> 6);
+    return {(double(k) + 0.5) * 0x1p-52, (double((uint64_t(1) << 52) - k) - 0.5) * 0x1p-52};
+}
+
+// Key and step words of the stream: key = seed, counter = (slot, step lo, step hi, tag).
+struct Rng {
+    uint32_t k0, k1, s0, s1;
+};
+__device__ __forceinline__ Rng make_rng(const bz_params &p) {
+    uint64_t st = p.step_ptr ? *p.step_ptr : p.step;
+    return {uint32_t(p.seed), uint32_t(p.seed >> 32), uint32_t(st), uint32_t(st >> 32)};
+}
+
+// Four uniforms for (slot, step, tag): one Philox call (float) or two (double).
+template <typename T> struct Draw4 { Uni<T> v[4]; };
+
+__device__ __forceinline__ void draw4(const Rng &g, uint32_t slot, uint32_t tag, Draw4<float> &d) {
+    u32x4 r = philox(slot, g.s0, g.s1, tag, g.k0, g.k1);
+    d.v[0] = uni_f(r.x); d.v[1] = uni_f(r.y); d.v[2] = uni_f(r.z); d.v[3] = uni_f(r.w);
+}
+__device__ __forceinline__ void draw4(const Rng &g, uint32_t slot, uint32_t tag, Draw4<double> &d) {
+    u32x4 a = philox(slot, g.s0, g.s1, tag, g.k0, g.k1);
+    u32x4 b = philox(slot, g.s0, g.s1, tag | (1u << 8), g.k0, g.k1);
+    d.v[0] = uni_d(a.x, a.y); d.v[1] = uni_d(a.z, a.w); d.v[2] = uni_d(b.x, b.y); d.v[3] = uni_d(b.z, b.w);
+}
+
+__device__ __forceinline__ void sincospi_t(float a, float *s, float *c) { sincospif(a, s, c); }
+__device__ __forceinline__ void sincospi_t(double a, double *s, double *c) { sincospi(a, s, c); }
+
+// Box-Muller pair from uniforms (a, b).
+template <typename T> __device__ __forceinline__ void box_muller(T a, T b, T &g0, T &g1) {
+    T r = sqrt(T(-2) * log(a));
+    T s, c;
+    sincospi_t(T(2) * b, &s, &c);
+    g0 = r * c;
+    g1 = r * s;
+}
+
+// --------------------------------------------------------------------------------------
+// Reference index arithmetic, exact. The reference forms these in float64 from
+// float64 positions; here x is float32 or float64. A float32 candidate is used
+// unless it lies near a boundary, where the float64 expression is evaluated.
+// --------------------------------------------------------------------------------------
+// The float candidate s carries a relative error below ~2.4e-7 (two roundings of
+// inputs and one of the product), so a margin of 1e-6*|s| + 1e-5 to the nearest integer
+// guarantees the truncation agrees with the float64 expression.
+__device__ __forceinline__ bool safe_trunc(float s) {
+    float fr = s - floorf(s);
+    float m = fmaf(fabsf(s), 1e-6f, 1e-5f);
+    return fr > m && fr < 1.0f - m;
+}
+// int(x / dx) (boltzmann.py:657): E-field face of the pre-push position.
+template <typename T> __device__ __forceinline__ int face_index(T x, double dx, float inv_dx_f) {
+    if (sizeof(T) == 4) {
+        float s = float(x) * inv_dx_f;
+        if (safe_trunc(s)) return int(s);
+    }
+    return int(double(x) / dx);
+}
+// int((x + 0.5 dx) / dx) (boltzmann.py:658): binning cell.
+template <typename T> __device__ __forceinline__ int cell_index(T x, double dx, float inv_dx_f) {
+    if (sizeof(T) == 4) {
+        float s = fmaf(float(x), inv_dx_f, 0.5f);
+        if (safe_trunc(s)) return int(s);
+    }
+    return int((double(x) + 0.5 * dx) / dx);
+}
+// int(int(((x + dx/2)/(L+dx)) * float(M)) / bnf) (post_processing_1D.py:44, kernels-new.cu:65,
+// redcheck block = fine / bnf): deposit node.
+struct NodeMap {
+    double half_dx, Lp, fM;  // 0.5*dx, L+dx, (double)(float)M
+    float a, b;              // float candidate: node ~= x*a + b
+    int bnf;
+};
+__host__ __device__ inline NodeMap make_node_map(const bz_params &p) {
+    NodeMap m;
+    int M = p.bnf * p.n_nodes;
+    m.half_dx = 0.5 * p.dx;
+    m.Lp = p.L + p.dx;
+    m.fM = double(float(M));
+    m.a = float(m.fM / m.Lp / p.bnf);
+    m.b = float(m.half_dx * m.fM / m.Lp / p.bnf);
+    m.bnf = p.bnf;
+    return m;
+}
+template <typename T> __device__ __forceinline__ int node_index(T x, const NodeMap &m) {
+    if (sizeof(T) == 4) {
+        float s = fmaf(float(x), m.a, m.b);
+        if (safe_trunc(s)) return int(s);
+    }
+    double tx = (double(x) + m.half_dx) / m.Lp;
+    int fine = int(tx * m.fM);
+    return fine / m.bnf;
+}
+
+// --------------------------------------------------------------------------------------
+// Decoupled look-back over tiles for two counters (survivors, children).
+// status word: [63:62] flag (1 aggregate, 2 inclusive prefix), [61:31] c, [30:0] s.
+// --------------------------------------------------------------------------------------
+constexpr uint64_t LB_AGG = 1ull << 62;
+constexpr uint64_t LB_PRE = 2ull << 62;
+constexpr uint64_t LB_MASK = (1ull << 31) - 1;
+
+__device__ __forceinline__ void st_release(uint64_t *p, uint64_t v) {
+    asm volatile("st.release.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ uint64_t ld_acquire(const uint64_t *p) {
+    uint64_t v;
+    asm volatile("ld.acquire.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ uint64_t lb_pack(uint64_t flag, uint32_t s, uint32_t c) {
+    return flag | (uint64_t(c & LB_MASK) << 31) | uint64_t(s & LB_MASK);
+}
+
+// Called by warp 0 of the block that owns ``tile``. Publishes (s, c) as the tile
+// aggregate, waits for predecessors (bounded), publishes the inclusive prefix and
+// returns the exclusive prefix in (*ps, *pc) on lane 0.
+__device__ inline void lookback(uint64_t *status_arr, int tile, uint32_t s, uint32_t c, uint32_t *ps, uint32_t *pc,
+                                uint32_t *err) {
+    const int lane = threadIdx.x & 31;
+    if (tile == 0) {
+        if (lane == 0) {
+            st_release(&status_arr[0], lb_pack(LB_PRE, s, c));
+            *ps = 0; *pc = 0;
+        }
+        return;
+    }
+    if (lane == 0) st_release(&status_arr[tile], lb_pack(LB_AGG, s, c));
+    uint32_t acc_s = 0, acc_c = 0;
+    int base = tile - 1;
+    uint32_t spins = 0;
+    bool timed_out = false;
+    while (true) {
+        int t = base - lane;
+        uint64_t v = (t >= 0) ? ld_acquire(&status_arr[t]) : LB_PRE;  // before tile 0: empty prefix
+        uint64_t flag = v & (3ull << 62);
+        unsigned pre = __ballot_sync(0xffffffffu, flag == LB_PRE);
+        int stop = pre ? (__ffs(pre) - 1) : 31;  // nearest predecessor holding an inclusive prefix
+        unsigned needed = (stop == 31) ? 0xffffffffu : ((1u << (stop + 1)) - 1u);
+        unsigned not_ready = __ballot_sync(0xffffffffu, flag == 0) & needed;
+        if (not_ready && !timed_out) {
+            if (++spins > (1u << 22)) {
+                timed_out = true;  // give up waiting: count missing tiles as empty, flag it
+                if (lane == 0) atomicOr(err, BZ_DEV_LOOKBACK);
+            } else {
+                __nanosleep(64);
+                continue;
+            }
+        }
+        uint32_t vs = uint32_t(v & LB_MASK), vc = uint32_t((v >> 31) & LB_MASK);
+        if (lane > stop || flag == 0) { vs = 0; vc = 0; }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            vs += __shfl_xor_sync(0xffffffffu, vs, o);
+            vc += __shfl_xor_sync(0xffffffffu, vc, o);
+        }
+        acc_s += vs;
+        acc_c += vc;
+        if (pre) break;
+        base -= 32;
+    }
+    if (lane == 0) {
+        st_release(&status_arr[tile], lb_pack(LB_PRE, acc_s + s, acc_c + c));
+        *ps = acc_s;
+        *pc = acc_c;
+    }
+}
+
+__host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+}  // namespace bz

@@ -1,0 +1,200 @@
+// Device-resident grid step: host-side grid update of the step loop, ion drift-
+// diffusion and Poisson solve, all float64, so that a CCP step needs no host round trip.
+// This file is compiled without FMA contraction so the float64 operation order of the
+// reference's numba code (EF_kernel_1D.py, heavies_kernel_1D.py) is kept.
+#include "bz_common.cuh"
+
+namespace bz {
+
+// boltzmann.py:643-647
+__global__ void k_grid_update(int nn, const double *mom, double *ni, double *Te, double *g2) {
+    for (int i = threadIdx.x + blockIdx.x * blockDim.x; i < nn; i += blockDim.x * gridDim.x) {
+        double ne = mom[i], src = mom[nn + i], nrg = mom[3 * nn + i];
+        if (ni) ni[i] = ni[i] + src;
+        if (Te) {
+            double t = (2. / 3.) * nrg / ne;
+            Te[i] = isfinite(t) ? t : (isnan(t) ? 0.0 : (t > 0 ? 1.7976931348623157e308 : -1.7976931348623157e308));
+        }
+        if (g2) g2[i] = g2[i] + src;
+    }
+}
+
+// heavies_kernel_1D.py:4-64, ion part. One CTA; the boundary nodes depend on the
+// interior update, so the phases are separated by barriers.
+__global__ void __launch_bounds__(1024) k_ion_fluid(int N, double dx, double dt, double mu_i, double D_i,
+                                                    const double *E, double *ni, double *Ji, int32_t *brk) {
+    __shared__ int s_brk;
+    if (threadIdx.x == 0) {
+        s_brk = 0;
+        double e0 = fmax(E[0], 0.0), eN = fmin(E[N - 1], 0.0);
+        ni[0] = ni[1] * ((D_i / dx - 0.5 * mu_i * e0) / (D_i / dx + 0.5 * mu_i * e0));
+        ni[N] = ni[N - 1] * ((D_i / dx + 0.5 * mu_i * eN) / (D_i / dx - 0.5 * mu_i * eN));
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < N; i += blockDim.x)
+        Ji[i] = (mu_i * (0.5 * (ni[i] + ni[i + 1])) * E[i] - D_i * (ni[i + 1] - ni[i]) / dx);
+    __syncthreads();
+    int b = 0;
+    for (int i = 1 + threadIdx.x; i < N; i += blockDim.x) {
+        double r = ni[i] - dt * (Ji[i] - Ji[i - 1]) / dx;
+        if (r < 0 && ni[i] > 0) b = 1;
+        ni[i] = r;  // each node reads only fluxes, which are final
+    }
+    if (b) atomicOr(&s_brk, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double e0 = fmax(E[0], 0.0), eN = fmin(E[N - 1], 0.0);
+        ni[0] = ni[1] * ((D_i / dx - 0.5 * mu_i * e0) / (D_i / dx + 0.5 * mu_i * e0));
+        ni[N] = ni[N - 1] * ((D_i / dx + 0.5 * mu_i * eN) / (D_i / dx - 0.5 * mu_i * eN));
+        if (brk) *brk = s_brk;
+    }
+}
+
+// banded Cholesky factor of tridiag(-1, 2, -1)/dx^2 (what boltzmann.py:744-755 gets from
+// scipy.linalg.cholesky_banded): d[0] = sqrt(a), l[i] = b/d[i-1], d[i] = sqrt(a - l[i]^2)
+__global__ void k_poisson_factor(int N, double dx, double *d, double *l) {
+    if (threadIdx.x || blockIdx.x) return;
+    int n = N - 1;
+    double a = 2. / (dx * dx), b = -1. / (dx * dx);
+    d[0] = sqrt(a);
+    l[0] = 0.0;
+    for (int i = 1; i < n; ++i) {
+        l[i] = b / d[i - 1];
+        d[i] = sqrt(a - l[i] * l[i]);
+    }
+}
+
+// EF_kernel_1D.py:26-42: forward/back substitution with the Cholesky factor, then face
+// fields. Each substitution is a first-order linear recurrence z_i = a_i z_{i-1} + b_i,
+// solved as a block-wide inclusive scan of affine maps (a, b) composed as
+// (a2, b2) o (a1, b1) = (a2 a1, a2 b1 + b2), 1024 rows per chunk with the carry
+// between chunks. One CTA; everything is float64.
+struct Aff { double a, b; };
+__device__ __forceinline__ Aff aff_compose(Aff early, Aff late) { return {late.a * early.a, late.a * early.b + late.b}; }
+
+constexpr int PS_T = 1024;
+
+__device__ Aff block_aff_scan(Aff v, Aff *sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        Aff t{__shfl_up_sync(0xffffffffu, v.a, o), __shfl_up_sync(0xffffffffu, v.b, o)};
+        if (lane >= o) v = aff_compose(t, v);
+    }
+    if (lane == 31) sh[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        Aff w = sh[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            Aff t{__shfl_up_sync(0xffffffffu, w.a, o), __shfl_up_sync(0xffffffffu, w.b, o)};
+            if (lane >= o) w = aff_compose(t, w);
+        }
+        sh[lane] = w;  // inclusive over warps
+    }
+    __syncthreads();
+    if (warp > 0) v = aff_compose(sh[warp - 1], v);
+    __syncthreads();
+    return v;
+}
+
+__global__ void __launch_bounds__(PS_T) k_poisson(int N, double dx, double eps0, double V0, double freq,
+                                                  double t_host, const double *t_dev, const double *ne,
+                                                  const double *ni, const double *d, const double *l, double *V,
+                                                  double *E, float *E32, double *y) {
+    __shared__ Aff sh[32];
+    __shared__ double carry;
+    const double t = t_dev ? *t_dev : t_host;
+    const int n = N - 1;
+    const double vs = V0 * sin(2 * 3.141592653589793 * freq * t);
+    // forward: y_i = (1/d_i)(r_i - l_i y_{i-1}), r_i = (ni - ne)/eps0 (+ boundary term at i = 0)
+    if (threadIdx.x == 0) carry = 0.0;
+    __syncthreads();
+    for (int c0 = 0; c0 < n; c0 += PS_T) {
+        int i = c0 + threadIdx.x;
+        Aff v{1.0, 0.0};
+        if (i < n) {
+            double r = (1.0 / eps0) * (ni[i + 1] - ne[i + 1]);
+            if (i == 0) r = r + (1.0 / (dx * dx)) * vs;
+            double inv = 1.0 / d[i];
+            v = (i == 0) ? Aff{0.0, r / d[0]} : Aff{-inv * l[i], inv * r};
+        }
+        Aff pre = block_aff_scan(v, sh);
+        double yi = pre.a * carry + pre.b;
+        if (i < n) y[i] = yi;
+        __syncthreads();
+        if (i == min(c0 + PS_T, n) - 1) carry = yi;
+        __syncthreads();
+    }
+    // backward: V_i = (1/d_i)(y_i - l_{i+1} V_{i+1}), V_{n-1} = y_{n-1}/d_{n-1}
+    if (threadIdx.x == 0) carry = 0.0;
+    __syncthreads();
+    for (int c0 = 0; c0 < n; c0 += PS_T) {
+        int j = c0 + threadIdx.x;  // j-th row from the end
+        int i = n - 1 - j;
+        Aff v{1.0, 0.0};
+        if (j < n) {
+            double inv = 1.0 / d[i];
+            v = (j == 0) ? Aff{0.0, y[i] / d[i]} : Aff{-inv * l[i + 1], inv * y[i]};
+        }
+        Aff pre = block_aff_scan(v, sh);
+        double vi = pre.a * carry + pre.b;
+        if (j < n) V[i] = vi;
+        __syncthreads();
+        if (j == min(c0 + PS_T, n) - 1) carry = vi;
+        __syncthreads();
+    }
+    // faces (EF_kernel_1D.py:39-42)
+    for (int i = threadIdx.x; i < N; i += PS_T) {
+        double e;
+        if (i == 0) e = -(V[0] - vs) / dx;
+        else if (i == N - 1) e = -(0 - V[N - 2]) / dx;
+        else e = -(V[i] - V[i - 1]) / dx;
+        E[i] = e;
+        if (E32) E32[i] = float(e);
+    }
+}
+
+__global__ void k_advance_clock(double *t, uint64_t *step, double dt) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        if (t) *t = *t + dt;
+        if (step) *step = *step + 1;
+    }
+}
+
+}  // namespace bz
+
+extern "C" {
+int bz_grid_update(int32_t n_nodes, const double *moments, double *ni, double *Te, double *g2, void *stream) {
+    if (n_nodes < 1 || !moments) return BZ_ERR_ARG;
+    bz::k_grid_update<<<(n_nodes + 255) / 256, 256, 0, bz::as_stream(stream)>>>(n_nodes, moments, ni, Te, g2);
+    return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+}
+int bz_ion_fluid(int32_t N, double dx, double dt, double mu_i, double D_i, const double *E, double *ni, double *Ji,
+                 int32_t *brk, void *stream) {
+    if (N < 2 || !E || !ni || !Ji) return BZ_ERR_ARG;
+    bz::k_ion_fluid<<<1, 1024, 0, bz::as_stream(stream)>>>(N, dx, dt, mu_i, D_i, E, ni, Ji, brk);
+    return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+}
+int bz_poisson_factor(int32_t N, double dx, double *chol_diag, double *chol_lower) {
+    if (N < 3 || !chol_diag || !chol_lower) return BZ_ERR_ARG;
+    bz::k_poisson_factor<<<1, 32>>>(N, dx, chol_diag, chol_lower);
+    if (cudaGetLastError() != cudaSuccess) return BZ_ERR_CUDA;
+    return cudaDeviceSynchronize() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+}
+int bz_poisson(int32_t N, double dx, double eps0, double V0, double freq, double t_host, const double *t_dev,
+               const double *ne, const double *ni, const double *chol_diag, const double *chol_lower, double *V,
+               double *E, float *E32, void *stream) {
+    if (N < 3 || !ne || !ni || !chol_diag || !chol_lower || !V || !E) return BZ_ERR_ARG;
+    // E doubles as the scratch of the forward substitution: it is written only after
+    // the backward substitution has consumed y (both inside the same CTA).
+    bz::k_poisson<<<1, bz::PS_T, 0, bz::as_stream(stream)>>>(N, dx, eps0, V0, freq, t_host, t_dev, ne, ni, chol_diag,
+                                                              chol_lower, V, E, E32, E);
+    return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+}
+int bz_advance_clock(double *t_dev, uint64_t *step_dev, double dt, void *stream) {
+    if (!t_dev && !step_dev) return BZ_ERR_ARG;
+    bz::k_advance_clock<<<1, 32, 0, bz::as_stream(stream)>>>(t_dev, step_dev, dt);
+    return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+}
+}

@@ -1,0 +1,582 @@
+// ES-WPNC particle resampling (split / merge per cell and energy bin) and the
+// order-preserving compaction that follows it.
+//
+// _check_for_resampling / _do_resampling (boltzmann.py:799-916; 3bin :813-1113;
+// 5bin :843-1334) loop over cells on the host with many small CuPy calls. Here:
+//   k_rs_decide  : one CTA classifies every (cell, bin) key, computes the append and
+//                  random-draw offsets (processing order = key order) and the trigger;
+//   k_rs_apply   : one CTA per key with work, float64 sums / scans / searches;
+//   k_compact    : decoupled look-back stream compaction of w != 0.
+#include <algorithm>
+
+#include "bz_common.cuh"
+
+namespace bz {
+
+template <typename T> struct SoAR { T *x, *vx, *vy, *vz, *w; };
+
+constexpr int RS_T = 256;
+enum { ACT_NONE = 0, ACT_SPLIT = 1, ACT_MERGE = 2 };
+
+struct RsWs {
+    size_t act, app_off, draw_off, misc, cdf, cnt, total;
+    RsWs(int64_t cap, int nkeys) {
+        size_t k = size_t(nkeys) + 1, c = size_t(std::max<int64_t>(cap, 1));
+        auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+        act = 0;
+        app_off = act + al(4 * k);
+        draw_off = app_off + al(4 * k);
+        misc = draw_off + al(4 * k);
+        cdf = misc + 256;
+        cnt = cdf + al(8 * c);
+        total = cnt + al(12 * c);  // three int32 regions: counts, candidate ids, copy targets
+    }
+};
+
+// misc[0] = total appended, misc[1] = need flag
+__global__ void __launch_bounds__(1024) k_rs_decide(const int32_t *counts, const int32_t *hw_counts, int n_nodes,
+                                                    int nb, const int32_t *targets, double split_below,
+                                                    double merge_at, double merge_keep, int flags, int32_t *act,
+                                                    int32_t *app_off, int32_t *draw_off, int32_t *misc,
+                                                    int32_t *need_out) {
+    __shared__ int64_t pa[1024], pd[1024];
+    __shared__ int s_need_last, s_need_any;
+    const int nkeys = n_nodes * nb;
+    if (threadIdx.x == 0) { s_need_last = 0; s_need_any = 0; }
+    __syncthreads();
+    const int per = (nkeys + 1023) / 1024;
+    const int lo = threadIdx.x * per, hi = min(nkeys, lo + per);
+    int64_t sa = 0, sd = 0;
+    int need_last = 0, need_any = 0;
+    for (int k = lo; k < hi; ++k) {
+        int b = k % nb;
+        int64_t n = counts[k];
+        int64_t T = targets[b];
+        int a = ACT_NONE;
+        int64_t app = 0;
+        if (n > 0 && double(n) < split_below * double(T) && hw_counts[k] > 0) {
+            a = ACT_SPLIT;
+            app = 2 * T - n;  // boltzmann.py:814
+        } else if (double(n) >= merge_at * double(T)) {
+            a = ACT_MERGE;
+            app = int64_t(merge_keep * double(T));  // boltzmann.py:829
+        }
+        if (n > 0 && double(n) < split_below * double(T)) need_any = 1;
+        if (double(n) >= merge_at * double(T)) {
+            need_any = 1;
+            if (b == nb - 1) need_last = 1;
+        }
+        act[k] = a;
+        sa += app;
+        sd += app;
+    }
+    if (need_last) atomicOr(&s_need_last, 1);
+    if (need_any) atomicOr(&s_need_any, 1);
+    pa[threadIdx.x] = sa;
+    pd[threadIdx.x] = sd;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        int64_t ta = threadIdx.x >= o ? pa[threadIdx.x - o] : 0;
+        int64_t td = threadIdx.x >= o ? pd[threadIdx.x - o] : 0;
+        __syncthreads();
+        pa[threadIdx.x] += ta;
+        pd[threadIdx.x] += td;
+        __syncthreads();
+    }
+    // the reference decides with its last max test only (boltzmann.py:913-916)
+    const int need = (flags & BZ_QUIRK_TRIGGER_LAST) ? s_need_last : s_need_any;
+    int64_t ra = pa[threadIdx.x] - sa, rd = pd[threadIdx.x] - sd;
+    for (int k = lo; k < hi; ++k) {
+        if (!need) act[k] = ACT_NONE;
+        int a = act[k];
+        app_off[k] = int32_t(ra);
+        draw_off[k] = int32_t(rd);
+        if (a != ACT_NONE) {
+            int b = k % nb;
+            int64_t n = counts[k], T = targets[b];
+            int64_t app = (a == ACT_SPLIT) ? 2 * T - n : int64_t(merge_keep * double(T));
+            ra += app;
+            rd += app;
+        }
+    }
+    if (threadIdx.x == 1023) {
+        misc[0] = need ? int32_t(pa[1023]) : 0;
+        misc[1] = need;
+        if (need_out) need_out[0] = need;
+    }
+}
+
+// uniform number j of key k: replayed, or Philox 52-bit (two per call)
+__device__ __forceinline__ double rs_uniform(const Rng &g, const double *replay_u, int64_t draw_base, int key,
+                                             int j) {
+    if (replay_u) return replay_u[draw_base + j];
+    u32x4 r = philox(uint32_t(key), uint32_t(j >> 1), g.s0, 3u | (g.s1 << 8), g.k0, g.k1);
+    return (j & 1) ? uni_d(r.z, r.w).u : uni_d(r.x, r.y).u;
+}
+
+__device__ __forceinline__ int lower_bound_d(const double *a, int n, double v) {
+    int lo = 0, hi = n;
+    while (lo < hi) { int m = (lo + hi) >> 1; if (a[m] < v) lo = m + 1; else hi = m; }
+    return lo;
+}
+__device__ __forceinline__ int upper_bound_d(const double *a, int n, double v) {
+    int lo = 0, hi = n;
+    while (lo < hi) { int m = (lo + hi) >> 1; if (a[m] <= v) lo = m + 1; else hi = m; }
+    return lo;
+}
+
+// block helpers (RS_T threads)
+template <typename V> __device__ V block_sum(V v, V *sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    V t = V(0);
+    if (threadIdx.x < RS_T / 32) t = sh[threadIdx.x];
+    if (warp == 0) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0) sh[0] = t;
+    }
+    __syncthreads();
+    V r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+// exclusive scan over the block in thread order; returns the exclusive prefix, *total
+template <typename V> __device__ V block_excl_scan(V v, V *sh, V *total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    V incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        V t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    __syncthreads();
+    if (lane == 31) sh[warp] = incl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        V run = V(0);
+        for (int w = 0; w < RS_T / 32; ++w) { V t = sh[w]; sh[w] = run; run += t; }
+        sh[RS_T / 32] = run;
+    }
+    __syncthreads();
+    V r = sh[warp] + incl - v;
+    *total = sh[RS_T / 32];
+    __syncthreads();
+    return r;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const int32_t *n_ptr, int64_t cap, int nb,
+                                                   const int32_t *targets, const int32_t *max_ppc, double min_wt,
+                                                   double merge_keep, const int32_t *perm, const int32_t *offsets,
+                                                   const int32_t *counts, const int32_t *act, const int32_t *app_off,
+                                                   const int32_t *draw_off, const double *replay_u, double *ws_cdf,
+                                                   int32_t *ws_cnt, double *cons_diag, uint32_t *status) {
+    __shared__ double shd[RS_T / 32 + 1];
+    __shared__ int64_t shi[RS_T / 32 + 1];
+    const int key = blockIdx.x;
+    const int a = act[key];
+    if (a == ACT_NONE) return;
+    const Rng rng = make_rng(p);
+    const int b = key % nb;
+    const int n_k = counts[key];
+    const int off = offsets[key];
+    if (int64_t(off) + n_k > cap || int64_t(*n_ptr) > cap) {  // inconsistent bins: touch nothing
+        if (threadIdx.x == 0) atomicOr(status, BZ_DEV_CAPACITY);
+        return;
+    }
+    const int64_t base = int64_t(*n_ptr) + app_off[key];
+    const int64_t T_ = targets[b];
+    const double efac = 0.5 * m_e() * j_ev();
+    double *cdf = ws_cdf + off;
+    int32_t *cnt = ws_cnt + off;
+    if (a == ACT_SPLIT) {
+        // ---- split (boltzmann.py:806-823): candidates w > min_wt, in index order
+        int nhw = 0;
+        double W = 0.0;
+        // compact candidates into cnt[] (their particle ids) with a block scan, chunk by chunk
+        for (int c0 = 0; c0 < n_k; c0 += RS_T) {
+            int j = c0 + threadIdx.x;
+            int id = j < n_k ? perm[off + j] : -1;
+            bool hw = id >= 0 && double(s.w[id]) > min_wt;
+            int64_t tot;
+            int64_t pos = block_excl_scan<int64_t>(hw ? 1 : 0, shi, &tot);
+            if (hw) cnt[nhw + pos] = id;
+            nhw += int(tot);
+        }
+        __syncthreads();
+        if (nhw == 0) return;
+        for (int j = threadIdx.x; j < nhw; j += RS_T) W += double(s.w[cnt[j]]);
+        W = block_sum<double>(W, shd);
+        // cdf = cumsum(w/W), then / cdf[-1] (CuPy RandomState.choice with p)
+        double carry = 0.0;
+        for (int c0 = 0; c0 < nhw; c0 += RS_T) {
+            int j = c0 + threadIdx.x;
+            double v = j < nhw ? double(s.w[cnt[j]]) / W : 0.0;
+            double tot;
+            double ex = block_excl_scan<double>(v, shd, &tot);
+            if (j < nhw) cdf[j] = carry + ex + v;
+            carry += tot;
+        }
+        __syncthreads();
+        const double last = cdf[nhw - 1];
+        for (int j = threadIdx.x; j < nhw; j += RS_T) cdf[j] = cdf[j] / last;
+        __syncthreads();
+        // scratch regions of this key: cnt = draw counts, hw_ids = candidate ids, tgt = copy targets
+        int32_t *hw_ids = ws_cnt + cap + off;
+        int32_t *tgt = ws_cnt + 2 * cap + off;
+        for (int j = threadIdx.x; j < nhw; j += RS_T) hw_ids[j] = cnt[j];
+        __syncthreads();
+        for (int j = threadIdx.x; j < nhw; j += RS_T) cnt[j] = 0;
+        __syncthreads();
+        const int m = int(2 * T_ - n_k);
+        for (int k = threadIdx.x; k < m; k += RS_T) {
+            double u = rs_uniform(rng, replay_u, draw_off[key], key, k);
+            int ix = upper_bound_d(cdf, nhw, u);
+            if (ix > nhw - 1) ix = nhw - 1;
+            atomicAdd(&cnt[ix], 1);
+        }
+        __syncthreads();
+        if (p.flags & BZ_QUIRK_SPLIT_WRAP) {
+            // HW_ids[unique_ids[v]]: the drawn particle id indexes the candidate list and
+            // CuPy wraps it modulo the list length (boltzmann.py:818-823). Sequential, since
+            // two entries may land on the same particle and divide its weight twice.
+            if (threadIdx.x == 0) {
+                for (int j = 0; j < nhw; ++j) {
+                    int c = cnt[j];
+                    if (!c) continue;
+                    int t = hw_ids[hw_ids[j] % nhw];
+                    double wt = double(s.w[t]) / double(c + 1);
+                    s.w[t] = T(wt);
+                    cdf[j] = double(T(wt));  // weight of this entry's copies
+                    tgt[j] = t;
+                }
+            }
+        } else {
+            for (int j = threadIdx.x; j < nhw; j += RS_T) {
+                int c = cnt[j];
+                if (!c) continue;
+                int t = hw_ids[j];
+                double wt = double(s.w[t]) / double(c + 1);
+                s.w[t] = T(wt);
+                cdf[j] = double(T(wt));
+                tgt[j] = t;
+            }
+        }
+        __syncthreads();
+        // copies, in entry order: exclusive scan of counts
+        int64_t carry2 = 0;
+        for (int c0 = 0; c0 < nhw; c0 += RS_T) {
+            int j = c0 + threadIdx.x;
+            int c = j < nhw ? cnt[j] : 0;
+            int64_t tot;
+            int64_t ex = block_excl_scan<int64_t>(c, shi, &tot);
+            if (c) {
+                int t = tgt[j];
+                T xx = s.x[t], a1 = s.vx[t], a2 = s.vy[t], a3 = s.vz[t], ww = T(cdf[j]);
+                for (int r = 0; r < c; ++r) {
+                    int64_t q = base + carry2 + ex + r;
+                    if (q < cap) {
+                        s.x[q] = xx; s.vx[q] = a1; s.vy[q] = a2; s.vz[q] = a3; s.w[q] = ww;
+                    } else {
+                        atomicOr(status, BZ_DEV_CAPACITY);
+                    }
+                }
+            }
+            carry2 += tot;
+        }
+        return;
+    }
+    // ---- merge (boltzmann.py:826-877)
+    const int np_ = min(n_k, int(max_ppc[b]));
+    const int K = int(merge_keep * double(T_));
+    if (K > np_) {  // survivors need their own scratch slots (max_ppc >= merge_keep*T)
+        if (threadIdx.x == 0) atomicOr(status, BZ_DEV_CAPACITY);
+        return;
+    }
+    double W = 0, px = 0, py = 0, pz = 0, ew = 0;
+    for (int j = threadIdx.x; j < np_; j += RS_T) {
+        int id = perm[off + j];
+        double w = s.w[id], vx = s.vx[id], vy = s.vy[id], vz = s.vz[id];
+        W += w;
+        px += vx * w;
+        py += vy * w;
+        pz += vz * w;
+        ew += w * (efac * (vx * vx + vy * vy + vz * vz));
+    }
+    W = block_sum<double>(W, shd);
+    px = block_sum<double>(px, shd);
+    py = block_sum<double>(py, shd);
+    pz = block_sum<double>(pz, shd);
+    ew = block_sum<double>(ew, shd);
+    const double ux = px / W, uy = py / W, uz = pz / W;
+    const double T_cell = (2.0 / 3.0) * (ew / W);
+    // cdf = cumsum(w/W) (not renormalised), stratified R_k = (1/K)(u_k + k)
+    double carry = 0.0;
+    for (int c0 = 0; c0 < np_; c0 += RS_T) {
+        int j = c0 + threadIdx.x;
+        double v = j < np_ ? double(s.w[perm[off + j]]) / W : 0.0;
+        double tot;
+        double ex = block_excl_scan<double>(v, shd, &tot);
+        if (j < np_) cdf[j] = carry + ex + v;
+        carry += tot;
+    }
+    __syncthreads();
+    const double wbar = W / double(K);
+    const T wbar_t = T(wbar);
+    double hx = 0, hy = 0, hz = 0, he = 0;
+    for (int k = threadIdx.x; k < K; k += RS_T) {
+        double u = rs_uniform(rng, replay_u, draw_off[key], key, k);
+        double R = (1.0 / double(K)) * (u + double(k));
+        int ix = lower_bound_d(cdf, np_, R);
+        ix = ix % np_;  // CuPy wraps ids[len] to ids[0]
+        int id = perm[off + ix];
+        cnt[k] = id;
+        double vx = s.vx[id], vy = s.vy[id], vz = s.vz[id];
+        hx += vx * wbar;
+        hy += vy * wbar;
+        hz += vz * wbar;
+        he += wbar * (efac * (vx * vx + vy * vy + vz * vz));
+    }
+    hx = block_sum<double>(hx, shd) / W;
+    hy = block_sum<double>(hy, shd) / W;
+    hz = block_sum<double>(hz, shd) / W;
+    he = block_sum<double>(he, shd);
+    const double Te_hat = (2.0 / 3.0) * he / W;
+    double Tfac;
+    if (p.flags & BZ_FIX_MERGE_ENERGY) {
+        // scale the thermal part only: sum w e about the kept mean equals the original
+        // thermal energy, so total energy is conserved (the reference's factor includes
+        // the drift energy, boltzmann.py:861-869)
+        double th_o = ew - efac * W * (ux * ux + uy * uy + uz * uz);
+        double th_k = he - efac * W * (hx * hx + hy * hy + hz * hz);
+        Tfac = sqrt(th_o / th_k);
+    } else {
+        Tfac = sqrt(T_cell / Te_hat);
+    }
+    __syncthreads();  // every read of the originals is done before they are zeroed / overwritten
+    double aW = 0, ax = 0, ay = 0, az = 0, ae = 0;
+    for (int k = threadIdx.x; k < K; k += RS_T) {
+        int id = cnt[k];
+        T xx = s.x[id];
+        double vx = ux + (double(s.vx[id]) - hx) * Tfac;
+        double vy = uy + (double(s.vy[id]) - hy) * Tfac;
+        double vz = uz + (double(s.vz[id]) - hz) * Tfac;
+        T tx = T(vx), ty = T(vy), tz = T(vz);
+        int64_t q = base + k;
+        if (q < cap) {
+            s.x[q] = xx; s.vx[q] = tx; s.vy[q] = ty; s.vz[q] = tz; s.w[q] = wbar_t;
+        } else {
+            atomicOr(status, BZ_DEV_CAPACITY);
+        }
+        double wd = double(wbar_t), dx = tx, dy = ty, dz = tz;
+        aW += wd;
+        ax += wd * dx;
+        ay += wd * dy;
+        az += wd * dz;
+        ae += wd * (efac * (dx * dx + dy * dy + dz * dz));
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < np_; j += RS_T) s.w[perm[off + j]] = T(0);
+    if (cons_diag) {
+        aW = block_sum<double>(aW, shd);
+        ax = block_sum<double>(ax, shd);
+        ay = block_sum<double>(ay, shd);
+        az = block_sum<double>(az, shd);
+        ae = block_sum<double>(ae, shd);
+        if (threadIdx.x == 0) {
+            double *d = cons_diag + size_t(key) * 10;
+            d[0] = W; d[1] = px; d[2] = py; d[3] = pz; d[4] = ew;
+            d[5] = aW; d[6] = ax; d[7] = ay; d[8] = az; d[9] = ae;
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// order-preserving compaction of w != 0 (boltzmann.py:879-883)
+// ------------------------------------------------------------------------------------
+constexpr int CT = 256, CI = 4, CTILE = CT * CI;
+
+template <typename T>
+__global__ void __launch_bounds__(CT) k_compact(SoAR<T> in, const int32_t *n_ptr, const int32_t *extra,
+                                                int64_t in_cap, SoAR<T> out, int64_t out_cap, int32_t *n_out,
+                                                unsigned int *ticket, uint64_t *tile_status, int max_tiles,
+                                                uint32_t *status) {
+    __shared__ int s_tile;
+    __shared__ uint32_t s_ps, s_pc, s_warp[CT / 32];
+    int64_t n = int64_t(max(*n_ptr, 0)) + (extra ? int64_t(max(*extra, 0)) : 0);
+    if (n > in_cap) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(status, BZ_DEV_CAPACITY);
+        n = in_cap;
+    }
+    const int ntiles = int(ceil_div(n, CTILE));
+    if (ntiles > max_tiles) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(status, BZ_DEV_CAPACITY);
+        return;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    while (true) {
+        if (threadIdx.x == 0) s_tile = int(atomicAdd(ticket, 1u));
+        __syncthreads();
+        const int tile = s_tile;
+        if (tile >= ntiles) break;
+        const int64_t b0 = int64_t(tile) * CTILE + int64_t(threadIdx.x) * CI;
+        uint32_t keep = 0;
+#pragma unroll
+        for (int j = 0; j < CI; ++j) {
+            int64_t i = b0 + j;
+            if (i < n && in.w[i] != T(0)) keep |= 1u << j;
+        }
+        uint32_t v = __popc(keep), incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (lane == 31) s_warp[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t wv = lane < CT / 32 ? s_warp[lane] : 0u, wi = wv;
+#pragma unroll
+            for (int o = 1; o < CT / 32; o <<= 1) {
+                uint32_t t = __shfl_up_sync(0xffffffffu, wi, o);
+                if (lane >= o) wi += t;
+            }
+            uint32_t tot = __shfl_sync(0xffffffffu, wi, CT / 32 - 1);
+            if (lane < CT / 32) s_warp[lane] = wi - wv;
+            lookback(tile_status, tile, tot, 0u, &s_ps, &s_pc, status);
+            if (lane == 0 && tile == ntiles - 1) *n_out = int32_t(min(int64_t(s_ps + tot), out_cap));
+        }
+        __syncthreads();
+        int64_t pos = int64_t(s_ps) + s_warp[warp] + incl - v;
+#pragma unroll
+        for (int j = 0; j < CI; ++j) {
+            if (keep & (1u << j)) {
+                int64_t i = b0 + j;
+                if (pos < out_cap) {
+                    out.x[pos] = in.x[i]; out.vx[pos] = in.vx[i]; out.vy[pos] = in.vy[i]; out.vz[pos] = in.vz[i];
+                    out.w[pos] = in.w[i];
+                } else {
+                    atomicOr(status, BZ_DEV_CAPACITY);
+                }
+                ++pos;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+struct CompactWs {
+    static size_t bytes(int64_t cap) { return 256 + 8 * size_t(ceil_div(std::max<int64_t>(cap, 1), CTILE)); }
+};
+
+template <typename T>
+static int launch_compact(SoAR<T> in, const int32_t *n, const int32_t *extra, int64_t in_cap, SoAR<T> out,
+                          int64_t out_cap, int32_t *n_out, void *ws, size_t ws_bytes, uint32_t *status,
+                          cudaStream_t st) {
+    if (ws_bytes < CompactWs::bytes(1)) return BZ_ERR_WORKSPACE;
+    if (cudaMemsetAsync(ws, 0, ws_bytes, st) != cudaSuccess) return BZ_ERR_CUDA;
+    if (cudaMemsetAsync(n_out, 0, sizeof(int32_t), st) != cudaSuccess) return BZ_ERR_CUDA;
+    int dev = 0, sms = 1, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_compact<T>, CT, 0);
+    int64_t max_tiles = int64_t((ws_bytes - 256) / 8);
+    unsigned char *b = static_cast<unsigned char *>(ws);
+    k_compact<T><<<sms * std::max(per_sm, 1), CT, 0, st>>>(in, n, extra, in_cap, out, out_cap, n_out,
+                                                           reinterpret_cast<unsigned int *>(b),
+                                                           reinterpret_cast<uint64_t *>(b + 256),
+                                                           int(std::min<int64_t>(max_tiles, INT32_MAX)), status);
+    return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+}
+
+template <typename T, typename P>
+static int resample_entry(const bz_params *pp, P s_, const int32_t *n, int64_t cap, P out_, int32_t *n_out, int nb,
+                          const int32_t *targets, const int32_t *max_ppc, double min_wt, double split_below,
+                          double merge_at, double merge_keep, const int32_t *perm, const int32_t *offsets,
+                          const int32_t *counts, const int32_t *hw_counts, const double *replay_u,
+                          int32_t *need_out, double *cons_diag, void *ws, size_t ws_bytes, uint32_t *status,
+                          void *stream) {
+    if (!pp || !n || cap <= 0 || !n_out || !targets || !max_ppc || !perm || !offsets || !counts || !hw_counts ||
+        !ws || !status)
+        return BZ_ERR_ARG;
+    if (!s_.x || !s_.vx || !s_.vy || !s_.vz || !s_.w || !out_.x || !out_.vx || !out_.vy || !out_.vz || !out_.w)
+        return BZ_ERR_ARG;
+    const bz_params &p = *pp;
+    if (nb < 1 || p.n_nodes < 1 || !(merge_at > split_below) || !(merge_keep > 0)) return BZ_ERR_ARG;
+    const int nkeys = p.n_nodes * nb;
+    RsWs L(cap, nkeys);
+    size_t cws = CompactWs::bytes(cap);
+    if (ws_bytes < L.total + cws) return BZ_ERR_WORKSPACE;
+    unsigned char *b = static_cast<unsigned char *>(ws);
+    int32_t *act = reinterpret_cast<int32_t *>(b + L.act);
+    int32_t *app_off = reinterpret_cast<int32_t *>(b + L.app_off);
+    int32_t *draw_off = reinterpret_cast<int32_t *>(b + L.draw_off);
+    int32_t *misc = reinterpret_cast<int32_t *>(b + L.misc);
+    double *cdf = reinterpret_cast<double *>(b + L.cdf);
+    int32_t *cnt = reinterpret_cast<int32_t *>(b + L.cnt);
+    cudaStream_t st = as_stream(stream);
+    k_rs_decide<<<1, 1024, 0, st>>>(counts, hw_counts, p.n_nodes, nb, targets, split_below, merge_at, merge_keep,
+                                    p.flags, act, app_off, draw_off, misc, need_out);
+    if (cons_diag && cudaMemsetAsync(cons_diag, 0, sizeof(double) * 10 * nkeys, st) != cudaSuccess) return BZ_ERR_CUDA;
+    SoAR<T> s{s_.x, s_.vx, s_.vy, s_.vz, s_.w};
+    SoAR<T> o{out_.x, out_.vx, out_.vy, out_.vz, out_.w};
+    k_rs_apply<T><<<nkeys, RS_T, 0, st>>>(p, s, n, cap, nb, targets, max_ppc, min_wt, merge_keep, perm, offsets,
+                                          counts, act, app_off, draw_off, replay_u, cdf, cnt, cons_diag, status);
+    if (cudaGetLastError() != cudaSuccess) return BZ_ERR_CUDA;
+    return launch_compact<T>(s, n, misc, cap, o, cap, n_out, b + L.total, ws_bytes - L.total, status, st);
+}
+
+}  // namespace bz
+
+extern "C" {
+size_t bz_resample_workspace(int64_t capacity, int32_t nkeys) {
+    return bz::RsWs(capacity, nkeys).total + bz::CompactWs::bytes(capacity);
+}
+int bz_resample_f32(const bz_params *p, bz_particles_f32 s, const int32_t *n, int64_t capacity, bz_particles_f32 out,
+                    int32_t *n_out, int32_t nbins, const int32_t *targets, const int32_t *max_ppc, double min_wt,
+                    double split_below, double merge_at, double merge_keep, const int32_t *perm,
+                    const int32_t *offsets, const int32_t *counts, const int32_t *hw_counts, const double *replay_u,
+                    int32_t *need_out, double *cons_diag, void *workspace, size_t workspace_bytes, uint32_t *status,
+                    void *stream) {
+    return bz::resample_entry<float>(p, s, n, capacity, out, n_out, nbins, targets, max_ppc, min_wt, split_below,
+                                     merge_at, merge_keep, perm, offsets, counts, hw_counts, replay_u, need_out,
+                                     cons_diag, workspace, workspace_bytes, status, stream);
+}
+int bz_resample_f64(const bz_params *p, bz_particles_f64 s, const int32_t *n, int64_t capacity, bz_particles_f64 out,
+                    int32_t *n_out, int32_t nbins, const int32_t *targets, const int32_t *max_ppc, double min_wt,
+                    double split_below, double merge_at, double merge_keep, const int32_t *perm,
+                    const int32_t *offsets, const int32_t *counts, const int32_t *hw_counts, const double *replay_u,
+                    int32_t *need_out, double *cons_diag, void *workspace, size_t workspace_bytes, uint32_t *status,
+                    void *stream) {
+    return bz::resample_entry<double>(p, s, n, capacity, out, n_out, nbins, targets, max_ppc, min_wt, split_below,
+                                      merge_at, merge_keep, perm, offsets, counts, hw_counts, replay_u, need_out,
+                                      cons_diag, workspace, workspace_bytes, status, stream);
+}
+size_t bz_compact_workspace(int64_t capacity) { return bz::CompactWs::bytes(capacity); }
+int bz_compact_f32(bz_particles_f32 in, const int32_t *n, int64_t in_capacity, bz_particles_f32 out,
+                   int64_t out_capacity, int32_t *n_out, void *workspace, size_t workspace_bytes, uint32_t *status,
+                   void *stream) {
+    if (!n || !n_out || !workspace || !status || in_capacity < 0 || out_capacity < 0) return BZ_ERR_ARG;
+    if (!in.x || !in.vx || !in.vy || !in.vz || !in.w || !out.x || !out.vx || !out.vy || !out.vz || !out.w)
+        return BZ_ERR_ARG;
+    bz::SoAR<float> a{in.x, in.vx, in.vy, in.vz, in.w}, b{out.x, out.vx, out.vy, out.vz, out.w};
+    return bz::launch_compact<float>(a, n, nullptr, in_capacity, b, out_capacity, n_out, workspace, workspace_bytes,
+                                     status, bz::as_stream(stream));
+}
+int bz_compact_f64(bz_particles_f64 in, const int32_t *n, int64_t in_capacity, bz_particles_f64 out,
+                   int64_t out_capacity, int32_t *n_out, void *workspace, size_t workspace_bytes, uint32_t *status,
+                   void *stream) {
+    if (!n || !n_out || !workspace || !status || in_capacity < 0 || out_capacity < 0) return BZ_ERR_ARG;
+    if (!in.x || !in.vx || !in.vy || !in.vz || !in.w || !out.x || !out.vx || !out.vy || !out.vz || !out.w)
+        return BZ_ERR_ARG;
+    bz::SoAR<double> a{in.x, in.vx, in.vy, in.vz, in.w}, b{out.x, out.vx, out.vy, out.vz, out.w};
+    return bz::launch_compact<double>(a, n, nullptr, in_capacity, b, out_capacity, n_out, workspace,
+                                      workspace_bytes, status, bz::as_stream(stream));
+}
+}

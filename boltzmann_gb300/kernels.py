@@ -1,0 +1,187 @@
+"""Device buffers and thin wrappers over the libbz entry points.
+
+PyTorch is used only to own device memory and to supply the current CUDA stream;
+every computation is a libbz kernel. Function names follow the reference's kernel
+modules (electron_kernel, bin_particles, post_processing / reduction, EF_kernel,
+heavies_kernel_fluid); argument meaning follows ``include/bz.h``.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import BzParams, Particles, call
+
+
+def _ptr(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class ParticleSet:
+    """Structure-of-arrays particle state (x, vx, vy, vz, w) of fixed capacity on one
+    GPU, plus an int32 count word array: cnt[0] survivors, cnt[1] children, cnt[2] n."""
+
+    FIELDS = ("x", "vx", "vy", "vz", "w")
+
+    def __init__(self, capacity, dtype=torch.float32, device="cuda"):
+        self.capacity = int(capacity)
+        self.dtype = dtype
+        # one allocation, 5 arrays, each 256-byte aligned
+        esz = torch.finfo(dtype).bits // 8
+        stride = ((self.capacity * esz + 255) // 256) * 256 // esz
+        self._buf = torch.zeros(5 * stride, dtype=dtype, device=device)
+        for k, f in enumerate(self.FIELDS):
+            setattr(self, f, self._buf[k * stride: k * stride + self.capacity])
+        self.cnt = torch.zeros(4, dtype=torch.int32, device=device)
+
+    @property
+    def suffix(self):
+        return "f32" if self.dtype == torch.float32 else "f64"
+
+    def struct(self):
+        return Particles(*(getattr(self, f).data_ptr() for f in self.FIELDS))
+
+    def n_ptr(self):
+        return ctypes.c_void_p(self.cnt.data_ptr() + 8)
+
+    def counts_ptr(self):
+        return ctypes.c_void_p(self.cnt.data_ptr())
+
+    def n(self):
+        """Particle count (reads device memory: a synchronisation)."""
+        return int(self.cnt[2].item())
+
+    def load(self, x, vx, vy, vz, w):
+        n = len(x)
+        if n > self.capacity:
+            raise ValueError(f"{n} particles exceed capacity {self.capacity}")
+        for f, a in zip(self.FIELDS, (x, vx, vy, vz, w)):
+            getattr(self, f)[:n].copy_(torch.as_tensor(np.asarray(a), dtype=self.dtype))
+        self.cnt.zero_()
+        self.cnt[2] = n
+        self.cnt[0] = n
+
+    def to_numpy(self, n=None):
+        n = self.n() if n is None else n
+        return {f: getattr(self, f)[:n].detach().cpu().numpy().astype(np.float64) for f in self.FIELDS}
+
+
+class Workspace:
+    """Grow-only device scratch per purpose."""
+
+    def __init__(self, device="cuda"):
+        self.device = device
+        self._bufs = {}
+
+    def get(self, name, nbytes):
+        b = self._bufs.get(name)
+        if b is None or b.numel() < nbytes:
+            b = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=self.device)
+            self._bufs[name] = b
+        return b
+
+
+def make_params(*, n_faces, n_nodes, bnf, advect, L, dx, dt, nn, gas_sigma=0.0, e_exc=11.5, nu_max=0.0,
+                xs_mode=_lib.XS_TABLE, coll_model=_lib.COLL_DIRECT, xs_table=None, xs_emin=0.01, xs_emax=1000.0,
+                flags=0, seed=0, step=0, step_ptr=None):
+    p = BzParams()
+    p.n_faces, p.n_nodes, p.bnf, p.advect = int(n_faces), int(n_nodes), int(bnf), int(advect)
+    p.L, p.dx, p.dt, p.nn = float(L), float(dx), float(dt), float(nn)
+    p.gas_sigma, p.e_exc, p.nu_max = float(gas_sigma), float(e_exc), float(nu_max)
+    p.xs_mode, p.coll_model, p.flags = int(xs_mode), int(coll_model), int(flags)
+    if xs_table is not None:
+        p.xs_n = int(xs_table.shape[1])
+        p.xs_table = xs_table.data_ptr()
+    else:
+        p.xs_n = 0
+        p.xs_table = None
+    p.xs_emin, p.xs_emax = float(xs_emin), float(xs_emax)
+    p.seed, p.step = int(seed), int(step)
+    p.step_ptr = None if step_ptr is None else step_ptr.data_ptr()
+    return p
+
+
+# --------------------------------------------------------------------------------------
+# entry points
+# --------------------------------------------------------------------------------------
+
+def electron_kernel(params, src: ParticleSet, dst: ParticleSet, E, status, ws: Workspace, moments=None,
+                    replay_R=None, replay_gas=None):
+    """Push + collide src into dst (compacted, children appended); optionally deposit
+    moments [4, n_nodes] (float64, accumulated). electron_kernel_numba.py:291-303 plus
+    the deposit and compaction of post_processing_1D.py:40-68."""
+    if src.dtype != dst.dtype:
+        raise TypeError("src and dst precision differ")
+    if E.dtype != src.dtype:
+        raise TypeError("E must have the particle precision")
+    nbytes = _lib.load().bz_push_workspace(max(src.capacity, dst.capacity))
+    w = ws.get("push", nbytes)
+    call(f"bz_push_collide_{src.suffix}", ctypes.byref(params), src.struct(), src.n_ptr(), src.capacity, dst.struct(),
+         dst.capacity, dst.counts_ptr(), _ptr(E), _ptr(replay_R), _ptr(replay_gas), _ptr(moments), _ptr(w),
+         w.numel(), _ptr(status), _stream())
+
+
+def deposit(params, s: ParticleSet, moments, ionflag=None):
+    """The moments post_processing deposits (kernels-new.cu reda/redcheck), race-free."""
+    call(f"bz_deposit_{s.suffix}", ctypes.byref(params), s.struct(), s.n_ptr(), s.capacity, _ptr(ionflag),
+         _ptr(moments), _stream())
+
+
+def bin_particles(params, s: ParticleSet, edges, min_wt, perm, offsets, counts, hw_counts, status, ws: Workspace):
+    """Cell x energy-bin stable sort (bin_particles.py:7-31 and its 3/5-bin versions)."""
+    nb = int(edges.numel()) + 1
+    nkeys = params.n_nodes * nb
+    nbytes = _lib.load().bz_bin_workspace(s.capacity, nkeys)
+    w = ws.get("bin", nbytes)
+    call(f"bz_bin_{s.suffix}", ctypes.byref(params), s.struct(), s.n_ptr(), s.capacity, nb,
+         _ptr(edges) if nb > 1 else None, float(min_wt), _ptr(perm), _ptr(offsets), _ptr(counts), _ptr(hw_counts),
+         _ptr(w), w.numel(), _ptr(status), _stream())
+
+
+def resample(params, s: ParticleSet, out: ParticleSet, nb, targets, max_ppc, min_wt, split_below, merge_at,
+             merge_keep, perm, offsets, counts, hw_counts, status, ws: Workspace, need=None, replay_u=None,
+             cons_diag=None):
+    """ES-WPNC split / merge (boltzmann.py:799-890), appended into s, compacted into out."""
+    nkeys = params.n_nodes * nb
+    nbytes = _lib.load().bz_resample_workspace(s.capacity, nkeys)
+    w = ws.get("resample", nbytes)
+    call(f"bz_resample_{s.suffix}", ctypes.byref(params), s.struct(), s.n_ptr(), s.capacity, out.struct(),
+         out.n_ptr(), nb, _ptr(targets), _ptr(max_ppc), float(min_wt), float(split_below), float(merge_at),
+         float(merge_keep), _ptr(perm), _ptr(offsets), _ptr(counts), _ptr(hw_counts), _ptr(replay_u), _ptr(need),
+         _ptr(cons_diag), _ptr(w), w.numel(), _ptr(status), _stream())
+
+
+def compact(s: ParticleSet, out: ParticleSet, status, ws: Workspace):
+    """Order-preserving removal of w == 0 particles (boltzmann.py:879-883)."""
+    w = ws.get("compact", _lib.load().bz_compact_workspace(s.capacity))
+    call(f"bz_compact_{s.suffix}", s.struct(), s.n_ptr(), s.capacity, out.struct(), out.capacity, out.n_ptr(), _ptr(w),
+         w.numel(), _ptr(status), _stream())
+
+
+def grid_update(n_nodes, moments, ni, Te, g2):
+    call("bz_grid_update", int(n_nodes), _ptr(moments), _ptr(ni), _ptr(Te), _ptr(g2), _stream())
+
+
+def heavies_kernel_fluid(N, dx, dt, mu_i, D_i, E, ni, Ji, brk=None):
+    call("bz_ion_fluid", int(N), float(dx), float(dt), float(mu_i), float(D_i), _ptr(E), _ptr(ni), _ptr(Ji),
+         _ptr(brk), _stream())
+
+
+def poisson_factor(N, dx, diag, lower):
+    call("bz_poisson_factor", int(N), float(dx), _ptr(diag), _ptr(lower))
+
+
+def EF_kernel(N, dx, eps0, V0, freq, t, ne, ni, diag, lower, V, E, E32=None, t_dev=None):
+    call("bz_poisson", int(N), float(dx), float(eps0), float(V0), float(freq), float(t), _ptr(t_dev), _ptr(ne),
+         _ptr(ni), _ptr(diag), _ptr(lower), _ptr(V), _ptr(E), _ptr(E32), _stream())
+
+
+def advance_clock(t_dev, step_dev, dt):
+    call("bz_advance_clock", _ptr(t_dev), _ptr(step_dev), float(dt), _stream())

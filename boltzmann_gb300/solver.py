@@ -1,0 +1,272 @@
+"""Device-resident hybrid electron PIC-MCC solver with the reference's entry points.
+
+``BoltzmannGB300`` mirrors ``BoltzmannDSMC`` (boltzmann.py:22-916): the same step
+order (resample check every ``resample_freq`` steps, push + collide, deposit and
+compaction, grid update, ion fluid, Poisson; boltzmann.py:570-678) and the same method
+names (electron_kernel, post_processing, bin_particles, _check_for_resampling,
+_do_resampling, heavies_kernel_fluid, EF_kernel, run, data_write). Everything runs
+on one GPU stream; counts, the step clock and the RF time live in device memory, so a
+step is captured once into a CUDA graph and replayed.
+"""
+from __future__ import annotations
+
+import math
+import os
+
+import numpy as np
+import torch
+
+from . import _lib, kernels as K
+from .config import CCPConfig
+
+KTM = 1.5 * 1.17255e11  # (m/s)^2 per eV of temperature (boltzmann.py:263)
+
+
+class BoltzmannGB300:
+    def __init__(self, cfg: CCPConfig, device="cuda", capacity=None):
+        self.cfg = cfg
+        self.device = device
+        self.dtype = torch.float32 if cfg.precision == "float32" else torch.float64
+        N = cfg.N
+        self.N = N
+        self.nnodes = N + 1
+        dev = device
+        f64 = dict(dtype=torch.float64, device=dev)
+        # particles: initial condition (boltzmann.py:242-333)
+        x, vx, vy, vz, w = self._initial_condition()
+        n0 = x.numel()
+        cap = capacity or int(math.ceil(cfg.capacity_factor * max(n0, cfg.num_particles)))
+        self.capacity = cap
+        self.A = K.ParticleSet(cap, self.dtype, dev)
+        self.B = K.ParticleSet(cap, self.dtype, dev)
+        for f, a in zip(K.ParticleSet.FIELDS, (x, vx, vy, vz, w)):
+            getattr(self.A, f)[:n0].copy_(a.to(self.dtype))
+        self.A.cnt.zero_()
+        self.A.cnt[2] = n0
+        del x, vx, vy, vz, w
+        # grid arrays (boltzmann.py:94-109)
+        self.E = torch.zeros(N, **f64)
+        self.E_push = torch.zeros(N, dtype=self.dtype, device=dev)
+        self.V = torch.zeros(N - 1, **f64)
+        self.Ji = torch.zeros(N, **f64)
+        self.moments = torch.zeros(4, self.nnodes, **f64)
+        self.ni = torch.as_tensor(self._ne_profile(), **f64).clone()
+        self.Te = torch.zeros(self.nnodes, **f64)
+        self.g2 = torch.zeros(self.nnodes, **f64)
+        self.chol_d = torch.zeros(max(N - 1, 1), **f64)
+        self.chol_l = torch.zeros(max(N - 1, 1), **f64)
+        self.t = torch.zeros(1, **f64)
+        self.step_dev = torch.zeros(1, dtype=torch.int64, device=dev)
+        self.brk = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.ws = K.Workspace(dev)
+        # cross sections
+        tab = cfg.xs_table()
+        self.xs = tab
+        self.xs_t = None if tab is None else torch.as_tensor(tab.nsigma(cfg.nn_m3), device=dev)
+        # ES-WPNC tables (boltzmann.py:538-548)
+        nb = cfg.nbins
+        self.nb = nb
+        nkeys = self.nnodes * nb
+        self.edges = torch.as_tensor(np.asarray(cfg.bin_edges, dtype=np.float64).reshape(-1) if nb > 1
+                                     else np.zeros(1), device=dev)
+        self.targets = torch.as_tensor(np.asarray(cfg.targets(), dtype=np.int32), device=dev)
+        self.max_ppc = torch.as_tensor(np.asarray(cfg.max_ppc(), dtype=np.int32), device=dev)
+        self.perm = torch.zeros(cap, dtype=torch.int32, device=dev)
+        self.offsets = torch.zeros(nkeys + 1, dtype=torch.int32, device=dev)
+        self.bin_counts = torch.zeros(nkeys, dtype=torch.int32, device=dev)
+        self.hw_counts = torch.zeros(nkeys, dtype=torch.int32, device=dev)
+        self.need = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.bigstep = 0
+        self.particle_steps = torch.zeros(1, dtype=torch.int64, device=dev)
+        self._graphs = {}
+        self._seen = set()
+        if N >= 3:
+            K.poisson_factor(N, cfg.dx, self.chol_d, self.chol_l)
+        # first deposit and field solve (boltzmann.py:363-399)
+        K.deposit(self.params(), self.A, self.moments)
+        self.ni.add_(self.moments[1])
+        self._grid_solves(advance=False)
+
+    # ---------------------------------------------------------------------------------
+    def _ne_profile(self):
+        cfg = self.cfg
+        xg = np.linspace(0, cfg.L, self.nnodes)
+        if cfg.ne_profile == "uniform":
+            return np.full(self.nnodes, cfg.ne_uniform)
+        return cfg.pressure_torr * (1e7 + 1e9 * (1 - xg / cfg.L) ** 2 * (xg / cfg.L) ** 2)  # boltzmann.py:247
+
+    def _initial_condition(self):
+        """Particles per node at the node position (dx/4 inside at the walls), isotropic
+        Maxwellian at Te_init, weight = density / particles per node (boltzmann.py:256-300);
+        or, for ne_profile == 'uniform', positions uniform in (0, L)."""
+        cfg = self.cfg
+        g = torch.Generator(device=self.device)
+        g.manual_seed(int(cfg.seed))
+        dev = self.device
+        ppc = int(sum(cfg.targets()))
+        ne = self._ne_profile()
+        sig = math.sqrt(cfg.Te_init_eV * KTM)
+        if cfg.ne_profile == "uniform":
+            n = int(cfg.num_particles)
+            x = torch.rand(n, generator=g, device=dev, dtype=torch.float64) * cfg.L
+            x = x.clamp(1e-6 * cfg.L, cfg.L * (1 - 1e-6))
+            w = torch.full((n,), cfg.ne_uniform * self.nnodes / n, device=dev, dtype=torch.float64)
+        else:
+            n = ppc * self.nnodes
+            xg = torch.linspace(0, cfg.L, self.nnodes, device=dev, dtype=torch.float64)
+            xg[0] += cfg.dx / 4.0
+            xg[-1] -= cfg.dx / 4.0
+            x = xg.repeat_interleave(ppc)
+            w = torch.as_tensor(ne / ppc, device=dev).repeat_interleave(ppc)
+        v = torch.randn(n, 3, generator=g, device=dev, dtype=torch.float64) * sig
+        perm = torch.randperm(n, generator=g, device=dev)  # the reference shuffles (boltzmann.py:315-318)
+        return x[perm], v[perm, 0].contiguous(), v[perm, 1].contiguous(), v[perm, 2].contiguous(), w[perm]
+
+    def params(self, step_on_device=True):
+        cfg = self.cfg
+        tab = self.xs
+        return K.make_params(
+            n_faces=self.N, n_nodes=self.nnodes, bnf=cfg.bnf, advect=1, L=cfg.L, dx=cfg.dx, dt=cfg.dt,
+            nn=cfg.nn_m3, gas_sigma=cfg.gas_sigma(), e_exc=(tab.e_exc if tab else 11.5),
+            nu_max=(tab.nu_max(cfg.nn_m3) if tab else 0.0), xs_mode=cfg.xs_mode(), coll_model=cfg.coll_model,
+            xs_table=self.xs_t, xs_emin=(tab.emin if tab else 0.01), xs_emax=(tab.emax if tab else 1000.0),
+            flags=cfg.quirks, seed=cfg.seed, step=self.bigstep,
+            step_ptr=self.step_dev if step_on_device else None)
+
+    # --------------------------------------------------------------------------------- reference entry points
+    def electron_kernel(self):
+        """Push + collide the current particles; deposit and compaction are fused in
+        (electron_kernel_numba.py:291-303 with post_processing_1D.py:40-68)."""
+        self.moments.zero_()
+        K.electron_kernel(self.params(), self.A, self.B, self.E_push, self.status, self.ws, moments=self.moments)
+        self.particle_steps.add_(self.A.cnt[2:3].to(torch.int64))
+        self.A, self.B = self.B, self.A
+
+    def post_processing(self):
+        """Grid moments of the last step: (ne, ni_src, ns_src, nrg) device tensors
+        (post_processing_1D.py:40-68 returns them as host arrays)."""
+        return self.moments[0], self.moments[1], self.moments[2], self.moments[3]
+
+    def bin_particles(self):
+        K.bin_particles(self.params(), self.A, self.edges[: self.nb - 1] if self.nb > 1 else self.edges[:0],
+                        self.cfg.min_wt, self.perm, self.offsets, self.bin_counts, self.hw_counts, self.status,
+                        self.ws)
+
+    def _check_for_resampling(self):
+        """Bin the particles (the trigger itself is evaluated on the device inside
+        _do_resampling, boltzmann.py:894-916)."""
+        self.bin_particles()
+
+    def _do_resampling(self):
+        cfg = self.cfg
+        K.resample(self.params(), self.A, self.B, self.nb, self.targets, self.max_ppc, cfg.min_wt, cfg.split_below,
+                   cfg.merge_at, cfg.merge_keep, self.perm, self.offsets, self.bin_counts, self.hw_counts,
+                   self.status, self.ws, need=self.need)
+        self.A, self.B = self.B, self.A
+
+    def heavies_kernel_fluid(self):
+        cfg = self.cfg
+        K.heavies_kernel_fluid(self.N, cfg.dx, cfg.dt, cfg.mu_i, cfg.D_i, self.E, self.ni, self.Ji, self.brk)
+
+    def EF_kernel(self):
+        cfg = self.cfg
+        K.EF_kernel(self.N, cfg.dx, cfg.eps0, cfg.V0, cfg.freq, 0.0, self.moments[0], self.ni, self.chol_d,
+                    self.chol_l, self.V, self.E, self.E_push if self.dtype == torch.float32 else None, t_dev=self.t)
+        if self.dtype == torch.float64:
+            self.E_push.copy_(self.E)
+
+    def _grid_solves(self, advance=True):
+        cfg = self.cfg
+        if advance:
+            K.grid_update(self.nnodes, self.moments, self.ni, self.Te, self.g2)
+            K.advance_clock(self.t, self.step_dev, cfg.dt)
+            self.heavies_kernel_fluid()
+        self.EF_kernel()
+
+    # --------------------------------------------------------------------------------- stepping
+    def _step_body(self, resample):
+        if resample:
+            self._check_for_resampling()
+            self._do_resampling()
+        self.electron_kernel()
+        self._grid_solves(advance=True)
+
+    def step(self, use_graph=True):
+        """One step of the hybrid loop (boltzmann.py:570-678). With ``use_graph`` the
+        step is captured into a CUDA graph the second time its kind (resample or not,
+        which buffer holds the particles) occurs, and replayed from then on; the first
+        occurrence runs eagerly so that every kernel is loaded and configured before
+        any capture."""
+        resample = (self.bigstep % self.cfg.resample_freq) == 0
+        key = (resample, self.A is self._first_A())
+        if use_graph and key in self._seen:
+            gr = self._graphs.get(key)
+            if gr is None:
+                gr = self._capture(resample)
+                self._graphs[key] = gr
+            gr.replay()
+            # the graph swaps A and B internally; mirror the swaps on the host side
+            for _ in range(2 if resample else 1):
+                self.A, self.B = self.B, self.A
+        else:
+            self._seen.add(key)
+            self._step_body(resample)
+        self.bigstep += 1
+
+    def _first_A(self):
+        if not hasattr(self, "_A0"):
+            self._A0 = self.A
+        return self._A0
+
+    def _capture(self, resample):
+        s = torch.cuda.Stream(device=self.device)
+        s.wait_stream(torch.cuda.current_stream())
+        g = torch.cuda.CUDAGraph()
+        saved = (self.A, self.B)
+        with torch.cuda.stream(s):
+            self._warm(resample)
+        torch.cuda.current_stream().wait_stream(s)
+        with torch.cuda.graph(g, stream=s, capture_error_mode="relaxed"):
+            self._step_body(resample)
+        self.A, self.B = saved
+        return g
+
+    def _warm(self, resample):
+        """Allocate every workspace the step uses without running the step."""
+        cap = self.capacity
+        self.ws.get("push", _lib.load().bz_push_workspace(cap))
+        if resample:
+            self.ws.get("bin", _lib.load().bz_bin_workspace(cap, self.nnodes * self.nb))
+            self.ws.get("resample", _lib.load().bz_resample_workspace(cap, self.nnodes * self.nb))
+
+    def run(self, num_steps, name="", restart_cyclenum=0, use_graph=True, write=False):
+        """The step loop (boltzmann.py:565-716), with cycle averages and, when ``write``,
+        the reference's per-cycle output files."""
+        cfg = self.cfg
+        spc = cfg.steps_per_cycle
+        acc = {k: torch.zeros_like(getattr(self, k)) for k in ("ni", "Te", "E")}
+        acc["ne"] = torch.zeros_like(self.moments[0])
+        for _ in range(num_steps):
+            self.step(use_graph=use_graph)
+            if (self.bigstep % spc) != 0:
+                acc["ne"].add_(self.moments[0]); acc["ni"].add_(self.ni)
+                acc["Te"].add_(self.Te); acc["E"].add_(self.E)
+            else:
+                ca = {k: (v / spc) for k, v in acc.items()}
+                if write:
+                    from . import io as bzio
+                    bzio.data_write(self, name, self.bigstep // spc + restart_cyclenum, ca)
+                for v in acc.values():
+                    v.zero_()
+        return self
+
+    # --------------------------------------------------------------------------------- diagnostics
+    def n(self):
+        return self.A.n()
+
+    def device_status(self):
+        return int(self.status.item())
+
+    def ne(self):
+        return self.moments[0]

@@ -1,0 +1,207 @@
+/* libbz: GB300 (sm_103a) electron PIC-MCC hot path behind a C ABI.
+ *
+ * Drop-in replacement for the device work that jfabell/boltzmann's solver class binds
+ * in BoltzmannDSMC._init_kernels (boltzmann.py:758-795). Every function:
+ *   - takes plain device pointers owned by the caller (any allocator: torch, cudaMalloc);
+ *   - enqueues work on the caller's stream (``stream`` is a cudaStream_t) and does not
+ *     synchronise; particle counts live in device memory, so a whole step can be
+ *     captured in a CUDA graph;
+ *   - returns a bz_status code (0 = enqueued); conditions found on the device
+ *     (capacity exhausted, look-back timeout, NaN) are OR-ed into the caller's
+ *     ``status`` word as BZ_DEV_* bits, which the host reads when it wants to.
+ * Errors never trap or abort on the device.
+ *
+ * Particle state is structure-of-arrays (x, vx, vy, vz, w), all float32 (``_f32``
+ * entry points) or all float64 (``_f64``), with x in cm, v in m/s and w in the
+ * reference's density units. The reference keeps y, z positions that no 1D quantity
+ * reads (boltzmann.py:271); they are not stored.
+ */
+#ifndef BZ_H
+#define BZ_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* host-side return codes */
+enum bz_status {
+    BZ_OK = 0,
+    BZ_ERR_ARG = 1,       /* null pointer, bad size or mode            */
+    BZ_ERR_CUDA = 2,      /* a CUDA call failed (launch, memset)        */
+    BZ_ERR_WORKSPACE = 3, /* workspace smaller than bz_*_workspace says  */
+    BZ_ERR_UNSUPPORTED = 4
+};
+
+/* device-side status bits (OR-ed into *status) */
+#define BZ_DEV_CAPACITY 0x1u   /* output capacity exceeded; extra particles dropped */
+#define BZ_DEV_LOOKBACK 0x2u   /* a look-back wait hit its iteration limit            */
+#define BZ_DEV_NONFINITE 0x4u  /* non-finite velocity or weight produced               */
+#define BZ_DEV_BINRANGE 0x8u   /* a live particle outside every cell / energy bin        */
+
+/* reference behaviours reproduced on request (bz_params.flags) */
+#define BZ_QUIRK_SPLIT_WRAP 0x1u     /* split copies HW_ids[id % nHW] (boltzmann.py:820-822, CuPy wrap) */
+#define BZ_QUIRK_DEAD_IONFLAG 0x2u   /* an ionized particle that leaves adds 1 to ni_src[0]
+                                        (unweighted ion flag at x=1e-8, post_processing_1D.py:50-55) */
+#define BZ_QUIRK_TRIGGER_LAST 0x4u   /* resampling decided by the last bin's max test only
+                                        (boltzmann.py:913-916, 3bin :1108-1111, 5bin :1329-1334) */
+#define BZ_FIX_MERGE_ENERGY 0x8u     /* merge rescales the thermal part only: energy conserving */
+
+/* cross-section modes */
+#define BZ_XS_TABLE 0     /* n*sigma tables on a log energy grid (elastic, excitation, ionization) */
+#define BZ_XS_REF_FITS 1  /* the reference's log10-quadratic fits, evaluated in FP64
+                             (electron_kernel_numba.py:66-174) */
+/* collision models */
+#define BZ_COLL_DIRECT 0  /* P = 1-exp(-n sigma_tot v dt), process by R0 (electron_kernel_numba.py:187-198) */
+#define BZ_COLL_NULL 1    /* null collision with bound nu_max */
+
+typedef struct bz_params {
+    /* grid: N faces (E), N+1 nodes (deposit / binning cells) */
+    int32_t n_faces;
+    int32_t n_nodes;
+    int32_t bnf;        /* fine bins per node of the reference deposit (post_processing bnf) */
+    int32_t advect;     /* 1: 1D advection with absorbing walls at 0 and L; 0: 0-D swarm */
+    double L, dx;       /* cm */
+    /* physics */
+    double dt;          /* s */
+    double nn;          /* neutral density, m^-3 */
+    double gas_sigma;   /* std dev of each gas velocity component, m/s (0: off) */
+    double e_exc;       /* excitation threshold and energy loss, eV */
+    double nu_max;      /* null-collision bound, s^-1 */
+    int32_t xs_mode;    /* BZ_XS_* */
+    int32_t coll_model; /* BZ_COLL_* */
+    int32_t xs_n;       /* points of the n*sigma table */
+    int32_t flags;      /* BZ_QUIRK_* | BZ_FIX_* */
+    double xs_emin, xs_emax;  /* eV, log grid end points */
+    const float *xs_table;    /* device, [3][xs_n], n*sigma in m^-1 (elastic, excitation, ionization) */
+    /* counter-based random numbers: Philox4x32-10 keyed by seed, counter (slot, step) */
+    uint64_t seed;
+    uint64_t step;
+    const uint64_t *step_ptr; /* device; when set, the step is read from it (CUDA graph replay) */
+} bz_params;
+
+typedef struct bz_particles_f32 { float *x, *vx, *vy, *vz, *w; } bz_particles_f32;
+typedef struct bz_particles_f64 { double *x, *vx, *vy, *vz, *w; } bz_particles_f64;
+
+/* ---------------------------------------------------------------------------------- */
+/* push + collide (+ fused deposit and compaction)                                     */
+/* ---------------------------------------------------------------------------------- */
+/* Replaces electron_kernel (electron_kernel_numba.py:291-303) together with the
+ * deposit and per-step compaction of post_processing (post_processing_1D.py:40-68,
+ * reduction/__init__.py:3-11 -> kernels-new.cu calls).
+ *
+ * in[0 .. *n_in) is pushed and collided; particles that stay alive are written to
+ * out[0 .. ns) in input order, then the ionization children in parent order,
+ * out[ns .. ns+nc): the reference's order after reshuffle_data_atomics. counts[0] = ns,
+ * counts[1] = nc, counts[2] = ns+nc. Input particles with w <= 0 are dropped.
+ * moments (optional, [4][n_nodes] float64, accumulated into: zero it first) receives
+ * (sum w, sum w*ionflag, 0, sum w*energy) at node int(((x+dx/2)/(L+dx))*bnf*n_nodes)/bnf,
+ * the reference's ne, ni_src, ns_src, nrg before the division by the host.
+ * Random numbers: Philox (replay_R == NULL) or replayed, R[i][7] and gas[i][3]
+ * float64 arrays in the reference's layout (electron_kernel_numba.py:195-238, boltzmann.py:589).
+ * in and out must not overlap. A count above in_capacity is clamped to it and
+ * BZ_DEV_CAPACITY is raised; out_capacity must leave room for ns + 2*nc (children are
+ * staged at the tail before they are moved behind the survivors). */
+size_t bz_push_workspace(int64_t capacity);
+int bz_push_collide_f32(const bz_params *p, bz_particles_f32 in, const int32_t *n_in, int64_t in_capacity,
+                        bz_particles_f32 out, int64_t out_capacity, int32_t *counts,
+                        const float *E, const double *replay_R, const double *replay_gas,
+                        double *moments, void *workspace, size_t workspace_bytes,
+                        uint32_t *status, void *stream);
+int bz_push_collide_f64(const bz_params *p, bz_particles_f64 in, const int32_t *n_in, int64_t in_capacity,
+                        bz_particles_f64 out, int64_t out_capacity, int32_t *counts,
+                        const double *E, const double *replay_R, const double *replay_gas,
+                        double *moments, void *workspace, size_t workspace_bytes,
+                        uint32_t *status, void *stream);
+
+/* Deposit only: the moments post_processing forms for a state (kernels-new.cu:56-132,
+ * race-free). ionflag (optional, uint8 per particle) is the reference's tosum[:,1]. */
+int bz_deposit_f32(const bz_params *p, bz_particles_f32 s, const int32_t *n, int64_t capacity,
+                   const uint8_t *ionflag, double *moments, void *stream);
+int bz_deposit_f64(const bz_params *p, bz_particles_f64 s, const int32_t *n, int64_t capacity,
+                   const uint8_t *ionflag, double *moments, void *stream);
+
+/* ---------------------------------------------------------------------------------- */
+/* binning: cell x energy-bin key, stable counting sort                                 */
+/* ---------------------------------------------------------------------------------- */
+/* Replaces define_particle_bins (bin_particles.py:7-22; 3bin/5bin :7-49) and the table
+ * fills of _check_for_resampling (boltzmann.py:898-903). Key = cell*nbins + ebin with
+ * cell = int((x+dx/2)/dx) (boltzmann.py:658) and ebin from the energy against
+ * edges[nbins-1] (eV, ascending). Live particles only (w > 0).
+ * perm[0 .. live) lists particle indices sorted by key, ascending index within a key;
+ * offsets[k] / counts[k] give key k's slice; hw_counts[k] counts particles with
+ * w > min_wt (split candidates, boltzmann.py:809). nkeys = n_nodes*nbins <= 65535. */
+size_t bz_bin_workspace(int64_t capacity, int32_t nkeys);
+int bz_bin_f32(const bz_params *p, bz_particles_f32 s, const int32_t *n, int64_t capacity, int32_t nbins,
+               const double *edges, double min_wt, int32_t *perm, int32_t *offsets, int32_t *counts,
+               int32_t *hw_counts, void *workspace, size_t workspace_bytes, uint32_t *status, void *stream);
+int bz_bin_f64(const bz_params *p, bz_particles_f64 s, const int32_t *n, int64_t capacity, int32_t nbins,
+               const double *edges, double min_wt, int32_t *perm, int32_t *offsets, int32_t *counts,
+               int32_t *hw_counts, void *workspace, size_t workspace_bytes, uint32_t *status, void *stream);
+
+/* ---------------------------------------------------------------------------------- */
+/* ES-WPNC resampling                                                                   */
+/* ---------------------------------------------------------------------------------- */
+/* Replaces _check_for_resampling + _do_resampling (boltzmann.py:799-916; 3bin
+ * :813-1113; 5bin :843-1334): per (cell, bin), split when 0 < n < split_below*T and a
+ * particle has w > min_wt (draw 2T-n copies with probability w), merge when
+ * n >= merge_at*T (keep int(merge_keep*T) by stratified sampling, weight W/K, velocity
+ * rescale). targets[nbins], max_ppc[nbins] as the reference (T, 10T).
+ * Appended particles go to s[*n ..) in (cell, bin) order; merged originals get w = 0;
+ * then the state is compacted into ``out`` (w != 0 kept in order, boltzmann.py:879-890).
+ * Random numbers: Philox (replay_u == NULL) or replay_u[] consumed in processing order
+ * (per key: split draws or merge draws). need_out[0] = 1 when resampling ran.
+ * capacity bounds both s and out.
+ * cons_diag (optional, [nkeys][10] float64): W, px, py, pz, sum w*energy before the
+ * merge, then the same of the stored survivors. */
+size_t bz_resample_workspace(int64_t capacity, int32_t nkeys);
+int bz_resample_f32(const bz_params *p, bz_particles_f32 s, const int32_t *n, int64_t capacity,
+                    bz_particles_f32 out, int32_t *n_out, int32_t nbins, const int32_t *targets,
+                    const int32_t *max_ppc, double min_wt, double split_below, double merge_at,
+                    double merge_keep, const int32_t *perm, const int32_t *offsets, const int32_t *counts,
+                    const int32_t *hw_counts, const double *replay_u, int32_t *need_out, double *cons_diag,
+                    void *workspace, size_t workspace_bytes, uint32_t *status, void *stream);
+int bz_resample_f64(const bz_params *p, bz_particles_f64 s, const int32_t *n, int64_t capacity,
+                    bz_particles_f64 out, int32_t *n_out, int32_t nbins, const int32_t *targets,
+                    const int32_t *max_ppc, double min_wt, double split_below, double merge_at,
+                    double merge_keep, const int32_t *perm, const int32_t *offsets, const int32_t *counts,
+                    const int32_t *hw_counts, const double *replay_u, int32_t *need_out, double *cons_diag,
+                    void *workspace, size_t workspace_bytes, uint32_t *status, void *stream);
+
+/* Order-preserving compaction of w != 0 (boltzmann.py:879-883). */
+size_t bz_compact_workspace(int64_t capacity);
+int bz_compact_f32(bz_particles_f32 in, const int32_t *n, int64_t in_capacity, bz_particles_f32 out,
+                   int64_t out_capacity, int32_t *n_out, void *workspace, size_t workspace_bytes,
+                   uint32_t *status, void *stream);
+int bz_compact_f64(bz_particles_f64 in, const int32_t *n, int64_t in_capacity, bz_particles_f64 out,
+                   int64_t out_capacity, int32_t *n_out, void *workspace, size_t workspace_bytes,
+                   uint32_t *status, void *stream);
+
+/* ---------------------------------------------------------------------------------- */
+/* grid: ion fluid and Poisson (FP64, device resident)                                  */
+/* ---------------------------------------------------------------------------------- */
+/* Host-side grid update of the step loop (boltzmann.py:643-647): ni += ni_src,
+ * Te = (2/3) nrg/ne (NaN -> 0), g2 += ni_src, from moments[4][n_nodes]. */
+int bz_grid_update(int32_t n_nodes, const double *moments, double *ni, double *Te, double *g2, void *stream);
+/* heavies_kernel_fluid (heavies_kernel_1D.py:4-64), ion part; break flag -> *brk. */
+int bz_ion_fluid(int32_t N, double dx, double dt, double mu_i, double D_i, const double *E, double *ni,
+                 double *Ji, int32_t *brk, void *stream);
+/* EF_kernel (EF_kernel_1D.py:7-44) with the banded Cholesky factor of boltzmann.py:744-755
+ * (chol_diag[N-1], chol_lower[N-1] from bz_poisson_factor). t is read from *t_dev when
+ * t_dev != NULL (graph capture), else t_host. Writes V[N-1] and E (float64 [N]);
+ * E32 (optional) receives a float32 copy for the float32 push. */
+int bz_poisson_factor(int32_t N, double dx, double *chol_diag, double *chol_lower);
+int bz_poisson(int32_t N, double dx, double eps0, double V0, double freq, double t_host, const double *t_dev,
+               const double *ne, const double *ni, const double *chol_diag, const double *chol_lower,
+               double *V, double *E, float *E32, void *stream);
+/* Step clock on the device (graph-capturable): *t_dev += dt, *step_dev += 1 (either may be NULL). */
+int bz_advance_clock(double *t_dev, uint64_t *step_dev, double dt, void *stream);
+
+/* library identification */
+const char *bz_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

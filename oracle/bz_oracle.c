@@ -136,7 +136,7 @@ static void sigma_table(const orc_params *p, double e, double *ns) {
 /* ------------------------------------------------------------------------------------ */
 /* push + collide (electron_kernel_numba.py:38-287)                                      */
 /* ------------------------------------------------------------------------------------ */
-typedef struct { double x, y, z, vx, vy, vz, w, e, flag; int child; double cx, cy, cz, cvx, cvy, cvz, ce, cw; } push_out;
+typedef struct { double x, y, z, vx, vy, vz, w, e, flag; int child; double cx, cy, cz, cvx, cvy, cvz, ce, cw, margin; } push_out;
 
 static void push_one(const orc_params *p, int64_t i, const double *in_d, const double *in_t, const double *E,
                      const double *R, const double *gas, push_out *o) {
@@ -181,6 +181,8 @@ static void push_one(const orc_params *p, int64_t i, const double *in_d, const d
         double ns[3];
         sigma_table(p, e_el, ns);
         s0 = ns[0]; s1 = ns[1]; s2 = ns[2];
+        if (e_el < p->e_exc) s1 = 0.0; /* no process below its threshold */
+        if (e_el < E_ION) s2 = 0.0;
     }
     double r0, r1, r2;
     if (p->coll_model == 0) {
@@ -200,6 +202,8 @@ static void push_one(const orc_params *p, int64_t i, const double *in_d, const d
     o->child = 0;
     o->flag = 0.0;
     double u0 = Ru[0];
+    /* distance of the decision uniform to the nearest process boundary */
+    o->margin = fmin(fmin(fabs(u0 - r0), fabs(u0 - r1)), fabs(u0 - r2));
     if (u0 < r0) {
         /* elastic, electron_kernel_numba.py:197-209 */
         double cos_chi = 2 * Ru[1] - 1;
@@ -211,6 +215,7 @@ static void push_one(const orc_params *p, int64_t i, const double *in_d, const d
         vz = vn * cos(chi);
     } else if (r0 < u0 && u0 < r1) {
         /* excitation (table mode only; the reference has none): loss e_exc, isotropic */
+        if ((e_el - p->e_exc) < 0.05 * e_el) o->margin = 0.0; /* ill-conditioned in float32 */
         double cos_chi = 2 * Ru[1] - 1;
         double chi = acos(cos_chi);
         double phi = 2 * M_PI * Ru[2];
@@ -221,6 +226,7 @@ static void push_one(const orc_params *p, int64_t i, const double *in_d, const d
         vz = vn * cos(chi);
     } else if (r1 < u0 && u0 < r2) {
         /* ionization, electron_kernel_numba.py:211-255 */
+        if ((e_el - E_ION) < 0.05 * e_el) o->margin = 0.0; /* ill-conditioned in float32 */
         double cos_chi = 2 * Ru[1] - 1;
         double chi = acos(cos_chi);
         double phi = 2 * M_PI * Ru[2];
@@ -256,6 +262,7 @@ static void push_one(const orc_params *p, int64_t i, const double *in_d, const d
     }
     vx -= p->dt * (q_e / m_e) * (100 * E[idx]);
     int valid = p->advect ? ((0 < xx && xx < p->L) && d_w > 0) : (d_w > 0);
+    if (p->advect) o->margin = fmin(o->margin, fmin(fabs(xx), fabs(xx - p->L)) / p->L);
     o->w = valid * d_w;
     o->x = valid * xx + (1 - valid) * 0.00000001;
     o->y = valid * xy;
@@ -269,10 +276,16 @@ static void push_one(const orc_params *p, int64_t i, const double *in_d, const d
 
 int64_t orc_push(const orc_params *p, int64_t n, double *data, double *tosum, const double *E,
                  const double *R, const double *gas) {
+    return orc_push_margin(p, n, data, tosum, E, R, gas, NULL);
+}
+
+int64_t orc_push_margin(const orc_params *p, int64_t n, double *data, double *tosum, const double *E,
+                        const double *R, const double *gas, double *margin) {
     int64_t nni = 0;
     for (int64_t i = 0; i < n; ++i) {
         push_out o;
         push_one(p, i, data + i * 6, tosum + i * 4, E, R, gas, &o);
+        if (margin) margin[i] = o.margin;
         if (o.child) {
             int64_t wi = n + nni++;
             double *d = data + wi * 6, *t = tosum + wi * 4;
@@ -585,6 +598,8 @@ int64_t orc_step_omp(const orc_params *p, int64_t n, int64_t cap, double *data, 
     double half = 0.5 * p->dx, Lp = p->L + p->dx;
     double fM = (double)(float)M;
     int nt = nthreads > 0 ? nthreads : 1;
+    /* every particle may leave one child: the output needs 2n rows, the temporaries 2n */
+    if (n < 0 || 2 * n > cap) return -1;
     int64_t *cnt_s = (int64_t *)calloc((size_t)nt + 1, sizeof(int64_t));
     int64_t *cnt_c = (int64_t *)calloc((size_t)nt + 1, sizeof(int64_t));
     double *fine = (double *)calloc((size_t)nt * M * 4, sizeof(double));

@@ -46,6 +46,14 @@ void orc_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 int64_t orc_push(const orc_params *p, int64_t n, double *data, double *tosum, const double *E,
                  const double *R, const double *gas);
 
+/* orc_push, and margin[i] = distance of particle i's decision uniform to the nearest
+ * process boundary, or of its new position to a wall (/L), whichever is smaller: where
+ * float32 and float64 arithmetic may legitimately decide differently. It is 0 for an
+ * inelastic collision within 5% of its threshold, where e - threshold amplifies the
+ * rounding of float32 inputs beyond 1e-6 of the scattered speed. */
+int64_t orc_push_margin(const orc_params *p, int64_t n, double *data, double *tosum, const double *E,
+                        const double *R, const double *gas, double *margin);
+
 /* post_processing_1D.py:40-68 with kernels-new.cu reda/redcheck (race-free): moments
  * out[4][n_nodes] = (ne, ni_src, ns_src, nrg); compacts w>0 in place; returns Nnew. */
 int64_t orc_post(const orc_params *p, int64_t n_total, double *data, double *tosum, double *moments);
@@ -84,7 +92,7 @@ int orc_fluid(int N, double dx, double dt, double mu_i, double D_i, const double
 
 /* Full-step CPU baseline (OpenMP over particles): push (Philox, table) + deposit +
  * compaction, the reference's step order. data/tosum have capacity cap >= 2n; the
- * temporaries hold 2n rows. Returns Nnew. */
+ * temporaries hold 2n rows. Returns Nnew, or -1 (nothing written) when 2n > cap. */
 int64_t orc_step_omp(const orc_params *p, int64_t n, int64_t cap, double *data, double *tosum,
                      double *data_tmp, double *tosum_tmp, const double *E, double *moments,
                      int nthreads);

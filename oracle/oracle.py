@@ -56,6 +56,9 @@ def lib():
                                  np.ctypeslib.ndpointer(np.uint32)]
         L.orc_push.argtypes = [P, ctypes.c_int64, _f64p, _f64p, _f64p, ctypes.c_void_p, ctypes.c_void_p]
         L.orc_push.restype = ctypes.c_int64
+        L.orc_push_margin.argtypes = [P, ctypes.c_int64, _f64p, _f64p, _f64p, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_void_p]
+        L.orc_push_margin.restype = ctypes.c_int64
         L.orc_post.argtypes = [P, ctypes.c_int64, _f64p, _f64p, _f64p]
         L.orc_post.restype = ctypes.c_int64
         L.orc_deposit.argtypes = [P, ctypes.c_int64, _f64p, _f64p, _f64p]
@@ -132,6 +135,17 @@ def push(p, data, tosum, n, E, R=None, gas=None):
     E = np.ascontiguousarray(E, dtype=np.float64)
     return lib().orc_push(ctypes.byref(p), n, data, tosum, E,
                           None if Rp is None else Rp.ctypes.data, None if gp is None else gp.ctypes.data)
+
+
+def push_margin(p, data, tosum, n, E, R=None, gas=None):
+    """orc_push with per-particle decision margins. Returns (children, margin[n])."""
+    Rp = None if R is None else np.ascontiguousarray(R, dtype=np.float64)
+    gp = None if gas is None else np.ascontiguousarray(gas, dtype=np.float64)
+    E = np.ascontiguousarray(E, dtype=np.float64)
+    m = np.zeros(n)
+    nni = lib().orc_push_margin(ctypes.byref(p), n, data, tosum, E, None if Rp is None else Rp.ctypes.data,
+                                None if gp is None else gp.ctypes.data, m.ctypes.data)
+    return nni, m
 
 
 def post(p, data, tosum, n_total):

@@ -1,0 +1,74 @@
+"""CPU-side checks of the C ABI: the library loads without a GPU, exports exactly the
+symbols include/bz.h declares, the ctypes layout of bz_params matches the header, and
+argument validation rejects bad calls before anything is launched."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+from boltzmann_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    txt = open(os.path.join(ROOT, "include", "bz.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    names = re.findall(r"^[a-z_ ]*?[\w\*]+\s+\**(bz_\w+)\s*\(", txt, flags=re.M)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(_lib.LIB_PATH):
+        from boltzmann_gb300 import build
+        build.build()
+    return _lib.load()
+
+
+def test_header_and_bindings_agree():
+    assert header_functions() == _lib.exported_symbols()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r" T (bz_\w+)", out))
+    for name in header_functions():
+        assert name in exported, name
+        assert getattr(lib, name) is not None
+
+
+def test_version(lib):
+    assert b"sm_103a" in lib.bz_version()
+
+
+def test_params_layout_matches_header(lib):
+    # offsets of the C struct on LP64: 4 int32, 2 double, 5 double, 4 int32, 2 double, ptr, 2 u64, ptr
+    P = _lib.BzParams
+    assert P.L.offset == 16 and P.dt.offset == 32 and P.xs_mode.offset == 72
+    assert P.xs_emin.offset == 88 and P.xs_table.offset == 104 and P.seed.offset == 112
+    assert P.step_ptr.offset == 128 and ctypes.sizeof(P) == 136
+
+
+def test_argument_validation_without_gpu(lib):
+    p = _lib.BzParams()
+    empty = _lib.Particles()
+    # null pointers are rejected before any CUDA call
+    rc = lib.bz_push_collide_f32(ctypes.byref(p), empty, None, 10, empty, 10, None, None, None, None, None, None, 0,
+                                 None, None)
+    assert rc == _lib.BZ_ERR_ARG
+    rc = lib.bz_bin_f32(ctypes.byref(p), empty, None, 10, 1, None, 0.1, None, None, None, None, None, 0, None, None)
+    assert rc == _lib.BZ_ERR_ARG
+    assert lib.bz_poisson(2, 0.1, 1.0, 1.0, 1.0, 0.0, None, None, None, None, None, None, None, None, None) == \
+        _lib.BZ_ERR_ARG
+    assert lib.bz_push_workspace(1 << 20) >= 8 * 1024
+    assert lib.bz_bin_workspace(1 << 20, 5000) > 6 * (1 << 20)
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    monkeypatch.setattr(_lib, "_lib", None)
+    monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "libbz.so"))
+    with pytest.raises(_lib.BzLibraryError):
+        _lib.load()

@@ -1,0 +1,63 @@
+"""GPU parity of the device-resident grid step: Poisson solve (EF_kernel_1D.py) and
+ion drift-diffusion (heavies_kernel_1D.py) against the reference's own outputs."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+from boltzmann_gb300 import kernels as K  # noqa: E402
+
+G = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def test_poisson_and_fluid_match_reference():
+    g = np.load(os.path.join(G, "field.npz"))
+    N = int(g["N"])
+    dx = float(g["dx"])
+    dev = "cuda"
+    d = torch.zeros(N - 1, dtype=torch.float64, device=dev)
+    l = torch.zeros(N - 1, dtype=torch.float64, device=dev)
+    K.poisson_factor(N, dx, d, l)
+    ne = torch.as_tensor(g["ne"], device=dev)
+    ni = torch.as_tensor(g["ni"], device=dev)
+    V = torch.zeros(N - 1, dtype=torch.float64, device=dev)
+    E = torch.zeros(N, dtype=torch.float64, device=dev)
+    E32 = torch.zeros(N, dtype=torch.float32, device=dev)
+    K.EF_kernel(N, dx, float(g["eps0"]), float(g["V0"]), float(g["freq"]), float(g["t"]), ne, ni, d, l, V, E, E32)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(V.cpu().numpy(), g["V"], rtol=1e-11, atol=1e-9)
+    np.testing.assert_allclose(E.cpu().numpy(), g["E"], rtol=1e-11, atol=1e-7)
+    np.testing.assert_allclose(E32.cpu().numpy(), g["E"], rtol=1e-6, atol=1e-4)
+    Ji = torch.zeros(N, dtype=torch.float64, device=dev)
+    brk = torch.zeros(1, dtype=torch.int32, device=dev)
+    Eg = torch.as_tensor(g["E"], device=dev)
+    K.heavies_kernel_fluid(N, dx, float(g["dt"]), float(g["mu_i"]), float(g["D_i"]), Eg, ni, Ji, brk)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(ni.cpu().numpy(), g["ni_out"], rtol=1e-13)
+    np.testing.assert_allclose(Ji.cpu().numpy(), g["Ji"], rtol=1e-12, atol=1e-3)
+    assert int(brk.item()) == int(g["brk"])
+
+
+def test_grid_update_and_clock():
+    n = 33
+    mom = torch.rand(4, n, dtype=torch.float64, device="cuda")
+    mom[0, 3] = 0.0
+    mom[3, 3] = 0.0
+    ni = torch.ones(n, dtype=torch.float64, device="cuda")
+    Te = torch.zeros(n, dtype=torch.float64, device="cuda")
+    g2 = torch.zeros(n, dtype=torch.float64, device="cuda")
+    K.grid_update(n, mom, ni, Te, g2)
+    t = torch.zeros(1, dtype=torch.float64, device="cuda")
+    step = torch.zeros(1, dtype=torch.int64, device="cuda")
+    for _ in range(3):
+        K.advance_clock(t, step, 0.5)
+    torch.cuda.synchronize()
+    m = mom.cpu().numpy()
+    np.testing.assert_allclose(ni.cpu().numpy(), 1.0 + m[1])
+    te = (2.0 / 3.0) * m[3] / m[0]
+    te[3] = 0.0  # 0/0 -> nan -> 0 (np.nan_to_num, boltzmann.py:646)
+    np.testing.assert_allclose(Te.cpu().numpy(), te)
+    assert float(t.item()) == 1.5 and int(step.item()) == 3
