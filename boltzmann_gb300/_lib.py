@@ -11,13 +11,14 @@ import os
 PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libbz.so")
 
-BZ_OK, BZ_ERR_ARG, BZ_ERR_CUDA, BZ_ERR_WORKSPACE, BZ_ERR_UNSUPPORTED = 0, 1, 2, 3, 4
+BZ_OK, BZ_ERR_ARG, BZ_ERR_CUDA, BZ_ERR_WORKSPACE, BZ_ERR_UNSUPPORTED, BZ_ERR_TOO_LARGE = 0, 1, 2, 3, 4, 5
 DEV_CAPACITY, DEV_LOOKBACK, DEV_NONFINITE, DEV_BINRANGE = 0x1, 0x2, 0x4, 0x8
 QUIRK_SPLIT_WRAP, QUIRK_DEAD_IONFLAG, QUIRK_TRIGGER_LAST, FIX_MERGE_ENERGY = 0x1, 0x2, 0x4, 0x8
 XS_TABLE, XS_REF_FITS = 0, 1
 COLL_DIRECT, COLL_NULL = 0, 1
 
-_ERRNAMES = {1: "invalid argument", 2: "CUDA error", 3: "workspace too small", 4: "unsupported configuration"}
+_ERRNAMES = {1: "invalid argument", 2: "CUDA error", 3: "workspace too small", 4: "unsupported configuration",
+             5: "input larger than the entry point's fixed limit"}
 
 
 class BzLibraryError(RuntimeError):
@@ -83,6 +84,8 @@ _PROTOS = {
     "bz_poisson_factor": (ctypes.c_int, [_i32, _f64, _vp, _vp]),
     "bz_poisson": (ctypes.c_int, [_i32, _f64, _f64, _f64, _f64, _f64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "bz_advance_clock": (ctypes.c_int, [_vp, _vp, _f64, _vp]),
+    "bz_push_collide_f32_noalloc": (ctypes.c_int, [_P, Particles, _vp, _i64, Particles, _i64, _vp, _vp, _vp, _vp,
+                                                   _vp, _vp, _vp]),
 }
 
 

@@ -14,6 +14,7 @@
 // shared-memory grid and merged into the float64 moments once per CTA.
 #include <algorithm>
 #include <cstdio>
+#include <mutex>
 
 #include "bz_common.cuh"
 
@@ -596,5 +597,58 @@ int bz_push_collide_f64(const bz_params *p, bz_particles_f64 in, const int32_t *
 }
 
 const char *bz_version(void) { return "libbz 0.1 sm_103a"; }
+
+}  // extern "C"
+
+// ------------------------------------------------------------------------------------
+// Allocation-free variant of the push: the look-back scratch (a tile ticket and one
+// status word per 1024-particle tile) lives in a fixed array compiled into the library,
+// so a caller that cannot allocate device memory only passes inputs and outputs.
+// ------------------------------------------------------------------------------------
+namespace bz {
+
+static_assert(BZ_PUSH_NOALLOC_MAX_PARTICLES % PTILE == 0, "scratch holds whole tiles");
+static_assert(PushWsLayout::ticket_bytes == 256, "scratch header matches the workspace layout");
+
+// One copy per GPU that loads the library, alive until the process exits.
+static __device__ __align__(256) unsigned char g_push_noalloc_scratch[BZ_PUSH_NOALLOC_SCRATCH_BYTES];
+
+// Device address of the scratch array on the current device. The array's name in host
+// code only stands in for the symbol, so the address is asked of the runtime once per
+// device (with that device current) and remembered.
+constexpr int kMaxDevices = 64;
+static std::mutex g_noalloc_mu;
+static void *g_noalloc_ptr[kMaxDevices] = {};
+
+static int noalloc_scratch(void **out) {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return BZ_ERR_CUDA;
+    if (dev < 0 || dev >= kMaxDevices) return BZ_ERR_UNSUPPORTED;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *ptr = nullptr;
+        if (cudaGetSymbolAddress(&ptr, g_push_noalloc_scratch) != cudaSuccess || !ptr) return BZ_ERR_CUDA;
+        g_noalloc_ptr[dev] = ptr;
+    }
+    *out = g_noalloc_ptr[dev];
+    return BZ_OK;
+}
+
+}  // namespace bz
+
+extern "C" {
+
+int bz_push_collide_f32_noalloc(const bz_params *p, bz_particles_f32 in, const int32_t *n_in, int64_t in_capacity,
+                                bz_particles_f32 out, int64_t out_capacity, int32_t *counts, const float *E,
+                                const double *replay_R, const double *replay_gas, double *moments, uint32_t *status,
+                                void *stream) {
+    if (in_capacity > BZ_PUSH_NOALLOC_MAX_PARTICLES) return BZ_ERR_TOO_LARGE;
+    void *scratch = nullptr;
+    int rc = bz::noalloc_scratch(&scratch);
+    if (rc != BZ_OK) return rc;
+    // the scratch is cleared by the launch (cudaMemsetAsync on the caller's stream)
+    return bz::push_entry<float>(p, in, n_in, in_capacity, out, out_capacity, counts, E, replay_R, replay_gas,
+                                 moments, scratch, BZ_PUSH_NOALLOC_SCRATCH_BYTES, status, stream);
+}
 
 }  // extern "C"

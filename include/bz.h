@@ -31,7 +31,8 @@ enum bz_status {
     BZ_ERR_ARG = 1,       /* null pointer, bad size or mode            */
     BZ_ERR_CUDA = 2,      /* a CUDA call failed (launch, memset)        */
     BZ_ERR_WORKSPACE = 3, /* workspace smaller than bz_*_workspace says  */
-    BZ_ERR_UNSUPPORTED = 4
+    BZ_ERR_UNSUPPORTED = 4,
+    BZ_ERR_TOO_LARGE = 5  /* input larger than a fixed-size entry point supports */
 };
 
 /* device-side status bits (OR-ed into *status) */
@@ -197,6 +198,32 @@ int bz_poisson(int32_t N, double dx, double eps0, double V0, double freq, double
                double *V, double *E, float *E32, void *stream);
 /* Step clock on the device (graph-capturable): *t_dev += dt, *step_dev += 1 (either may be NULL). */
 int bz_advance_clock(double *t_dev, uint64_t *step_dev, double dt, void *stream);
+
+/* ---------------------------------------------------------------------------------- */
+/* allocation-free push                                                                 */
+/* ---------------------------------------------------------------------------------- */
+/* No counterpart in the reference. The same fused push + collide + deposit + compaction
+ * as bz_push_collide_f32, for callers that cannot allocate device memory: code running
+ * inside a host process whose allocator it does not own (a plugin loaded into another
+ * solver, or a tool that must not grow the pool of a framework sharing the GPU) and
+ * code that must not call cudaMalloc at all. Instead of a caller workspace it uses one
+ * scratch array compiled into the library (BZ_PUSH_NOALLOC_SCRATCH_BYTES, 512 KiB plus
+ * a 256-byte header), which the CUDA runtime places on every GPU that loads the library
+ * and keeps until the process exits. Limits and behaviour:
+ *   - in_capacity may not exceed BZ_PUSH_NOALLOC_MAX_PARTICLES (64 Mi particles);
+ *     larger inputs return BZ_ERR_TOO_LARGE and nothing is launched;
+ *   - the first call on a device looks up the array's device address (with that device
+ *     current); make that first call before capturing any stream;
+ *   - every call on a device shares the one array and clears it first, so calls that
+ *     overlap on the GPU (two streams, or two threads) race: serialise them;
+ *   - nothing is allocated: no cudaMalloc, no cudaFree, no allocating library call. */
+#define BZ_PUSH_NOALLOC_MAX_PARTICLES (64ll * 1024 * 1024)
+#define BZ_PUSH_NOALLOC_SCRATCH_BYTES (256 + 8 * (BZ_PUSH_NOALLOC_MAX_PARTICLES / 1024))
+int bz_push_collide_f32_noalloc(const bz_params *p, bz_particles_f32 in, const int32_t *n_in,
+                                int64_t in_capacity, bz_particles_f32 out, int64_t out_capacity,
+                                int32_t *counts, const float *E, const double *replay_R,
+                                const double *replay_gas, double *moments, uint32_t *status,
+                                void *stream);
 
 /* library identification */
 const char *bz_version(void);
