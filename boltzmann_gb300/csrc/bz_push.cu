@@ -92,11 +92,14 @@ __device__ __forceinline__ void iso_dir(Uni<T> a, Uni<T> b, T vn, T &vx, T &vy, 
     T cc = a.u - a.c;
     T sc = T(2) * sqrt(a.u * a.c);
     T sp, cp;
-    sincospi_t(T(2) * b.u, &sp, &cp);
+    sincos2pi(b.u, &sp, &cp);
     vx = vn * sc * cp;
     vy = vn * sc * sp;
     vz = vn * cc;
 }
+
+__device__ __forceinline__ float fdiv_fast(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double fdiv_fast(double a, double b) { return a / b; }
 
 template <typename T> __device__ __forceinline__ Uni<T> uni_from_replay(double r) {
     return {T(r), T(1.0 - r)};
@@ -176,7 +179,7 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
         vmag = T(vm);
     } else {
         // n*sigma table, linear in log2(e) on the log grid
-        float lt = fmaf(log2f(float(e)), k.xs_inv_d, -k.xs_off);
+        float lt = fmaf(__log2f(float(e)), k.xs_inv_d, -k.xs_off);
         lt = fminf(fmaxf(lt, 0.0f), float(p.xs_n - 1));
         int i = min(int(lt), p.xs_n - 2);
         float f = lt - float(i);
@@ -190,7 +193,7 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
         if (p.coll_model == BZ_COLL_DIRECT) {
             T st = s0 + s1 + s2;
             T P = -expm1(-T(p.dt) * vmag * st);
-            T pc = P / st;
+            T pc = fdiv_fast(P, st);
             r0 = s0 * pc;
             r1 = r0 + s1 * pc;
             r2 = r1 + s2 * pc;
@@ -209,16 +212,23 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
         // |v| (1 - 2 m_e/m_n)^1/2, isotropic (electron_kernel_numba.py:197-209)
         iso_dir(u1, u2, vmag * k.f_el, nvx, nvy, nvz);
     } else if (proc != P_NONE) {
-        // energy bookkeeping in float64: e - threshold cancels near threshold
-        double ed = k.efac_d * (double(ax) * double(ax) + double(ay) * double(ay) + double(az) * double(az));
+        // energy left after the threshold: in the working precision when e - threshold
+        // keeps at least a quarter of e, else in float64 (the subtraction cancels)
+        const double thr = (proc == P_EXCITE) ? p.e_exc : E_ION;
+        T vn;
+        if (sizeof(T) == 8 || e - T(thr) >= T(0.25) * e) {
+            T en = (proc == P_EXCITE) ? (e - T(thr)) : T(0.5) * (e - T(thr));
+            vn = sqrt(en * k.e2v);
+        } else {
+            double ed = k.efac_d * (double(ax) * double(ax) + double(ay) * double(ay) + double(az) * double(az));
+            double en = (proc == P_EXCITE) ? fabs(ed - thr) : fabs(0.5 * (ed - thr));
+            vn = T(sqrt(en * k.e2v_d));
+        }
         if (proc == P_EXCITE) {
             // lose e_exc, isotropic (the reference has no excitation: sigma_g1 = 0)
-            T vn = T(sqrt(fabs(ed - p.e_exc) * k.e2v_d));
             iso_dir(u1, u2, vn, nvx, nvy, nvz);
         } else {
             // ionization, equal sharing of e - 15.76 (electron_kernel_numba.py:211-255)
-            double e_ej = fabs(0.5 * (ed - E_ION));
-            T vn = T(sqrt(2 * e_ej / (j_ev() * m_e())));
             iso_dir(u1, u2, vn, nvx, nvy, nvz);
             Uni<T> u5;
             if (REPLAY) {
@@ -260,7 +270,10 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
 template <typename T> struct AccT { using t = T; };
 
 template <typename T, bool REPLAY, int XS, bool DEPOSIT>
-__global__ void __launch_bounds__(PT) k_push(bz_params p, PushConst<T> kc, SoA<T> in, const int32_t *n_in,
+#ifndef BZ_PUSH_MINB
+#define BZ_PUSH_MINB 3
+#endif
+__global__ void __launch_bounds__(PT, BZ_PUSH_MINB) k_push(bz_params p, PushConst<T> kc, SoA<T> in, const int32_t *n_in,
                                              int64_t in_cap, SoA<T> out, int64_t cap, int32_t *counts, const T *E,
                                              const double *R, const double *gas, double *moments,
                                              unsigned int *ticket, uint64_t *tile_status, int max_tiles,
@@ -511,6 +524,8 @@ static int launch_push_t(const bz_params &p, SoA<T> in, const int32_t *n_in, int
         if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess)
             return BZ_ERR_UNSUPPORTED;
     }
+    // prefer shared memory over L1 so that shared memory never limits the resident CTAs
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PT, smem) != cudaSuccess || per_sm < 1)
         return BZ_ERR_UNSUPPORTED;
