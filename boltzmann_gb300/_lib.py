@@ -50,6 +50,15 @@ class Particles(ctypes.Structure):
                 ("vz", ctypes.c_void_p), ("w", ctypes.c_void_p)]
 
 
+class Segments(ctypes.Structure):
+    """bz_segments_f32 / bz_segments_f64: five device pointers, counts, nseg, half."""
+    _fields_ = [("x", ctypes.c_void_p), ("vx", ctypes.c_void_p), ("vy", ctypes.c_void_p),
+                ("vz", ctypes.c_void_p), ("w", ctypes.c_void_p), ("counts", ctypes.c_void_p),
+                ("nseg", ctypes.c_int32), ("half", ctypes.c_int32)]
+
+
+SEG_NEEDS_REPACK = 0x1
+
 _lib = None
 
 _vp = ctypes.c_void_p
@@ -84,6 +93,24 @@ _PROTOS = {
     "bz_poisson_factor": (ctypes.c_int, [_i32, _f64, _vp, _vp]),
     "bz_poisson": (ctypes.c_int, [_i32, _f64, _f64, _f64, _f64, _f64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "bz_advance_clock": (ctypes.c_int, [_vp, _vp, _f64, _vp]),
+    "bz_seg_push_workspace": (_sz, []),
+    "bz_seg_push_collide_f32": (ctypes.c_int, [_P, Segments, Segments, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp, _vp]),
+    "bz_seg_push_collide_f64": (ctypes.c_int, [_P, Segments, Segments, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp, _vp]),
+    "bz_seg_repack_workspace": (_sz, [_i32]),
+    "bz_seg_repack_f32": (ctypes.c_int, [ctypes.POINTER(Segments), Particles, _vp, _i64, Segments, _vp, _sz, _vp,
+                                         _vp, _vp, _vp]),
+    "bz_seg_repack_f64": (ctypes.c_int, [ctypes.POINTER(Segments), Particles, _vp, _i64, Segments, _vp, _sz, _vp,
+                                         _vp, _vp, _vp]),
+    "bz_seg_deposit_f32": (ctypes.c_int, [_P, Segments, _vp, _vp]),
+    "bz_seg_deposit_f64": (ctypes.c_int, [_P, Segments, _vp, _vp]),
+    "bz_seg_bin_workspace": (_sz, [_i32, _i64]),
+    "bz_seg_bin_f32": (ctypes.c_int, [_P, Segments, _i32, _vp, _f64, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp]),
+    "bz_seg_bin_f64": (ctypes.c_int, [_P, Segments, _i32, _vp, _f64, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp]),
+    "bz_seg_resample_workspace": (_sz, [_i32, _i64, _i32]),
+    "bz_seg_resample_f32": (ctypes.c_int, [_P, Segments, Particles, _i64, Segments, _i32, _vp, _vp, _f64, _f64, _f64,
+                                           _f64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp, _vp]),
+    "bz_seg_resample_f64": (ctypes.c_int, [_P, Segments, Particles, _i64, Segments, _i32, _vp, _vp, _f64, _f64, _f64,
+                                           _f64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp, _vp]),
     "bz_push_collide_f32_noalloc": (ctypes.c_int, [_P, Particles, _vp, _i64, Particles, _i64, _vp, _vp, _vp, _vp,
                                                    _vp, _vp, _vp]),
 }

@@ -282,6 +282,140 @@ static int bin_entry(const bz_params *pp, P s, const int32_t *n, int64_t cap, in
     return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
 }
 
+// ------------------------------------------------------------------------------------
+// segmented state: keys are written densely (segment order, run 0 then run 1) together
+// with each particle's slot, and the same radix passes sort the slots.
+// ------------------------------------------------------------------------------------
+__global__ void k_seg_totals(const int32_t *cnt, int nseg, int half, int32_t *tot) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nseg; s += gridDim.x * blockDim.x)
+        tot[s] = min(max(cnt[2 * s], 0), half) + min(max(cnt[2 * s + 1], 0), half);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_seg_bin_keys(bz_params p, const T *x, const T *vx, const T *vy, const T *vz,
+                                                      const T *w, const int32_t *cnt, int nseg, int half,
+                                                      const int32_t *pre, int nb, const double *edges, double min_wt,
+                                                      uint16_t *keys, uint32_t *slots, int32_t *counts,
+                                                      int32_t *hw_counts, int nkeys, uint32_t *status) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint32_t *c_s = reinterpret_cast<uint32_t *>(smem);
+    uint32_t *h_s = c_s + nkeys;
+    __shared__ double edges_s[16];
+    for (int i = threadIdx.x; i < 2 * nkeys; i += blockDim.x) c_s[i] = 0;
+    if (threadIdx.x < 16) edges_s[threadIdx.x] = threadIdx.x < nb - 1 ? edges[threadIdx.x] : 0.0;
+    __syncthreads();
+    const float inv_dx_f = float(1.0 / p.dx);
+    const float efac_f = float(0.5 * m_e() * j_ev());
+    const double efac_d = 0.5 * m_e() * j_ev();
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    uint32_t err = 0;
+    for (int seg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; seg < nseg; seg += warps) {
+        int64_t v0 = pre[seg];
+        for (int run = 0; run < 2; ++run) {
+            const int c = min(max(cnt[2 * seg + run], 0), half);
+            const int64_t b = int64_t(seg) * 2 * half + int64_t(run) * half;
+            for (int j = lane; j < c; j += 32) {
+                const int64_t i = b + j;
+                const T wi = w[i];
+                int key = nkeys;
+                if (wi > T(0)) {
+                    int cell = p.advect ? cell_index(x[i], p.dx, inv_dx_f) : 0;
+                    int e = energy_bin(vx[i], vy[i], vz[i], wi, nb, edges_s, efac_f, efac_d);
+                    if (cell >= 0 && cell < p.n_nodes && e >= 0) {
+                        key = cell * nb + e;
+                        atomicAdd(&c_s[key], 1u);
+                        if (double(wi) > min_wt) atomicAdd(&h_s[key], 1u);
+                    } else {
+                        err |= BZ_DEV_BINRANGE;
+                    }
+                }
+                keys[v0 + j] = uint16_t(key);
+                slots[v0 + j] = uint32_t(i);
+            }
+            v0 += c;
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < nkeys; k += blockDim.x) {
+        if (c_s[k]) atomicAdd(reinterpret_cast<unsigned int *>(&counts[k]), c_s[k]);
+        if (h_s[k]) atomicAdd(reinterpret_cast<unsigned int *>(&hw_counts[k]), h_s[k]);
+    }
+    if (err) atomicOr(status, err);
+}
+
+struct SegBinWs {
+    size_t keys_a, keys_b, vals_a, slots, hist, tot, pre, total;
+    SegBinWs(int nseg, int64_t cap) {
+        auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+        size_t c = size_t(std::max<int64_t>(cap, 1));
+        size_t nt = size_t(ceil_div(int64_t(c), RB_TILE));
+        keys_a = 0;
+        keys_b = keys_a + al(2 * c);
+        vals_a = keys_b + al(2 * c);
+        slots = vals_a + al(4 * c);
+        hist = slots + al(4 * c);
+        tot = hist + al(nt * RADIX * 4);
+        pre = tot + al(4 * size_t(nseg));
+        total = pre + al(4 * (size_t(nseg) + 1));
+    }
+};
+
+template <typename T, typename S>
+static int seg_bin_entry(const bz_params *pp, S s, int nb, const double *edges, double min_wt, int32_t *perm,
+                         int32_t *offsets, int32_t *counts, int32_t *hw_counts, void *ws, size_t ws_bytes,
+                         uint32_t *status, void *stream) {
+    if (!pp || !perm || !offsets || !counts || !hw_counts || !ws || !status) return BZ_ERR_ARG;
+    if (!s.x || !s.vx || !s.vy || !s.vz || !s.w || !s.counts || s.nseg <= 0 || s.half <= 0) return BZ_ERR_ARG;
+    const bz_params &p = *pp;
+    if (nb < 1 || nb > 16 || (nb > 1 && !edges) || p.n_nodes < 1 || (p.advect && p.dx <= 0)) return BZ_ERR_ARG;
+    const int nkeys = p.n_nodes * nb;
+    if (nkeys >= 65535) return BZ_ERR_UNSUPPORTED;
+    const int64_t cap = int64_t(s.nseg) * 2 * s.half;
+    if (cap > int64_t(UINT32_MAX)) return BZ_ERR_UNSUPPORTED;
+    SegBinWs L(s.nseg, cap);
+    if (ws_bytes < L.total) return BZ_ERR_WORKSPACE;
+    unsigned char *b = static_cast<unsigned char *>(ws);
+    uint16_t *keys_a = reinterpret_cast<uint16_t *>(b + L.keys_a);
+    uint16_t *keys_b = reinterpret_cast<uint16_t *>(b + L.keys_b);
+    uint32_t *vals_a = reinterpret_cast<uint32_t *>(b + L.vals_a);
+    uint32_t *slots = reinterpret_cast<uint32_t *>(b + L.slots);
+    uint32_t *hist = reinterpret_cast<uint32_t *>(b + L.hist);
+    int32_t *tot = reinterpret_cast<int32_t *>(b + L.tot);
+    int32_t *pre = reinterpret_cast<int32_t *>(b + L.pre);
+    cudaStream_t st = as_stream(stream);
+    if (cudaMemsetAsync(counts, 0, sizeof(int32_t) * nkeys, st) != cudaSuccess) return BZ_ERR_CUDA;
+    if (cudaMemsetAsync(hw_counts, 0, sizeof(int32_t) * nkeys, st) != cudaSuccess) return BZ_ERR_CUDA;
+    k_seg_totals<<<int(std::min<int64_t>(ceil_div(s.nseg, 256), 4096)), 256, 0, st>>>(s.counts, s.nseg, s.half, tot);
+    k_key_offsets<<<1, 1024, 0, st>>>(tot, s.nseg, pre);
+    const int32_t *n = pre + s.nseg;  // live total on the device
+    size_t smem = sizeof(uint32_t) * 2 * size_t(nkeys);
+    auto kk = k_seg_bin_keys<T>;
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(kk, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess)
+        return BZ_ERR_UNSUPPORTED;
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int kb = std::max(1, std::min(sms * 4, int(ceil_div(s.nseg, 8))));
+    kk<<<kb, 256, smem, st>>>(p, s.x, s.vx, s.vy, s.vz, s.w, s.counts, s.nseg, s.half, pre, nb, edges, min_wt, keys_a,
+                              slots, counts, hw_counts, nkeys, status);
+    const int grid = int(ceil_div(cap, RB_TILE));
+    const bool two = nkeys >= RADIX;
+    k_radix_hist<<<grid, RB_T, 0, st>>>(keys_a, n, cap, 0, hist);
+    k_radix_scan<<<1, 1024, 0, st>>>(hist, n, cap);
+    k_radix_scatter<<<grid, RB_T, 0, st>>>(keys_a, slots, n, cap, 0, hist, keys_b,
+                                           two ? vals_a : reinterpret_cast<uint32_t *>(perm));
+    if (two) {
+        k_radix_hist<<<grid, RB_T, 0, st>>>(keys_b, n, cap, 8, hist);
+        k_radix_scan<<<1, 1024, 0, st>>>(hist, n, cap);
+        k_radix_scatter<<<grid, RB_T, 0, st>>>(keys_b, vals_a, n, cap, 8, hist, keys_a,
+                                               reinterpret_cast<uint32_t *>(perm));
+    }
+    k_key_offsets<<<1, 1024, 0, st>>>(counts, nkeys, offsets);
+    return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+}
+
 }  // namespace bz
 
 extern "C" {
@@ -294,6 +428,19 @@ int bz_bin_f32(const bz_params *p, bz_particles_f32 s, const int32_t *n, int64_t
                int32_t *hw_counts, void *workspace, size_t workspace_bytes, uint32_t *status, void *stream) {
     return bz::bin_entry<float>(p, s, n, capacity, nbins, edges, min_wt, perm, offsets, counts, hw_counts, workspace,
                                 workspace_bytes, status, stream);
+}
+size_t bz_seg_bin_workspace(int32_t nseg, int64_t capacity) { return bz::SegBinWs(nseg, capacity).total; }
+int bz_seg_bin_f32(const bz_params *p, bz_segments_f32 s, int32_t nbins, const double *edges, double min_wt,
+                   int32_t *perm, int32_t *offsets, int32_t *counts, int32_t *hw_counts, void *workspace,
+                   size_t workspace_bytes, uint32_t *status, void *stream) {
+    return bz::seg_bin_entry<float>(p, s, nbins, edges, min_wt, perm, offsets, counts, hw_counts, workspace,
+                                    workspace_bytes, status, stream);
+}
+int bz_seg_bin_f64(const bz_params *p, bz_segments_f64 s, int32_t nbins, const double *edges, double min_wt,
+                   int32_t *perm, int32_t *offsets, int32_t *counts, int32_t *hw_counts, void *workspace,
+                   size_t workspace_bytes, uint32_t *status, void *stream) {
+    return bz::seg_bin_entry<double>(p, s, nbins, edges, min_wt, perm, offsets, counts, hw_counts, workspace,
+                                     workspace_bytes, status, stream);
 }
 int bz_bin_f64(const bz_params *p, bz_particles_f64 s, const int32_t *n, int64_t capacity, int32_t nbins,
                const double *edges, double min_wt, int32_t *perm, int32_t *offsets, int32_t *counts,

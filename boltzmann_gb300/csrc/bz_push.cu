@@ -16,258 +16,10 @@
 #include <cstdio>
 #include <mutex>
 
-#include "bz_common.cuh"
+#include "bz_push_core.cuh"
 
 namespace bz {
 
-constexpr int PT = 256;            // threads per CTA
-constexpr int PI = 4;              // consecutive particles per thread per tile
-constexpr int PTILE = PT * PI;     // particles per tile
-constexpr int PWARPS = PT / 32;
-
-template <typename T> struct SoA { T *x, *vx, *vy, *vz, *w; };
-
-// The reference's cross-section fits (electron_kernel_numba.py:66-174), float64.
-__constant__ double c_el_a[12] = {-0.02704763, -0.08847237, -0.37608274, -1.4874467, -0.9870356, 14.28063581,
-                                  -2.12069169, -0.3585636, 1.25262128, -2.28332905, -1.47508661, -0.11090525};
-__constant__ double c_el_b[12] = {-0.23720051, -0.6084786, -1.8167778, -4.82420619, -4.2206026, 18.92275458,
-                                  0.7555105, 0.79246666, -0.40002029, 4.89566076, 2.82263476, -0.77506081};
-__constant__ double c_el_c[12] = {-19.67900951, -20.24111992, -21.51414308, -23.55745478, -23.44715988,
-                                  -14.70556113, -19.71943671, -19.71260274, -19.48909003, -21.46789173,
-                                  -20.1928456, -17.81752307};
-__constant__ double c_el_e[11] = {0.000780396, 0.006098667, 0.0476269, 0.1015574, 0.1943527, 0.2995781,
-                                  1.097156, 2.339524, 4.988691, 10.63765, 22.68322};
-__constant__ double c_io_a[8] = {-2149239.99337822, -227229.83440255, -20173.68563579, -1838.90888364,
-                                 -186.98923927, -24.48843901, -4.33101714, -0.68345667};
-__constant__ double c_io_b[8] = {5150451.29014456, 545171.14839945, 48599.13254342, 4491.58838596,
-                                 477.04784782, 69.43965607, 14.47124519, 2.6053539};
-__constant__ double c_io_c[8] = {-3085665.64874862, -327016.69508374, -29290.96100603, -2763.82866252,
-                                 -324.75732578, -69.145292411, -31.66224458, -21.99823511};
-__constant__ double c_io_e[7] = {15.77742, 15.81964, 15.96196, 16.44162, 18.05837, 23.50771, 41.87498};
-
-__device__ inline void sigma_fits(double e, double &s_el, double &s_ion) {
-    double le = log10(e);
-    int k = 0;
-    while (k < 11 && !(e < c_el_e[k])) ++k;
-    s_el = pow(10.0, (c_el_a[k] * le + c_el_b[k]) * le + c_el_c[k]);
-    double lg = 0.0;  // at e == 15.76 no piece matches and the reference's sum is 0
-    if (E_ION < e && e < c_io_e[0]) {
-        lg = (c_io_a[0] * le + c_io_b[0]) * le + c_io_c[0];
-    } else {
-        for (int j = 1; j < 8; ++j) {
-            bool hi_ok = (j == 7) || (e < c_io_e[j]);
-            if (c_io_e[j - 1] <= e && hi_ok) { lg = (c_io_a[j] * le + c_io_b[j]) * le + c_io_c[j]; break; }
-        }
-    }
-    double s2 = pow(10.0, lg);
-    s_ion = (e < E_ION) ? 0.0 : s2;
-}
-
-// Per-launch constants derived on the host.
-template <typename T> struct PushConst {
-    T efac;         // 0.5 m_e j_ev: |v|^2 (m^2/s^2) -> eV
-    T c100dt;       // 100 dt: m/s -> cm per step
-    T kick;         // dt (q/m) 100: V/cm -> m/s per step
-    T f_el;         // sqrt(1 - 2 m_e/m_n)
-    T e2v;          // 2/(j_ev m_e): eV -> (m/s)^2
-    T gas_sigma;
-    T L;
-    float inv_dx_f;
-    float xs_inv_d, xs_off;  // t = log2(e)*xs_inv_d - xs_off
-    double efac_d, e2v_d, c100dt_d;
-    T p_null;       // 1 - exp(-dt nu_max) (null collision)
-    T inv_nu_max;
-};
-
-template <typename T> struct Item {
-    T x, vx, vy, vz;      // state after the step (w unchanged)
-    T cx, cvx, cvy, cvz;  // child
-    T e, ce;              // energies (eV) after the step, for the deposit
-    bool alive, child, ionized;
-};
-
-template <typename T>
-__device__ __forceinline__ void iso_dir(Uni<T> a, Uni<T> b, T vn, T &vx, T &vy, T &vz) {
-    // cos(chi) = 2a-1, sin(chi) = 2 sqrt(a(1-a)), phi = 2 pi b (electron_kernel_numba.py:202-209)
-    T cc = a.u - a.c;
-    T sc = T(2) * sqrt(a.u * a.c);
-    T sp, cp;
-    sincos2pi(b.u, &sp, &cp);
-    vx = vn * sc * cp;
-    vy = vn * sc * sp;
-    vz = vn * cc;
-}
-
-__device__ __forceinline__ float fdiv_fast(float a, float b) { return __fdividef(a, b); }
-__device__ __forceinline__ double fdiv_fast(double a, double b) { return a / b; }
-
-template <typename T> __device__ __forceinline__ Uni<T> uni_from_replay(double r) {
-    return {T(r), T(1.0 - r)};
-}
-
-enum { P_NONE = 0, P_ELASTIC = 1, P_EXCITE = 2, P_IONIZE = 3 };
-
-// The reference's test (electron_kernel_numba.py:195-212): elastic if u < r0, then the
-// next process if r0 < u < r1, and so on; strict inequalities as in the reference.
-template <typename U> __device__ __forceinline__ int choose(U u, U r0, U r1, U r2) {
-    if (u < r0) return P_ELASTIC;
-    if (r0 < u && u < r1) return P_EXCITE;
-    if (r1 < u && u < r2) return P_IONIZE;
-    return P_NONE;
-}
-
-template <typename T, bool REPLAY, int XS>
-__device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T> &k, const Rng &rng, uint32_t slot, T x, T vx, T vy,
-                                          T vz, const T *E_s, const float4 *xs_s, const double *R,
-                                          const double *gas, Item<T> &o) {
-    // gas velocity (boltzmann.py:589, electron_kernel_numba.py:51-53) and uniforms
-    T g0 = 0, g1 = 0, g2 = 0;
-    Uni<T> u0, u1, u2, u3;
-    double r0_replay = 0.0;
-    if (REPLAY) {
-        g0 = T(gas[size_t(slot) * 3 + 0]);
-        g1 = T(gas[size_t(slot) * 3 + 1]);
-        g2 = T(gas[size_t(slot) * 3 + 2]);
-        r0_replay = R[size_t(slot) * 7 + 0];
-        u0 = uni_from_replay<T>(r0_replay);
-        u1 = uni_from_replay<T>(R[size_t(slot) * 7 + 1]);
-        u2 = uni_from_replay<T>(R[size_t(slot) * 7 + 2]);
-        u3 = uni_from_replay<T>(R[size_t(slot) * 7 + 3]);
-    } else {
-        if (k.gas_sigma > T(0)) {
-            Draw4<T> d;
-            draw4(rng, slot, 0u, d);
-            T h;
-            box_muller(d.v[0].u, d.v[1].u, g0, g1);
-            box_muller(d.v[2].u, d.v[3].u, g2, h);
-            g0 *= k.gas_sigma; g1 *= k.gas_sigma; g2 *= k.gas_sigma;
-        }
-        Draw4<T> d;
-        draw4(rng, slot, 1u, d);
-        u0 = d.v[0]; u1 = d.v[1]; u2 = d.v[2]; u3 = d.v[3];
-        r0_replay = double(u0.u);
-    }
-    // energy of the gas-relative velocity (electron_kernel_numba.py:55-63)
-    T ax = vx - g0, ay = vy - g1, az = vz - g2;
-    T v2 = ax * ax + ay * ay + az * az;
-    T vmag = sqrt(v2);
-    T e = k.efac * v2;
-    int proc;
-    if (XS == BZ_XS_REF_FITS) {
-        // the reference's fits and collision test, in float64 (electron_kernel_numba.py:64-198)
-        double ad = double(ax), bd = double(ay), cd = double(az);
-        double v2d = ad * ad + bd * bd + cd * cd;
-        double vm = sqrt(v2d);
-        double ed = k.efac_d * v2d;
-        double s0, s2;
-        sigma_fits(ed, s0, s2);
-        s0 *= p.nn;
-        s2 *= p.nn;
-        double q0, q2;
-        if (p.coll_model == BZ_COLL_DIRECT) {
-            double st = s0 + s2;
-            double P = 1.0 - exp(-p.dt * vm * st);
-            double pc = P * (1.0 / st);
-            q0 = s0 * pc;
-            q2 = q0 + s2 * pc;
-        } else {
-            double c = (1.0 - exp(-p.dt * p.nu_max)) * vm / p.nu_max;
-            q0 = s0 * c;
-            q2 = q0 + s2 * c;
-        }
-        proc = choose<double>(r0_replay, q0, q0, q2);
-        vmag = T(vm);
-    } else {
-        // n*sigma table, linear in log2(e) on the log grid
-        float lt = fmaf(__log2f(float(e)), k.xs_inv_d, -k.xs_off);
-        lt = fminf(fmaxf(lt, 0.0f), float(p.xs_n - 1));
-        int i = min(int(lt), p.xs_n - 2);
-        float f = lt - float(i);
-        float4 a = xs_s[i], b = xs_s[i + 1];
-        T s0 = T(fmaf(f, b.x - a.x, a.x));
-        T s1 = T(fmaf(f, b.y - a.y, a.y));
-        T s2 = T(fmaf(f, b.z - a.z, a.z));
-        if (e < T(p.e_exc)) s1 = T(0);
-        if (e < T(E_ION)) s2 = T(0);
-        T r0, r1, r2;
-        if (p.coll_model == BZ_COLL_DIRECT) {
-            T st = s0 + s1 + s2;
-            T P = -expm1(-T(p.dt) * vmag * st);
-            T pc = fdiv_fast(P, st);
-            r0 = s0 * pc;
-            r1 = r0 + s1 * pc;
-            r2 = r1 + s2 * pc;
-        } else {
-            T c = k.p_null * vmag * k.inv_nu_max;
-            r0 = s0 * c;
-            r1 = r0 + s1 * c;
-            r2 = r1 + s2 * c;
-        }
-        proc = choose<T>(u0.u, r0, r1, r2);
-    }
-    o.child = false;
-    o.ionized = false;
-    T nvx = vx, nvy = vy, nvz = vz;
-    if (proc == P_ELASTIC) {
-        // |v| (1 - 2 m_e/m_n)^1/2, isotropic (electron_kernel_numba.py:197-209)
-        iso_dir(u1, u2, vmag * k.f_el, nvx, nvy, nvz);
-    } else if (proc != P_NONE) {
-        // energy left after the threshold: in the working precision when e - threshold
-        // keeps at least a quarter of e, else in float64 (the subtraction cancels)
-        const double thr = (proc == P_EXCITE) ? p.e_exc : E_ION;
-        T vn;
-        if (sizeof(T) == 8 || e - T(thr) >= T(0.25) * e) {
-            T en = (proc == P_EXCITE) ? (e - T(thr)) : T(0.5) * (e - T(thr));
-            vn = sqrt(en * k.e2v);
-        } else {
-            double ed = k.efac_d * (double(ax) * double(ax) + double(ay) * double(ay) + double(az) * double(az));
-            double en = (proc == P_EXCITE) ? fabs(ed - thr) : fabs(0.5 * (ed - thr));
-            vn = T(sqrt(en * k.e2v_d));
-        }
-        if (proc == P_EXCITE) {
-            // lose e_exc, isotropic (the reference has no excitation: sigma_g1 = 0)
-            iso_dir(u1, u2, vn, nvx, nvy, nvz);
-        } else {
-            // ionization, equal sharing of e - 15.76 (electron_kernel_numba.py:211-255)
-            iso_dir(u1, u2, vn, nvx, nvy, nvz);
-            Uni<T> u5;
-            if (REPLAY) {
-                u5 = uni_from_replay<T>(R[size_t(slot) * 7 + 5]);
-            } else {
-                Draw4<T> d;
-                draw4(rng, slot, 2u, d);
-                u5 = d.v[0];
-            }
-            iso_dir(u3, u5, vn, o.cvx, o.cvy, o.cvz);
-            o.cx = x;
-            o.child = true;
-            o.ionized = true;
-            o.ce = k.efac * (o.cvx * o.cvx + o.cvy * o.cvy + o.cvz * o.cvz);
-        }
-    }
-    // drift with the post-collision velocity, kick with E at the pre-push face,
-    // absorbing walls (electron_kernel_numba.py:257-276)
-    T xn = x;
-    int face = 0;
-    bool valid = true;
-    if (p.advect) {
-        xn = x + k.c100dt * nvx;
-        face = face_index(x, p.dx, k.inv_dx_f);
-        face = min(max(face, 0), p.n_faces - 1);
-        if (xn < k.L * T(1e-3) || xn > k.L * T(1 - 1e-3)) {
-            // near a wall: decide in float64 like the reference
-            double xd = double(x) + k.c100dt_d * double(nvx);
-            valid = (0.0 < xd) && (xd < p.L);
-            xn = T(xd);
-        }
-    }
-    nvx -= k.kick * E_s[face];
-    o.alive = valid;
-    o.x = xn; o.vx = nvx; o.vy = nvy; o.vz = nvz;
-    o.e = k.efac * (nvx * nvx + nvy * nvy + nvz * nvz);
-}
-
-template <typename T> struct AccT { using t = T; };
 
 template <typename T, bool REPLAY, int XS, bool DEPOSIT>
 #ifndef BZ_PUSH_MINB
@@ -466,44 +218,6 @@ __global__ void k_append_children(SoA<T> out, int64_t cap, int32_t *counts, uint
 // --------------------------------------------------------------------------------------
 // host side
 // --------------------------------------------------------------------------------------
-static int g_num_sms = 0;
-static int num_sms() {
-    if (g_num_sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
-        if (g_num_sms <= 0) g_num_sms = 1;
-    }
-    return g_num_sms;
-}
-
-template <typename T> PushConst<T> make_push_const(const bz_params &p) {
-    PushConst<T> k;
-    double me = m_e(), jev = j_ev(), qe = q_e(), mn = m_n();
-    k.efac = T(0.5 * me * jev);
-    k.efac_d = 0.5 * me * jev;
-    k.c100dt = T(100 * p.dt);
-    k.c100dt_d = 100 * p.dt;
-    k.kick = T(p.dt * (qe / me) * 100);
-    k.f_el = T(sqrt(1 - (2 * me / mn)));
-    k.e2v = T(2.0 / (jev * me));
-    k.e2v_d = 2.0 / (jev * me);
-    k.gas_sigma = T(p.gas_sigma);
-    k.L = T(p.L);
-    k.inv_dx_f = float(1.0 / p.dx);
-    if (p.xs_n >= 2 && p.xs_emax > p.xs_emin && p.xs_emin > 0) {
-        double inv_d = double(p.xs_n - 1) / log2(p.xs_emax / p.xs_emin);
-        k.xs_inv_d = float(inv_d);
-        k.xs_off = float(log2(p.xs_emin) * inv_d);
-    } else {
-        k.xs_inv_d = 0.f;
-        k.xs_off = 0.f;
-    }
-    k.p_null = T(p.nu_max > 0 ? -expm1(-p.dt * p.nu_max) : 0.0);
-    k.inv_nu_max = T(p.nu_max > 0 ? 1.0 / p.nu_max : 0.0);
-    return k;
-}
-
 struct PushWsLayout {
     static constexpr size_t ticket_bytes = 256;
     static size_t tiles(int64_t capacity) { return size_t(ceil_div(std::max<int64_t>(capacity, 1), PTILE)); }

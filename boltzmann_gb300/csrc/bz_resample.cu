@@ -176,7 +176,8 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
                                                    double merge_keep, const int32_t *perm, const int32_t *offsets,
                                                    const int32_t *counts, const int32_t *act, const int32_t *app_off,
                                                    const int32_t *draw_off, const double *replay_u, double *ws_cdf,
-                                                   int32_t *ws_cnt, double *cons_diag, uint32_t *status) {
+                                                   int32_t *ws_cnt, double *cons_diag, SoAR<T> app, int64_t app_cap,
+                                                   uint32_t *status) {
     __shared__ double shd[RS_T / 32 + 1];
     __shared__ int64_t shi[RS_T / 32 + 1];
     const int key = blockIdx.x;
@@ -186,11 +187,15 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
     const int b = key % nb;
     const int n_k = counts[key];
     const int off = offsets[key];
-    if (int64_t(off) + n_k > cap || int64_t(*n_ptr) > cap) {  // inconsistent bins: touch nothing
+    // appended particles go behind the n particles of s, or into app when it is given
+    const bool to_app = app.w != nullptr;
+    if (int64_t(off) + n_k > cap || (!to_app && int64_t(*n_ptr) > cap)) {  // inconsistent bins: touch nothing
         if (threadIdx.x == 0) atomicOr(status, BZ_DEV_CAPACITY);
         return;
     }
-    const int64_t base = int64_t(*n_ptr) + app_off[key];
+    const int64_t base = (to_app ? 0 : int64_t(*n_ptr)) + app_off[key];
+    SoAR<T> dst = to_app ? app : s;
+    const int64_t dcap = to_app ? app_cap : cap;
     const int64_t T_ = targets[b];
     const double efac = 0.5 * m_e() * j_ev();
     double *cdf = ws_cdf + off;
@@ -281,8 +286,8 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
                 T xx = s.x[t], a1 = s.vx[t], a2 = s.vy[t], a3 = s.vz[t], ww = T(cdf[j]);
                 for (int r = 0; r < c; ++r) {
                     int64_t q = base + carry2 + ex + r;
-                    if (q < cap) {
-                        s.x[q] = xx; s.vx[q] = a1; s.vy[q] = a2; s.vz[q] = a3; s.w[q] = ww;
+                    if (q < dcap) {
+                        dst.x[q] = xx; dst.vx[q] = a1; dst.vy[q] = a2; dst.vz[q] = a3; dst.w[q] = ww;
                     } else {
                         atomicOr(status, BZ_DEV_CAPACITY);
                     }
@@ -369,8 +374,8 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
         double vz = uz + (double(s.vz[id]) - hz) * Tfac;
         T tx = T(vx), ty = T(vy), tz = T(vz);
         int64_t q = base + k;
-        if (q < cap) {
-            s.x[q] = xx; s.vx[q] = tx; s.vy[q] = ty; s.vz[q] = tz; s.w[q] = wbar_t;
+        if (q < dcap) {
+            dst.x[q] = xx; dst.vx[q] = tx; dst.vy[q] = ty; dst.vz[q] = tz; dst.w[q] = wbar_t;
         } else {
             atomicOr(status, BZ_DEV_CAPACITY);
         }
@@ -527,9 +532,96 @@ static int resample_entry(const bz_params *pp, P s_, const int32_t *n, int64_t c
     SoAR<T> s{s_.x, s_.vx, s_.vy, s_.vz, s_.w};
     SoAR<T> o{out_.x, out_.vx, out_.vy, out_.vz, out_.w};
     k_rs_apply<T><<<nkeys, RS_T, 0, st>>>(p, s, n, cap, nb, targets, max_ppc, min_wt, merge_keep, perm, offsets,
-                                          counts, act, app_off, draw_off, replay_u, cdf, cnt, cons_diag, status);
+                                          counts, act, app_off, draw_off, replay_u, cdf, cnt, cons_diag,
+                                          SoAR<T>{nullptr, nullptr, nullptr, nullptr, nullptr}, 0, status);
     if (cudaGetLastError() != cudaSuccess) return BZ_ERR_CUDA;
     return launch_compact<T>(s, n, misc, cap, o, cap, n_out, b + L.total, ws_bytes - L.total, status, st);
+}
+
+template <typename T, typename S, typename P>
+static int seg_resample_entry(const bz_params *pp, S s_, P app_, int64_t app_cap, S out_, int nb,
+                              const int32_t *targets, const int32_t *max_ppc, double min_wt, double split_below,
+                              double merge_at, double merge_keep, const int32_t *perm, const int32_t *offsets,
+                              const int32_t *counts, const int32_t *hw_counts, const double *replay_u,
+                              int32_t *need_out, double *cons_diag, void *ws, size_t ws_bytes, uint32_t *seg_flags,
+                              uint32_t *status, void *stream);
+
+}  // namespace bz
+
+extern "C" {
+size_t bz_seg_resample_workspace(int32_t nseg, int64_t capacity, int32_t nkeys) {
+    return bz::RsWs(capacity, nkeys).total + bz_seg_repack_workspace(nseg);
+}
+int bz_seg_resample_f32(const bz_params *p, bz_segments_f32 s, bz_particles_f32 app, int64_t app_capacity,
+                        bz_segments_f32 out, int32_t nbins, const int32_t *targets, const int32_t *max_ppc,
+                        double min_wt, double split_below, double merge_at, double merge_keep, const int32_t *perm,
+                        const int32_t *offsets, const int32_t *counts, const int32_t *hw_counts,
+                        const double *replay_u, int32_t *need_out, double *cons_diag, void *workspace,
+                        size_t workspace_bytes, uint32_t *seg_flags, uint32_t *status, void *stream) {
+    return bz::seg_resample_entry<float>(p, s, app, app_capacity, out, nbins, targets, max_ppc, min_wt, split_below,
+                                         merge_at, merge_keep, perm, offsets, counts, hw_counts, replay_u, need_out,
+                                         cons_diag, workspace, workspace_bytes, seg_flags, status, stream);
+}
+int bz_seg_resample_f64(const bz_params *p, bz_segments_f64 s, bz_particles_f64 app, int64_t app_capacity,
+                        bz_segments_f64 out, int32_t nbins, const int32_t *targets, const int32_t *max_ppc,
+                        double min_wt, double split_below, double merge_at, double merge_keep, const int32_t *perm,
+                        const int32_t *offsets, const int32_t *counts, const int32_t *hw_counts,
+                        const double *replay_u, int32_t *need_out, double *cons_diag, void *workspace,
+                        size_t workspace_bytes, uint32_t *seg_flags, uint32_t *status, void *stream) {
+    return bz::seg_resample_entry<double>(p, s, app, app_capacity, out, nbins, targets, max_ppc, min_wt, split_below,
+                                          merge_at, merge_keep, perm, offsets, counts, hw_counts, replay_u, need_out,
+                                          cons_diag, workspace, workspace_bytes, seg_flags, status, stream);
+}
+}  // extern "C"
+
+namespace bz {
+template <typename T, typename S, typename P>
+static int seg_resample_entry(const bz_params *pp, S s_, P app_, int64_t app_cap, S out_, int nb,
+                              const int32_t *targets, const int32_t *max_ppc, double min_wt, double split_below,
+                              double merge_at, double merge_keep, const int32_t *perm, const int32_t *offsets,
+                              const int32_t *counts, const int32_t *hw_counts, const double *replay_u,
+                              int32_t *need_out, double *cons_diag, void *ws, size_t ws_bytes, uint32_t *seg_flags,
+                              uint32_t *status, void *stream) {
+    if (!pp || !targets || !max_ppc || !perm || !offsets || !counts || !hw_counts || !ws || !status) return BZ_ERR_ARG;
+    if (!s_.x || !s_.vx || !s_.vy || !s_.vz || !s_.w || !s_.counts || s_.nseg <= 0 || s_.half <= 0) return BZ_ERR_ARG;
+    if (!app_.x || !app_.vx || !app_.vy || !app_.vz || !app_.w || app_cap <= 0) return BZ_ERR_ARG;
+    const bz_params &p = *pp;
+    if (nb < 1 || p.n_nodes < 1 || !(merge_at > split_below) || !(merge_keep > 0)) return BZ_ERR_ARG;
+    const int nkeys = p.n_nodes * nb;
+    const int64_t cap = int64_t(s_.nseg) * 2 * s_.half;
+    RsWs L(cap, nkeys);
+    const size_t rws = bz_seg_repack_workspace(s_.nseg);
+    if (ws_bytes < L.total + rws) return BZ_ERR_WORKSPACE;
+    unsigned char *b = static_cast<unsigned char *>(ws);
+    int32_t *act = reinterpret_cast<int32_t *>(b + L.act);
+    int32_t *app_off = reinterpret_cast<int32_t *>(b + L.app_off);
+    int32_t *draw_off = reinterpret_cast<int32_t *>(b + L.draw_off);
+    int32_t *misc = reinterpret_cast<int32_t *>(b + L.misc);
+    double *cdf = reinterpret_cast<double *>(b + L.cdf);
+    int32_t *cnt = reinterpret_cast<int32_t *>(b + L.cnt);
+    cudaStream_t st = as_stream(stream);
+    k_rs_decide<<<1, 1024, 0, st>>>(counts, hw_counts, p.n_nodes, nb, targets, split_below, merge_at, merge_keep,
+                                    p.flags, act, app_off, draw_off, misc, need_out);
+    if (cons_diag && cudaMemsetAsync(cons_diag, 0, sizeof(double) * 10 * nkeys, st) != cudaSuccess) return BZ_ERR_CUDA;
+    SoAR<T> s{s_.x, s_.vx, s_.vy, s_.vz, s_.w};
+    SoAR<T> app{app_.x, app_.vx, app_.vy, app_.vz, app_.w};
+    k_rs_apply<T><<<nkeys, RS_T, 0, st>>>(p, s, nullptr, cap, nb, targets, max_ppc, min_wt, merge_keep, perm, offsets,
+                                          counts, act, app_off, draw_off, replay_u, cdf, cnt, cons_diag, app, app_cap,
+                                          status);
+    if (cudaGetLastError() != cudaSuccess) return BZ_ERR_CUDA;
+    // everything left in s (w != 0) followed by the appended particles, spread over out
+    int rc;
+    if (sizeof(T) == 4)
+        rc = bz_seg_repack_f32(reinterpret_cast<const bz_segments_f32 *>(&s_),
+                               *reinterpret_cast<const bz_particles_f32 *>(&app_), misc, app_cap,
+                               *reinterpret_cast<const bz_segments_f32 *>(&out_), b + L.total, rws, nullptr, seg_flags,
+                               status, stream);
+    else
+        rc = bz_seg_repack_f64(reinterpret_cast<const bz_segments_f64 *>(&s_),
+                               *reinterpret_cast<const bz_particles_f64 *>(&app_), misc, app_cap,
+                               *reinterpret_cast<const bz_segments_f64 *>(&out_), b + L.total, rws, nullptr, seg_flags,
+                               status, stream);
+    return rc;
 }
 
 }  // namespace bz

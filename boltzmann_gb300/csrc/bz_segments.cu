@@ -1,0 +1,531 @@
+// Segmented particle layout for the solver's hot loop.
+//
+// The dense push (bz_push.cu) keeps the reference's global order (survivors, then
+// children) with a decoupled look-back across tiles; measured on GB300, waiting for
+// predecessor tiles halves its throughput. Here the particles live in nseg segments of
+// 2*half slots. Segment s holds two runs: run 0 at slots [s*2h, s*2h + n0) and run 1 at
+// [s*2h + h, s*2h + h + n1). One warp pushes one whole segment: survivors of run 0 and
+// run 1 (in that order) go to run 0 of the same output segment, children (parent order)
+// to run 1. No two warps share anything but the shared-memory deposit grid, so the loop
+// has no barrier and no inter-warp wait. Within one segment the order is exactly the
+// reference's (reshuffle_data_atomics keeps survivors in order, then appends children).
+// A segment whose input holds at most half particles cannot overflow: every particle
+// leaves at most one survivor and one child. After a push, a segment above half raises
+// BZ_SEG_NEEDS_REPACK; k_seg_repack* then spreads all particles evenly again.
+#include <algorithm>
+
+#include "bz_push_core.cuh"
+
+namespace bz {
+
+constexpr int SG_T = 256;              // threads per CTA (8 independent warps)
+constexpr int SG_W = SG_T / 32;
+constexpr int SG_I = 4;                // consecutive particles per lane per round
+constexpr int SG_R = 32 * SG_I;        // particles per warp round
+
+template <typename T> struct Seg {
+    SoA<T> a;
+    int32_t *cnt;  // [2*nseg]
+    int nseg, half;
+};
+
+__device__ __forceinline__ int64_t seg_slot(int seg, int run, int half, int j) {
+    return int64_t(seg) * (2 * int64_t(half)) + int64_t(run) * half + j;
+}
+
+#ifndef BZ_SEG_MINB
+#define BZ_SEG_MINB 3
+#endif
+
+template <typename T, bool REPLAY, int XS, bool DEPOSIT>
+__global__ void __launch_bounds__(SG_T, BZ_SEG_MINB)
+    k_seg_push(bz_params p, PushConst<T> kc, Seg<T> in, Seg<T> out, const T *E, const double *R, const double *gas,
+               double *moments, unsigned int *ticket, uint32_t *seg_flags, uint32_t *status) {
+    using A = typename AccT<T>::t;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int nf = p.advect ? p.n_faces : 1;
+    const int nnodes = p.n_nodes;
+    const int xsn = (XS == BZ_XS_TABLE) ? p.xs_n : 0;
+    float4 *xs_s = reinterpret_cast<float4 *>(smem);
+    A *mom_s = reinterpret_cast<A *>(smem + size_t(xsn) * sizeof(float4));
+    T *E_s = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(mom_s) +
+                                   (DEPOSIT ? size_t(3) * nnodes * sizeof(A) : 0));
+    for (int i = threadIdx.x; i < nf; i += SG_T) E_s[i] = E[i];
+    if (XS == BZ_XS_TABLE)
+        for (int i = threadIdx.x; i < xsn; i += SG_T)
+            xs_s[i] = make_float4(p.xs_table[i], p.xs_table[xsn + i], p.xs_table[2 * xsn + i], 0.0f);
+    if (DEPOSIT)
+        for (int i = threadIdx.x; i < 3 * nnodes; i += SG_T) mom_s[i] = A(0);
+    __syncthreads();
+    const NodeMap nm = make_node_map(p);
+    const Rng rng = make_rng(p);
+    const int lane = threadIdx.x & 31;
+    const int H = in.half;
+    uint32_t err = 0;
+    bool overfull = false;
+    while (true) {
+        int seg = 0;
+        if (lane == 0) seg = int(atomicAdd(ticket, 1u));
+        seg = __shfl_sync(0xffffffffu, seg, 0);
+        if (seg >= in.nseg) break;
+        uint32_t ns_off = 0, nc_off = 0;  // warp-uniform running output offsets
+        for (int run = 0; run < 2; ++run) {
+            int cnt = in.cnt[2 * seg + run];
+            if (cnt < 0 || cnt > H) {  // corrupt count: touch nothing beyond the run
+                err |= BZ_DEV_CAPACITY;
+                cnt = cnt < 0 ? 0 : H;
+            }
+            const int64_t rbase = seg_slot(seg, run, H, 0);
+            for (int r0 = 0; r0 < cnt; r0 += SG_R) {
+                const int j0 = r0 + lane * SG_I;
+                T x[SG_I], vx[SG_I], vy[SG_I], vz[SG_I], w[SG_I];
+                if (sizeof(T) == 4 && j0 + SG_I <= cnt && (H % 4) == 0) {
+                    const int64_t b = rbase + j0;
+                    float4 qa = *reinterpret_cast<const float4 *>(in.a.x + b);
+                    float4 qb = *reinterpret_cast<const float4 *>(in.a.vx + b);
+                    float4 qc = *reinterpret_cast<const float4 *>(in.a.vy + b);
+                    float4 qd = *reinterpret_cast<const float4 *>(in.a.vz + b);
+                    float4 qf = *reinterpret_cast<const float4 *>(in.a.w + b);
+                    x[0] = qa.x; x[1] = qa.y; x[2] = qa.z; x[3] = qa.w;
+                    vx[0] = qb.x; vx[1] = qb.y; vx[2] = qb.z; vx[3] = qb.w;
+                    vy[0] = qc.x; vy[1] = qc.y; vy[2] = qc.z; vy[3] = qc.w;
+                    vz[0] = qd.x; vz[1] = qd.y; vz[2] = qd.z; vz[3] = qd.w;
+                    w[0] = qf.x; w[1] = qf.y; w[2] = qf.z; w[3] = qf.w;
+                } else {
+#pragma unroll
+                    for (int k = 0; k < SG_I; ++k) {
+                        const bool ok = j0 + k < cnt;
+                        const int64_t b = rbase + j0 + k;
+                        x[k] = ok ? in.a.x[b] : T(0);
+                        vx[k] = ok ? in.a.vx[b] : T(0);
+                        vy[k] = ok ? in.a.vy[b] : T(0);
+                        vz[k] = ok ? in.a.vz[b] : T(0);
+                        w[k] = ok ? in.a.w[b] : T(0);
+                    }
+                }
+                Item<T> it[SG_I];
+                uint32_t ns = 0, nc = 0;
+#pragma unroll
+                for (int k = 0; k < SG_I; ++k) {
+                    it[k].alive = false;
+                    it[k].child = false;
+                    it[k].ionized = false;
+                    if (w[k] > T(0)) {
+                        push_item<T, REPLAY, XS>(p, kc, rng, uint32_t(rbase + j0 + k), x[k], vx[k], vy[k], vz[k], E_s,
+                                                 xs_s, R, gas, it[k]);
+                        ns += it[k].alive;
+                        nc += it[k].child;
+                        if (!(isfinite(it[k].vx) && isfinite(it[k].vy) && isfinite(it[k].vz))) err |= BZ_DEV_NONFINITE;
+                        if (DEPOSIT) {
+                            if (it[k].alive) {
+                                int nd = p.advect ? node_index(it[k].x, nm) : 0;
+                                if (nd >= 0 && nd < nnodes) {
+                                    atomicAdd(&mom_s[nd], A(w[k]));
+                                    if (it[k].ionized) atomicAdd(&mom_s[nnodes + nd], A(w[k]));
+                                    atomicAdd(&mom_s[2 * nnodes + nd], A(w[k] * it[k].e));
+                                }
+                            } else if (it[k].ionized && (p.flags & BZ_QUIRK_DEAD_IONFLAG)) {
+                                atomicAdd(&mom_s[nnodes + 0], A(1));
+                            }
+                            if (it[k].child) {
+                                int nd = p.advect ? node_index(it[k].cx, nm) : 0;
+                                if (nd >= 0 && nd < nnodes) {
+                                    atomicAdd(&mom_s[nd], A(w[k]));
+                                    atomicAdd(&mom_s[2 * nnodes + nd], A(w[k] * it[k].ce));
+                                }
+                            }
+                        }
+                    }
+                }
+                // warp scan of (ns, nc): 16+16 bits (at most 128 each per round)
+                const uint32_t v = ns | (nc << 16);
+                uint32_t incl = v;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += t;
+                }
+                const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
+                const uint32_t excl = incl - v;
+                uint32_t ps = ns_off + (excl & 0xffffu);
+                uint32_t pc = nc_off + (excl >> 16);
+#pragma unroll
+                for (int k = 0; k < SG_I; ++k) {
+                    if (it[k].alive) {
+                        if (ps < uint32_t(H)) {
+                            const int64_t q = seg_slot(seg, 0, H, int(ps));
+                            out.a.x[q] = it[k].x; out.a.vx[q] = it[k].vx; out.a.vy[q] = it[k].vy;
+                            out.a.vz[q] = it[k].vz; out.a.w[q] = w[k];
+                        } else {
+                            err |= BZ_DEV_CAPACITY;
+                        }
+                        ++ps;
+                    }
+                    if (it[k].child) {
+                        if (pc < uint32_t(H)) {
+                            const int64_t q = seg_slot(seg, 1, H, int(pc));
+                            out.a.x[q] = it[k].cx; out.a.vx[q] = it[k].cvx; out.a.vy[q] = it[k].cvy;
+                            out.a.vz[q] = it[k].cvz; out.a.w[q] = w[k];
+                        } else {
+                            err |= BZ_DEV_CAPACITY;
+                        }
+                        ++pc;
+                    }
+                }
+                ns_off += tot & 0xffffu;
+                nc_off += tot >> 16;
+            }
+        }
+        if (lane == 0) {
+            out.cnt[2 * seg] = int32_t(min(ns_off, uint32_t(H)));
+            out.cnt[2 * seg + 1] = int32_t(min(nc_off, uint32_t(H)));
+        }
+        if (ns_off + nc_off > uint32_t(H)) overfull = true;  // next push could overflow: repack first
+    }
+    if (err) atomicOr(status, err);
+    if (overfull && lane == 0) atomicOr(seg_flags, BZ_SEG_NEEDS_REPACK);
+    if (DEPOSIT) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < 3 * nnodes; i += SG_T) {
+            A val = mom_s[i];
+            if (val != A(0)) {
+                int col = i / nnodes, nd = i - col * nnodes;
+                atomicAdd(&moments[(col == 2 ? 3 : col) * nnodes + nd], double(val));
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// repack: all particles with w != 0, in order (segment by segment, run 0 then run 1,
+// then an optional dense append buffer), spread evenly over the output segments
+// (fill = ceil(total / nseg) in run 0). Count -> scan -> scatter; deterministic.
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ bool repack_skip(const uint32_t *only_if) {
+    return only_if && !(*only_if & BZ_SEG_NEEDS_REPACK);
+}
+
+template <typename T>
+__global__ void k_seg_count_live(Seg<T> in, int32_t *live, const uint32_t *only_if) {
+    if (repack_skip(only_if)) return;
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int seg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; seg < in.nseg; seg += warps) {
+        int c = 0;
+        for (int run = 0; run < 2; ++run) {
+            const int cnt = min(max(in.cnt[2 * seg + run], 0), in.half);
+            const int64_t b = seg_slot(seg, run, in.half, 0);
+            for (int j = lane; j < cnt; j += 32) c += (in.a.w[b + j] != T(0));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+        if (lane == 0) live[seg] = c;
+    }
+}
+
+// exclusive scan of live[0..m) into pre[0..m], one CTA; pre[m] = total
+__global__ void __launch_bounds__(1024) k_scan_live(const int32_t *live, int m, const int32_t *app_n,
+                                                    int64_t app_cap, int32_t *pre, const uint32_t *only_if) {
+    if (repack_skip(only_if)) return;
+    __shared__ int64_t part[1024];
+    const int per = (m + 1023) / 1024;
+    const int lo = threadIdx.x * per, hi = min(m, lo + per);
+    int64_t s = 0;
+    for (int k = lo; k < hi; ++k) s += live[k];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        int64_t t = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+        __syncthreads();
+        part[threadIdx.x] += t;
+        __syncthreads();
+    }
+    int64_t run = part[threadIdx.x] - s;
+    for (int k = lo; k < hi; ++k) { pre[k] = int32_t(run); run += live[k]; }
+    if (threadIdx.x == 1023) {
+        int64_t a = app_n ? min(int64_t(max(*app_n, 0)), app_cap) : 0;
+        pre[m] = int32_t(part[1023]);
+        pre[m + 1] = int32_t(part[1023] + a);  // total including the append buffer
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void repack_put(Seg<T> &out, int64_t v, int fill, T x, T vx, T vy, T vz, T w,
+                                           uint32_t &err) {
+    const int seg = int(v / fill), j = int(v - int64_t(seg) * fill);
+    if (seg < out.nseg && j < out.half) {
+        const int64_t q = seg_slot(seg, 0, out.half, j);
+        out.a.x[q] = x; out.a.vx[q] = vx; out.a.vy[q] = vy; out.a.vz[q] = vz; out.a.w[q] = w;
+    } else {
+        err |= BZ_DEV_CAPACITY;
+    }
+}
+
+__device__ __forceinline__ int repack_fill(int64_t total, int nseg) {
+    return int(max(int64_t(1), (total + nseg - 1) / nseg));
+}
+
+template <typename T>
+__global__ void k_seg_scatter(Seg<T> in, const int32_t *pre, Seg<T> out, const uint32_t *only_if,
+                              uint32_t *status) {
+    if (repack_skip(only_if)) return;
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    const int fill = repack_fill(pre[in.nseg + 1], out.nseg);
+    uint32_t err = 0;
+    for (int seg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; seg < in.nseg; seg += warps) {
+        int64_t off = pre[seg];
+        for (int run = 0; run < 2; ++run) {
+            const int cnt = min(max(in.cnt[2 * seg + run], 0), in.half);
+            const int64_t b = seg_slot(seg, run, in.half, 0);
+            for (int j0 = 0; j0 < cnt; j0 += 32) {
+                const int j = j0 + lane;
+                const bool ok = j < cnt;
+                T w = ok ? in.a.w[b + j] : T(0);
+                const bool keep = ok && w != T(0);
+                const unsigned m = __ballot_sync(0xffffffffu, keep);
+                if (keep) {
+                    const int64_t v = off + __popc(m & ((1u << lane) - 1u));
+                    repack_put(out, v, fill, in.a.x[b + j], in.a.vx[b + j], in.a.vy[b + j], in.a.vz[b + j], w, err);
+                }
+                off += __popc(m);
+            }
+        }
+    }
+    if (err) atomicOr(status, err);
+}
+
+template <typename T>
+__global__ void k_app_scatter(SoA<T> app, const int32_t *app_n, int64_t app_cap, const int32_t *pre, int nseg_in,
+                              Seg<T> out, const uint32_t *only_if, uint32_t *status) {
+    if (repack_skip(only_if)) return;
+    const int64_t base = pre[nseg_in];
+    const int64_t total = pre[nseg_in + 1];
+    const int64_t n = total - base;
+    const int fill = repack_fill(total, out.nseg);
+    uint32_t err = 0;
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n && i < app_cap;
+         i += int64_t(gridDim.x) * blockDim.x)
+        repack_put(out, base + i, fill, app.x[i], app.vx[i], app.vy[i], app.vz[i], app.w[i], err);
+    if (err) atomicOr(status, err);
+}
+
+// one CTA: every thread reads the request flag before thread 0 clears it
+__global__ void __launch_bounds__(1024) k_seg_set_counts(int32_t *cnt, int nseg, int half, const int32_t *pre,
+                                                         int nseg_in, uint32_t *seg_flags, const uint32_t *only_if) {
+    const bool skip = repack_skip(only_if);
+    __syncthreads();
+    if (skip) return;
+    const int64_t total = pre[nseg_in + 1];
+    const int fill = repack_fill(total, nseg);
+    for (int s = threadIdx.x; s < nseg; s += blockDim.x) {
+        int64_t c = min(max(total - int64_t(s) * fill, int64_t(0)), int64_t(min(fill, half)));
+        cnt[2 * s] = int32_t(c);
+        cnt[2 * s + 1] = 0;
+    }
+    if (threadIdx.x == 0 && seg_flags) *seg_flags = 0u;  // repacked: clear the request
+}
+
+// moments of a segmented state (post_processing_1D.py:44-57), one warp per segment
+template <typename T>
+__global__ void __launch_bounds__(256) k_seg_deposit(bz_params p, Seg<T> s, double *moments) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    T *m = reinterpret_cast<T *>(smem);
+    const int nn = p.n_nodes;
+    for (int i = threadIdx.x; i < 3 * nn; i += blockDim.x) m[i] = T(0);
+    __syncthreads();
+    const NodeMap nm = make_node_map(p);
+    const T efac = T(0.5 * m_e() * j_ev());
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int seg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; seg < s.nseg; seg += warps) {
+        for (int run = 0; run < 2; ++run) {
+            const int cnt = min(max(s.cnt[2 * seg + run], 0), s.half);
+            const int64_t b = seg_slot(seg, run, s.half, 0);
+            for (int j = lane; j < cnt; j += 32) {
+                const T wi = s.a.w[b + j];
+                if (!(wi > T(0))) continue;
+                const int nd = p.advect ? node_index(s.a.x[b + j], nm) : 0;
+                if (nd < 0 || nd >= nn) continue;
+                const T vx = s.a.vx[b + j], vy = s.a.vy[b + j], vz = s.a.vz[b + j];
+                atomicAdd(&m[nd], wi);
+                atomicAdd(&m[2 * nn + nd], wi * efac * (vx * vx + vy * vy + vz * vz));
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 3 * nn; i += blockDim.x) {
+        const T v = m[i];
+        if (v != T(0)) {
+            const int col = i / nn, nd = i - col * nn;
+            atomicAdd(&moments[(col == 2 ? 3 : col) * nn + nd], double(v));
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// host side
+// ------------------------------------------------------------------------------------
+template <typename T, typename S> static bool seg_ok(const S &s) {
+    return s.x && s.vx && s.vy && s.vz && s.w && s.counts && s.nseg > 0 && s.half > 0 && (s.half % 4) == 0;
+}
+template <typename T, typename S> static Seg<T> to_seg(const S &s) {
+    return Seg<T>{SoA<T>{s.x, s.vx, s.vy, s.vz, s.w}, s.counts, s.nseg, s.half};
+}
+
+template <typename T, bool REPLAY, int XS, bool DEPOSIT>
+static int launch_seg_push(const bz_params &p, Seg<T> in, Seg<T> out, const T *E, const double *R, const double *gas,
+                           double *moments, void *ws, uint32_t *seg_flags, uint32_t *status, cudaStream_t st) {
+    using A = typename AccT<T>::t;
+    const int nf = p.advect ? p.n_faces : 1;
+    const int xsn = (XS == BZ_XS_TABLE) ? p.xs_n : 0;
+    const size_t smem = size_t(xsn) * sizeof(float4) + (DEPOSIT ? size_t(3) * p.n_nodes * sizeof(A) : 0) +
+                        size_t(nf) * sizeof(T);
+    auto kern = k_seg_push<T, REPLAY, XS, DEPOSIT>;
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess)
+        return BZ_ERR_UNSUPPORTED;
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, SG_T, smem) != cudaSuccess || per_sm < 1)
+        return BZ_ERR_UNSUPPORTED;
+    if (cudaMemsetAsync(ws, 0, 256, st) != cudaSuccess) return BZ_ERR_CUDA;
+    int grid = num_sms() * per_sm;
+    grid = std::max(1, std::min(grid, int(ceil_div(in.nseg, SG_W))));
+    kern<<<grid, SG_T, smem, st>>>(p, make_push_const<T>(p), in, out, E, R, gas, moments,
+                                   static_cast<unsigned int *>(ws), seg_flags, status);
+    return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+}
+
+template <typename T, typename S>
+static int seg_push_entry(const bz_params *pp, S in_, S out_, const T *E, const double *R, const double *gas,
+                          double *moments, void *ws, size_t ws_bytes, uint32_t *seg_flags, uint32_t *status,
+                          void *stream) {
+    if (!pp || !E || !ws || !status || !seg_flags || !seg_ok<T>(in_) || !seg_ok<T>(out_)) return BZ_ERR_ARG;
+    if (in_.nseg != out_.nseg || in_.half != out_.half) return BZ_ERR_ARG;
+    if (ws_bytes < 256) return BZ_ERR_WORKSPACE;
+    if ((R == nullptr) != (gas == nullptr)) return BZ_ERR_ARG;
+    const bz_params &p = *pp;
+    if (p.advect && (p.n_faces < 1 || p.dx <= 0 || p.L <= 0)) return BZ_ERR_ARG;
+    if (p.n_nodes < 1 || p.bnf < 1) return BZ_ERR_ARG;
+    if (p.xs_mode == BZ_XS_TABLE && (p.xs_n < 2 || !p.xs_table || !(p.xs_emax > p.xs_emin) || p.xs_emin <= 0))
+        return BZ_ERR_ARG;
+    if (p.xs_mode != BZ_XS_TABLE && p.xs_mode != BZ_XS_REF_FITS) return BZ_ERR_ARG;
+    if (p.coll_model == BZ_COLL_NULL && !(p.nu_max > 0)) return BZ_ERR_ARG;
+    auto al = [](const void *q) { return (reinterpret_cast<uintptr_t>(q) & 15u) == 0; };
+    if (sizeof(T) == 4 && !(al(in_.x) && al(in_.vx) && al(in_.vy) && al(in_.vz) && al(in_.w))) return BZ_ERR_ARG;
+    Seg<T> in = to_seg<T>(in_), out = to_seg<T>(out_);
+    cudaStream_t st = as_stream(stream);
+    const bool replay = R != nullptr, dep = moments != nullptr;
+#define BZ_SEG_CASE(RP, XSM, DP)                                                                                    \
+    if (replay == RP && p.xs_mode == XSM && dep == DP)                                                             \
+        return launch_seg_push<T, RP, XSM, DP>(p, in, out, E, R, gas, moments, ws, seg_flags, status, st);
+    BZ_SEG_CASE(false, BZ_XS_TABLE, true)
+    BZ_SEG_CASE(false, BZ_XS_TABLE, false)
+    BZ_SEG_CASE(false, BZ_XS_REF_FITS, true)
+    BZ_SEG_CASE(false, BZ_XS_REF_FITS, false)
+    BZ_SEG_CASE(true, BZ_XS_TABLE, true)
+    BZ_SEG_CASE(true, BZ_XS_TABLE, false)
+    BZ_SEG_CASE(true, BZ_XS_REF_FITS, true)
+    BZ_SEG_CASE(true, BZ_XS_REF_FITS, false)
+#undef BZ_SEG_CASE
+    return BZ_ERR_ARG;
+}
+
+struct RepackWs {
+    size_t live, pre, total;
+    explicit RepackWs(int nseg) {
+        auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+        live = 0;
+        pre = al(4 * size_t(nseg));
+        total = pre + al(4 * (size_t(nseg) + 2));
+    }
+};
+
+template <typename T, typename S, typename P>
+static int seg_repack_entry(const S *in_, P app_, const int32_t *app_n, int64_t app_cap, S out_, void *ws,
+                            size_t ws_bytes, const uint32_t *only_if, uint32_t *seg_flags, uint32_t *status,
+                            void *stream) {
+    if (!ws || !status || !seg_ok<T>(out_)) return BZ_ERR_ARG;
+    if (in_ && !seg_ok<T>(*in_)) return BZ_ERR_ARG;
+    const bool has_app = app_n != nullptr;
+    if (has_app && (!app_.x || !app_.vx || !app_.vy || !app_.vz || !app_.w || app_cap < 0)) return BZ_ERR_ARG;
+    if (!in_ && !has_app) return BZ_ERR_ARG;
+    const int nseg_in = in_ ? in_->nseg : 0;
+    RepackWs L(nseg_in);
+    if (ws_bytes < L.total) return BZ_ERR_WORKSPACE;
+    unsigned char *b = static_cast<unsigned char *>(ws);
+    int32_t *live = reinterpret_cast<int32_t *>(b + L.live);
+    int32_t *pre = reinterpret_cast<int32_t *>(b + L.pre);
+    cudaStream_t st = as_stream(stream);
+    Seg<T> out = to_seg<T>(out_);
+    SoA<T> app{app_.x, app_.vx, app_.vy, app_.vz, app_.w};
+    const int blocks = std::max(1, std::min(num_sms() * 8, int(ceil_div(std::max(nseg_in, out.nseg), 8))));
+    if (in_) {
+        Seg<T> in = to_seg<T>(*in_);
+        k_seg_count_live<T><<<blocks, 256, 0, st>>>(in, live, only_if);
+        k_scan_live<<<1, 1024, 0, st>>>(live, nseg_in, app_n, app_cap, pre, only_if);
+        k_seg_scatter<T><<<blocks, 256, 0, st>>>(in, pre, out, only_if, status);
+    } else {
+        k_scan_live<<<1, 1024, 0, st>>>(live, 0, app_n, app_cap, pre, only_if);
+    }
+    if (has_app)
+        k_app_scatter<T><<<num_sms() * 4, 256, 0, st>>>(app, app_n, app_cap, pre, nseg_in, out, only_if, status);
+    k_seg_set_counts<<<1, 1024, 0, st>>>(out.cnt, out.nseg, out.half, pre, nseg_in, seg_flags, only_if);
+    return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+}
+
+template <typename T, typename S>
+static int seg_deposit_entry(const bz_params *pp, S s_, double *moments, void *stream) {
+    if (!pp || !moments || !seg_ok<T>(s_)) return BZ_ERR_ARG;
+    const bz_params &p = *pp;
+    if (p.n_nodes < 1 || p.bnf < 1 || (p.advect && (p.dx <= 0 || p.L <= 0))) return BZ_ERR_ARG;
+    const size_t smem = size_t(3) * p.n_nodes * sizeof(T);
+    auto kern = k_seg_deposit<T>;
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess)
+        return BZ_ERR_UNSUPPORTED;
+    const int blocks = std::max(1, std::min(num_sms() * 4, int(ceil_div(s_.nseg, 8))));
+    kern<<<blocks, 256, smem, as_stream(stream)>>>(p, to_seg<T>(s_), moments);
+    return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+}
+
+}  // namespace bz
+
+extern "C" {
+
+size_t bz_seg_push_workspace(void) { return 256; }
+size_t bz_seg_repack_workspace(int32_t nseg_in) { return bz::RepackWs(nseg_in).total; }
+
+int bz_seg_push_collide_f32(const bz_params *p, bz_segments_f32 in, bz_segments_f32 out, const float *E,
+                            const double *replay_R, const double *replay_gas, double *moments, void *workspace,
+                            size_t workspace_bytes, uint32_t *seg_flags, uint32_t *status, void *stream) {
+    return bz::seg_push_entry<float>(p, in, out, E, replay_R, replay_gas, moments, workspace, workspace_bytes,
+                                     seg_flags, status, stream);
+}
+int bz_seg_push_collide_f64(const bz_params *p, bz_segments_f64 in, bz_segments_f64 out, const double *E,
+                            const double *replay_R, const double *replay_gas, double *moments, void *workspace,
+                            size_t workspace_bytes, uint32_t *seg_flags, uint32_t *status, void *stream) {
+    return bz::seg_push_entry<double>(p, in, out, E, replay_R, replay_gas, moments, workspace, workspace_bytes,
+                                      seg_flags, status, stream);
+}
+int bz_seg_repack_f32(const bz_segments_f32 *in, bz_particles_f32 app, const int32_t *app_n, int64_t app_capacity,
+                      bz_segments_f32 out, void *workspace, size_t workspace_bytes, const uint32_t *only_if,
+                      uint32_t *seg_flags, uint32_t *status, void *stream) {
+    return bz::seg_repack_entry<float>(in, app, app_n, app_capacity, out, workspace, workspace_bytes, only_if,
+                                       seg_flags, status, stream);
+}
+int bz_seg_repack_f64(const bz_segments_f64 *in, bz_particles_f64 app, const int32_t *app_n, int64_t app_capacity,
+                      bz_segments_f64 out, void *workspace, size_t workspace_bytes, const uint32_t *only_if,
+                      uint32_t *seg_flags, uint32_t *status, void *stream) {
+    return bz::seg_repack_entry<double>(in, app, app_n, app_capacity, out, workspace, workspace_bytes, only_if,
+                                        seg_flags, status, stream);
+}
+int bz_seg_deposit_f32(const bz_params *p, bz_segments_f32 s, double *moments, void *stream) {
+    return bz::seg_deposit_entry<float>(p, s, moments, stream);
+}
+int bz_seg_deposit_f64(const bz_params *p, bz_segments_f64 s, double *moments, void *stream) {
+    return bz::seg_deposit_entry<double>(p, s, moments, stream);
+}
+
+}  // extern "C"

@@ -13,7 +13,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._lib import BzParams, Particles, call
+from ._lib import BzParams, Particles, Segments, call
 
 
 def _ptr(t):
@@ -71,6 +71,68 @@ class ParticleSet:
     def to_numpy(self, n=None):
         n = self.n() if n is None else n
         return {f: getattr(self, f)[:n].detach().cpu().numpy().astype(np.float64) for f in self.FIELDS}
+
+
+class SegmentSet:
+    """Segmented particle state (include/bz.h, bz_segments_*): nseg segments of 2*half
+    slots; segment s holds run 0 at [s*2h, s*2h+counts[2s]) and run 1 at
+    [s*2h+h, s*2h+h+counts[2s+1]). The solver's hot loop pushes these one warp per
+    segment with no ordering between segments."""
+
+    FIELDS = ParticleSet.FIELDS
+
+    def __init__(self, nseg, half, dtype=torch.float32, device="cuda"):
+        if half % 4:
+            raise ValueError("half must be a multiple of 4")
+        self.nseg, self.half, self.dtype = int(nseg), int(half), dtype
+        self.capacity = self.nseg * 2 * self.half
+        esz = torch.finfo(dtype).bits // 8
+        stride = ((self.capacity * esz + 255) // 256) * 256 // esz
+        self._buf = torch.zeros(5 * stride, dtype=dtype, device=device)
+        for k, f in enumerate(self.FIELDS):
+            setattr(self, f, self._buf[k * stride: k * stride + self.capacity])
+        self.counts = torch.zeros(2 * self.nseg, dtype=torch.int32, device=device)
+        self.device = device
+
+    @property
+    def suffix(self):
+        return "f32" if self.dtype == torch.float32 else "f64"
+
+    def struct(self):
+        return Segments(*(getattr(self, f).data_ptr() for f in self.FIELDS), self.counts.data_ptr(), self.nseg,
+                        self.half)
+
+    def n(self):
+        return int(self.counts.sum().item())
+
+    def load(self, x, vx, vy, vz, w, ws=None, status=None):
+        """Spread a dense particle list evenly over the segments (on the device)."""
+        n = len(x)
+        tmp = ParticleSet(max(n, 1), self.dtype, self.device)
+        tmp.load(x, vx, vy, vz, w)
+        if n > self.nseg * self.half:
+            raise RuntimeError(f"{n} particles exceed the {self.nseg} x {self.half} slots of run 0")
+        st = status if status is not None else torch.zeros(1, dtype=torch.int32, device=self.device)
+        seg_repack(None, self, st, ws or Workspace(self.device), app=tmp)
+        return st
+
+    def slots(self, order="runs"):
+        """Host-side slot indices of the live particles. order='runs': run 0 of every
+        segment, then run 1 of every segment (survivors in input order, then children in
+        parent order after one push); order='segments': segment by segment."""
+        c = self.counts.cpu().numpy().reshape(-1, 2)
+        base = np.arange(self.nseg, dtype=np.int64) * 2 * self.half
+        r0 = [np.arange(b, b + k) for b, k in zip(base, c[:, 0])]
+        r1 = [np.arange(b + self.half, b + self.half + k) for b, k in zip(base, c[:, 1])]
+        if order == "runs":
+            parts = r0 + r1
+        else:
+            parts = [a for pair in zip(r0, r1) for a in pair]
+        return np.concatenate(parts) if parts else np.zeros(0, dtype=np.int64)
+
+    def to_numpy(self, order="runs"):
+        idx = torch.as_tensor(self.slots(order), device=self.device)
+        return {f: getattr(self, f)[idx].detach().cpu().numpy().astype(np.float64) for f in self.FIELDS}
 
 
 class Workspace:
@@ -163,6 +225,58 @@ def compact(s: ParticleSet, out: ParticleSet, status, ws: Workspace):
     w = ws.get("compact", _lib.load().bz_compact_workspace(s.capacity))
     call(f"bz_compact_{s.suffix}", s.struct(), s.n_ptr(), s.capacity, out.struct(), out.capacity, out.n_ptr(), _ptr(w),
          w.numel(), _ptr(status), _stream())
+
+
+# --------------------------------------------------------------------------------------
+# segmented state
+# --------------------------------------------------------------------------------------
+
+def seg_electron_kernel(params, src: SegmentSet, dst: SegmentSet, E, status, seg_flags, ws: Workspace, moments=None,
+                        replay_R=None, replay_gas=None):
+    """Push + collide a segmented state (one warp per segment, no inter-segment order)."""
+    if src.dtype != dst.dtype or E.dtype != src.dtype:
+        raise TypeError("precision mismatch")
+    w = ws.get("seg_push", _lib.load().bz_seg_push_workspace())
+    call(f"bz_seg_push_collide_{src.suffix}", ctypes.byref(params), src.struct(), dst.struct(), _ptr(E),
+         _ptr(replay_R), _ptr(replay_gas), _ptr(moments), _ptr(w), w.numel(), _ptr(seg_flags), _ptr(status), _stream())
+
+
+def seg_repack(src, dst: SegmentSet, status, ws: Workspace, app: ParticleSet = None, app_n=None, only_if=None,
+               clear=None, name="seg_repack"):
+    """Particles with w != 0 of src (may be None), then app[0:n), spread over dst."""
+    nseg_in = src.nseg if src is not None else 0
+    w = ws.get(name, _lib.load().bz_seg_repack_workspace(nseg_in))
+    suffix = dst.suffix
+    ins = ctypes.byref(src.struct()) if src is not None else None
+    if app is not None:
+        ap, an, acap = app.struct(), (app_n if app_n is not None else app.n_ptr()), app.capacity
+    else:
+        ap, an, acap = Particles(), None, 0
+    call(f"bz_seg_repack_{suffix}", ins, ap, an, acap, dst.struct(), _ptr(w), w.numel(), _ptr(only_if), _ptr(clear),
+         _ptr(status), _stream())
+
+
+def seg_deposit(params, s: SegmentSet, moments):
+    call(f"bz_seg_deposit_{s.suffix}", ctypes.byref(params), s.struct(), _ptr(moments), _stream())
+
+
+def seg_bin_particles(params, s: SegmentSet, edges, min_wt, perm, offsets, counts, hw_counts, status, ws: Workspace):
+    nb = int(edges.numel()) + 1
+    w = ws.get("seg_bin", _lib.load().bz_seg_bin_workspace(s.nseg, s.capacity))
+    call(f"bz_seg_bin_{s.suffix}", ctypes.byref(params), s.struct(), nb, _ptr(edges) if nb > 1 else None,
+         float(min_wt), _ptr(perm), _ptr(offsets), _ptr(counts), _ptr(hw_counts), _ptr(w), w.numel(), _ptr(status),
+         _stream())
+
+
+def seg_resample(params, s: SegmentSet, app: ParticleSet, out: SegmentSet, nb, targets, max_ppc, min_wt, split_below,
+                 merge_at, merge_keep, perm, offsets, counts, hw_counts, status, seg_flags, ws: Workspace, need=None,
+                 replay_u=None, cons_diag=None):
+    nkeys = params.n_nodes * nb
+    w = ws.get("seg_resample", _lib.load().bz_seg_resample_workspace(s.nseg, s.capacity, nkeys))
+    call(f"bz_seg_resample_{s.suffix}", ctypes.byref(params), s.struct(), app.struct(), app.capacity, out.struct(), nb,
+         _ptr(targets), _ptr(max_ppc), float(min_wt), float(split_below), float(merge_at), float(merge_keep),
+         _ptr(perm), _ptr(offsets), _ptr(counts), _ptr(hw_counts), _ptr(replay_u), _ptr(need), _ptr(cons_diag),
+         _ptr(w), w.numel(), _ptr(seg_flags), _ptr(status), _stream())
 
 
 def grid_update(n_nodes, moments, ni, Te, g2):

@@ -32,18 +32,25 @@ class BoltzmannGB300:
         self.nnodes = N + 1
         dev = device
         f64 = dict(dtype=torch.float64, device=dev)
-        # particles: initial condition (boltzmann.py:242-333)
+        # particles: initial condition (boltzmann.py:242-333), spread over the segments
         x, vx, vy, vz, w = self._initial_condition()
         n0 = x.numel()
         cap = capacity or int(math.ceil(cfg.capacity_factor * max(n0, cfg.num_particles)))
         self.capacity = cap
-        self.A = K.ParticleSet(cap, self.dtype, dev)
-        self.B = K.ParticleSet(cap, self.dtype, dev)
+        half = int(cfg.seg_half)
+        nseg = max(1, -(-cap // half))
+        self.A = K.SegmentSet(nseg, half, self.dtype, dev)
+        self.B = K.SegmentSet(nseg, half, self.dtype, dev)
+        self.app = K.ParticleSet(max(cap, 1), self.dtype, dev)  # resampling appends, then the IC staging
         for f, a in zip(K.ParticleSet.FIELDS, (x, vx, vy, vz, w)):
-            getattr(self.A, f)[:n0].copy_(a.to(self.dtype))
-        self.A.cnt.zero_()
-        self.A.cnt[2] = n0
+            getattr(self.app, f)[:n0].copy_(a.to(self.dtype))
+        self.app.cnt.zero_()
+        self.app.cnt[2] = n0
         del x, vx, vy, vz, w
+        self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.seg_flags = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.ws = K.Workspace(dev)
+        K.seg_repack(None, self.A, self.status, self.ws, app=self.app)
         # grid arrays (boltzmann.py:94-109)
         self.E = torch.zeros(N, **f64)
         self.E_push = torch.zeros(N, dtype=self.dtype, device=dev)
@@ -58,8 +65,6 @@ class BoltzmannGB300:
         self.t = torch.zeros(1, **f64)
         self.step_dev = torch.zeros(1, dtype=torch.int64, device=dev)
         self.brk = torch.zeros(1, dtype=torch.int32, device=dev)
-        self.status = torch.zeros(1, dtype=torch.int32, device=dev)
-        self.ws = K.Workspace(dev)
         # cross sections
         tab = cfg.xs_table()
         self.xs = tab
@@ -72,7 +77,7 @@ class BoltzmannGB300:
                                      else np.zeros(1), device=dev)
         self.targets = torch.as_tensor(np.asarray(cfg.targets(), dtype=np.int32), device=dev)
         self.max_ppc = torch.as_tensor(np.asarray(cfg.max_ppc(), dtype=np.int32), device=dev)
-        self.perm = torch.zeros(cap, dtype=torch.int32, device=dev)
+        self.perm = torch.zeros(self.A.capacity, dtype=torch.int32, device=dev)
         self.offsets = torch.zeros(nkeys + 1, dtype=torch.int32, device=dev)
         self.bin_counts = torch.zeros(nkeys, dtype=torch.int32, device=dev)
         self.hw_counts = torch.zeros(nkeys, dtype=torch.int32, device=dev)
@@ -84,7 +89,7 @@ class BoltzmannGB300:
         if N >= 3:
             K.poisson_factor(N, cfg.dx, self.chol_d, self.chol_l)
         # first deposit and field solve (boltzmann.py:363-399)
-        K.deposit(self.params(), self.A, self.moments)
+        K.seg_deposit(self.params(), self.A, self.moments)
         self.ni.add_(self.moments[1])
         self._grid_solves(advance=False)
 
@@ -139,8 +144,9 @@ class BoltzmannGB300:
         """Push + collide the current particles; deposit and compaction are fused in
         (electron_kernel_numba.py:291-303 with post_processing_1D.py:40-68)."""
         self.moments.zero_()
-        K.electron_kernel(self.params(), self.A, self.B, self.E_push, self.status, self.ws, moments=self.moments)
-        self.particle_steps.add_(self.A.cnt[2:3].to(torch.int64))
+        self.particle_steps.add_(self.A.counts.sum(dtype=torch.int64))
+        K.seg_electron_kernel(self.params(), self.A, self.B, self.E_push, self.status, self.seg_flags, self.ws,
+                              moments=self.moments)
         self.A, self.B = self.B, self.A
 
     def post_processing(self):
@@ -149,9 +155,9 @@ class BoltzmannGB300:
         return self.moments[0], self.moments[1], self.moments[2], self.moments[3]
 
     def bin_particles(self):
-        K.bin_particles(self.params(), self.A, self.edges[: self.nb - 1] if self.nb > 1 else self.edges[:0],
-                        self.cfg.min_wt, self.perm, self.offsets, self.bin_counts, self.hw_counts, self.status,
-                        self.ws)
+        K.seg_bin_particles(self.params(), self.A, self.edges[: self.nb - 1] if self.nb > 1 else self.edges[:0],
+                            self.cfg.min_wt, self.perm, self.offsets, self.bin_counts, self.hw_counts, self.status,
+                            self.ws)
 
     def _check_for_resampling(self):
         """Bin the particles (the trigger itself is evaluated on the device inside
@@ -160,10 +166,17 @@ class BoltzmannGB300:
 
     def _do_resampling(self):
         cfg = self.cfg
-        K.resample(self.params(), self.A, self.B, self.nb, self.targets, self.max_ppc, cfg.min_wt, cfg.split_below,
-                   cfg.merge_at, cfg.merge_keep, self.perm, self.offsets, self.bin_counts, self.hw_counts,
-                   self.status, self.ws, need=self.need)
+        K.seg_resample(self.params(), self.A, self.app, self.B, self.nb, self.targets, self.max_ppc, cfg.min_wt,
+                       cfg.split_below, cfg.merge_at, cfg.merge_keep, self.perm, self.offsets, self.bin_counts,
+                       self.hw_counts, self.status, self.seg_flags, self.ws, need=self.need)
         self.A, self.B = self.B, self.A
+
+    def _repack_if_needed(self):
+        """Spread the particles evenly again when the last push left a segment above
+        half its capacity (decided on the device; A -> B -> A so the roles stay fixed)."""
+        K.seg_repack(self.A, self.B, self.status, self.ws, only_if=self.seg_flags, clear=None, name="repack_ab")
+        K.seg_repack(self.B, self.A, self.status, self.ws, only_if=self.seg_flags, clear=self.seg_flags,
+                     name="repack_ba")
 
     def heavies_kernel_fluid(self):
         cfg = self.cfg
@@ -189,6 +202,8 @@ class BoltzmannGB300:
         if resample:
             self._check_for_resampling()
             self._do_resampling()
+        else:
+            self._repack_if_needed()
         self.electron_kernel()
         self._grid_solves(advance=True)
 
@@ -234,11 +249,14 @@ class BoltzmannGB300:
 
     def _warm(self, resample):
         """Allocate every workspace the step uses without running the step."""
-        cap = self.capacity
-        self.ws.get("push", _lib.load().bz_push_workspace(cap))
+        lib = _lib.load()
+        nkeys = self.nnodes * self.nb
+        self.ws.get("seg_push", lib.bz_seg_push_workspace())
+        self.ws.get("repack_ab", lib.bz_seg_repack_workspace(self.A.nseg))
+        self.ws.get("repack_ba", lib.bz_seg_repack_workspace(self.A.nseg))
         if resample:
-            self.ws.get("bin", _lib.load().bz_bin_workspace(cap, self.nnodes * self.nb))
-            self.ws.get("resample", _lib.load().bz_resample_workspace(cap, self.nnodes * self.nb))
+            self.ws.get("seg_bin", lib.bz_seg_bin_workspace(self.A.nseg, self.A.capacity))
+            self.ws.get("seg_resample", lib.bz_seg_resample_workspace(self.A.nseg, self.A.capacity, nkeys))
 
     def run(self, num_steps, name="", restart_cyclenum=0, use_graph=True, write=False):
         """The step loop (boltzmann.py:565-716), with cycle averages and, when ``write``,

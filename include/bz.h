@@ -200,6 +200,73 @@ int bz_poisson(int32_t N, double dx, double eps0, double V0, double freq, double
 int bz_advance_clock(double *t_dev, uint64_t *step_dev, double dt, void *stream);
 
 /* ---------------------------------------------------------------------------------- */
+/* segmented particle state (the solver's hot loop)                                      */
+/* ---------------------------------------------------------------------------------- */
+/* No counterpart in the reference; a layout of the same particles. nseg segments of
+ * 2*half slots (half a multiple of 4); segment s holds run 0 at slots
+ * [s*2*half, s*2*half + counts[2s]) and run 1 at [s*2*half + half, ... + counts[2s+1]).
+ * The segmented push processes every segment with one warp and needs no ordering
+ * between segments; within a segment the output order is the reference's (survivors of
+ * run 0 then run 1 in order into run 0, children in parent order into run 1). A segment
+ * must hold at most half particles before a push; a push that leaves a segment above
+ * half sets BZ_SEG_NEEDS_REPACK in *seg_flags, and bz_seg_repack_* (conditional on that
+ * flag when only_if is given) spreads the particles evenly again. */
+typedef struct bz_segments_f32 { float *x, *vx, *vy, *vz, *w; int32_t *counts; int32_t nseg, half; } bz_segments_f32;
+typedef struct bz_segments_f64 { double *x, *vx, *vy, *vz, *w; int32_t *counts; int32_t nseg, half; } bz_segments_f64;
+#define BZ_SEG_NEEDS_REPACK 0x1u
+
+/* Push + collide (+ deposit) of a segmented state into another (same nseg, half); the
+ * per-particle arithmetic of bz_push_collide_*. Philox counters use the input slot. */
+size_t bz_seg_push_workspace(void);
+int bz_seg_push_collide_f32(const bz_params *p, bz_segments_f32 in, bz_segments_f32 out, const float *E,
+                            const double *replay_R, const double *replay_gas, double *moments,
+                            void *workspace, size_t workspace_bytes, uint32_t *seg_flags,
+                            uint32_t *status, void *stream);
+int bz_seg_push_collide_f64(const bz_params *p, bz_segments_f64 in, bz_segments_f64 out, const double *E,
+                            const double *replay_R, const double *replay_gas, double *moments,
+                            void *workspace, size_t workspace_bytes, uint32_t *seg_flags,
+                            uint32_t *status, void *stream);
+/* All particles with w != 0 of *in (segment order, run 0 then run 1; in may be NULL)
+ * followed by app[0 .. *app_n) (may be absent: app_n NULL), spread over out's segments,
+ * ceil(total/nseg) each in run 0. Skipped entirely when only_if != NULL and its
+ * BZ_SEG_NEEDS_REPACK bit is clear; clears *seg_flags when it runs (if given). */
+size_t bz_seg_repack_workspace(int32_t nseg_in);
+int bz_seg_repack_f32(const bz_segments_f32 *in, bz_particles_f32 app, const int32_t *app_n,
+                      int64_t app_capacity, bz_segments_f32 out, void *workspace, size_t workspace_bytes,
+                      const uint32_t *only_if, uint32_t *seg_flags, uint32_t *status, void *stream);
+int bz_seg_repack_f64(const bz_segments_f64 *in, bz_particles_f64 app, const int32_t *app_n,
+                      int64_t app_capacity, bz_segments_f64 out, void *workspace, size_t workspace_bytes,
+                      const uint32_t *only_if, uint32_t *seg_flags, uint32_t *status, void *stream);
+/* Moments (sum w, 0, 0, sum w*energy) of a segmented state (no ion flags are stored). */
+int bz_seg_deposit_f32(const bz_params *p, bz_segments_f32 s, double *moments, void *stream);
+int bz_seg_deposit_f64(const bz_params *p, bz_segments_f64 s, double *moments, void *stream);
+/* Binning of a segmented state: as bz_bin_*, perm holds slot indices. */
+size_t bz_seg_bin_workspace(int32_t nseg, int64_t capacity);
+int bz_seg_bin_f32(const bz_params *p, bz_segments_f32 s, int32_t nbins, const double *edges, double min_wt,
+                   int32_t *perm, int32_t *offsets, int32_t *counts, int32_t *hw_counts, void *workspace,
+                   size_t workspace_bytes, uint32_t *status, void *stream);
+int bz_seg_bin_f64(const bz_params *p, bz_segments_f64 s, int32_t nbins, const double *edges, double min_wt,
+                   int32_t *perm, int32_t *offsets, int32_t *counts, int32_t *hw_counts, void *workspace,
+                   size_t workspace_bytes, uint32_t *status, void *stream);
+/* ES-WPNC resampling of a segmented state: as bz_resample_*, with the appended particles
+ * collected in app (capacity app_capacity) and everything repacked into out. */
+size_t bz_seg_resample_workspace(int32_t nseg, int64_t capacity, int32_t nkeys);
+int bz_seg_resample_f32(const bz_params *p, bz_segments_f32 s, bz_particles_f32 app, int64_t app_capacity,
+                        bz_segments_f32 out, int32_t nbins, const int32_t *targets, const int32_t *max_ppc,
+                        double min_wt, double split_below, double merge_at, double merge_keep,
+                        const int32_t *perm, const int32_t *offsets, const int32_t *counts,
+                        const int32_t *hw_counts, const double *replay_u, int32_t *need_out,
+                        double *cons_diag, void *workspace, size_t workspace_bytes, uint32_t *seg_flags,
+                        uint32_t *status, void *stream);
+int bz_seg_resample_f64(const bz_params *p, bz_segments_f64 s, bz_particles_f64 app, int64_t app_capacity,
+                        bz_segments_f64 out, int32_t nbins, const int32_t *targets, const int32_t *max_ppc,
+                        double min_wt, double split_below, double merge_at, double merge_keep,
+                        const int32_t *perm, const int32_t *offsets, const int32_t *counts,
+                        const int32_t *hw_counts, const double *replay_u, int32_t *need_out,
+                        double *cons_diag, void *workspace, size_t workspace_bytes, uint32_t *seg_flags,
+                        uint32_t *status, void *stream);
+
+/* ---------------------------------------------------------------------------------- */
 /* allocation-free push                                                                 */
 /* ---------------------------------------------------------------------------------- */
 /* No counterpart in the reference. The same fused push + collide + deposit + compaction

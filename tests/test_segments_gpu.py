@@ -1,0 +1,218 @@
+"""GPU parity of the segmented particle state used by the solver's hot loop.
+
+One segment reproduces the reference's order exactly (survivors, then children), so it
+is checked against the golden vectors like the dense push; many segments are checked
+against the oracle run on the slot-indexed array (Philox counters are slot indices);
+repack, binning, resampling and deposit are checked against their dense counterparts.
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+from boltzmann_gb300 import _lib, kernels as K, xsec  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+from test_push_gpu import (check_moments, check_state, golden, node_allowance, params_for,  # noqa: E402
+                           velocity_scale)
+
+DT = {"f32": torch.float32, "f64": torch.float64}
+
+
+def seg_push(seg_in, p, E, R=None, gas=None):
+    out = K.SegmentSet(seg_in.nseg, seg_in.half, seg_in.dtype)
+    mom = torch.zeros(4, p.n_nodes, dtype=torch.float64, device="cuda")
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    fl = torch.zeros(1, dtype=torch.int32, device="cuda")
+    Et = torch.as_tensor(np.asarray(E), dtype=seg_in.dtype, device="cuda")
+    Rt = None if R is None else torch.as_tensor(R, dtype=torch.float64, device="cuda").contiguous()
+    gt = None if gas is None else torch.as_tensor(gas, dtype=torch.float64, device="cuda").contiguous()
+    K.seg_electron_kernel(p, seg_in, out, Et, st, fl, K.Workspace(), moments=mom, replay_R=Rt, replay_gas=gt)
+    torch.cuda.synchronize()
+    return out, mom.cpu().numpy(), int(st.item()), int(fl.item())
+
+
+@pytest.mark.parametrize("case", ["push_1torr", "push_0p1torr"])
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_one_segment_matches_reference_golden(case, prec):
+    g = golden(case + ".npz")
+    n = len(g["x"])
+    seg = K.SegmentSet(1, ((n + 3) // 4) * 4, DT[prec])
+    seg.load(g["x"], g["v"][:, 0], g["v"][:, 1], g["v"][:, 2], g["w"])
+    # slots equal particle indices in one segment, so R[i] / gas[i] line up
+    out, mom, st, fl = seg_push(seg, params_for(g, _lib.XS_REF_FITS), g["E"], g["R"], g["gas"])
+    assert st == 0
+    c = out.counts.cpu().numpy()
+    assert int(c[0] + c[1]) == int(g["Nnew"]) and int(c[1]) == int(g["nni"])
+    o = out.to_numpy("runs")
+    cd, ct = g["c_data"], g["c_tosum"]
+    rtol = 1e-12 if prec == "f64" else 1e-6
+    vs = velocity_scale(g["x"], g["v"], g["w"], g["k_tosum"][:n, 0] > 0, g["E"], float(g["dt"]), float(g["L"]),
+                        int(g["N"]), g["k_data"][n:, 3:6])
+    check_state(o, cd[:, 0], cd[:, 3:6], ct[:, 0], rtol, dt=float(g["dt"]), vscale=vs)
+    N, L = int(g["N"]), float(g["L"])
+    col = {"ne": ct[:, 0], "ni_src": ct[:, 0], "nrg": ct[:, 0] * ct[:, 3]}
+    for j, k in ((0, "ne"), (1, "ni_src"), (3, "nrg")):
+        allow = node_allowance(cd[:, 0], col[k], L, N, 4, prec == "f32")
+        check_moments(mom[j], g[k], 1e-12 if prec == "f64" else 1e-5, allow)
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_many_segments_match_oracle_philox(prec):
+    rng = np.random.default_rng(8)
+    n, N, L, nseg, half = 100_000, 256, 2.54, 64, 2048
+    x = rng.uniform(1e-4, L - 1e-4, n).astype(np.float32).astype(np.float64)
+    v = rng.normal(0, 1.3e6, (n, 3)).astype(np.float32).astype(np.float64)
+    w = rng.uniform(1e4, 1e5, n).astype(np.float32).astype(np.float64)
+    E = rng.uniform(-1500, 1500, N).astype(np.float32).astype(np.float64)
+    seg = K.SegmentSet(nseg, half, DT[prec])
+    seg.load(x, v[:, 0], v[:, 1], v[:, 2], w)
+    cap = seg.capacity
+    # the oracle sees the slot-indexed array: holes are w = 0 particles it drops
+    sl = seg.slots("segments")
+    xs_ = np.zeros(cap); vxs = np.zeros(cap); vys = np.zeros(cap); vzs = np.zeros(cap); ws_ = np.zeros(cap)
+    st_np = seg.to_numpy("segments")
+    xs_[sl], vxs[sl], vys[sl], vzs[sl], ws_[sl] = st_np["x"], st_np["vx"], st_np["vy"], st_np["vz"], st_np["w"]
+    tab = xsec.analytic_argon(2000)
+    nn, dt, gas_sigma = 3.22e22, 1.0 / 13.56e6 / 400, 6.74e4
+    op = O.make_params(N, L=L, dt=dt, nn=nn, rng_mode=1, precision=64 if prec == "f64" else 32, seed=4, step=3,
+                       gas_sigma=gas_sigma, xs_table=tab.nsigma(nn), xs_emin=tab.emin, xs_emax=tab.emax,
+                       e_exc=tab.e_exc)
+    data, tosum = O.soa_to_aos(xs_, vxs, vys, vzs, ws_, cap=2 * cap)
+    _, margin = O.push_margin(op, data.copy(), tosum.copy(), cap, E)
+    amb = (margin < 1e-5) & (ws_ > 0)
+    ws_[amb] = 0.0
+    seg.w[torch.as_tensor(np.nonzero(amb)[0], device="cuda")] = 0.0
+    data, tosum = O.soa_to_aos(xs_, vxs, vys, vzs, ws_, cap=2 * cap)
+    nni = O.push(op, data, tosum, cap, E)
+    vs = velocity_scale(xs_, np.stack([vxs, vys, vzs], 1), ws_, tosum[:cap, 0] > 0, E, dt, L, N,
+                        data[cap:cap + nni, 3:6])
+    mom_o, nnew = O.post(op, data, tosum, cap + nni)
+    xt = torch.as_tensor(tab.nsigma(nn), device="cuda")
+    p = K.make_params(n_faces=N, n_nodes=N + 1, bnf=4, advect=1, L=L, dx=L / N, dt=dt, nn=nn, gas_sigma=gas_sigma,
+                      e_exc=tab.e_exc, xs_mode=_lib.XS_TABLE, xs_table=xt, xs_emin=tab.emin, xs_emax=tab.emax,
+                      flags=_lib.QUIRK_DEAD_IONFLAG, seed=4, step=3)
+    out, mom, st, fl = seg_push(seg, p, E)
+    assert st == 0
+    o = out.to_numpy("runs")
+    assert len(o["x"]) == nnew
+    assert int(out.counts.cpu().numpy()[1::2].sum()) == nni
+    rtol = 1e-10 if prec == "f64" else 1e-6
+    check_state(o, data[:nnew, 0], data[:nnew, 3:6], tosum[:nnew, 0], rtol, dt=dt, vscale=vs)
+    col = {0: tosum[:nnew, 0], 1: tosum[:nnew, 0], 3: tosum[:nnew, 0] * tosum[:nnew, 3]}
+    for j in (0, 1, 3):
+        allow = node_allowance(data[:nnew, 0], col[j], L, N, 4, prec == "f32")
+        check_moments(mom[j], mom_o[j], 1e-10 if prec == "f64" else 1e-5, allow)
+
+
+def test_repack_keeps_order_and_balances():
+    rng = np.random.default_rng(2)
+    nseg, half = 50, 256
+    a = K.SegmentSet(nseg, half)
+    c = rng.integers(0, half + 1, (nseg, 2)).astype(np.int32)
+    a.counts.copy_(torch.as_tensor(c.reshape(-1), device="cuda"))
+    for f in a.FIELDS:
+        getattr(a, f).copy_(torch.rand(a.capacity, device="cuda") + 0.5)
+    dead = torch.rand(a.capacity, device="cuda") < 0.1
+    a.w[dead] = 0.0
+    before = a.to_numpy("segments")
+    keep = before["w"] != 0
+    b = K.SegmentSet(nseg, half)
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    K.seg_repack(a, b, st, K.Workspace())
+    torch.cuda.synchronize()
+    assert int(st.item()) == 0
+    after = b.to_numpy("segments")
+    for f in a.FIELDS:
+        np.testing.assert_array_equal(after[f], before[f][keep])
+    cb = b.counts.cpu().numpy().reshape(-1, 2)
+    assert cb[:, 1].sum() == 0
+    fill = -(-int(keep.sum()) // nseg)
+    assert cb[:, 0].max() == min(fill, half)
+
+
+def test_conditional_repack_skips_without_request():
+    a = K.SegmentSet(4, 64)
+    a.counts.copy_(torch.tensor([10, 5, 0, 0, 7, 0, 3, 3], dtype=torch.int32, device="cuda"))
+    a.w.fill_(1.0)
+    b = K.SegmentSet(4, 64)
+    b.counts.fill_(-7)
+    flags = torch.zeros(1, dtype=torch.int32, device="cuda")
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    K.seg_repack(a, b, st, K.Workspace(), only_if=flags, clear=flags)
+    torch.cuda.synchronize()
+    assert b.counts.cpu().tolist() == [-7] * 8  # nothing ran
+    flags.fill_(_lib.SEG_NEEDS_REPACK)
+    K.seg_repack(a, b, st, K.Workspace(), only_if=flags, clear=flags)
+    torch.cuda.synchronize()
+    assert int(flags.item()) == 0 and b.n() == 28
+
+
+@pytest.mark.parametrize("variant", ["3bin", "5bin"])
+def test_seg_bin_and_resample_match_dense(variant):
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", f"resample_{variant}.npz"))
+    N, L = int(g["N"]), float(g["L"])
+    x, v, w = g["x"], g["v"], g["w"]
+    n = len(x)
+    T = g["targets"]
+    nb = len(T)
+    edges = g["edges"]
+    p = K.make_params(n_faces=N, n_nodes=N + 1, bnf=4, advect=1, L=L, dx=L / N, dt=1e-12, nn=3.22e22,
+                      flags=_lib.QUIRK_SPLIT_WRAP | _lib.QUIRK_TRIGGER_LAST)
+    nkeys = (N + 1) * nb
+    seg = K.SegmentSet(1, ((4 * n + 3) // 4) * 4)
+    seg.load(x, v[:, 0], v[:, 1], v[:, 2], w)
+    ed = torch.as_tensor(np.asarray(edges, dtype=np.float64), device="cuda")
+    perm = torch.zeros(seg.capacity, dtype=torch.int32, device="cuda")
+    offs = torch.zeros(nkeys + 1, dtype=torch.int32, device="cuda")
+    cnts = torch.zeros(nkeys, dtype=torch.int32, device="cuda")
+    hw = torch.zeros(nkeys, dtype=torch.int32, device="cuda")
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    fl = torch.zeros(1, dtype=torch.int32, device="cuda")
+    ws = K.Workspace()
+    K.seg_bin_particles(p, seg, ed, float(g["min_wt"]), perm, offs, cnts, hw, st, ws)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(cnts.cpu().numpy().reshape(N + 1, nb).T, g["counts"])
+    app = K.ParticleSet(4 * n)
+    out = K.SegmentSet(1, seg.half)
+    tg = torch.as_tensor(np.asarray(T, dtype=np.int32), device="cuda")
+    mp = torch.as_tensor((10 * T).astype(np.int32), device="cuda")
+    ru = torch.as_tensor(g["draw_u"], device="cuda")
+    need = torch.zeros(1, dtype=torch.int32, device="cuda")
+    K.seg_resample(p, seg, app, out, nb, tg, mp, float(g["min_wt"]), 0.5, 3.0, 0.6, perm, offs, cnts, hw, st, fl, ws,
+                   need=need, replay_u=ru)
+    torch.cuda.synchronize()
+    assert int(st.item()) == 0 and int(need.item()) == int(g["need"])
+    o = out.to_numpy("runs")
+    assert len(o["x"]) == int(g["out_n"])
+    od, ot = g["out_data"], g["out_tosum"]
+    np.testing.assert_allclose(o["x"], od[:, 0], rtol=2e-6)
+    np.testing.assert_allclose(o["w"], ot[:, 0], rtol=2e-6)
+
+
+def test_load_refuses_more_than_the_segments_hold():
+    seg = K.SegmentSet(2, 8)
+    with pytest.raises(RuntimeError):
+        seg.load(np.ones(20), np.ones(20), np.ones(20), np.ones(20), np.ones(20))
+
+
+def test_seg_deposit_matches_dense():
+    rng = np.random.default_rng(5)
+    n, N = 50_000, 128
+    x = rng.uniform(0.01, 2.53, n)
+    v = rng.normal(0, 1e6, (n, 3))
+    w = rng.uniform(1, 2, n)
+    p = K.make_params(n_faces=N, n_nodes=N + 1, bnf=4, advect=1, L=2.54, dx=2.54 / N, dt=1e-12, nn=1e22)
+    seg = K.SegmentSet(80, 1024)
+    seg.load(x, v[:, 0], v[:, 1], v[:, 2], w)
+    dense = K.ParticleSet(n)
+    dense.load(x, v[:, 0], v[:, 1], v[:, 2], w)
+    m1 = torch.zeros(4, N + 1, dtype=torch.float64, device="cuda")
+    m2 = torch.zeros_like(m1)
+    K.seg_deposit(p, seg, m1)
+    K.deposit(p, dense, m2)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(m1.cpu().numpy(), m2.cpu().numpy(), rtol=1e-5, atol=1e-9)
