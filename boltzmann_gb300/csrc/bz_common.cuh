@@ -27,11 +27,15 @@ __device__ __forceinline__ u32x4 philox(uint32_t c0, uint32_t c1, uint32_t c2, u
                                         uint32_t k1) {
 #pragma unroll
     for (int r = 0; r < 10; ++r) {
-        uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
-        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
-        uint32_t n0 = hi1 ^ c1 ^ k0;
-        uint32_t n2 = hi0 ^ c3 ^ k1;
-        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        // one 32x32 -> 64-bit product per multiplier gives both halves
+        const uint64_t p0 = uint64_t(0xD2511F53u) * c0;
+        const uint64_t p1 = uint64_t(0xCD9E8D57u) * c2;
+        const uint32_t hi0 = uint32_t(p0 >> 32), lo0 = uint32_t(p0);
+        const uint32_t hi1 = uint32_t(p1 >> 32), lo1 = uint32_t(p1);
+        c0 = hi1 ^ c1 ^ k0;
+        c1 = lo1;
+        c2 = hi0 ^ c3 ^ k1;
+        c3 = lo0;
         k0 += 0x9E3779B9u;
         k1 += 0xBB67AE85u;
     }
@@ -44,8 +48,12 @@ __device__ __forceinline__ u32x4 philox(uint32_t c0, uint32_t c1, uint32_t c2, u
 template <typename T> struct Uni { T u, c; };
 
 __device__ __forceinline__ Uni<float> uni_f(uint32_t r) {
-    uint32_t k = r >> 9;
-    return {(float(k) + 0.5f) * 0x1p-23f, (float(0x800000u - k) - 0.5f) * 0x1p-23f};
+    // k = r >> 9 spliced into the mantissa of 1.0 gives 1 + k 2^-23 exactly; subtracting
+    // 1 - 2^-24 (exact, Sterbenz) leaves (k + 1/2) 2^-23. The complement uses 2^23-1-k.
+    const float one_minus = 0x1.fffffep-1f;  // 1 - 2^-24
+    const float u = __int_as_float(0x3F800000u | (r >> 9)) - one_minus;
+    const float c = __int_as_float(0x3F800000u | (~r >> 9)) - one_minus;
+    return {u, c};
 }
 __device__ __forceinline__ Uni<double> uni_d(uint32_t a, uint32_t b) {
     uint64_t k = (uint64_t(a >> 6) << 26) | uint64_t(b >> 6);
@@ -89,9 +97,14 @@ __device__ __forceinline__ void sincos2pi(float u, float *s, float *c) {
 }
 __device__ __forceinline__ void sincos2pi(double u, double *s, double *c) { sincospi(2.0 * u, s, c); }
 
+// square root of a positive argument: x * rsqrt(x) in float (relative error ~1e-7),
+// correctly rounded in double
+__device__ __forceinline__ float sqrt_pos(float x) { return x * rsqrtf(x); }
+__device__ __forceinline__ double sqrt_pos(double x) { return sqrt(x); }
+
 // Box-Muller pair from uniforms (a, b): r = sqrt(-2 ln a), angle 2 pi b.
 template <typename T> __device__ __forceinline__ void box_muller(T a, T b, T &g0, T &g1) {
-    T r = sqrt(T(-2) * log(a));
+    T r = sqrt_pos(T(-2) * log(a));
     T s, c;
     sincos2pi(b, &s, &c);
     g0 = r * c;

@@ -78,13 +78,19 @@ template <typename T>
 __device__ __forceinline__ void iso_dir(Uni<T> a, Uni<T> b, T vn, T &vx, T &vy, T &vz) {
     // cos(chi) = 2a-1, sin(chi) = 2 sqrt(a(1-a)), phi = 2 pi b (electron_kernel_numba.py:202-209)
     T cc = a.u - a.c;
-    T sc = T(2) * sqrt(a.u * a.c);
+    T sc = T(2) * sqrt_pos(a.u * a.c);
     T sp, cp;
     sincos2pi(b.u, &sp, &cp);
     vx = vn * sc * cp;
     vy = vn * sc * sp;
     vz = vn * cc;
 }
+
+// 1 - exp(-x), x >= 0. float: the hardware exponential, absolute error ~2e-7 (the
+// collision test compares this probability with a uniform, so an absolute error is what
+// matters); double: expm1.
+__device__ __forceinline__ float coll_prob(float x) { return 1.0f - __expf(-x); }
+__device__ __forceinline__ double coll_prob(double x) { return -expm1(-x); }
 
 __device__ __forceinline__ float fdiv_fast(float a, float b) { return __fdividef(a, b); }
 __device__ __forceinline__ double fdiv_fast(double a, double b) { return a / b; }
@@ -138,7 +144,7 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
     // energy of the gas-relative velocity (electron_kernel_numba.py:55-63)
     T ax = vx - g0, ay = vy - g1, az = vz - g2;
     T v2 = ax * ax + ay * ay + az * az;
-    T vmag = sqrt(v2);
+    T vmag = sqrt_pos(v2 > T(0) ? v2 : T(1e-30));
     T e = k.efac * v2;
     int proc;
     if (XS == BZ_XS_REF_FITS) {
@@ -180,7 +186,7 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
         T r0, r1, r2;
         if (p.coll_model == BZ_COLL_DIRECT) {
             T st = s0 + s1 + s2;
-            T P = -expm1(-T(p.dt) * vmag * st);
+            T P = coll_prob(T(p.dt) * vmag * st);
             T pc = fdiv_fast(P, st);
             r0 = s0 * pc;
             r1 = r0 + s1 * pc;
@@ -206,7 +212,7 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
         T vn;
         if (sizeof(T) == 8 || e - T(thr) >= T(0.25) * e) {
             T en = (proc == P_EXCITE) ? (e - T(thr)) : T(0.5) * (e - T(thr));
-            vn = sqrt(en * k.e2v);
+            vn = sqrt_pos(en * k.e2v);
         } else {
             double ed = k.efac_d * (double(ax) * double(ax) + double(ay) * double(ay) + double(az) * double(az));
             double en = (proc == P_EXCITE) ? fabs(ed - thr) : fabs(0.5 * (ed - thr));
