@@ -223,11 +223,12 @@ def run_ours(args, world, rank, local, pg):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     cfg = config.ccp_1024(num_particles=int(args.particles), gridpts=args.cells + 1, resample_freq=args.rsf,
-                          seed=1 + rank)
+                          seed=1 + rank, autotune=not args.no_autotune)
     sol = BoltzmannGB300(cfg, device=dev)
     n_start = sol.n()
     for _ in range(args.warmup):
         sol.step()
+    sol.capture_all()  # no graph capture inside the timed loop
     torch.cuda.synchronize()
     ps0 = int(sol.particle_steps.item())
     n_resample = sum(1 for s in range(sol.bigstep, sol.bigstep + args.steps) if s % cfg.resample_freq == 0)
@@ -284,35 +285,33 @@ def run_ours(args, world, rank, local, pg):
             tj = json.load(f)
         traffic = tj["dram_bytes_per_particle"] * n_now
 
-    # e2e through the solver API with the reference's per-step host traffic
+    # e2e through the solver API with the reference's per-step host traffic: every step the
+    # host->device copy of [E, ne, ni, ns, Te] (5N+4 float64, _copy_to_GPU,
+    # boltzmann.py:719-741) from pinned memory, the step, and the device->host read of the
+    # moments post_processing returns (back_to_cpu, post_processing_1D.py:6-24) together
+    # with the fields the device now owns (the whole 9N+8 block), then a synchronisation
+    # before the host may read the result; the copies are part of each step's graph
     e2e = None
     if not args.no_e2e:
-        grid_h = torch.zeros(5 * sol.N + 4, dtype=torch.float64, pin_memory=True)
-        grid_d = torch.zeros_like(grid_h, device=dev)
-        back_h = torch.zeros(4 * sol.nnodes + sol.N + sol.nnodes, dtype=torch.float64, pin_memory=True)
-        N = sol.N
-        grid_h[:N] = sol.E.cpu()
-        grid_h[2 * N + 1: 3 * N + 2] = sol.ni.cpu()
+        io_h = torch.empty(sol.io.numel(), dtype=torch.float64, pin_memory=True)
+        io_h.copy_(sol.io)
+        n_in = sol.io_in
+        sol.attach_host_io(io_h)
+        sol.capture_all()
         K2 = max(10, args.steps // 2)
         torch.cuda.synchronize()
         ps_e0 = int(sol.particle_steps.item())
         t0 = time.perf_counter()
         for _ in range(K2):
-            grid_d.copy_(grid_h, non_blocking=True)        # _copy_to_GPU (boltzmann.py:719-741)
-            sol.E.copy_(grid_d[:N])
-            sol.ni.copy_(grid_d[2 * N + 1: 3 * N + 2])
             sol.step()
-            back = torch.cat([sol.moments.reshape(-1), sol.E, sol.ni])
-            back_h.copy_(back, non_blocking=True)           # back_to_cpu (post_processing_1D.py:6-24)
             torch.cuda.synchronize()
-            grid_h[:N] = back_h[4 * sol.nnodes: 4 * sol.nnodes + N]
-            grid_h[2 * N + 1: 3 * N + 2] = back_h[4 * sol.nnodes + N:]
         el = time.perf_counter() - t0
+        sol.attach_host_io(None)
         ps_e = int(sol.particle_steps.item()) - ps_e0
         el = max_over_ranks(pg, el, dev)
         ps_e = sum_over_ranks(pg, ps_e, dev)
-        e2e = {"value": ps_e / el, "unit": UNIT, "h2d_bytes_per_step": int(grid_h.numel() * 8),
-               "d2h_bytes_per_step": int(back_h.numel() * 8), "steps": K2}
+        e2e = {"value": ps_e / el, "unit": UNIT, "h2d_bytes_per_step": int(n_in * 8),
+               "d2h_bytes_per_step": int(sol.io.numel() * 8), "steps": K2}
 
     if rank != 0:
         return
@@ -322,18 +321,19 @@ def run_ours(args, world, rank, local, pg):
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{n} particles x {k} steps of the same CCP step, float64 AoS (reference layout), "
                          f"OpenMP {threads} threads"}
-    launches_per_step = 6
-    launches_resample = 10
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic", "config": workload_config(args),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "kernel": "k_seg_push (fused push+collide+deposit+compaction)",
-                     "launch_ms": push_ms, "particles_per_launch": n_now, "peak_kind": kind},
+                     "launch_ms": push_ms, "particles_per_launch": n_now, "peak_kind": kind,
+                     "cta_shape": (None if sol.push_shape is None else
+                                   dict(zip(("threads", "per_lane", "min_blocks"), sol.push_shape["shape"])))},
         "cpu_baseline": cpu,
         "e2e": e2e,
-        "gpu_launches": launches_per_step * args.steps + launches_resample * n_resample,
+        "gpu_launches": (sol.kernel_launches(False) * (args.steps - n_resample)
+                         + sol.kernel_launches(True) * n_resample),
         "clocks": clk.summary(),
         "particles_start": n_start, "particles_end": int(n_now), "device_status": status,
     }
@@ -351,6 +351,7 @@ def main():
     ap.add_argument("--rsf", type=int, default=50)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the push's default CTA shape")
     ap.add_argument("--cpu-sample", type=float, default=1e6)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--ref-sample", type=float, default=2e6)

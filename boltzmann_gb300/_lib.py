@@ -14,6 +14,8 @@ LIB_PATH = os.path.join(PKG, "libbz.so")
 BZ_OK, BZ_ERR_ARG, BZ_ERR_CUDA, BZ_ERR_WORKSPACE, BZ_ERR_UNSUPPORTED, BZ_ERR_TOO_LARGE = 0, 1, 2, 3, 4, 5
 DEV_CAPACITY, DEV_LOOKBACK, DEV_NONFINITE, DEV_BINRANGE = 0x1, 0x2, 0x4, 0x8
 QUIRK_SPLIT_WRAP, QUIRK_DEAD_IONFLAG, QUIRK_TRIGGER_LAST, FIX_MERGE_ENERGY = 0x1, 0x2, 0x4, 0x8
+PER_KEY_TARGETS, MOMENT_EXCITATION = 0x10, 0x20
+ADVECT_NONE, ADVECT_1D, ADVECT_ENSEMBLE = 0, 1, 2
 XS_TABLE, XS_REF_FITS = 0, 1
 COLL_DIRECT, COLL_NULL = 0, 1
 
@@ -94,6 +96,10 @@ _PROTOS = {
     "bz_poisson": (ctypes.c_int, [_i32, _f64, _f64, _f64, _f64, _f64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "bz_advance_clock": (ctypes.c_int, [_vp, _vp, _f64, _vp]),
     "bz_seg_push_workspace": (_sz, []),
+    "bz_seg_push_shapes": (ctypes.c_int32, []),
+    "bz_seg_push_shape_info": (ctypes.c_int, [ctypes.c_int32, _vp, _vp, _vp]),
+    "bz_seg_push_select": (ctypes.c_int, [ctypes.c_int32]),
+    "bz_seg_push_selected": (ctypes.c_int32, []),
     "bz_seg_push_collide_f32": (ctypes.c_int, [_P, Segments, Segments, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp, _vp]),
     "bz_seg_push_collide_f64": (ctypes.c_int, [_P, Segments, Segments, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp, _vp]),
     "bz_seg_repack_workspace": (_sz, [_i32]),
@@ -103,6 +109,8 @@ _PROTOS = {
                                          _vp, _vp, _vp]),
     "bz_seg_deposit_f32": (ctypes.c_int, [_P, Segments, _vp, _vp]),
     "bz_seg_deposit_f64": (ctypes.c_int, [_P, Segments, _vp, _vp]),
+    "bz_seg_eedf_f32": (ctypes.c_int, [_P, Segments, ctypes.c_int32, ctypes.c_double, ctypes.c_double, _vp, _vp]),
+    "bz_seg_eedf_f64": (ctypes.c_int, [_P, Segments, ctypes.c_int32, ctypes.c_double, ctypes.c_double, _vp, _vp]),
     "bz_seg_bin_workspace": (_sz, [_i32, _i64]),
     "bz_seg_bin_f32": (ctypes.c_int, [_P, Segments, _i32, _vp, _f64, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp]),
     "bz_seg_bin_f64": (ctypes.c_int, [_P, Segments, _i32, _vp, _f64, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp]),

@@ -82,6 +82,7 @@ class CCPConfig:
     gas_velocity: str = "reference"   # "reference", "argon", "off"
     # numerics
     precision: str = "float32"        # particle state: "float32" or "float64"
+    autotune: bool = True             # time the push's CTA shapes once at start and keep the fastest
     seed: int = 1
     quirks: int = _lib.QUIRK_SPLIT_WRAP | _lib.QUIRK_DEAD_IONFLAG | _lib.QUIRK_TRIGGER_LAST
 

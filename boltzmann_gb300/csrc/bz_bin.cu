@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(RB_T) k_bin_keys(bz_params p, const T *x, cons
         T wi = w[i];
         int key = nkeys;  // invalid: sorted past every bin
         if (wi > T(0)) {
-            int cell = p.advect ? cell_index(x[i], p.dx, inv_dx_f) : 0;
+            int cell = bin_cell(p.advect, x[i], p.dx, inv_dx_f);
             int b = energy_bin(vx[i], vy[i], vz[i], wi, nb, edges_s, efac_f, efac_d);
             if (cell >= 0 && cell < p.n_nodes && b >= 0) {
                 key = cell * nb + b;
@@ -247,7 +247,7 @@ static int bin_entry(const bz_params *pp, P s, const int32_t *n, int64_t cap, in
     if (!pp || !n || cap <= 0 || !perm || !offsets || !counts || !hw_counts || !ws || !status) return BZ_ERR_ARG;
     if (!s.x || !s.vx || !s.vy || !s.vz || !s.w) return BZ_ERR_ARG;
     const bz_params &p = *pp;
-    if (nb < 1 || nb > 16 || (nb > 1 && !edges) || p.n_nodes < 1 || (p.advect && p.dx <= 0)) return BZ_ERR_ARG;
+    if (nb < 1 || nb > 16 || (nb > 1 && !edges) || p.n_nodes < 1 || (p.advect == BZ_ADVECT_1D && p.dx <= 0)) return BZ_ERR_ARG;
     const int nkeys = p.n_nodes * nb;
     if (nkeys >= 65535) return BZ_ERR_UNSUPPORTED;
     BinWs L(cap);
@@ -320,7 +320,7 @@ __global__ void __launch_bounds__(256) k_seg_bin_keys(bz_params p, const T *x, c
                 const T wi = w[i];
                 int key = nkeys;
                 if (wi > T(0)) {
-                    int cell = p.advect ? cell_index(x[i], p.dx, inv_dx_f) : 0;
+                    int cell = bin_cell(p.advect, x[i], p.dx, inv_dx_f);
                     int e = energy_bin(vx[i], vy[i], vz[i], wi, nb, edges_s, efac_f, efac_d);
                     if (cell >= 0 && cell < p.n_nodes && e >= 0) {
                         key = cell * nb + e;
@@ -368,7 +368,7 @@ static int seg_bin_entry(const bz_params *pp, S s, int nb, const double *edges, 
     if (!pp || !perm || !offsets || !counts || !hw_counts || !ws || !status) return BZ_ERR_ARG;
     if (!s.x || !s.vx || !s.vy || !s.vz || !s.w || !s.counts || s.nseg <= 0 || s.half <= 0) return BZ_ERR_ARG;
     const bz_params &p = *pp;
-    if (nb < 1 || nb > 16 || (nb > 1 && !edges) || p.n_nodes < 1 || (p.advect && p.dx <= 0)) return BZ_ERR_ARG;
+    if (nb < 1 || nb > 16 || (nb > 1 && !edges) || p.n_nodes < 1 || (p.advect == BZ_ADVECT_1D && p.dx <= 0)) return BZ_ERR_ARG;
     const int nkeys = p.n_nodes * nb;
     if (nkeys >= 65535) return BZ_ERR_UNSUPPORTED;
     const int64_t cap = int64_t(s.nseg) * 2 * s.half;

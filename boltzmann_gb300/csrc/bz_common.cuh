@@ -116,19 +116,22 @@ template <typename T> __device__ __forceinline__ void box_muller(T a, T b, T &g0
 // float64 positions; here x is float32 or float64. A float32 candidate is used
 // unless it lies near a boundary, where the float64 expression is evaluated.
 // --------------------------------------------------------------------------------------
-// The float candidate s carries a relative error below ~2.4e-7 (two roundings of
-// inputs and one of the product), so a margin of 1e-6*|s| + 1e-5 to the nearest integer
-// guarantees the truncation agrees with the float64 expression.
-__device__ __forceinline__ bool safe_trunc(float s) {
+// The float candidate s carries a relative error below 2^-23 (~1.2e-7): the float
+// reciprocal or slope and the product or fma are each rounded once to float, and the
+// float64 expression itself is within a few 2^-53 of the exact value. mag bounds the
+// magnitudes that were summed into s (|s| when nothing cancels), so a distance from s
+// to the nearest integer above 2.5e-7*mag + 1e-7 (twice the bound, plus room for the
+// roundings of the test itself) guarantees that truncating s gives the float64 result.
+__device__ __forceinline__ bool safe_trunc(float s, float mag) {
     float fr = s - floorf(s);
-    float m = fmaf(fabsf(s), 1e-6f, 1e-5f);
+    float m = fmaf(mag, 2.5e-7f, 1e-7f);
     return fr > m && fr < 1.0f - m;
 }
 // int(x / dx) (boltzmann.py:657): E-field face of the pre-push position.
 template <typename T> __device__ __forceinline__ int face_index(T x, double dx, float inv_dx_f) {
     if (sizeof(T) == 4) {
         float s = float(x) * inv_dx_f;
-        if (safe_trunc(s)) return int(s);
+        if (safe_trunc(s, fabsf(s))) return int(s);
     }
     return int(double(x) / dx);
 }
@@ -136,7 +139,7 @@ template <typename T> __device__ __forceinline__ int face_index(T x, double dx, 
 template <typename T> __device__ __forceinline__ int cell_index(T x, double dx, float inv_dx_f) {
     if (sizeof(T) == 4) {
         float s = fmaf(float(x), inv_dx_f, 0.5f);
-        if (safe_trunc(s)) return int(s);
+        if (safe_trunc(s, fmaf(fabsf(float(x)), inv_dx_f, 0.5f))) return int(s);
     }
     return int((double(x) + 0.5 * dx) / dx);
 }
@@ -147,7 +150,8 @@ struct NodeMap {
     float a, b;              // float candidate: node ~= x*a + b
     int bnf;
 };
-__host__ __device__ inline NodeMap make_node_map(const bz_params &p) {
+// formed on the host and passed to the kernels (its float64 divisions stay off the GPU)
+inline NodeMap make_node_map(const bz_params &p) {
     NodeMap m;
     int M = p.bnf * p.n_nodes;
     m.half_dx = 0.5 * p.dx;
@@ -158,10 +162,20 @@ __host__ __device__ inline NodeMap make_node_map(const bz_params &p) {
     m.bnf = p.bnf;
     return m;
 }
+template <typename T> __device__ __forceinline__ int node_index(T x, const NodeMap &m);
+// deposit node of a particle for each motion mode (out-of-range values are dropped by the
+// callers; in an ensemble x is the swarm index)
+template <typename T> __device__ __forceinline__ int deposit_node(int advect, T x, const NodeMap &m) {
+    return advect == BZ_ADVECT_1D ? node_index(x, m) : (advect == BZ_ADVECT_ENSEMBLE ? int(x) : 0);
+}
+// binning cell of a particle for each motion mode
+template <typename T> __device__ __forceinline__ int bin_cell(int advect, T x, double dx, float inv_dx_f) {
+    return advect == BZ_ADVECT_1D ? cell_index(x, dx, inv_dx_f) : (advect == BZ_ADVECT_ENSEMBLE ? int(x) : 0);
+}
 template <typename T> __device__ __forceinline__ int node_index(T x, const NodeMap &m) {
     if (sizeof(T) == 4) {
         float s = fmaf(float(x), m.a, m.b);
-        if (safe_trunc(s)) return int(s);
+        if (safe_trunc(s, fmaf(fabsf(float(x)), m.a, m.b))) return int(s);
     }
     double tx = (double(x) + m.half_dx) / m.Lp;
     int fine = int(tx * m.fM);

@@ -9,7 +9,7 @@ namespace bz {
 constexpr int DT = 256;
 
 template <typename T>
-__global__ void __launch_bounds__(DT) k_deposit(bz_params p, const T *x, const T *vx, const T *vy, const T *vz,
+__global__ void __launch_bounds__(DT) k_deposit(bz_params p, NodeMap nm, const T *x, const T *vx, const T *vy, const T *vz,
                                                 const T *w, const int32_t *n_ptr, int64_t cap, const uint8_t *flag,
                                                 double *moments) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -17,12 +17,11 @@ __global__ void __launch_bounds__(DT) k_deposit(bz_params p, const T *x, const T
     const int nn = p.n_nodes;
     for (int i = threadIdx.x; i < 3 * nn; i += DT) m[i] = T(0);
     __syncthreads();
-    const NodeMap nm = make_node_map(p);
     const T efac = T(0.5 * m_e() * j_ev());
     const int64_t n = min(int64_t(max(*n_ptr, 0)), cap);
     for (int64_t i = blockIdx.x * DT + threadIdx.x; i < n; i += int64_t(gridDim.x) * DT) {
         T wi = w[i];
-        int nd = p.advect ? node_index(x[i], nm) : 0;
+        int nd = deposit_node(p.advect, x[i], nm);
         if (nd < 0 || nd >= nn) continue;
         T f = flag ? T(flag[i]) : T(0);
         if (wi > T(0)) {
@@ -49,7 +48,7 @@ static int deposit_entry(const bz_params *pp, P s, const int32_t *n, int64_t cap
                          double *moments, void *stream) {
     if (!pp || !n || !moments || !s.x || !s.vx || !s.vy || !s.vz || !s.w) return BZ_ERR_ARG;
     const bz_params &p = *pp;
-    if (p.n_nodes < 1 || p.bnf < 1 || (p.advect && (p.dx <= 0 || p.L <= 0))) return BZ_ERR_ARG;
+    if (p.n_nodes < 1 || p.bnf < 1 || (p.advect == BZ_ADVECT_1D && (p.dx <= 0 || p.L <= 0))) return BZ_ERR_ARG;
     size_t smem = size_t(3) * p.n_nodes * sizeof(T);
     auto kern = k_deposit<T>;
     if (smem > 48 * 1024 &&
@@ -60,7 +59,7 @@ static int deposit_entry(const bz_params *pp, P s, const int32_t *n, int64_t cap
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, DT, smem) != cudaSuccess || per_sm < 1)
         return BZ_ERR_UNSUPPORTED;
-    kern<<<sms * per_sm, DT, smem, as_stream(stream)>>>(p, s.x, s.vx, s.vy, s.vz, s.w, n, cap, flag, moments);
+    kern<<<sms * per_sm, DT, smem, as_stream(stream)>>>(p, make_node_map(p), s.x, s.vx, s.vy, s.vz, s.w, n, cap, flag, moments);
     return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
 }
 

@@ -103,13 +103,17 @@ __global__ void __launch_bounds__(PS_T) k_poisson(int N, double dx, double eps0,
                                                   const double *ni, const double *d, const double *l, double *V,
                                                   double *E, float *E32, double *y) {
     __shared__ Aff sh[32];
-    __shared__ double carry;
-    const double t = t_dev ? *t_dev : t_host;
+    __shared__ double carry, vs_s;
     const int n = N - 1;
-    const double vs = V0 * sin(2 * 3.141592653589793 * freq * t);
-    // forward: y_i = (1/d_i)(r_i - l_i y_{i-1}), r_i = (ni - ne)/eps0 (+ boundary term at i = 0)
-    if (threadIdx.x == 0) carry = 0.0;
+    // electrode voltage, evaluated once (float64 sin is costly on this part's narrow FP64 pipe)
+    if (threadIdx.x == 0) {
+        const double t = t_dev ? *t_dev : t_host;
+        vs_s = V0 * sin(2 * 3.141592653589793 * freq * t);
+        carry = 0.0;
+    }
     __syncthreads();
+    const double vs = vs_s;
+    // forward: y_i = (1/d_i)(r_i - l_i y_{i-1}), r_i = (ni - ne)/eps0 (+ boundary term at i = 0)
     for (int c0 = 0; c0 < n; c0 += PS_T) {
         int i = c0 + threadIdx.x;
         Aff v{1.0, 0.0};

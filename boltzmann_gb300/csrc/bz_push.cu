@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(PT, BZ_PUSH_MINB) k_push(bz_params p, PushCons
             xs_s[i] = make_float4(p.xs_table[i], p.xs_table[xsn + i], p.xs_table[2 * xsn + i], 0.0f);
     if (DEPOSIT)
         for (int i = threadIdx.x; i < 3 * nnodes; i += PT) mom_s[i] = A(0);
-    const NodeMap nm = make_node_map(p);
+    const NodeMap &nm = kc.nm;
     const Rng rng = make_rng(p);
     int n = *n_in;
     if (n < 0 || int64_t(n) > in_cap) {
@@ -100,6 +100,7 @@ __global__ void __launch_bounds__(PT, BZ_PUSH_MINB) k_push(bz_params p, PushCons
             it[j].alive = false;
             it[j].child = false;
             it[j].ionized = false;
+            it[j].excited = false;
             if (w[j] > T(0)) {
                 push_item<T, REPLAY, XS>(p, kc, rng, uint32_t(base + j), x[j], vx[j], vy[j], vz[j], E_s, xs_s, R, gas,
                                          it[j]);
@@ -108,17 +109,19 @@ __global__ void __launch_bounds__(PT, BZ_PUSH_MINB) k_push(bz_params p, PushCons
                 if (!(isfinite(it[j].vx) && isfinite(it[j].vy) && isfinite(it[j].vz))) err |= BZ_DEV_NONFINITE;
                 if (DEPOSIT) {
                     if (it[j].alive) {
-                        int nd = p.advect ? node_index(it[j].x, nm) : 0;
+                        int nd = deposit_node(p.advect, it[j].x, nm);
                         if (nd >= 0 && nd < nnodes) {
                             atomicAdd(&mom_s[nd], A(w[j]));
                             if (it[j].ionized) atomicAdd(&mom_s[nnodes + nd], A(w[j]));
                             atomicAdd(&mom_s[2 * nnodes + nd], A(w[j] * it[j].e));
+                            if (it[j].excited && (p.flags & BZ_MOMENT_EXCITATION))
+                                atomicAdd(&moments[2 * nnodes + nd], double(w[j]));  // rare: straight to the grid
                         }
                     } else if (it[j].ionized && (p.flags & BZ_QUIRK_DEAD_IONFLAG)) {
                         atomicAdd(&mom_s[nnodes + 0], A(1));
                     }
                     if (it[j].child) {
-                        int nd = p.advect ? node_index(it[j].cx, nm) : 0;
+                        int nd = deposit_node(p.advect, it[j].cx, nm);
                         if (nd >= 0 && nd < nnodes) {
                             atomicAdd(&mom_s[nd], A(w[j]));
                             atomicAdd(&mom_s[2 * nnodes + nd], A(w[j] * it[j].ce));
@@ -272,7 +275,9 @@ static int push_entry(const bz_params *pp, P in_, const int32_t *n_in, int64_t i
     if (!in_.x || !in_.vx || !in_.vy || !in_.vz || !in_.w || !out_.x || !out_.vx || !out_.vy || !out_.vz || !out_.w)
         return BZ_ERR_ARG;
     if ((R == nullptr) != (gas == nullptr)) return BZ_ERR_ARG;
-    if (p.advect && (p.n_faces < 1 || p.dx <= 0 || p.L <= 0)) return BZ_ERR_ARG;
+    if (p.advect < BZ_ADVECT_NONE || p.advect > BZ_ADVECT_ENSEMBLE) return BZ_ERR_ARG;
+    if (p.advect == BZ_ADVECT_1D && (p.n_faces < 1 || p.dx <= 0 || p.L <= 0)) return BZ_ERR_ARG;
+    if (p.advect == BZ_ADVECT_ENSEMBLE && p.n_faces < 1) return BZ_ERR_ARG;
     if (p.n_nodes < 1 || p.bnf < 1) return BZ_ERR_ARG;
     if (p.xs_mode == BZ_XS_TABLE && (p.xs_n < 2 || !p.xs_table || !(p.xs_emax > p.xs_emin) || p.xs_emin <= 0))
         return BZ_ERR_ARG;

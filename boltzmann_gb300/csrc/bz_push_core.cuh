@@ -65,13 +65,15 @@ template <typename T> struct PushConst {
     double efac_d, e2v_d, c100dt_d;
     T p_null;       // 1 - exp(-dt nu_max) (null collision)
     T inv_nu_max;
+    T dt, e_exc;    // dt and the excitation threshold in the working precision
+    NodeMap nm;     // deposit node map
 };
 
 template <typename T> struct Item {
     T x, vx, vy, vz;      // state after the step (w unchanged)
     T cx, cvx, cvy, cvz;  // child
     T e, ce;              // energies (eV) after the step, for the deposit
-    bool alive, child, ionized;
+    bool alive, child, ionized, excited;
 };
 
 template <typename T>
@@ -181,12 +183,12 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
         T s0 = T(fmaf(f, b.x - a.x, a.x));
         T s1 = T(fmaf(f, b.y - a.y, a.y));
         T s2 = T(fmaf(f, b.z - a.z, a.z));
-        if (e < T(p.e_exc)) s1 = T(0);
+        if (e < k.e_exc) s1 = T(0);
         if (e < T(E_ION)) s2 = T(0);
         T r0, r1, r2;
         if (p.coll_model == BZ_COLL_DIRECT) {
             T st = s0 + s1 + s2;
-            T P = coll_prob(T(p.dt) * vmag * st);
+            T P = coll_prob(k.dt * vmag * st);
             T pc = fdiv_fast(P, st);
             r0 = s0 * pc;
             r1 = r0 + s1 * pc;
@@ -201,6 +203,7 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
     }
     o.child = false;
     o.ionized = false;
+    o.excited = (proc == P_EXCITE);
     T nvx = vx, nvy = vy, nvz = vz;
     if (proc == P_ELASTIC) {
         // |v| (1 - 2 m_e/m_n)^1/2, isotropic (electron_kernel_numba.py:197-209)
@@ -244,7 +247,9 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
     T xn = x;
     int face = 0;
     bool valid = true;
-    if (p.advect) {
+    if (p.advect == BZ_ADVECT_ENSEMBLE) {
+        face = min(max(int(x), 0), p.n_faces - 1);
+    } else if (p.advect) {
         xn = x + k.c100dt * nvx;
         face = face_index(x, p.dx, k.inv_dx_f);
         face = min(max(face, 0), p.n_faces - 1);
@@ -298,6 +303,9 @@ template <typename T> inline PushConst<T> make_push_const(const bz_params &p) {
     }
     k.p_null = T(p.nu_max > 0 ? -expm1(-p.dt * p.nu_max) : 0.0);
     k.inv_nu_max = T(p.nu_max > 0 ? 1.0 / p.nu_max : 0.0);
+    k.dt = T(p.dt);
+    k.e_exc = T(p.e_exc);
+    k.nm = make_node_map(p);
     return k;
 }
 

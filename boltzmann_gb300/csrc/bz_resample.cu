@@ -48,10 +48,11 @@ __global__ void __launch_bounds__(1024) k_rs_decide(const int32_t *counts, const
     const int lo = threadIdx.x * per, hi = min(nkeys, lo + per);
     int64_t sa = 0, sd = 0;
     int need_last = 0, need_any = 0;
+    const bool per_key = (flags & BZ_PER_KEY_TARGETS) != 0;
     for (int k = lo; k < hi; ++k) {
         int b = k % nb;
         int64_t n = counts[k];
-        int64_t T = targets[b];
+        int64_t T = targets[per_key ? k : b];
         int a = ACT_NONE;
         int64_t app = 0;
         if (n > 0 && double(n) < split_below * double(T) && hw_counts[k] > 0) {
@@ -93,7 +94,7 @@ __global__ void __launch_bounds__(1024) k_rs_decide(const int32_t *counts, const
         draw_off[k] = int32_t(rd);
         if (a != ACT_NONE) {
             int b = k % nb;
-            int64_t n = counts[k], T = targets[b];
+            int64_t n = counts[k], T = targets[per_key ? k : b];
             int64_t app = (a == ACT_SPLIT) ? 2 * T - n : int64_t(merge_keep * double(T));
             ra += app;
             rd += app;
@@ -196,7 +197,8 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
     const int64_t base = (to_app ? 0 : int64_t(*n_ptr)) + app_off[key];
     SoAR<T> dst = to_app ? app : s;
     const int64_t dcap = to_app ? app_cap : cap;
-    const int64_t T_ = targets[b];
+    const int tk = (p.flags & BZ_PER_KEY_TARGETS) ? key : b;  // target / max_ppc entry
+    const int64_t T_ = targets[tk];
     const double efac = 0.5 * m_e() * j_ev();
     double *cdf = ws_cdf + off;
     int32_t *cnt = ws_cnt + off;
@@ -298,7 +300,7 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
         return;
     }
     // ---- merge (boltzmann.py:826-877)
-    const int np_ = min(n_k, int(max_ppc[b]));
+    const int np_ = min(n_k, int(max_ppc[tk]));
     const int K = int(merge_keep * double(T_));
     if (K > np_) {  // survivors need their own scratch slots (max_ppc >= merge_keep*T)
         if (threadIdx.x == 0) atomicOr(status, BZ_DEV_CAPACITY);

@@ -18,10 +18,14 @@
 
 namespace bz {
 
-constexpr int SG_T = 256;              // threads per CTA (8 independent warps)
-constexpr int SG_W = SG_T / 32;
-constexpr int SG_I = 4;                // consecutive particles per lane per round
-constexpr int SG_R = 32 * SG_I;        // particles per warp round
+// CTA shapes of the push: threads per CTA, consecutive particles per lane per round and
+// the minimum resident CTAs per SM the registers are budgeted for. Entry 0 is the
+// default; bz_seg_push_select() picks another for the float32 table + deposit push (the
+// solver's hot loop), which is what the autotuner times.
+struct SegShape { int threads, per_lane, min_blocks; };
+constexpr SegShape kSegShapes[] = {{320, 1, 4}, {256, 1, 4}, {256, 2, 4}, {512, 1, 3}, {640, 1, 2}, {256, 4, 3}};
+constexpr int kSegNumShapes = int(sizeof(kSegShapes) / sizeof(kSegShapes[0]));
+static int g_seg_shape = 0;
 
 template <typename T> struct Seg {
     SoA<T> a;
@@ -33,15 +37,12 @@ __device__ __forceinline__ int64_t seg_slot(int seg, int run, int half, int j) {
     return int64_t(seg) * (2 * int64_t(half)) + int64_t(run) * half + j;
 }
 
-#ifndef BZ_SEG_MINB
-#define BZ_SEG_MINB 3
-#endif
-
-template <typename T, bool REPLAY, int XS, bool DEPOSIT>
-__global__ void __launch_bounds__(SG_T, BZ_SEG_MINB)
+template <typename T, bool REPLAY, int XS, bool DEPOSIT, int SG_T, int SG_I, int MINB>
+__global__ void __launch_bounds__(SG_T, MINB)
     k_seg_push(bz_params p, PushConst<T> kc, Seg<T> in, Seg<T> out, const T *E, const double *R, const double *gas,
                double *moments, unsigned int *ticket, uint32_t *seg_flags, uint32_t *status) {
     using A = typename AccT<T>::t;
+    constexpr int SG_R = 32 * SG_I;  // particles per warp round
     extern __shared__ __align__(16) unsigned char smem[];
     const int nf = p.advect ? p.n_faces : 1;
     const int nnodes = p.n_nodes;
@@ -57,7 +58,7 @@ __global__ void __launch_bounds__(SG_T, BZ_SEG_MINB)
     if (DEPOSIT)
         for (int i = threadIdx.x; i < 3 * nnodes; i += SG_T) mom_s[i] = A(0);
     __syncthreads();
-    const NodeMap nm = make_node_map(p);
+    const NodeMap &nm = kc.nm;
     const Rng rng = make_rng(p);
     const int lane = threadIdx.x & 31;
     const int H = in.half;
@@ -79,7 +80,10 @@ __global__ void __launch_bounds__(SG_T, BZ_SEG_MINB)
             for (int r0 = 0; r0 < cnt; r0 += SG_R) {
                 const int j0 = r0 + lane * SG_I;
                 T x[SG_I], vx[SG_I], vy[SG_I], vz[SG_I], w[SG_I];
-                if (sizeof(T) == 4 && j0 + SG_I <= cnt && (H % 4) == 0) {
+                bool vec = false;
+                if constexpr (SG_I == 4 && sizeof(T) == 4) {
+                  if (j0 + SG_I <= cnt && (H % 4) == 0) {
+                    vec = true;
                     const int64_t b = rbase + j0;
                     float4 qa = *reinterpret_cast<const float4 *>(in.a.x + b);
                     float4 qb = *reinterpret_cast<const float4 *>(in.a.vx + b);
@@ -91,7 +95,24 @@ __global__ void __launch_bounds__(SG_T, BZ_SEG_MINB)
                     vy[0] = qc.x; vy[1] = qc.y; vy[2] = qc.z; vy[3] = qc.w;
                     vz[0] = qd.x; vz[1] = qd.y; vz[2] = qd.z; vz[3] = qd.w;
                     w[0] = qf.x; w[1] = qf.y; w[2] = qf.z; w[3] = qf.w;
-                } else {
+                  }
+                } else if constexpr (SG_I == 2 && sizeof(T) == 4) {
+                  if (j0 + SG_I <= cnt && (H % 2) == 0) {
+                    vec = true;
+                    const int64_t b = rbase + j0;
+                    float2 qa = *reinterpret_cast<const float2 *>(in.a.x + b);
+                    float2 qb = *reinterpret_cast<const float2 *>(in.a.vx + b);
+                    float2 qc = *reinterpret_cast<const float2 *>(in.a.vy + b);
+                    float2 qd = *reinterpret_cast<const float2 *>(in.a.vz + b);
+                    float2 qf = *reinterpret_cast<const float2 *>(in.a.w + b);
+                    x[0] = qa.x; x[1] = qa.y;
+                    vx[0] = qb.x; vx[1] = qb.y;
+                    vy[0] = qc.x; vy[1] = qc.y;
+                    vz[0] = qd.x; vz[1] = qd.y;
+                    w[0] = qf.x; w[1] = qf.y;
+                  }
+                }
+                if (!vec) {
 #pragma unroll
                     for (int k = 0; k < SG_I; ++k) {
                         const bool ok = j0 + k < cnt;
@@ -104,31 +125,32 @@ __global__ void __launch_bounds__(SG_T, BZ_SEG_MINB)
                     }
                 }
                 Item<T> it[SG_I];
-                uint32_t ns = 0, nc = 0;
 #pragma unroll
                 for (int k = 0; k < SG_I; ++k) {
                     it[k].alive = false;
                     it[k].child = false;
                     it[k].ionized = false;
+                    it[k].excited = false;
                     if (w[k] > T(0)) {
                         push_item<T, REPLAY, XS>(p, kc, rng, uint32_t(rbase + j0 + k), x[k], vx[k], vy[k], vz[k], E_s,
                                                  xs_s, R, gas, it[k]);
-                        ns += it[k].alive;
-                        nc += it[k].child;
-                        if (!(isfinite(it[k].vx) && isfinite(it[k].vy) && isfinite(it[k].vz))) err |= BZ_DEV_NONFINITE;
+                        // one test for the three components (a sum of finite speeds stays finite)
+                        if (!isfinite(it[k].vx + it[k].vy + it[k].vz)) err |= BZ_DEV_NONFINITE;
                         if (DEPOSIT) {
                             if (it[k].alive) {
-                                int nd = p.advect ? node_index(it[k].x, nm) : 0;
+                                int nd = deposit_node(p.advect, it[k].x, nm);
                                 if (nd >= 0 && nd < nnodes) {
                                     atomicAdd(&mom_s[nd], A(w[k]));
                                     if (it[k].ionized) atomicAdd(&mom_s[nnodes + nd], A(w[k]));
                                     atomicAdd(&mom_s[2 * nnodes + nd], A(w[k] * it[k].e));
+                                    if (it[k].excited && (p.flags & BZ_MOMENT_EXCITATION))
+                                        atomicAdd(&moments[2 * nnodes + nd], double(w[k]));  // rare: straight to the grid
                                 }
                             } else if (it[k].ionized && (p.flags & BZ_QUIRK_DEAD_IONFLAG)) {
                                 atomicAdd(&mom_s[nnodes + 0], A(1));
                             }
                             if (it[k].child) {
-                                int nd = p.advect ? node_index(it[k].cx, nm) : 0;
+                                int nd = deposit_node(p.advect, it[k].cx, nm);
                                 if (nd >= 0 && nd < nnodes) {
                                     atomicAdd(&mom_s[nd], A(w[k]));
                                     atomicAdd(&mom_s[2 * nnodes + nd], A(w[k] * it[k].ce));
@@ -137,18 +159,19 @@ __global__ void __launch_bounds__(SG_T, BZ_SEG_MINB)
                         }
                     }
                 }
-                // warp scan of (ns, nc): 16+16 bits (at most 128 each per round)
-                const uint32_t v = ns | (nc << 16);
-                uint32_t incl = v;
+                // output offsets in input order (lane-major, then k): one ballot per flag and
+                // k; the lanes below contribute popc(mask & lanes_below)
+                const uint32_t below = (1u << lane) - 1u;
+                uint32_t ps = ns_off, pc = nc_off, ts = 0, tc = 0;
 #pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= o) incl += t;
+                for (int k = 0; k < SG_I; ++k) {
+                    const uint32_t ma = __ballot_sync(0xffffffffu, it[k].alive);
+                    const uint32_t mc = __ballot_sync(0xffffffffu, it[k].child);
+                    ps += __popc(ma & below);
+                    pc += __popc(mc & below);
+                    ts += __popc(ma);
+                    tc += __popc(mc);
                 }
-                const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
-                const uint32_t excl = incl - v;
-                uint32_t ps = ns_off + (excl & 0xffffu);
-                uint32_t pc = nc_off + (excl >> 16);
 #pragma unroll
                 for (int k = 0; k < SG_I; ++k) {
                     if (it[k].alive) {
@@ -172,8 +195,8 @@ __global__ void __launch_bounds__(SG_T, BZ_SEG_MINB)
                         ++pc;
                     }
                 }
-                ns_off += tot & 0xffffu;
-                nc_off += tot >> 16;
+                ns_off += ts;
+                nc_off += tc;
             }
         }
         if (lane == 0) {
@@ -328,13 +351,12 @@ __global__ void __launch_bounds__(1024) k_seg_set_counts(int32_t *cnt, int nseg,
 
 // moments of a segmented state (post_processing_1D.py:44-57), one warp per segment
 template <typename T>
-__global__ void __launch_bounds__(256) k_seg_deposit(bz_params p, Seg<T> s, double *moments) {
+__global__ void __launch_bounds__(256) k_seg_deposit(bz_params p, NodeMap nm, Seg<T> s, double *moments) {
     extern __shared__ __align__(16) unsigned char smem[];
     T *m = reinterpret_cast<T *>(smem);
     const int nn = p.n_nodes;
     for (int i = threadIdx.x; i < 3 * nn; i += blockDim.x) m[i] = T(0);
     __syncthreads();
-    const NodeMap nm = make_node_map(p);
     const T efac = T(0.5 * m_e() * j_ev());
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
@@ -345,7 +367,7 @@ __global__ void __launch_bounds__(256) k_seg_deposit(bz_params p, Seg<T> s, doub
             for (int j = lane; j < cnt; j += 32) {
                 const T wi = s.a.w[b + j];
                 if (!(wi > T(0))) continue;
-                const int nd = p.advect ? node_index(s.a.x[b + j], nm) : 0;
+                const int nd = deposit_node(p.advect, s.a.x[b + j], nm);
                 if (nd < 0 || nd >= nn) continue;
                 const T vx = s.a.vx[b + j], vy = s.a.vy[b + j], vz = s.a.vz[b + j];
                 atomicAdd(&m[nd], wi);
@@ -373,7 +395,8 @@ template <typename T, typename S> static Seg<T> to_seg(const S &s) {
     return Seg<T>{SoA<T>{s.x, s.vx, s.vy, s.vz, s.w}, s.counts, s.nseg, s.half};
 }
 
-template <typename T, bool REPLAY, int XS, bool DEPOSIT>
+template <typename T, bool REPLAY, int XS, bool DEPOSIT, int SG_T = kSegShapes[0].threads,
+          int SG_I = kSegShapes[0].per_lane, int MINB = kSegShapes[0].min_blocks>
 static int launch_seg_push(const bz_params &p, Seg<T> in, Seg<T> out, const T *E, const double *R, const double *gas,
                            double *moments, void *ws, uint32_t *seg_flags, uint32_t *status, cudaStream_t st) {
     using A = typename AccT<T>::t;
@@ -381,7 +404,7 @@ static int launch_seg_push(const bz_params &p, Seg<T> in, Seg<T> out, const T *E
     const int xsn = (XS == BZ_XS_TABLE) ? p.xs_n : 0;
     const size_t smem = size_t(xsn) * sizeof(float4) + (DEPOSIT ? size_t(3) * p.n_nodes * sizeof(A) : 0) +
                         size_t(nf) * sizeof(T);
-    auto kern = k_seg_push<T, REPLAY, XS, DEPOSIT>;
+    auto kern = k_seg_push<T, REPLAY, XS, DEPOSIT, SG_T, SG_I, MINB>;
     if (smem > 48 * 1024 &&
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess)
         return BZ_ERR_UNSUPPORTED;
@@ -391,7 +414,7 @@ static int launch_seg_push(const bz_params &p, Seg<T> in, Seg<T> out, const T *E
         return BZ_ERR_UNSUPPORTED;
     if (cudaMemsetAsync(ws, 0, 256, st) != cudaSuccess) return BZ_ERR_CUDA;
     int grid = num_sms() * per_sm;
-    grid = std::max(1, std::min(grid, int(ceil_div(in.nseg, SG_W))));
+    grid = std::max(1, std::min(grid, int(ceil_div(in.nseg, SG_T / 32))));
     kern<<<grid, SG_T, smem, st>>>(p, make_push_const<T>(p), in, out, E, R, gas, moments,
                                    static_cast<unsigned int *>(ws), seg_flags, status);
     return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
@@ -406,7 +429,9 @@ static int seg_push_entry(const bz_params *pp, S in_, S out_, const T *E, const 
     if (ws_bytes < 256) return BZ_ERR_WORKSPACE;
     if ((R == nullptr) != (gas == nullptr)) return BZ_ERR_ARG;
     const bz_params &p = *pp;
-    if (p.advect && (p.n_faces < 1 || p.dx <= 0 || p.L <= 0)) return BZ_ERR_ARG;
+    if (p.advect < BZ_ADVECT_NONE || p.advect > BZ_ADVECT_ENSEMBLE) return BZ_ERR_ARG;
+    if (p.advect == BZ_ADVECT_1D && (p.n_faces < 1 || p.dx <= 0 || p.L <= 0)) return BZ_ERR_ARG;
+    if (p.advect == BZ_ADVECT_ENSEMBLE && p.n_faces < 1) return BZ_ERR_ARG;
     if (p.n_nodes < 1 || p.bnf < 1) return BZ_ERR_ARG;
     if (p.xs_mode == BZ_XS_TABLE && (p.xs_n < 2 || !p.xs_table || !(p.xs_emax > p.xs_emin) || p.xs_emin <= 0))
         return BZ_ERR_ARG;
@@ -417,6 +442,24 @@ static int seg_push_entry(const bz_params *pp, S in_, S out_, const T *E, const 
     Seg<T> in = to_seg<T>(in_), out = to_seg<T>(out_);
     cudaStream_t st = as_stream(stream);
     const bool replay = R != nullptr, dep = moments != nullptr;
+    if constexpr (sizeof(T) == 4) {
+        if (!replay && p.xs_mode == BZ_XS_TABLE && dep) {  // the hot loop: tunable CTA shape
+#define BZ_SEG_SHAPE(K)                                                                                            \
+    case K:                                                                                                        \
+        return launch_seg_push<T, false, BZ_XS_TABLE, true, kSegShapes[K].threads, kSegShapes[K].per_lane,           \
+                               kSegShapes[K].min_blocks>(p, in, out, E, R, gas, moments, ws, seg_flags, status, st);
+            switch (g_seg_shape) {
+                BZ_SEG_SHAPE(1)
+                BZ_SEG_SHAPE(2)
+                BZ_SEG_SHAPE(3)
+                BZ_SEG_SHAPE(4)
+                BZ_SEG_SHAPE(5)
+                default: break;
+            }
+#undef BZ_SEG_SHAPE
+        }
+    }
+    static_assert(kSegNumShapes == 6, "one case per CTA shape");
 #define BZ_SEG_CASE(RP, XSM, DP)                                                                                    \
     if (replay == RP && p.xs_mode == XSM && dep == DP)                                                             \
         return launch_seg_push<T, RP, XSM, DP>(p, in, out, E, R, gas, moments, ws, seg_flags, status, st);
@@ -475,18 +518,72 @@ static int seg_repack_entry(const S *in_, P app_, const int32_t *app_n, int64_t 
     return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
 }
 
+// energy distribution per node (swarm): one warp per segment. The bin is taken from a
+// float log2 unless it lies within 1e-4 of a bin edge, where it is recomputed in float64
+// (the float estimate is off by far less than that).
+template <typename T>
+__global__ void __launch_bounds__(256) k_seg_eedf(bz_params p, NodeMap nm, Seg<T> s, int nbins, float a_f, float b_f,
+                                                  double lemin, double scale, double *hist) {
+    const double efac = 0.5 * m_e() * j_ev();
+    const float efac_f = float(efac);
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    const int nn = p.n_nodes;
+    for (int seg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; seg < s.nseg; seg += warps) {
+        for (int run = 0; run < 2; ++run) {
+            const int cnt = min(max(s.cnt[2 * seg + run], 0), s.half);
+            const int64_t b = seg_slot(seg, run, s.half, 0);
+            for (int j = lane; j < cnt; j += 32) {
+                const T wi = s.a.w[b + j];
+                if (!(wi > T(0))) continue;
+                const int nd = deposit_node(p.advect, s.a.x[b + j], nm);
+                if (nd < 0 || nd >= nn) continue;
+                const T vx = s.a.vx[b + j], vy = s.a.vy[b + j], vz = s.a.vz[b + j];
+                const float v2 = float(vx) * float(vx) + float(vy) * float(vy) + float(vz) * float(vz);
+                if (!(v2 > 0.f)) continue;
+                const float t = fmaf(__log2f(efac_f * v2), a_f, -b_f);
+                if (!(t > -1.f && t < float(nbins) + 1.f)) continue;  // far outside [emin, emax)
+                const float fr = t - floorf(t);
+                int k;
+                if (fr > 1e-4f && fr < 1.f - 1e-4f) {
+                    k = int(floorf(t));
+                } else {
+                    const double e = efac * (double(vx) * double(vx) + double(vy) * double(vy) + double(vz) * double(vz));
+                    if (!(e > 0.0)) continue;
+                    k = int(floor((log(e) - lemin) * scale));
+                }
+                if (k < 0 || k >= nbins) continue;
+                atomicAdd(&hist[int64_t(nd) * nbins + k], double(wi));
+            }
+        }
+    }
+}
+
+template <typename T, typename S>
+static int seg_eedf_entry(const bz_params *pp, S s_, int nbins, double emin, double emax, double *hist, void *stream) {
+    if (!pp || !hist || !seg_ok<T>(s_) || nbins < 1 || !(emin > 0) || !(emax > emin)) return BZ_ERR_ARG;
+    const bz_params &p = *pp;
+    if (p.n_nodes < 1 || p.bnf < 1 || (p.advect == BZ_ADVECT_1D && (p.dx <= 0 || p.L <= 0))) return BZ_ERR_ARG;
+    const double scale = double(nbins) / log(emax / emin);  // bins per e-fold
+    const int blocks = std::max(1, std::min(num_sms() * 8, int(ceil_div(s_.nseg, 8))));
+    k_seg_eedf<T><<<blocks, 256, 0, as_stream(stream)>>>(p, make_node_map(p), to_seg<T>(s_), nbins,
+                                                         float(scale * log(2.0)), float(log(emin) * scale),
+                                                         log(emin), scale, hist);
+    return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+}
+
 template <typename T, typename S>
 static int seg_deposit_entry(const bz_params *pp, S s_, double *moments, void *stream) {
     if (!pp || !moments || !seg_ok<T>(s_)) return BZ_ERR_ARG;
     const bz_params &p = *pp;
-    if (p.n_nodes < 1 || p.bnf < 1 || (p.advect && (p.dx <= 0 || p.L <= 0))) return BZ_ERR_ARG;
+    if (p.n_nodes < 1 || p.bnf < 1 || (p.advect == BZ_ADVECT_1D && (p.dx <= 0 || p.L <= 0))) return BZ_ERR_ARG;
     const size_t smem = size_t(3) * p.n_nodes * sizeof(T);
     auto kern = k_seg_deposit<T>;
     if (smem > 48 * 1024 &&
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess)
         return BZ_ERR_UNSUPPORTED;
     const int blocks = std::max(1, std::min(num_sms() * 4, int(ceil_div(s_.nseg, 8))));
-    kern<<<blocks, 256, smem, as_stream(stream)>>>(p, to_seg<T>(s_), moments);
+    kern<<<blocks, 256, smem, as_stream(stream)>>>(p, make_node_map(p), to_seg<T>(s_), moments);
     return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
 }
 
@@ -495,6 +592,20 @@ static int seg_deposit_entry(const bz_params *pp, S s_, double *moments, void *s
 extern "C" {
 
 size_t bz_seg_push_workspace(void) { return 256; }
+int32_t bz_seg_push_shapes(void) { return bz::kSegNumShapes; }
+int bz_seg_push_shape_info(int32_t shape, int32_t *threads, int32_t *per_lane, int32_t *min_blocks) {
+    if (shape < 0 || shape >= bz::kSegNumShapes) return BZ_ERR_ARG;
+    if (threads) *threads = bz::kSegShapes[shape].threads;
+    if (per_lane) *per_lane = bz::kSegShapes[shape].per_lane;
+    if (min_blocks) *min_blocks = bz::kSegShapes[shape].min_blocks;
+    return BZ_OK;
+}
+int bz_seg_push_select(int32_t shape) {
+    if (shape < 0 || shape >= bz::kSegNumShapes) return BZ_ERR_ARG;
+    bz::g_seg_shape = shape;
+    return BZ_OK;
+}
+int32_t bz_seg_push_selected(void) { return bz::g_seg_shape; }
 size_t bz_seg_repack_workspace(int32_t nseg_in) { return bz::RepackWs(nseg_in).total; }
 
 int bz_seg_push_collide_f32(const bz_params *p, bz_segments_f32 in, bz_segments_f32 out, const float *E,
@@ -526,6 +637,14 @@ int bz_seg_deposit_f32(const bz_params *p, bz_segments_f32 s, double *moments, v
 }
 int bz_seg_deposit_f64(const bz_params *p, bz_segments_f64 s, double *moments, void *stream) {
     return bz::seg_deposit_entry<double>(p, s, moments, stream);
+}
+int bz_seg_eedf_f32(const bz_params *p, bz_segments_f32 s, int32_t nbins, double emin, double emax, double *hist,
+                    void *stream) {
+    return bz::seg_eedf_entry<float>(p, s, nbins, emin, emax, hist, stream);
+}
+int bz_seg_eedf_f64(const bz_params *p, bz_segments_f64 s, int32_t nbins, double emin, double emax, double *hist,
+                    void *stream) {
+    return bz::seg_eedf_entry<double>(p, s, nbins, emin, emax, hist, stream);
 }
 
 }  // extern "C"

@@ -241,6 +241,51 @@ def seg_electron_kernel(params, src: SegmentSet, dst: SegmentSet, E, status, seg
          _ptr(replay_R), _ptr(replay_gas), _ptr(moments), _ptr(w), w.numel(), _ptr(seg_flags), _ptr(status), _stream())
 
 
+def seg_push_shapes():
+    """CTA shapes (threads, particles per lane, CTAs per SM) of the float32 table +
+    deposit segmented push; index 0 is the library default."""
+    lib = _lib.load()
+    out = []
+    for k in range(lib.bz_seg_push_shapes()):
+        t, i, m = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        call("bz_seg_push_shape_info", k, ctypes.byref(t), ctypes.byref(i), ctypes.byref(m))
+        out.append((t.value, i.value, m.value))
+    return out
+
+
+def select_seg_push_shape(k):
+    call("bz_seg_push_select", int(k))
+
+
+def autotune_seg_push(params, src: SegmentSet, dst: SegmentSet, E, status, seg_flags, ws: Workspace, moments,
+                      reps=5, warmup=2):
+    """Time every CTA shape of the float32 table + deposit push on src -> dst with CUDA
+    events and select the fastest (process-wide, for later launches and captures). src
+    is only read; dst, moments and the flag words are left as before the call. Returns
+    (selected index, per-shape milliseconds)."""
+    shapes = seg_push_shapes()
+    if src.dtype != torch.float32 or len(shapes) < 2:
+        return _lib.load().bz_seg_push_selected(), []
+    saved = (status.clone(), seg_flags.clone(), moments.clone(), dst.counts.clone())
+    st = torch.cuda.current_stream()
+    times = []
+    for k in range(len(shapes)):
+        select_seg_push_shape(k)
+        for _ in range(warmup):
+            seg_electron_kernel(params, src, dst, E, status, seg_flags, ws, moments=moments)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            seg_electron_kernel(params, src, dst, E, status, seg_flags, ws, moments=moments)
+        e1.record(st)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) / reps)
+    best = int(np.argmin(times))
+    select_seg_push_shape(best)
+    status.copy_(saved[0]); seg_flags.copy_(saved[1]); moments.copy_(saved[2]); dst.counts.copy_(saved[3])
+    return best, times
+
+
 def seg_repack(src, dst: SegmentSet, status, ws: Workspace, app: ParticleSet = None, app_n=None, only_if=None,
                clear=None, name="seg_repack"):
     """Particles with w != 0 of src (may be None), then app[0:n), spread over dst."""
@@ -258,6 +303,12 @@ def seg_repack(src, dst: SegmentSet, status, ws: Workspace, app: ParticleSet = N
 
 def seg_deposit(params, s: SegmentSet, moments):
     call(f"bz_seg_deposit_{s.suffix}", ctypes.byref(params), s.struct(), _ptr(moments), _stream())
+
+
+def seg_eedf(params, s: SegmentSet, hist, emin, emax):
+    """Add sum(w) per (deposit node, log energy bin) to hist [n_nodes, nbins] (float64)."""
+    call(f"bz_seg_eedf_{s.suffix}", ctypes.byref(params), s.struct(), int(hist.shape[1]), float(emin), float(emax),
+         _ptr(hist), _stream())
 
 
 def seg_bin_particles(params, s: SegmentSet, edges, min_wt, perm, offsets, counts, hw_counts, status, ws: Workspace):

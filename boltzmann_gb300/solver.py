@@ -51,14 +51,23 @@ class BoltzmannGB300:
         self.seg_flags = torch.zeros(1, dtype=torch.int32, device=dev)
         self.ws = K.Workspace(dev)
         K.seg_repack(None, self.A, self.status, self.ws, app=self.app)
-        # grid arrays (boltzmann.py:94-109)
-        self.E = torch.zeros(N, **f64)
+        # grid arrays (boltzmann.py:94-109). E, ni, Te and the moments are views of one
+        # float64 block so that a host loop moves them with one copy each way: the first
+        # 5N+4 values are the reference's per-step host->device block [E, ne, ni, ns, Te]
+        # (boltzmann.py:719-741; the ne and ns slots are host-side only, the device reads
+        # the deposited moments), followed by the moments [4][N+1] that post_processing
+        # returns (ne, ni_src, ns_src, nrg)
+        nn = self.nnodes
+        self.io = torch.zeros(5 * N + 4 + 4 * nn, **f64)
+        self.io_in = 5 * N + 4
+        self.E = self.io[0:N]
+        self.ni = self.io[2 * N + 1: 3 * N + 2]
+        self.Te = self.io[4 * N + 3: 5 * N + 4]
+        self.moments = self.io[5 * N + 4:].view(4, nn)
+        self.ni.copy_(torch.as_tensor(self._ne_profile(), **f64))
         self.E_push = torch.zeros(N, dtype=self.dtype, device=dev)
         self.V = torch.zeros(N - 1, **f64)
         self.Ji = torch.zeros(N, **f64)
-        self.moments = torch.zeros(4, self.nnodes, **f64)
-        self.ni = torch.as_tensor(self._ne_profile(), **f64).clone()
-        self.Te = torch.zeros(self.nnodes, **f64)
         self.g2 = torch.zeros(self.nnodes, **f64)
         self.chol_d = torch.zeros(max(N - 1, 1), **f64)
         self.chol_l = torch.zeros(max(N - 1, 1), **f64)
@@ -85,13 +94,20 @@ class BoltzmannGB300:
         self.bigstep = 0
         self.particle_steps = torch.zeros(1, dtype=torch.int64, device=dev)
         self._graphs = {}
-        self._seen = set()
+        self._kinds = set()
+        self._host_io = None
         if N >= 3:
             K.poisson_factor(N, cfg.dx, self.chol_d, self.chol_l)
         # first deposit and field solve (boltzmann.py:363-399)
         K.seg_deposit(self.params(), self.A, self.moments)
         self.ni.add_(self.moments[1])
         self._grid_solves(advance=False)
+        # CTA shape of the push, timed on the initial state (A is only read)
+        self.push_shape = None
+        if cfg.autotune and self.dtype == torch.float32:
+            best, times = K.autotune_seg_push(self.params(step_on_device=False), self.A, self.B, self.E_push,
+                                              self.status, self.seg_flags, self.ws, self.moments)
+            self.push_shape = {"shape": K.seg_push_shapes()[best], "ms": times}
 
     # ---------------------------------------------------------------------------------
     def _ne_profile(self):
@@ -199,6 +215,8 @@ class BoltzmannGB300:
 
     # --------------------------------------------------------------------------------- stepping
     def _step_body(self, resample):
+        if self._host_io is not None:  # _copy_to_GPU (boltzmann.py:719-741)
+            self.io[:self.io_in].copy_(self._host_io[:self.io_in], non_blocking=True)
         if resample:
             self._check_for_resampling()
             self._do_resampling()
@@ -206,28 +224,58 @@ class BoltzmannGB300:
             self._repack_if_needed()
         self.electron_kernel()
         self._grid_solves(advance=True)
+        if self._host_io is not None:  # back_to_cpu (post_processing_1D.py:6-24)
+            self._host_io.copy_(self.io, non_blocking=True)
 
     def step(self, use_graph=True):
-        """One step of the hybrid loop (boltzmann.py:570-678). With ``use_graph`` the
-        step is captured into a CUDA graph the second time its kind (resample or not,
-        which buffer holds the particles) occurs, and replayed from then on; the first
-        occurrence runs eagerly so that every kernel is loaded and configured before
-        any capture."""
+        """One step of the hybrid loop (boltzmann.py:570-678). With ``use_graph`` a step
+        kind (resample or not) runs eagerly the first time, so that every kernel is
+        loaded and configured; after that each (kind, which buffer holds the particles)
+        is captured into a CUDA graph once and replayed."""
         resample = (self.bigstep % self.cfg.resample_freq) == 0
         key = (resample, self.A is self._first_A())
-        if use_graph and key in self._seen:
-            gr = self._graphs.get(key)
-            if gr is None:
-                gr = self._capture(resample)
-                self._graphs[key] = gr
+        if use_graph and resample in self._kinds:
+            gr = self._graphs.get(key) or self._capture_key(key)
             gr.replay()
             # the graph swaps A and B internally; mirror the swaps on the host side
             for _ in range(2 if resample else 1):
                 self.A, self.B = self.B, self.A
         else:
-            self._seen.add(key)
+            self._kinds.add(resample)
             self._step_body(resample)
         self.bigstep += 1
+
+    def capture_all(self):
+        """Capture the graphs of every step kind that has run once, for both buffer
+        roles, so that no capture (which synchronises the device) falls inside a timed
+        loop."""
+        for resample in sorted(self._kinds):
+            for first in (True, False):
+                if (resample, first) not in self._graphs:
+                    self._capture_key((resample, first))
+
+    def attach_host_io(self, host_block):
+        """Make every step copy the first ``io_in`` values of a pinned host block (the
+        reference's per-step [E, ne, ni, ns, Te], boltzmann.py:719-741) to the device
+        before it runs and the whole grid block (those plus the moments) back after it,
+        inside the step's graph. ``None`` detaches. Graphs are re-captured."""
+        if host_block is not None:
+            if not host_block.is_pinned() or host_block.numel() != self.io.numel() or \
+                    host_block.dtype != torch.float64:
+                raise ValueError(f"host block must be pinned float64 of {self.io.numel()} values")
+        self._host_io = host_block
+        self._graphs = {}
+
+    def _capture_key(self, key):
+        resample, first = key
+        swap = (self.A is self._first_A()) != first
+        if swap:
+            self.A, self.B = self.B, self.A
+        g = self._capture(resample)
+        if swap:
+            self.A, self.B = self.B, self.A
+        self._graphs[key] = g
+        return g
 
     def _first_A(self):
         if not hasattr(self, "_A0"):
@@ -280,6 +328,16 @@ class BoltzmannGB300:
         return self
 
     # --------------------------------------------------------------------------------- diagnostics
+    def kernel_launches(self, resample):
+        """libbz kernels one step launches (torch's own memset/sum kernels not counted).
+        Every step: the push, grid update, clock, ion fluid and Poisson (5); a plain step
+        adds the two conditional repacks (count, scan, scatter, set counts: 4 each); a
+        resampling step adds binning (segment totals, key offsets twice, keys, then per
+        8-bit radix pass a histogram, scan and scatter), decide + apply (2) and the repack
+        of the survivors with the appended particles (5)."""
+        passes = 2 if self.nnodes * self.nb >= 256 else 1
+        return 5 + (4 + 3 * passes + 2 + 5 if resample else 8)
+
     def n(self):
         return self.A.n()
 

@@ -48,6 +48,16 @@ enum bz_status {
 #define BZ_QUIRK_TRIGGER_LAST 0x4u   /* resampling decided by the last bin's max test only
                                         (boltzmann.py:913-916, 3bin :1108-1111, 5bin :1329-1334) */
 #define BZ_FIX_MERGE_ENERGY 0x8u     /* merge rescales the thermal part only: energy conserving */
+#define BZ_PER_KEY_TARGETS 0x10u     /* resampling targets and max_ppc are given per (cell, bin) key
+                                        (key = cell*nbins + bin) instead of per bin */
+#define BZ_MOMENT_EXCITATION 0x20u   /* the push's deposit adds sum(w) of the particles that excited
+                                        this step to moments row 2 (ns_src, always 0 in the reference) */
+
+/* particle motion (bz_params.advect) */
+#define BZ_ADVECT_NONE 0      /* one 0-D swarm: no drift, E[0] everywhere, every particle in node/cell 0 */
+#define BZ_ADVECT_1D 1        /* 1D drift with absorbing walls at 0 and L; E at face int(x/dx) */
+#define BZ_ADVECT_ENSEMBLE 2  /* independent 0-D swarms: x holds the swarm index s (an integer value);
+                                 no drift; swarm s sees E[s] and deposits / bins into node / cell s */
 
 /* cross-section modes */
 #define BZ_XS_TABLE 0     /* n*sigma tables on a log energy grid (elastic, excitation, ionization) */
@@ -62,7 +72,7 @@ typedef struct bz_params {
     int32_t n_faces;
     int32_t n_nodes;
     int32_t bnf;        /* fine bins per node of the reference deposit (post_processing bnf) */
-    int32_t advect;     /* 1: 1D advection with absorbing walls at 0 and L; 0: 0-D swarm */
+    int32_t advect;     /* BZ_ADVECT_*: 1D advection, one 0-D swarm, or an ensemble of swarms */
     double L, dx;       /* cm */
     /* physics */
     double dt;          /* s */
@@ -226,6 +236,15 @@ int bz_seg_push_collide_f64(const bz_params *p, bz_segments_f64 in, bz_segments_
                             const double *replay_R, const double *replay_gas, double *moments,
                             void *workspace, size_t workspace_bytes, uint32_t *seg_flags,
                             uint32_t *status, void *stream);
+/* CTA shapes of the float32 table + deposit segmented push (threads per CTA, particles
+ * per lane per round, CTAs per SM the registers are budgeted for). Shape 0 is the
+ * default; bz_seg_push_select sets the shape later launches use (process-wide; select
+ * before capturing a graph). Results do not depend on the shape except for the
+ * summation order of the float moments. */
+int32_t bz_seg_push_shapes(void);
+int bz_seg_push_shape_info(int32_t shape, int32_t *threads, int32_t *per_lane, int32_t *min_blocks);
+int bz_seg_push_select(int32_t shape);
+int32_t bz_seg_push_selected(void);
 /* All particles with w != 0 of *in (segment order, run 0 then run 1; in may be NULL)
  * followed by app[0 .. *app_n) (may be absent: app_n NULL), spread over out's segments,
  * ceil(total/nseg) each in run 0. Skipped entirely when only_if != NULL and its
@@ -240,6 +259,15 @@ int bz_seg_repack_f64(const bz_segments_f64 *in, bz_particles_f64 app, const int
 /* Moments (sum w, 0, 0, sum w*energy) of a segmented state (no ion flags are stored). */
 int bz_seg_deposit_f32(const bz_params *p, bz_segments_f32 s, double *moments, void *stream);
 int bz_seg_deposit_f64(const bz_params *p, bz_segments_f64 s, double *moments, void *stream);
+/* Electron energy distribution: adds sum(w) per (node, energy bin) to hist[n_nodes][nbins]
+ * (float64, accumulated; zero it first). Bin k covers [emin r^k, emin r^(k+1)) eV with
+ * r = (emax/emin)^(1/nbins), i.e. k = floor(nbins ln(e/emin) / ln(emax/emin)) with e in
+ * float64 from the stored velocities; energies outside [emin, emax) are not counted. The
+ * node is the deposit node (the swarm in an ensemble). */
+int bz_seg_eedf_f32(const bz_params *p, bz_segments_f32 s, int32_t nbins, double emin, double emax, double *hist,
+                    void *stream);
+int bz_seg_eedf_f64(const bz_params *p, bz_segments_f64 s, int32_t nbins, double emin, double emax, double *hist,
+                    void *stream);
 /* Binning of a segmented state: as bz_bin_*, perm holds slot indices. */
 size_t bz_seg_bin_workspace(int32_t nseg, int64_t capacity);
 int bz_seg_bin_f32(const bz_params *p, bz_segments_f32 s, int32_t nbins, const double *edges, double min_wt,

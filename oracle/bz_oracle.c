@@ -136,7 +136,7 @@ static void sigma_table(const orc_params *p, double e, double *ns) {
 /* ------------------------------------------------------------------------------------ */
 /* push + collide (electron_kernel_numba.py:38-287)                                      */
 /* ------------------------------------------------------------------------------------ */
-typedef struct { double x, y, z, vx, vy, vz, w, e, flag; int child; double cx, cy, cz, cvx, cvy, cvz, ce, cw, margin; } push_out;
+typedef struct { double x, y, z, vx, vy, vz, w, e, flag; int child, exc; double cx, cy, cz, cvx, cvy, cvz, ce, cw, margin; } push_out;
 
 static void push_one(const orc_params *p, int64_t i, const double *in_d, const double *in_t, const double *E,
                      const double *R, const double *gas, push_out *o) {
@@ -200,6 +200,7 @@ static void push_one(const orc_params *p, int64_t i, const double *in_d, const d
         r2 = r1 + s2 * c;
     }
     o->child = 0;
+    o->exc = 0;
     o->flag = 0.0;
     double u0 = Ru[0];
     /* distance of the decision uniform to the nearest process boundary */
@@ -216,6 +217,7 @@ static void push_one(const orc_params *p, int64_t i, const double *in_d, const d
     } else if (r0 < u0 && u0 < r1) {
         /* excitation (table mode only; the reference has none): loss e_exc, isotropic */
         if ((e_el - p->e_exc) < 0.05 * e_el) o->margin = 0.0; /* ill-conditioned in float32 */
+        o->exc = 1;
         double cos_chi = 2 * Ru[1] - 1;
         double chi = acos(cos_chi);
         double phi = 2 * M_PI * Ru[2];
@@ -249,7 +251,12 @@ static void push_one(const orc_params *p, int64_t i, const double *in_d, const d
         o->cw = d_w;
     }
     int idx = 0;
-    if (p->advect) {
+    if (p->advect == 2) {
+        /* ensemble of 0-D swarms: x holds the swarm index, the swarm's field is E[x] */
+        idx = (int)xx;
+        if (idx < 0) idx = 0;
+        if (idx > p->n_faces - 1) idx = p->n_faces - 1;
+    } else if (p->advect) {
         /* X-ADV (electron_kernel_numba.py:258-260) with the post-collision velocity */
         double x_old = xx;
         xx += 100 * p->dt * vx;
@@ -261,8 +268,8 @@ static void push_one(const orc_params *p, int64_t i, const double *in_d, const d
         if (idx > p->n_faces - 1) idx = p->n_faces - 1;
     }
     vx -= p->dt * (q_e / m_e) * (100 * E[idx]);
-    int valid = p->advect ? ((0 < xx && xx < p->L) && d_w > 0) : (d_w > 0);
-    if (p->advect) o->margin = fmin(o->margin, fmin(fabs(xx), fabs(xx - p->L)) / p->L);
+    int valid = p->advect == 1 ? ((0 < xx && xx < p->L) && d_w > 0) : (d_w > 0);
+    if (p->advect == 1) o->margin = fmin(o->margin, fmin(fabs(xx), fabs(xx - p->L)) / p->L);
     o->w = valid * d_w;
     o->x = valid * xx + (1 - valid) * 0.00000001;
     o->y = valid * xy;
@@ -296,6 +303,7 @@ int64_t orc_push_margin(const orc_params *p, int64_t n, double *data, double *to
         }
         double *d = data + i * 6, *t = tosum + i * 4;
         if (o.flag != 0.0) t[1] = 1.0;
+        if (p->moment_exc) t[2] = (o.exc && o.w > 0) ? 1.0 : 0.0; /* survivors only, like the kernels */
         t[0] = o.w;
         d[0] = o.x; d[1] = o.y; d[2] = o.z;
         t[3] = o.e;
@@ -307,6 +315,14 @@ int64_t orc_push_margin(const orc_params *p, int64_t n, double *data, double *to
 /* ------------------------------------------------------------------------------------ */
 /* deposit: post_processing_1D.py:44-62 + kernels-new.cu reda (:56-73) / redcheck (:8-50) */
 /* ------------------------------------------------------------------------------------ */
+/* fine deposit bin int(((x + dx/2)/(L + dx)) * float(M)) (post_processing_1D.py:44); in an
+ * ensemble the swarm index times bnf (its node), for one 0-D swarm bin 0 */
+static int fine_bin(const orc_params *p, double x, double half, double Lp, double fM) {
+    if (p->advect == 1) return (int)(((x + half) / Lp) * fM);
+    if (p->advect == 2) return (int)x * p->bnf;
+    return 0;
+}
+
 static void deposit_impl(const orc_params *p, int64_t n_total, const double *data, const double *tosum,
                          double *moments, int weight_cols) {
     int RN = p->n_nodes;
@@ -315,11 +331,10 @@ static void deposit_impl(const orc_params *p, int64_t n_total, const double *dat
     double half = 0.5 * p->dx, Lp = p->L + p->dx;
     double fM = (double)(float)M;
     for (int64_t i = 0; i < n_total; ++i) {
-        double tx = (data[i * 6] + half) / Lp;
         const double *t = tosum + i * 4;
         double v[4] = {t[0], t[1], t[2], t[3]};
         if (weight_cols && t[0] > 0.0) { v[1] = t[1] * t[0]; v[2] = t[2] * t[0]; v[3] = t[3] * t[0]; }
-        int b = (int)(tx * fM);
+        int b = fine_bin(p, data[i * 6], half, Lp, fM);
         if (b < 0 || b >= M) continue;
         for (int j = 0; j < 4; ++j) fine[(size_t)b * 4 + j] += v[j];
     }
@@ -385,7 +400,7 @@ void orc_bin(const orc_params *p, int64_t n, const double *x, const double *vx, 
     for (int64_t k = 0; k < (int64_t)nb * max_ppc * RN; ++k) lists[k] = -1;
     for (int64_t j = 0; j < n; ++j) {
         if (!(w[j] > 0)) continue;
-        int64_t cc = p->advect ? (int64_t)((x[j] + 0.5 * p->dx) / p->dx) : 0;
+        int64_t cc = p->advect == 1 ? (int64_t)((x[j] + 0.5 * p->dx) / p->dx) : (p->advect == 2 ? (int64_t)x[j] : 0);
         if (cc < 0 || cc > RN - 1) continue;
         int b = 0;
         if (nb > 1) {
@@ -413,6 +428,25 @@ static int64_t upper_bound(const double *a, int64_t n, double v) { /* searchsort
     return lo;
 }
 
+void orc_eedf(const orc_params *p, int64_t n, const double *x, const double *vx, const double *vy,
+              const double *vz, const double *w, int nbins, double emin, double emax, double *hist) {
+    int RN = p->n_nodes;
+    int M = p->bnf * RN;
+    double half = 0.5 * p->dx, Lp = p->L + p->dx, fM = (double)(float)M;
+    double efac = 0.5 * c_me() * c_jev(), lemin = log(emin), scale = (double)nbins / log(emax / emin);
+    for (int64_t j = 0; j < n; ++j) {
+        if (!(w[j] > 0)) continue;
+        int fb = fine_bin(p, x[j], half, Lp, fM);
+        if (fb < 0 || fb >= M) continue;
+        int nd = fb / p->bnf;
+        double e = efac * (vx[j] * vx[j] + vy[j] * vy[j] + vz[j] * vz[j]);
+        if (!(e > 0)) continue;
+        double t = (log(e) - lemin) * scale;
+        if (!(t >= 0 && t < nbins)) continue;
+        hist[(int64_t)nd * nbins + (int)floor(t)] += w[j];
+    }
+}
+
 static int cmp_i64(const void *a, const void *b) {
     int64_t x = *(const int64_t *)a, y = *(const int64_t *)b;
     return (x > y) - (x < y);
@@ -421,20 +455,25 @@ static int cmp_i64(const void *a, const void *b) {
 int64_t orc_resample(const orc_params *p, int64_t n, double *data, double *tosum, int nb,
                      const int64_t *targets, double min_wt, const int64_t *max_ppc,
                      const int64_t *counts, const int64_t *lists, int64_t list_stride,
-                     const double *u, int64_t n_u, int64_t *n_used, int flags) {
+                     const double *u, int64_t n_u, int64_t *n_used, int flags, const double *thr) {
     const double m_e = c_me(), j_ev = c_jev();
     int RN = p->n_nodes;
+    /* split below thr[0]*T, merge at thr[1]*T down to int(thr[2]*T) survivors;
+     * the reference's 0.5, 3 and 0.6 (boltzmann.py:807, 826, 829) when thr is NULL */
+    const double split_below = thr ? thr[0] : 0.5, merge_at = thr ? thr[1] : 3.0,
+                 merge_keep = thr ? thr[2] : 0.6;
     int64_t Nc = n;
     int64_t ui = 0;
     /* list_stride = max list length stored per (bin, cell) */
     for (int cc = 0; cc < RN; ++cc) {
         for (int b = 0; b < nb; ++b) {
-            int64_t T = targets[b];
+            const int64_t tk = (flags & 0x10) ? (int64_t)cc * nb + b : b; /* per-key or per-bin */
+            int64_t T = targets[tk];
             int64_t cnt = counts[(int64_t)b * RN + cc];
             const int64_t *lst = lists + (int64_t)b * list_stride * RN; /* [slot][cell] */
 #define LIST(s) lst[(int64_t)(s) * RN + cc]
             /* too few: split (boltzmann.py:806-823) */
-            if (0 < cnt && (double)cnt < 0.5 * (double)T) {
+            if (0 < cnt && (double)cnt < split_below * (double)T) {
                 int64_t nhw = 0;
                 int64_t *hw = (int64_t *)malloc(sizeof(int64_t) * (size_t)cnt);
                 for (int64_t s = 0; s < cnt; ++s) { int64_t id = LIST(s); if (tosum[id * 4] > min_wt) hw[nhw++] = id; }
@@ -473,9 +512,9 @@ int64_t orc_resample(const orc_params *p, int64_t n, double *data, double *tosum
                 free(hw);
             }
             /* too many: merge (boltzmann.py:826-877) */
-            if ((double)cnt >= 3.0 * (double)T) {
-                int64_t np_ = cnt < max_ppc[b] ? cnt : max_ppc[b];
-                int64_t K = (int64_t)(0.6 * (double)T);
+            if ((double)cnt >= merge_at * (double)T) {
+                int64_t np_ = cnt < max_ppc[tk] ? cnt : max_ppc[tk];
+                int64_t K = (int64_t)(merge_keep * (double)T);
                 double W = 0.0, sx = 0.0, sy = 0.0, sz = 0.0, se = 0.0;
                 for (int64_t s = 0; s < np_; ++s) W += tosum[LIST(s) * 4];
                 for (int64_t s = 0; s < np_; ++s) { int64_t id = LIST(s); sx += data[id * 6 + 3] * tosum[id * 4]; }
@@ -622,18 +661,21 @@ int64_t orc_step_omp(const orc_params *p, int64_t n, int64_t cap, double *data, 
             push_one(p, i, data + i * 6, tosum + i * 4, E, NULL, NULL, &o);
             int b;
             if (o.w > 0) {
-                b = (int)(((o.x + half) / Lp) * fM);
-                if (b >= 0 && b < M) { my[b * 4 + 0] += o.w; my[b * 4 + 1] += o.flag * o.w; my[b * 4 + 3] += o.e * o.w; }
+                b = fine_bin(p, o.x, half, Lp, fM);
+                if (b >= 0 && b < M) {
+                    my[b * 4 + 0] += o.w; my[b * 4 + 1] += o.flag * o.w; my[b * 4 + 3] += o.e * o.w;
+                    if (p->moment_exc && o.exc) my[b * 4 + 2] += o.w;
+                }
                 double *d = data_tmp + (lo + ns) * 6, *t = tosum_tmp + (lo + ns) * 4;
                 d[0] = o.x; d[1] = o.y; d[2] = o.z; d[3] = o.vx; d[4] = o.vy; d[5] = o.vz;
                 t[0] = o.w; t[1] = 0; t[2] = 0; t[3] = o.e;
                 ++ns;
             } else if (o.flag != 0.0) {
-                b = (int)(((o.x + half) / Lp) * fM);
+                b = fine_bin(p, o.x, half, Lp, fM);
                 if (b >= 0 && b < M) my[b * 4 + 1] += o.flag;
             }
             if (o.child) {
-                b = (int)(((o.cx + half) / Lp) * fM);
+                b = fine_bin(p, o.cx, half, Lp, fM);
                 if (b >= 0 && b < M) { my[b * 4 + 0] += o.cw; my[b * 4 + 3] += o.ce * o.cw; }
                 /* children are parked in the second half of the temporaries (capacity 2n) */
                 double *d = data_tmp + (n + lo + nc) * 6, *t = tosum_tmp + (n + lo + nc) * 4;

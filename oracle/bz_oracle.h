@@ -36,6 +36,7 @@ typedef struct orc_params {
     const float *xs_table;
     double nu_max;      /* null-collision bound, s^-1 (coll_model 1) */
     double e_exc;       /* excitation threshold and loss, eV (table mode) */
+    int moment_exc;     /* 1: tosum column 2 holds this step's excitation flag (deposited as sum w) */
 } orc_params;
 
 /* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11). */
@@ -75,12 +76,19 @@ void orc_bin(const orc_params *p, int64_t n, const double *x, const double *vx, 
  * counts/lists from orc_bin. Random numbers are consumed from u[] in processing order
  * (cell ascending, bins ascending in energy; split draws then merge draws).
  * flags bit0: reproduce the reference's split indexing (HW_ids[unique_ids[v]] with
- * CuPy's wrap-around); bit1: energy-conserving merge rescale (thermal part only).
+ * CuPy's wrap-around); bit1: energy-conserving merge rescale (thermal part only);
+ * bit4: targets and max_ppc per (cell, bin) key, index cell*nb + bin.
+ * thr = {split_below, merge_at, merge_keep}, or NULL for the reference's 0.5, 3, 0.6.
  * Returns the particle count after the final compaction; *n_used = uniforms consumed. */
 int64_t orc_resample(const orc_params *p, int64_t n, double *data, double *tosum, int nb,
                      const int64_t *targets, double min_wt, const int64_t *max_ppc,
                      const int64_t *counts, const int64_t *lists, int64_t list_stride,
-                     const double *u, int64_t n_u, int64_t *n_used, int flags);
+                     const double *u, int64_t n_u, int64_t *n_used, int flags, const double *thr);
+
+/* Energy distribution per deposit node (the swarm in an ensemble): hist[n_nodes][nbins]
+ * += w in bin floor(nbins ln(e/emin)/ln(emax/emin)); energies outside [emin, emax) skipped. */
+void orc_eedf(const orc_params *p, int64_t n, const double *x, const double *vx, const double *vy,
+              const double *vz, const double *w, int nbins, double emin, double emax, double *hist);
 
 /* EF_kernel_1D.py:7-44 with the banded Cholesky factor of boltzmann.py:744-755. */
 void orc_poisson(int N, double dx, double eps0, double V0, double freq, double t, const double *ne,

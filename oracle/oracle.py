@@ -28,6 +28,7 @@ class OrcParams(ctypes.Structure):
         ("seed", ctypes.c_uint64), ("step", ctypes.c_uint64), ("gas_sigma", ctypes.c_double),
         ("xs_n", ctypes.c_int), ("xs_emin", ctypes.c_double), ("xs_emax", ctypes.c_double),
         ("xs_table", ctypes.c_void_p), ("nu_max", ctypes.c_double), ("e_exc", ctypes.c_double),
+        ("moment_exc", ctypes.c_int),
     ]
 
 
@@ -66,8 +67,10 @@ def lib():
                               ctypes.c_int64, _i64p, _i64p]
         L.orc_resample.argtypes = [P, ctypes.c_int64, _f64p, _f64p, ctypes.c_int, _i64p, ctypes.c_double, _i64p,
                                    _i64p, _i64p, ctypes.c_int64, _f64p, ctypes.c_int64,
-                                   ctypes.POINTER(ctypes.c_int64), ctypes.c_int]
+                                   ctypes.POINTER(ctypes.c_int64), ctypes.c_int, ctypes.c_void_p]
         L.orc_resample.restype = ctypes.c_int64
+        L.orc_eedf.argtypes = [P, ctypes.c_int64, _f64p, _f64p, _f64p, _f64p, _f64p, ctypes.c_int, ctypes.c_double,
+                               ctypes.c_double, _f64p]
         L.orc_poisson.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                   ctypes.c_double, _f64p, _f64p, _f64p, _f64p]
         L.orc_fluid.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
@@ -82,7 +85,7 @@ def lib():
 
 def make_params(N, L=2.54, bnf=4, dt=1e-12, nn=3.22e22, xs_mode=0, coll_model=0, advect=1, rng_mode=0,
                 precision=32, seed=0, step=0, gas_sigma=0.0, xs_table=None, xs_emin=0.01, xs_emax=1000.0,
-                nu_max=0.0, e_exc=11.5):
+                nu_max=0.0, e_exc=11.5, moment_exc=0):
     """Parameters for an N-face / N+1-node grid. ``xs_table`` is an [3, n] float32 n*sigma table."""
     p = OrcParams()
     p.n_faces = N
@@ -102,6 +105,7 @@ def make_params(N, L=2.54, bnf=4, dt=1e-12, nn=3.22e22, xs_mode=0, coll_model=0,
     p.gas_sigma = gas_sigma
     p.nu_max = nu_max
     p.e_exc = e_exc
+    p.moment_exc = int(moment_exc)
     p._keep = None
     if xs_table is not None:
         tab = np.ascontiguousarray(xs_table, dtype=np.float32)
@@ -170,15 +174,27 @@ def bin_particles(p, x, vx, vy, vz, w, edges, max_ppc):
     return counts, lists
 
 
-def resample(p, data, tosum, n, nb, targets, min_wt, max_ppc, counts, lists, u, flags=1):
+def resample(p, data, tosum, n, nb, targets, min_wt, max_ppc, counts, lists, u, flags=1, thr=None):
+    """thr = (split_below, merge_at, merge_keep); None: the reference's (0.5, 3, 0.6).
+    flags bit 4 (0x10): targets / max_ppc per (cell, bin) key, index cell*nb + bin."""
     used = ctypes.c_int64(0)
+    thr_a = None if thr is None else np.ascontiguousarray(thr, dtype=np.float64)
     targets = np.ascontiguousarray(targets, dtype=np.int64)
     max_ppc = np.ascontiguousarray(max_ppc, dtype=np.int64)
     u = np.ascontiguousarray(u, dtype=np.float64) if len(u) else np.zeros(1)
     na = lib().orc_resample(ctypes.byref(p), n, data, tosum, nb, targets, float(min_wt), max_ppc,
                             np.ascontiguousarray(counts, dtype=np.int64), np.ascontiguousarray(lists, dtype=np.int64),
-                            lists.shape[1], u, len(u), ctypes.byref(used), flags)
+                            lists.shape[1], u, len(u), ctypes.byref(used), flags,
+                            None if thr_a is None else thr_a.ctypes.data_as(ctypes.c_void_p))
     return na, used.value
+
+
+def eedf(p, x, vx, vy, vz, w, nbins, emin, emax):
+    hist = np.zeros((p.n_nodes, nbins))
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    lib().orc_eedf(ctypes.byref(p), len(x), f(x), f(vx), f(vy), f(vz), f(w), int(nbins), float(emin), float(emax),
+                   hist)
+    return hist
 
 
 def poisson(N, dx, eps0, V0, freq, t, ne, ni):

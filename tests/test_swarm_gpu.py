@@ -1,0 +1,282 @@
+"""GPU parity of the 0-D swarm ensemble (BZ_ADVECT_ENSEMBLE: x holds the swarm index).
+
+The push, binning, per-(swarm, bin) resampling and the energy distribution are checked
+against the oracle's ensemble mode on the same inputs; the driver is checked for graph
+replay = eager stepping, for its bookkeeping, and statistically against an ensemble of
+independent oracle swarms (mean energy, ionization rate coefficient and energy
+distribution).
+"""
+import math
+import os
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+from boltzmann_gb300 import _lib, kernels as K, swarm, xsec  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+from test_push_gpu import check_state, velocity_scale  # noqa: E402
+
+DT = {"f32": torch.float32, "f64": torch.float64}
+NN = 3.22e22
+
+
+def td_to_vcm(td):
+    return np.asarray(td) * 1e-21 * NN / 100.0
+
+
+def gpu_params(S, tab, xt, dt, flags, seed, step, gas=250.0):
+    return K.make_params(n_faces=S, n_nodes=S, bnf=1, advect=_lib.ADVECT_ENSEMBLE, L=float(S), dx=1.0, dt=dt, nn=NN,
+                         gas_sigma=gas, e_exc=tab.e_exc, xs_mode=_lib.XS_TABLE, xs_table=xt, xs_emin=tab.emin,
+                         xs_emax=tab.emax, flags=flags, seed=seed, step=step)
+
+
+def oracle_params(S, tab, dt, seed, step, prec, gas=250.0, moment_exc=1):
+    p = O.make_params(S, L=float(S), bnf=1, dt=dt, nn=NN, advect=2, rng_mode=1, precision=prec, seed=seed, step=step,
+                      gas_sigma=gas, xs_table=tab.nsigma(NN), xs_emin=tab.emin, xs_emax=tab.emax, e_exc=tab.e_exc,
+                      moment_exc=moment_exc)
+    p.n_nodes = S
+    p.dx = 1.0
+    return p
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_ensemble_push_matches_oracle(prec):
+    rng = np.random.default_rng(31)
+    S, per, nseg, half = 64, 1500, 96, 2048
+    n = S * per
+    dt = 1e-10
+    x = np.repeat(np.arange(S, dtype=np.float64), per)
+    v = rng.normal(0, 2.0e6, (n, 3)).astype(np.float32).astype(np.float64)
+    w = np.ones(n)
+    E = td_to_vcm(np.geomspace(10, 1000, S)).astype(np.float32).astype(np.float64)
+    seg = K.SegmentSet(nseg, half, DT[prec])
+    seg.load(x, v[:, 0], v[:, 1], v[:, 2], w)
+    cap = seg.capacity
+    sl = seg.slots("segments")
+    st_np = seg.to_numpy("segments")
+    arr = {f: np.zeros(cap) for f in K.SegmentSet.FIELDS}
+    for f in K.SegmentSet.FIELDS:
+        arr[f][sl] = st_np[f]
+    tab = xsec.analytic_argon(2000)
+    op = oracle_params(S, tab, dt, 6, 9, 64 if prec == "f64" else 32)
+    data, tosum = O.soa_to_aos(arr["x"], arr["vx"], arr["vy"], arr["vz"], arr["w"], cap=2 * cap)
+    _, margin = O.push_margin(op, data.copy(), tosum.copy(), cap, E)
+    amb = (margin < 1e-5) & (arr["w"] > 0)
+    arr["w"][amb] = 0.0
+    seg.w[torch.as_tensor(np.nonzero(amb)[0], device="cuda")] = 0.0
+    data, tosum = O.soa_to_aos(arr["x"], arr["vx"], arr["vy"], arr["vz"], arr["w"], cap=2 * cap)
+    nni = O.push(op, data, tosum, cap, E)
+    assert nni > 100
+    vs = velocity_scale(np.zeros(cap), np.stack([arr["vx"], arr["vy"], arr["vz"]], 1), arr["w"], tosum[:cap, 0] > 0,
+                        np.zeros(1), dt, 1.0, 1, data[cap:cap + nni, 3:6])
+    # the kick of a 0-D swarm uses its own field: widen the scale by it
+    kick = dt * (1.602 * 1e-19 / (9.10938 * 1e-31)) * 100.0 * np.abs(E).max()
+    vs = vs + kick
+    mom_o, nnew = O.post(op, data, tosum, cap + nni)
+    xt = torch.as_tensor(tab.nsigma(NN), device="cuda")
+    p = gpu_params(S, tab, xt, dt, _lib.MOMENT_EXCITATION, 6, 9)
+    out = K.SegmentSet(nseg, half, DT[prec])
+    mom = torch.zeros(4, S, dtype=torch.float64, device="cuda")
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    fl = torch.zeros(1, dtype=torch.int32, device="cuda")
+    Et = torch.as_tensor(E, dtype=DT[prec], device="cuda")
+    K.seg_electron_kernel(p, seg, out, Et, st, fl, K.Workspace(), moments=mom)
+    torch.cuda.synchronize()
+    assert int(st.item()) == 0
+    o = out.to_numpy("runs")
+    assert len(o["x"]) == nnew
+    assert int(out.counts.cpu().numpy()[1::2].sum()) == nni
+    np.testing.assert_array_equal(o["x"], data[:nnew, 0])  # every particle stays in its swarm
+    rtol = 1e-10 if prec == "f64" else 1e-6
+    check_state(o, data[:nnew, 0], data[:nnew, 3:6], tosum[:nnew, 0], rtol, dt=dt, vscale=vs)
+    m = mom.cpu().numpy()
+    for j in (0, 1, 2, 3):
+        np.testing.assert_allclose(m[j], mom_o[j], rtol=1e-10 if prec == "f64" else 1e-5,
+                                   atol=1e-12 * np.abs(mom_o[j]).max())
+    assert m[2].sum() > 10  # excitations were counted
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_ensemble_bins_and_per_swarm_resampling_match_oracle(prec):
+    """Binning keys on the swarm; split and merge with per-(swarm, bin) targets; counts
+    exact, particles to the resampling tolerance, replayed uniforms."""
+    rng = np.random.default_rng(5)
+    S = 24
+    sizes = rng.integers(800, 5000, S)
+    x = np.repeat(np.arange(S, dtype=np.float64), sizes)
+    n = len(x)
+    v = rng.normal(0, 1.2e6, (n, 3)) * rng.uniform(0.3, 1.6, n)[:, None]
+    v = v.astype(np.float32).astype(np.float64)
+    w = rng.uniform(0.05, 2.0, n).astype(np.float32).astype(np.float64)
+    edges = (4.0, 11.5)
+    nb = 3
+    targets = np.array([[int(f * c) for f in (0.5, 0.3, 0.2)] for c in rng.integers(600, 3000, S)], dtype=np.int64)
+    tflat = targets.reshape(-1)
+    max_ppc = 10 * tflat
+    tab = xsec.analytic_argon(2000)
+    op = oracle_params(S, tab, 1e-12, 0, 0, 64)
+    counts_o, lists_o = O.bin_particles(op, x, v[:, 0], v[:, 1], v[:, 2], w, list(edges), int(max_ppc.max()))
+    u = rng.random(400_000)
+    d, t = O.soa_to_aos(x, v[:, 0], v[:, 1], v[:, 2], w, cap=6 * n)
+    na, used = O.resample(op, d, t, n, nb, tflat, 0.1, max_ppc, counts_o, lists_o, u, flags=0x10 | 0x1)
+    assert used > 0 and na != n
+    # GPU, dense particle set
+    s = K.ParticleSet(6 * n, DT[prec])
+    out = K.ParticleSet(6 * n, DT[prec])
+    s.load(x, v[:, 0], v[:, 1], v[:, 2], w)
+    xt = torch.as_tensor(tab.nsigma(NN), device="cuda")
+    p = gpu_params(S, tab, xt, 1e-12, _lib.PER_KEY_TARGETS | _lib.QUIRK_SPLIT_WRAP, 0, 0)
+    nkeys = S * nb
+    ed = torch.as_tensor(np.asarray(edges), device="cuda")
+    perm = torch.zeros(s.capacity, dtype=torch.int32, device="cuda")
+    offsets = torch.zeros(nkeys + 1, dtype=torch.int32, device="cuda")
+    counts = torch.zeros(nkeys, dtype=torch.int32, device="cuda")
+    hw = torch.zeros(nkeys, dtype=torch.int32, device="cuda")
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    need = torch.zeros(1, dtype=torch.int32, device="cuda")
+    ws = K.Workspace()
+    K.bin_particles(p, s, ed, 0.1, perm, offsets, counts, hw, st, ws)
+    np.testing.assert_array_equal(counts.cpu().numpy().reshape(S, nb).T, counts_o)
+    tg = torch.as_tensor(tflat.astype(np.int32), device="cuda")
+    mp = torch.as_tensor(max_ppc.astype(np.int32), device="cuda")
+    ru = torch.as_tensor(u, device="cuda")
+    K.resample(p, s, out, nb, tg, mp, 0.1, 0.5, 3.0, 0.6, perm, offsets, counts, hw, st, ws, need=need, replay_u=ru)
+    torch.cuda.synchronize()
+    assert int(st.item()) == 0 and int(need.item()) == 1
+    o = out.to_numpy()
+    assert len(o["x"]) == na
+    rtol = 1e-12 if prec == "f64" else 2e-6
+    np.testing.assert_array_equal(o["x"], d[:na, 0])
+    np.testing.assert_allclose(o["w"], t[:na, 0], rtol=rtol)
+    speed = np.sqrt((d[:na, 3:6] ** 2).sum(axis=1))
+    for k, f in enumerate(("vx", "vy", "vz")):
+        assert np.all(np.abs(o[f] - d[:na, 3 + k]) <= rtol * speed * 4)
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_eedf_matches_oracle(prec):
+    rng = np.random.default_rng(12)
+    S, per = 16, 5000
+    x = np.repeat(np.arange(S, dtype=np.float64), per)
+    n = len(x)
+    v = (rng.normal(0, 1.0e6, (n, 3)) * rng.uniform(0.05, 4.0, n)[:, None]).astype(np.float32).astype(np.float64)
+    w = rng.uniform(0.5, 1.5, n).astype(np.float32).astype(np.float64)
+    seg = K.SegmentSet(100, 1024, DT[prec])
+    seg.load(x, v[:, 0], v[:, 1], v[:, 2], w)
+    tab = xsec.analytic_argon(2000)
+    xt = torch.as_tensor(tab.nsigma(NN), device="cuda")
+    p = gpu_params(S, tab, xt, 1e-12, 0, 0, 0)
+    h = torch.zeros(S, 64, dtype=torch.float64, device="cuda")
+    K.seg_eedf(p, seg, h, 0.01, 100.0)
+    torch.cuda.synchronize()
+    ho = O.eedf(oracle_params(S, tab, 1e-12, 0, 0, 64), x, v[:, 0], v[:, 1], v[:, 2], w, 64, 0.01, 100.0)
+    np.testing.assert_allclose(h.cpu().numpy(), ho, rtol=1e-12, atol=1e-9)
+    e = 0.5 * 9.10938e-31 * 6.241509e18 * (v ** 2).sum(axis=1)
+    inside = (e >= 0.01) & (e < 100.0)
+    assert inside.sum() > 0.5 * n
+    np.testing.assert_allclose(ho.sum(), w[inside].sum(), rtol=1e-6)
+
+
+def _small_ensemble(**kw):
+    base = dict(E_over_N_Td=tuple(np.geomspace(30, 1000, 12)), counts=(3000,) * 12, precision="float32",
+                bin_edges=(4.0, 11.5), bin_fractions=(0.7, 0.2, 0.1), merge_at=3.0, merge_keep=0.6,
+                resample_every=10, dt=5e-12, seed=4)
+    base.update(kw)
+    return swarm.SwarmConfig(**base)
+
+
+def test_ensemble_graph_replay_equals_eager():
+    a = swarm.SwarmEnsemble(_small_ensemble())
+    b = swarm.SwarmEnsemble(_small_ensemble())
+    a.run(45, use_graph=True)
+    b.run(45, use_graph=False)
+    torch.cuda.synchronize()
+    assert a.device_status() == 0 and b.device_status() == 0
+    sa, sb = a.A.to_numpy("segments"), b.A.to_numpy("segments")
+    for f in K.SegmentSet.FIELDS:
+        np.testing.assert_array_equal(sa[f], sb[f])
+    np.testing.assert_allclose(a.mean_energy(), b.mean_energy(), rtol=1e-5)
+    assert int(a.particle_steps.item()) == int(b.particle_steps.item())
+
+
+def test_ensemble_bookkeeping_and_trends():
+    e = swarm.SwarmEnsemble(_small_ensemble())
+    e.run(400)
+    torch.cuda.synchronize()
+    assert e.device_status() == 0
+    # every particle is in its swarm; per-swarm weights match the state
+    st = e.A.to_numpy("segments")
+    per = np.bincount(st["x"].astype(int), weights=st["w"], minlength=e.S)
+    np.testing.assert_allclose(per, e.counts(), rtol=1e-5)
+    me = e.mean_energy()
+    kiz, kex = e.rate_coefficients()
+    assert np.all(np.isfinite(me)) and np.all(me > 0)
+    # heating and inelastic rates rise with the reduced field
+    print("E/N", np.round(e.cfg.E_over_N_Td, 1), "mean energy", np.round(me, 3), "k_iz", kiz, "k_ex", kex)
+    rank = np.argsort(np.argsort(me))
+    assert np.corrcoef(np.arange(e.S), rank)[0, 1] > 0.8
+    assert me[-3:].mean() > 2 * me[:3].mean()
+    assert kex[-1] > kex[0] and kiz[-1] > 0
+    f = e.eedf()
+    np.testing.assert_allclose(f.sum(axis=1), 1.0, rtol=1e-12)
+
+
+def test_swarm_matches_oracle_ensemble_statistically():
+    """8 independent swarms at 500 Td (float64, 2e4 particles each, 1200 steps of 1 ps)
+    on the GPU against 8 independent oracle swarms: mean energy within 1% + 4 sigma of
+    the seed scatter, ionization rate coefficient within 4 sigma, energy distributions
+    within 0.02 in total variation."""
+    S, per, steps, dt, td = 8, 20_000, 1200, 1e-12, 500.0
+    cfg = swarm.SwarmConfig(E_over_N_Td=(td,) * S, counts=(per,) * S, precision="float64", dt=dt, seed=11,
+                            merge_at=50.0, resample_every=10_000, capacity_factor=4.0, T_gas=300.0)
+    e = swarm.SwarmEnsemble(cfg)
+    e.run(steps // 2)
+    e.reset_averages()
+    e.run(steps - steps // 2)
+    torch.cuda.synchronize()
+    assert e.device_status() == 0
+    me_g = e.mean_energy()
+    kiz_g, _ = e.rate_coefficients()
+    f_g = e.eedf(nbins=32, emin=0.1, emax=100.0).mean(axis=0)
+    # oracle: a lone 0-D swarm per seed, OpenMP
+    tab = xsec.analytic_argon(2000)
+    E = td_to_vcm([td])
+    gas = math.sqrt(1.380649e-23 * 300.0 / 6.6e-26)
+    me_o, kiz_o, f_o = [], [], []
+    lib = O.lib()
+    import ctypes
+    for s in range(S):
+        rng = np.random.default_rng(100 + s)
+        v = rng.normal(0, math.sqrt(1.0 * 1.5 * 1.17255e11), (per, 3))
+        cap = 4 * per
+        d, t = O.soa_to_aos(np.zeros(per), v[:, 0], v[:, 1], v[:, 2], np.ones(per), cap=cap)
+        dtmp, ttmp = np.zeros((2 * cap, 6)), np.zeros((2 * cap, 4))
+        p = O.make_params(1, L=1.0, bnf=1, dt=dt, nn=NN, advect=0, rng_mode=1, precision=64, seed=1000 + s,
+                          gas_sigma=gas, xs_table=tab.nsigma(NN), xs_emin=tab.emin, xs_emax=tab.emax, e_exc=tab.e_exc)
+        p.n_nodes = 1
+        mom = np.zeros((4, 1))
+        n = per
+        acc = np.zeros(4)
+        pre = 0.0
+        for k in range(steps):
+            p.step = k
+            n_new = lib.orc_step_omp(ctypes.byref(p), n, cap, d, t, dtmp, ttmp, E, mom, os.cpu_count() or 1)
+            assert n_new > 0
+            if k >= steps // 2:
+                acc += mom[:, 0]
+                pre += mom[0, 0] - mom[1, 0]
+            n = int(n_new)
+        me_o.append(acc[3] / acc[0])
+        kiz_o.append(acc[1] / (pre * NN * dt))
+        f_o.append(O.eedf(p, np.zeros(n), d[:n, 3], d[:n, 4], d[:n, 5], t[:n, 0], 32, 0.1, 100.0)[0] / t[:n, 0].sum())
+    me_o, kiz_o, f_o = np.array(me_o), np.array(kiz_o), np.mean(f_o, axis=0)
+    sig_me = math.sqrt(me_g.var(ddof=1) / S + me_o.var(ddof=1) / S)
+    assert abs(me_g.mean() - me_o.mean()) <= 0.01 * me_o.mean() + 4 * sig_me, (me_g.mean(), me_o.mean(), sig_me)
+    sig_k = math.sqrt(kiz_g.var(ddof=1) / S + kiz_o.var(ddof=1) / S)
+    assert kiz_o.mean() > 0
+    assert abs(kiz_g.mean() - kiz_o.mean()) <= 4 * sig_k + 0.01 * kiz_o.mean(), (kiz_g.mean(), kiz_o.mean(), sig_k)
+    assert 0.5 * np.abs(f_g - f_o).sum() < 0.02
