@@ -302,16 +302,20 @@ def run_ours(args, world, rank, local, pg):
         torch.cuda.synchronize()
         ps_e0 = int(sol.particle_steps.item())
         t0 = time.perf_counter()
+        marks = []
         for _ in range(K2):
             sol.step()
             torch.cuda.synchronize()
+            marks.append(time.perf_counter())
         el = time.perf_counter() - t0
         sol.attach_host_io(None)
+        per = np.diff(np.array([t0] + marks)) * 1e3
         ps_e = int(sol.particle_steps.item()) - ps_e0
         el = max_over_ranks(pg, el, dev)
         ps_e = sum_over_ranks(pg, ps_e, dev)
         e2e = {"value": ps_e / el, "unit": UNIT, "h2d_bytes_per_step": int(n_in * 8),
-               "d2h_bytes_per_step": int(sol.io.numel() * 8), "steps": K2}
+               "d2h_bytes_per_step": int(sol.io.numel() * 8), "steps": K2,
+               "ms_per_step_median": float(np.median(per)), "ms_per_step_max": float(per.max())}
 
     if rank != 0:
         return

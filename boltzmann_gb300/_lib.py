@@ -92,16 +92,18 @@ _PROTOS = {
     "bz_compact_f64": (ctypes.c_int, [Particles, _vp, _i64, Particles, _i64, _vp, _vp, _sz, _vp, _vp]),
     "bz_grid_update": (ctypes.c_int, [_i32, _vp, _vp, _vp, _vp, _vp]),
     "bz_ion_fluid": (ctypes.c_int, [_i32, _f64, _f64, _f64, _f64, _vp, _vp, _vp, _vp, _vp]),
-    "bz_poisson_factor": (ctypes.c_int, [_i32, _f64, _vp, _vp]),
-    "bz_poisson": (ctypes.c_int, [_i32, _f64, _f64, _f64, _f64, _f64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "bz_poisson_factor": (ctypes.c_int, [_i32, _f64, _vp, _vp, _vp]),
+    "bz_poisson": (ctypes.c_int, [_i32, _f64, _f64, _f64, _f64, _f64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "bz_advance_clock": (ctypes.c_int, [_vp, _vp, _f64, _vp]),
     "bz_seg_push_workspace": (_sz, []),
     "bz_seg_push_shapes": (ctypes.c_int32, []),
     "bz_seg_push_shape_info": (ctypes.c_int, [ctypes.c_int32, _vp, _vp, _vp]),
     "bz_seg_push_select": (ctypes.c_int, [ctypes.c_int32]),
     "bz_seg_push_selected": (ctypes.c_int32, []),
-    "bz_seg_push_collide_f32": (ctypes.c_int, [_P, Segments, Segments, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp, _vp]),
-    "bz_seg_push_collide_f64": (ctypes.c_int, [_P, Segments, Segments, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp, _vp]),
+    "bz_seg_push_collide_f32": (ctypes.c_int, [_P, Segments, Segments, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp,
+                                               _vp]),
+    "bz_seg_push_collide_f64": (ctypes.c_int, [_P, Segments, Segments, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp,
+                                               _vp]),
     "bz_seg_repack_workspace": (_sz, [_i32]),
     "bz_seg_repack_f32": (ctypes.c_int, [ctypes.POINTER(Segments), Particles, _vp, _i64, Segments, _vp, _sz, _vp,
                                          _vp, _vp, _vp]),
@@ -109,6 +111,8 @@ _PROTOS = {
                                          _vp, _vp, _vp]),
     "bz_seg_deposit_f32": (ctypes.c_int, [_P, Segments, _vp, _vp]),
     "bz_seg_deposit_f64": (ctypes.c_int, [_P, Segments, _vp, _vp]),
+    "bz_seg_rebalance_f32": (ctypes.c_int, [Segments, Segments, _vp, _sz, _vp, _vp, _vp, _vp]),
+    "bz_seg_rebalance_f64": (ctypes.c_int, [Segments, Segments, _vp, _sz, _vp, _vp, _vp, _vp]),
     "bz_seg_eedf_f32": (ctypes.c_int, [_P, Segments, ctypes.c_int32, ctypes.c_double, ctypes.c_double, _vp, _vp]),
     "bz_seg_eedf_f64": (ctypes.c_int, [_P, Segments, ctypes.c_int32, ctypes.c_double, ctypes.c_double, _vp, _vp]),
     "bz_seg_bin_workspace": (_sz, [_i32, _i64]),

@@ -51,8 +51,15 @@ __global__ void __launch_bounds__(1024) k_ion_fluid(int N, double dx, double dt,
 }
 
 // banded Cholesky factor of tridiag(-1, 2, -1)/dx^2 (what boltzmann.py:744-755 gets from
-// scipy.linalg.cholesky_banded): d[0] = sqrt(a), l[i] = b/d[i-1], d[i] = sqrt(a - l[i]^2)
-__global__ void k_poisson_factor(int N, double dx, double *d, double *l) {
+// scipy.linalg.cholesky_banded): d[0] = sqrt(a), l[i] = b/d[i-1], d[i] = sqrt(a - l[i]^2).
+// The two substitutions of the solve are first-order recurrences z_i = a_i z_{i-1} + b_i
+// with constant a_i, so they are precomputed here as prefix products: forward
+// y_i = (r_i - l_i y_{i-1})/d_i = P_i sum_{k<=i} r_k g_k with P_i = prod_{k=1..i}(-l_k/d_k),
+// g_k = 1/(d_k P_k); backward V_i = (y_i - l_{i+1} V_{i+1})/d_i = Q_i sum_{k>=i} y_k h_k with
+// Q_i = prod_{k=i..n-2}(-l_{k+1}/d_k), h_k = 1/(d_k Q_k). For this matrix P_i =
+// sqrt(2/((i+1)(i+2))) and Q_i = (i+1)/n: no overflow, no cancellation in the products.
+// plan = [P | g | Q | h], n = N-1 each. One thread: called once per grid.
+__global__ void k_poisson_factor(int N, double dx, double *d, double *l, double *plan) {
     if (threadIdx.x || blockIdx.x) return;
     int n = N - 1;
     double a = 2. / (dx * dx), b = -1. / (dx * dx);
@@ -62,49 +69,60 @@ __global__ void k_poisson_factor(int N, double dx, double *d, double *l) {
         l[i] = b / d[i - 1];
         d[i] = sqrt(a - l[i] * l[i]);
     }
+    double *P = plan, *g = plan + n, *Q = plan + 2 * n, *h = plan + 3 * n;
+    double pr = 1.0;
+    for (int i = 0; i < n; ++i) {
+        if (i > 0) pr = pr * (-l[i] / d[i]);
+        P[i] = pr;
+        g[i] = 1.0 / (d[i] * pr);
+    }
+    pr = 1.0;
+    for (int i = n - 1; i >= 0; --i) {
+        if (i < n - 1) pr = pr * (-l[i + 1] / d[i]);
+        Q[i] = pr;
+        h[i] = 1.0 / (d[i] * pr);
+    }
 }
-
-// EF_kernel_1D.py:26-42: forward/back substitution with the Cholesky factor, then face
-// fields. Each substitution is a first-order linear recurrence z_i = a_i z_{i-1} + b_i,
-// solved as a block-wide inclusive scan of affine maps (a, b) composed as
-// (a2, b2) o (a1, b1) = (a2 a1, a2 b1 + b2), 1024 rows per chunk with the carry
-// between chunks. One CTA; everything is float64.
-struct Aff { double a, b; };
-__device__ __forceinline__ Aff aff_compose(Aff early, Aff late) { return {late.a * early.a, late.a * early.b + late.b}; }
 
 constexpr int PS_T = 1024;
 
-__device__ Aff block_aff_scan(Aff v, Aff *sh) {
+// inclusive block-wide sum of v over PS_T threads in index order
+__device__ double block_inclusive_sum(double v, double *sh) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        Aff t{__shfl_up_sync(0xffffffffu, v.a, o), __shfl_up_sync(0xffffffffu, v.b, o)};
-        if (lane >= o) v = aff_compose(t, v);
+        double t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
     }
     if (lane == 31) sh[warp] = v;
     __syncthreads();
     if (warp == 0) {
-        Aff w = sh[lane];
+        double w = sh[lane];
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            Aff t{__shfl_up_sync(0xffffffffu, w.a, o), __shfl_up_sync(0xffffffffu, w.b, o)};
-            if (lane >= o) w = aff_compose(t, w);
+            double t = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += t;
         }
-        sh[lane] = w;  // inclusive over warps
+        sh[lane] = w;
     }
     __syncthreads();
-    if (warp > 0) v = aff_compose(sh[warp - 1], v);
+    if (warp > 0) v += sh[warp - 1];
     __syncthreads();
     return v;
 }
 
+// EF_kernel_1D.py:26-42: forward and backward substitution with the factor (as the two
+// prefix sums of the plan), then face fields. One CTA, float64; rows in chunks of PS_T
+// with the running sum carried between chunks. y (the forward result) lives in E until
+// the faces overwrite it.
 __global__ void __launch_bounds__(PS_T) k_poisson(int N, double dx, double eps0, double V0, double freq,
                                                   double t_host, const double *t_dev, const double *ne,
-                                                  const double *ni, const double *d, const double *l, double *V,
-                                                  double *E, float *E32, double *y) {
-    __shared__ Aff sh[32];
+                                                  const double *ni, const double *plan, double *V, double *E,
+                                                  float *E32, double *y) {
+    __shared__ double sh[32];
     __shared__ double carry, vs_s;
     const int n = N - 1;
+    const double *P = plan, *g = plan + n, *Q = plan + 2 * n, *h = plan + 3 * n;
     // electrode voltage, evaluated once (float64 sin is costly on this part's narrow FP64 pipe)
     if (threadIdx.x == 0) {
         const double t = t_dev ? *t_dev : t_host;
@@ -113,39 +131,32 @@ __global__ void __launch_bounds__(PS_T) k_poisson(int N, double dx, double eps0,
     }
     __syncthreads();
     const double vs = vs_s;
-    // forward: y_i = (1/d_i)(r_i - l_i y_{i-1}), r_i = (ni - ne)/eps0 (+ boundary term at i = 0)
+    // forward: r_i = (ni - ne)/eps0 (+ boundary term at i = 0); y_i = P_i sum_{k<=i} r_k g_k
     for (int c0 = 0; c0 < n; c0 += PS_T) {
-        int i = c0 + threadIdx.x;
-        Aff v{1.0, 0.0};
+        const int i = c0 + threadIdx.x;
+        double c = 0.0;
         if (i < n) {
             double r = (1.0 / eps0) * (ni[i + 1] - ne[i + 1]);
             if (i == 0) r = r + (1.0 / (dx * dx)) * vs;
-            double inv = 1.0 / d[i];
-            v = (i == 0) ? Aff{0.0, r / d[0]} : Aff{-inv * l[i], inv * r};
+            c = r * g[i];
         }
-        Aff pre = block_aff_scan(v, sh);
-        double yi = pre.a * carry + pre.b;
-        if (i < n) y[i] = yi;
+        const double s = block_inclusive_sum(c, sh) + carry;
+        if (i < n) y[i] = P[i] * s;
         __syncthreads();
-        if (i == min(c0 + PS_T, n) - 1) carry = yi;
+        if (i == min(c0 + PS_T, n) - 1) carry = s;
         __syncthreads();
     }
-    // backward: V_i = (1/d_i)(y_i - l_{i+1} V_{i+1}), V_{n-1} = y_{n-1}/d_{n-1}
+    // backward: V_i = Q_i sum_{k>=i} y_k h_k (rows taken from the end)
     if (threadIdx.x == 0) carry = 0.0;
     __syncthreads();
     for (int c0 = 0; c0 < n; c0 += PS_T) {
-        int j = c0 + threadIdx.x;  // j-th row from the end
-        int i = n - 1 - j;
-        Aff v{1.0, 0.0};
-        if (j < n) {
-            double inv = 1.0 / d[i];
-            v = (j == 0) ? Aff{0.0, y[i] / d[i]} : Aff{-inv * l[i + 1], inv * y[i]};
-        }
-        Aff pre = block_aff_scan(v, sh);
-        double vi = pre.a * carry + pre.b;
-        if (j < n) V[i] = vi;
+        const int j = c0 + threadIdx.x;  // j-th row from the end
+        const int i = n - 1 - j;
+        const double c = (j < n) ? y[i] * h[i] : 0.0;
+        const double s = block_inclusive_sum(c, sh) + carry;
+        if (j < n) V[i] = Q[i] * s;
         __syncthreads();
-        if (j == min(c0 + PS_T, n) - 1) carry = vi;
+        if (j == min(c0 + PS_T, n) - 1) carry = s;
         __syncthreads();
     }
     // faces (EF_kernel_1D.py:39-42)
@@ -180,20 +191,20 @@ int bz_ion_fluid(int32_t N, double dx, double dt, double mu_i, double D_i, const
     bz::k_ion_fluid<<<1, 1024, 0, bz::as_stream(stream)>>>(N, dx, dt, mu_i, D_i, E, ni, Ji, brk);
     return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
 }
-int bz_poisson_factor(int32_t N, double dx, double *chol_diag, double *chol_lower) {
-    if (N < 3 || !chol_diag || !chol_lower) return BZ_ERR_ARG;
-    bz::k_poisson_factor<<<1, 32>>>(N, dx, chol_diag, chol_lower);
+int bz_poisson_factor(int32_t N, double dx, double *chol_diag, double *chol_lower, double *plan) {
+    if (N < 3 || !chol_diag || !chol_lower || !plan) return BZ_ERR_ARG;
+    bz::k_poisson_factor<<<1, 32>>>(N, dx, chol_diag, chol_lower, plan);
     if (cudaGetLastError() != cudaSuccess) return BZ_ERR_CUDA;
     return cudaDeviceSynchronize() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
 }
 int bz_poisson(int32_t N, double dx, double eps0, double V0, double freq, double t_host, const double *t_dev,
-               const double *ne, const double *ni, const double *chol_diag, const double *chol_lower, double *V,
-               double *E, float *E32, void *stream) {
-    if (N < 3 || !ne || !ni || !chol_diag || !chol_lower || !V || !E) return BZ_ERR_ARG;
+               const double *ne, const double *ni, const double *plan, double *V, double *E, float *E32,
+               void *stream) {
+    if (N < 3 || !ne || !ni || !plan || !V || !E) return BZ_ERR_ARG;
     // E doubles as the scratch of the forward substitution: it is written only after
     // the backward substitution has consumed y (both inside the same CTA).
-    bz::k_poisson<<<1, bz::PS_T, 0, bz::as_stream(stream)>>>(N, dx, eps0, V0, freq, t_host, t_dev, ne, ni, chol_diag,
-                                                              chol_lower, V, E, E32, E);
+    bz::k_poisson<<<1, bz::PS_T, 0, bz::as_stream(stream)>>>(N, dx, eps0, V0, freq, t_host, t_dev, ne, ni, plan, V,
+                                                              E, E32, E);
     return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
 }
 int bz_advance_clock(double *t_dev, uint64_t *step_dev, double dt, void *stream) {

@@ -14,6 +14,8 @@
 // BZ_SEG_NEEDS_REPACK; k_seg_repack* then spreads all particles evenly again.
 #include <algorithm>
 
+#include <cooperative_groups.h>
+
 #include "bz_push_core.cuh"
 
 namespace bz {
@@ -40,7 +42,8 @@ __device__ __forceinline__ int64_t seg_slot(int seg, int run, int half, int j) {
 template <typename T, bool REPLAY, int XS, bool DEPOSIT, int SG_T, int SG_I, int MINB>
 __global__ void __launch_bounds__(SG_T, MINB)
     k_seg_push(bz_params p, PushConst<T> kc, Seg<T> in, Seg<T> out, const T *E, const double *R, const double *gas,
-               double *moments, unsigned int *ticket, uint32_t *seg_flags, uint32_t *status) {
+               double *moments, unsigned long long *n_pushed, unsigned int *ticket, uint32_t *seg_flags,
+               uint32_t *status) {
     using A = typename AccT<T>::t;
     constexpr int SG_R = 32 * SG_I;  // particles per warp round
     extern __shared__ __align__(16) unsigned char smem[];
@@ -76,6 +79,7 @@ __global__ void __launch_bounds__(SG_T, MINB)
                 err |= BZ_DEV_CAPACITY;
                 cnt = cnt < 0 ? 0 : H;
             }
+            if (n_pushed && lane == 0 && cnt > 0) atomicAdd(n_pushed, (unsigned long long)cnt);
             const int64_t rbase = seg_slot(seg, run, H, 0);
             for (int r0 = 0; r0 < cnt; r0 += SG_R) {
                 const int j0 = r0 + lane * SG_I;
@@ -222,54 +226,15 @@ __global__ void __launch_bounds__(SG_T, MINB)
 // ------------------------------------------------------------------------------------
 // repack: all particles with w != 0, in order (segment by segment, run 0 then run 1,
 // then an optional dense append buffer), spread evenly over the output segments
-// (fill = ceil(total / nseg) in run 0). Count -> scan -> scatter; deterministic.
+// (fill = ceil(total / nseg) in run 0). Count -> scan -> scatter -> set counts, as the
+// phases of one cooperative kernel separated by grid-wide barriers (the launch
+// guarantees that every CTA is resident); deterministic. Conditional on the request flag:
+// every CTA reads it at entry and it is cleared only after the last barrier.
 // ------------------------------------------------------------------------------------
+constexpr int RP_T = 256;
+
 __device__ __forceinline__ bool repack_skip(const uint32_t *only_if) {
     return only_if && !(*only_if & BZ_SEG_NEEDS_REPACK);
-}
-
-template <typename T>
-__global__ void k_seg_count_live(Seg<T> in, int32_t *live, const uint32_t *only_if) {
-    if (repack_skip(only_if)) return;
-    const int lane = threadIdx.x & 31;
-    const int warps = (gridDim.x * blockDim.x) >> 5;
-    for (int seg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; seg < in.nseg; seg += warps) {
-        int c = 0;
-        for (int run = 0; run < 2; ++run) {
-            const int cnt = min(max(in.cnt[2 * seg + run], 0), in.half);
-            const int64_t b = seg_slot(seg, run, in.half, 0);
-            for (int j = lane; j < cnt; j += 32) c += (in.a.w[b + j] != T(0));
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-        if (lane == 0) live[seg] = c;
-    }
-}
-
-// exclusive scan of live[0..m) into pre[0..m], one CTA; pre[m] = total
-__global__ void __launch_bounds__(1024) k_scan_live(const int32_t *live, int m, const int32_t *app_n,
-                                                    int64_t app_cap, int32_t *pre, const uint32_t *only_if) {
-    if (repack_skip(only_if)) return;
-    __shared__ int64_t part[1024];
-    const int per = (m + 1023) / 1024;
-    const int lo = threadIdx.x * per, hi = min(m, lo + per);
-    int64_t s = 0;
-    for (int k = lo; k < hi; ++k) s += live[k];
-    part[threadIdx.x] = s;
-    __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {
-        int64_t t = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
-        __syncthreads();
-        part[threadIdx.x] += t;
-        __syncthreads();
-    }
-    int64_t run = part[threadIdx.x] - s;
-    for (int k = lo; k < hi; ++k) { pre[k] = int32_t(run); run += live[k]; }
-    if (threadIdx.x == 1023) {
-        int64_t a = app_n ? min(int64_t(max(*app_n, 0)), app_cap) : 0;
-        pre[m] = int32_t(part[1023]);
-        pre[m + 1] = int32_t(part[1023] + a);  // total including the append buffer
-    }
 }
 
 template <typename T>
@@ -289,14 +254,57 @@ __device__ __forceinline__ int repack_fill(int64_t total, int nseg) {
 }
 
 template <typename T>
-__global__ void k_seg_scatter(Seg<T> in, const int32_t *pre, Seg<T> out, const uint32_t *only_if,
-                              uint32_t *status) {
-    if (repack_skip(only_if)) return;
+__global__ void __launch_bounds__(RP_T) k_seg_repack(Seg<T> in, SoA<T> app, const int32_t *app_n, int64_t app_cap,
+                                                     Seg<T> out, Seg<T> back, int32_t *live, int32_t *pre,
+                                                     const uint32_t *only_if, uint32_t *seg_flags, uint32_t *status) {
+    cooperative_groups::grid_group grid = cooperative_groups::this_grid();
+    if (repack_skip(only_if)) return;  // uniform: the flag is cleared after the last barrier
+    __shared__ int64_t part[RP_T];
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
-    const int fill = repack_fill(pre[in.nseg + 1], out.nseg);
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int m = in.nseg;
+    // 1. live particles per input segment
+    for (int seg = gw; seg < m; seg += warps) {
+        int c = 0;
+        for (int run = 0; run < 2; ++run) {
+            const int cnt = min(max(in.cnt[2 * seg + run], 0), in.half);
+            const int64_t b = seg_slot(seg, run, in.half, 0);
+            for (int j = lane; j < cnt; j += 32) c += (in.a.w[b + j] != T(0));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+        if (lane == 0) live[seg] = c;
+    }
+    grid.sync();
+    // 2. exclusive scan (CTA 0): pre[0..m), pre[m] = live total, pre[m+1] = + appended
+    if (blockIdx.x == 0) {
+        const int per = (m + RP_T - 1) / RP_T;
+        const int lo = threadIdx.x * per, hi = min(m, lo + per);
+        int64_t sum = 0;
+        for (int k = lo; k < hi; ++k) sum += live[k];
+        part[threadIdx.x] = sum;
+        __syncthreads();
+        for (int o = 1; o < RP_T; o <<= 1) {
+            const int64_t t = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+            __syncthreads();
+            part[threadIdx.x] += t;
+            __syncthreads();
+        }
+        int64_t run = part[threadIdx.x] - sum;
+        for (int k = lo; k < hi; ++k) { pre[k] = int32_t(run); run += live[k]; }
+        if (threadIdx.x == RP_T - 1) {
+            const int64_t a = app_n ? min(int64_t(max(*app_n, 0)), app_cap) : 0;
+            pre[m] = int32_t(part[RP_T - 1]);
+            pre[m + 1] = int32_t(part[RP_T - 1] + a);
+        }
+    }
+    grid.sync();
+    // 3. scatter: input segments (warp per segment, ballot compaction), then the appended
+    const int64_t total = pre[m + 1];
+    const int fill = repack_fill(total, out.nseg);
     uint32_t err = 0;
-    for (int seg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; seg < in.nseg; seg += warps) {
+    for (int seg = gw; seg < m; seg += warps) {
         int64_t off = pre[seg];
         for (int run = 0; run < 2; ++run) {
             const int cnt = min(max(in.cnt[2 * seg + run], 0), in.half);
@@ -304,49 +312,48 @@ __global__ void k_seg_scatter(Seg<T> in, const int32_t *pre, Seg<T> out, const u
             for (int j0 = 0; j0 < cnt; j0 += 32) {
                 const int j = j0 + lane;
                 const bool ok = j < cnt;
-                T w = ok ? in.a.w[b + j] : T(0);
+                const T w = ok ? in.a.w[b + j] : T(0);
                 const bool keep = ok && w != T(0);
-                const unsigned m = __ballot_sync(0xffffffffu, keep);
+                const unsigned mk = __ballot_sync(0xffffffffu, keep);
                 if (keep) {
-                    const int64_t v = off + __popc(m & ((1u << lane) - 1u));
+                    const int64_t v = off + __popc(mk & ((1u << lane) - 1u));
                     repack_put(out, v, fill, in.a.x[b + j], in.a.vx[b + j], in.a.vy[b + j], in.a.vz[b + j], w, err);
                 }
-                off += __popc(m);
+                off += __popc(mk);
             }
         }
     }
-    if (err) atomicOr(status, err);
-}
-
-template <typename T>
-__global__ void k_app_scatter(SoA<T> app, const int32_t *app_n, int64_t app_cap, const int32_t *pre, int nseg_in,
-                              Seg<T> out, const uint32_t *only_if, uint32_t *status) {
-    if (repack_skip(only_if)) return;
-    const int64_t base = pre[nseg_in];
-    const int64_t total = pre[nseg_in + 1];
-    const int64_t n = total - base;
-    const int fill = repack_fill(total, out.nseg);
-    uint32_t err = 0;
-    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n && i < app_cap;
-         i += int64_t(gridDim.x) * blockDim.x)
-        repack_put(out, base + i, fill, app.x[i], app.vx[i], app.vy[i], app.vz[i], app.w[i], err);
-    if (err) atomicOr(status, err);
-}
-
-// one CTA: every thread reads the request flag before thread 0 clears it
-__global__ void __launch_bounds__(1024) k_seg_set_counts(int32_t *cnt, int nseg, int half, const int32_t *pre,
-                                                         int nseg_in, uint32_t *seg_flags, const uint32_t *only_if) {
-    const bool skip = repack_skip(only_if);
-    __syncthreads();
-    if (skip) return;
-    const int64_t total = pre[nseg_in + 1];
-    const int fill = repack_fill(total, nseg);
-    for (int s = threadIdx.x; s < nseg; s += blockDim.x) {
-        int64_t c = min(max(total - int64_t(s) * fill, int64_t(0)), int64_t(min(fill, half)));
-        cnt[2 * s] = int32_t(c);
-        cnt[2 * s + 1] = 0;
+    if (app_n) {
+        const int64_t base = pre[m];
+        const int64_t na = total - base;
+        for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < na && i < app_cap;
+             i += int64_t(gridDim.x) * blockDim.x)
+            repack_put(out, base + i, fill, app.x[i], app.vx[i], app.vy[i], app.vz[i], app.w[i], err);
     }
-    if (threadIdx.x == 0 && seg_flags) *seg_flags = 0u;  // repacked: clear the request
+    if (err) atomicOr(status, err);
+    grid.sync();
+    // 4. output counts
+    for (int s2 = blockIdx.x * blockDim.x + threadIdx.x; s2 < out.nseg; s2 += gridDim.x * blockDim.x) {
+        const int64_t c = min(max(total - int64_t(s2) * fill, int64_t(0)), int64_t(min(fill, out.half)));
+        out.cnt[2 * s2] = int32_t(c);
+        out.cnt[2 * s2 + 1] = 0;
+    }
+    // 5. optionally copy the balanced layout back (same geometry): run 0 of every segment
+    if (back.nseg > 0) {
+        grid.sync();
+        const int64_t nslots = int64_t(out.nseg) * fill;
+        for (int64_t v = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; v < min(nslots, total);
+             v += int64_t(gridDim.x) * blockDim.x) {
+            const int seg = int(v / fill), j = int(v - int64_t(seg) * fill);
+            if (j >= out.half) continue;  // an overflowing layout was already reported
+            const int64_t q = seg_slot(seg, 0, out.half, j);
+            back.a.x[q] = out.a.x[q]; back.a.vx[q] = out.a.vx[q]; back.a.vy[q] = out.a.vy[q];
+            back.a.vz[q] = out.a.vz[q]; back.a.w[q] = out.a.w[q];
+        }
+        for (int s2 = blockIdx.x * blockDim.x + threadIdx.x; s2 < 2 * out.nseg; s2 += gridDim.x * blockDim.x)
+            back.cnt[s2] = out.cnt[s2];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && seg_flags) *seg_flags = 0u;  // the request is served
 }
 
 // moments of a segmented state (post_processing_1D.py:44-57), one warp per segment
@@ -398,7 +405,8 @@ template <typename T, typename S> static Seg<T> to_seg(const S &s) {
 template <typename T, bool REPLAY, int XS, bool DEPOSIT, int SG_T = kSegShapes[0].threads,
           int SG_I = kSegShapes[0].per_lane, int MINB = kSegShapes[0].min_blocks>
 static int launch_seg_push(const bz_params &p, Seg<T> in, Seg<T> out, const T *E, const double *R, const double *gas,
-                           double *moments, void *ws, uint32_t *seg_flags, uint32_t *status, cudaStream_t st) {
+                           double *moments, uint64_t *n_pushed, void *ws, uint32_t *seg_flags, uint32_t *status,
+                           cudaStream_t st) {
     using A = typename AccT<T>::t;
     const int nf = p.advect ? p.n_faces : 1;
     const int xsn = (XS == BZ_XS_TABLE) ? p.xs_n : 0;
@@ -416,13 +424,15 @@ static int launch_seg_push(const bz_params &p, Seg<T> in, Seg<T> out, const T *E
     int grid = num_sms() * per_sm;
     grid = std::max(1, std::min(grid, int(ceil_div(in.nseg, SG_T / 32))));
     kern<<<grid, SG_T, smem, st>>>(p, make_push_const<T>(p), in, out, E, R, gas, moments,
-                                   static_cast<unsigned int *>(ws), seg_flags, status);
+                                   reinterpret_cast<unsigned long long *>(n_pushed), static_cast<unsigned int *>(ws),
+                                   seg_flags, status);
     return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
 }
 
 template <typename T, typename S>
 static int seg_push_entry(const bz_params *pp, S in_, S out_, const T *E, const double *R, const double *gas,
-                          double *moments, void *ws, size_t ws_bytes, uint32_t *seg_flags, uint32_t *status,
+                          double *moments, uint64_t *n_pushed, void *ws, size_t ws_bytes, uint32_t *seg_flags,
+                          uint32_t *status,
                           void *stream) {
     if (!pp || !E || !ws || !status || !seg_flags || !seg_ok<T>(in_) || !seg_ok<T>(out_)) return BZ_ERR_ARG;
     if (in_.nseg != out_.nseg || in_.half != out_.half) return BZ_ERR_ARG;
@@ -447,7 +457,8 @@ static int seg_push_entry(const bz_params *pp, S in_, S out_, const T *E, const 
 #define BZ_SEG_SHAPE(K)                                                                                            \
     case K:                                                                                                        \
         return launch_seg_push<T, false, BZ_XS_TABLE, true, kSegShapes[K].threads, kSegShapes[K].per_lane,           \
-                               kSegShapes[K].min_blocks>(p, in, out, E, R, gas, moments, ws, seg_flags, status, st);
+                               kSegShapes[K].min_blocks>(p, in, out, E, R, gas, moments, n_pushed, ws, seg_flags,  \
+                                                         status, st);
             switch (g_seg_shape) {
                 BZ_SEG_SHAPE(1)
                 BZ_SEG_SHAPE(2)
@@ -462,7 +473,7 @@ static int seg_push_entry(const bz_params *pp, S in_, S out_, const T *E, const 
     static_assert(kSegNumShapes == 6, "one case per CTA shape");
 #define BZ_SEG_CASE(RP, XSM, DP)                                                                                    \
     if (replay == RP && p.xs_mode == XSM && dep == DP)                                                             \
-        return launch_seg_push<T, RP, XSM, DP>(p, in, out, E, R, gas, moments, ws, seg_flags, status, st);
+        return launch_seg_push<T, RP, XSM, DP>(p, in, out, E, R, gas, moments, n_pushed, ws, seg_flags, status, st);
     BZ_SEG_CASE(false, BZ_XS_TABLE, true)
     BZ_SEG_CASE(false, BZ_XS_TABLE, false)
     BZ_SEG_CASE(false, BZ_XS_REF_FITS, true)
@@ -488,8 +499,9 @@ struct RepackWs {
 template <typename T, typename S, typename P>
 static int seg_repack_entry(const S *in_, P app_, const int32_t *app_n, int64_t app_cap, S out_, void *ws,
                             size_t ws_bytes, const uint32_t *only_if, uint32_t *seg_flags, uint32_t *status,
-                            void *stream) {
+                            void *stream, const S *back_ = nullptr) {
     if (!ws || !status || !seg_ok<T>(out_)) return BZ_ERR_ARG;
+    if (back_ && (!seg_ok<T>(*back_) || back_->nseg != out_.nseg || back_->half != out_.half)) return BZ_ERR_ARG;
     if (in_ && !seg_ok<T>(*in_)) return BZ_ERR_ARG;
     const bool has_app = app_n != nullptr;
     if (has_app && (!app_.x || !app_.vx || !app_.vy || !app_.vz || !app_.w || app_cap < 0)) return BZ_ERR_ARG;
@@ -500,22 +512,22 @@ static int seg_repack_entry(const S *in_, P app_, const int32_t *app_n, int64_t 
     unsigned char *b = static_cast<unsigned char *>(ws);
     int32_t *live = reinterpret_cast<int32_t *>(b + L.live);
     int32_t *pre = reinterpret_cast<int32_t *>(b + L.pre);
-    cudaStream_t st = as_stream(stream);
+    Seg<T> in = in_ ? to_seg<T>(*in_) : Seg<T>{SoA<T>{nullptr, nullptr, nullptr, nullptr, nullptr}, nullptr, 0, 4};
     Seg<T> out = to_seg<T>(out_);
+    Seg<T> back = back_ ? to_seg<T>(*back_) : Seg<T>{SoA<T>{nullptr, nullptr, nullptr, nullptr, nullptr}, nullptr, 0, 4};
     SoA<T> app{app_.x, app_.vx, app_.vy, app_.vz, app_.w};
-    const int blocks = std::max(1, std::min(num_sms() * 8, int(ceil_div(std::max(nseg_in, out.nseg), 8))));
-    if (in_) {
-        Seg<T> in = to_seg<T>(*in_);
-        k_seg_count_live<T><<<blocks, 256, 0, st>>>(in, live, only_if);
-        k_scan_live<<<1, 1024, 0, st>>>(live, nseg_in, app_n, app_cap, pre, only_if);
-        k_seg_scatter<T><<<blocks, 256, 0, st>>>(in, pre, out, only_if, status);
-    } else {
-        k_scan_live<<<1, 1024, 0, st>>>(live, 0, app_n, app_cap, pre, only_if);
-    }
-    if (has_app)
-        k_app_scatter<T><<<num_sms() * 4, 256, 0, st>>>(app, app_n, app_cap, pre, nseg_in, out, only_if, status);
-    k_seg_set_counts<<<1, 1024, 0, st>>>(out.cnt, out.nseg, out.half, pre, nseg_in, seg_flags, only_if);
-    return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+    auto kern = k_seg_repack<T>;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, RP_T, 0) != cudaSuccess || per_sm < 1)
+        return BZ_ERR_UNSUPPORTED;
+    const int need = std::max(1, int(ceil_div(std::max(nseg_in, out.nseg), RP_T / 32)));
+    const int grid = std::max(1, std::min(num_sms() * per_sm, need));
+    void *args[] = {&in,   &app, (void *)&app_n, &app_cap, &out, &back, &live, &pre, (void *)&only_if, &seg_flags,
+                    &status};
+    if (cudaLaunchCooperativeKernel(reinterpret_cast<void *>(kern), dim3(grid), dim3(RP_T), args, 0,
+                                    as_stream(stream)) != cudaSuccess)
+        return BZ_ERR_CUDA;
+    return BZ_OK;
 }
 
 // energy distribution per node (swarm): one warp per segment. The bin is taken from a
@@ -609,16 +621,18 @@ int32_t bz_seg_push_selected(void) { return bz::g_seg_shape; }
 size_t bz_seg_repack_workspace(int32_t nseg_in) { return bz::RepackWs(nseg_in).total; }
 
 int bz_seg_push_collide_f32(const bz_params *p, bz_segments_f32 in, bz_segments_f32 out, const float *E,
-                            const double *replay_R, const double *replay_gas, double *moments, void *workspace,
-                            size_t workspace_bytes, uint32_t *seg_flags, uint32_t *status, void *stream) {
-    return bz::seg_push_entry<float>(p, in, out, E, replay_R, replay_gas, moments, workspace, workspace_bytes,
-                                     seg_flags, status, stream);
+                            const double *replay_R, const double *replay_gas, double *moments, uint64_t *n_pushed,
+                            void *workspace, size_t workspace_bytes, uint32_t *seg_flags, uint32_t *status,
+                            void *stream) {
+    return bz::seg_push_entry<float>(p, in, out, E, replay_R, replay_gas, moments, n_pushed, workspace,
+                                     workspace_bytes, seg_flags, status, stream);
 }
 int bz_seg_push_collide_f64(const bz_params *p, bz_segments_f64 in, bz_segments_f64 out, const double *E,
-                            const double *replay_R, const double *replay_gas, double *moments, void *workspace,
-                            size_t workspace_bytes, uint32_t *seg_flags, uint32_t *status, void *stream) {
-    return bz::seg_push_entry<double>(p, in, out, E, replay_R, replay_gas, moments, workspace, workspace_bytes,
-                                      seg_flags, status, stream);
+                            const double *replay_R, const double *replay_gas, double *moments, uint64_t *n_pushed,
+                            void *workspace, size_t workspace_bytes, uint32_t *seg_flags, uint32_t *status,
+                            void *stream) {
+    return bz::seg_push_entry<double>(p, in, out, E, replay_R, replay_gas, moments, n_pushed, workspace,
+                                      workspace_bytes, seg_flags, status, stream);
 }
 int bz_seg_repack_f32(const bz_segments_f32 *in, bz_particles_f32 app, const int32_t *app_n, int64_t app_capacity,
                       bz_segments_f32 out, void *workspace, size_t workspace_bytes, const uint32_t *only_if,
@@ -631,6 +645,16 @@ int bz_seg_repack_f64(const bz_segments_f64 *in, bz_particles_f64 app, const int
                       uint32_t *seg_flags, uint32_t *status, void *stream) {
     return bz::seg_repack_entry<double>(in, app, app_n, app_capacity, out, workspace, workspace_bytes, only_if,
                                         seg_flags, status, stream);
+}
+int bz_seg_rebalance_f32(bz_segments_f32 s, bz_segments_f32 scratch, void *workspace, size_t workspace_bytes,
+                         const uint32_t *only_if, uint32_t *seg_flags, uint32_t *status, void *stream) {
+    return bz::seg_repack_entry<float>(&s, bz_particles_f32{}, nullptr, 0, scratch, workspace, workspace_bytes,
+                                       only_if, seg_flags, status, stream, &s);
+}
+int bz_seg_rebalance_f64(bz_segments_f64 s, bz_segments_f64 scratch, void *workspace, size_t workspace_bytes,
+                         const uint32_t *only_if, uint32_t *seg_flags, uint32_t *status, void *stream) {
+    return bz::seg_repack_entry<double>(&s, bz_particles_f64{}, nullptr, 0, scratch, workspace, workspace_bytes,
+                                        only_if, seg_flags, status, stream, &s);
 }
 int bz_seg_deposit_f32(const bz_params *p, bz_segments_f32 s, double *moments, void *stream) {
     return bz::seg_deposit_entry<float>(p, s, moments, stream);

@@ -232,13 +232,17 @@ def compact(s: ParticleSet, out: ParticleSet, status, ws: Workspace):
 # --------------------------------------------------------------------------------------
 
 def seg_electron_kernel(params, src: SegmentSet, dst: SegmentSet, E, status, seg_flags, ws: Workspace, moments=None,
-                        replay_R=None, replay_gas=None):
-    """Push + collide a segmented state (one warp per segment, no inter-segment order)."""
+                        replay_R=None, replay_gas=None, n_pushed=None):
+    """Push + collide a segmented state (one warp per segment, no inter-segment order);
+    n_pushed (int64 device scalar, optional) accumulates the particles pushed."""
     if src.dtype != dst.dtype or E.dtype != src.dtype:
         raise TypeError("precision mismatch")
+    if n_pushed is not None and n_pushed.dtype != torch.int64:
+        raise TypeError("n_pushed must be int64")
     w = ws.get("seg_push", _lib.load().bz_seg_push_workspace())
     call(f"bz_seg_push_collide_{src.suffix}", ctypes.byref(params), src.struct(), dst.struct(), _ptr(E),
-         _ptr(replay_R), _ptr(replay_gas), _ptr(moments), _ptr(w), w.numel(), _ptr(seg_flags), _ptr(status), _stream())
+         _ptr(replay_R), _ptr(replay_gas), _ptr(moments), _ptr(n_pushed), _ptr(w), w.numel(), _ptr(seg_flags),
+         _ptr(status), _stream())
 
 
 def seg_push_shapes():
@@ -301,6 +305,15 @@ def seg_repack(src, dst: SegmentSet, status, ws: Workspace, app: ParticleSet = N
          _ptr(status), _stream())
 
 
+def seg_rebalance(s: SegmentSet, scratch: SegmentSet, status, ws: Workspace, only_if=None, clear=None,
+                  name="seg_rebalance"):
+    """Spread s's live particles evenly over its segments again (through scratch), in one
+    launch; skipped unless only_if's BZ_SEG_NEEDS_REPACK bit is set (when given)."""
+    w = ws.get(name, _lib.load().bz_seg_repack_workspace(s.nseg))
+    call(f"bz_seg_rebalance_{s.suffix}", s.struct(), scratch.struct(), _ptr(w), w.numel(), _ptr(only_if), _ptr(clear),
+         _ptr(status), _stream())
+
+
 def seg_deposit(params, s: SegmentSet, moments):
     call(f"bz_seg_deposit_{s.suffix}", ctypes.byref(params), s.struct(), _ptr(moments), _stream())
 
@@ -339,13 +352,14 @@ def heavies_kernel_fluid(N, dx, dt, mu_i, D_i, E, ni, Ji, brk=None):
          _ptr(brk), _stream())
 
 
-def poisson_factor(N, dx, diag, lower):
-    call("bz_poisson_factor", int(N), float(dx), _ptr(diag), _ptr(lower))
+def poisson_factor(N, dx, diag, lower, plan):
+    """Banded Cholesky factor (diag, lower: N-1 each) and the solve plan (4*(N-1))."""
+    call("bz_poisson_factor", int(N), float(dx), _ptr(diag), _ptr(lower), _ptr(plan))
 
 
-def EF_kernel(N, dx, eps0, V0, freq, t, ne, ni, diag, lower, V, E, E32=None, t_dev=None):
+def EF_kernel(N, dx, eps0, V0, freq, t, ne, ni, plan, V, E, E32=None, t_dev=None):
     call("bz_poisson", int(N), float(dx), float(eps0), float(V0), float(freq), float(t), _ptr(t_dev), _ptr(ne),
-         _ptr(ni), _ptr(diag), _ptr(lower), _ptr(V), _ptr(E), _ptr(E32), _stream())
+         _ptr(ni), _ptr(plan), _ptr(V), _ptr(E), _ptr(E32), _stream())
 
 
 def advance_clock(t_dev, step_dev, dt):

@@ -71,6 +71,7 @@ class BoltzmannGB300:
         self.g2 = torch.zeros(self.nnodes, **f64)
         self.chol_d = torch.zeros(max(N - 1, 1), **f64)
         self.chol_l = torch.zeros(max(N - 1, 1), **f64)
+        self.poisson_plan = torch.zeros(4 * max(N - 1, 1), **f64)
         self.t = torch.zeros(1, **f64)
         self.step_dev = torch.zeros(1, dtype=torch.int64, device=dev)
         self.brk = torch.zeros(1, dtype=torch.int32, device=dev)
@@ -97,7 +98,7 @@ class BoltzmannGB300:
         self._kinds = set()
         self._host_io = None
         if N >= 3:
-            K.poisson_factor(N, cfg.dx, self.chol_d, self.chol_l)
+            K.poisson_factor(N, cfg.dx, self.chol_d, self.chol_l, self.poisson_plan)
         # first deposit and field solve (boltzmann.py:363-399)
         K.seg_deposit(self.params(), self.A, self.moments)
         self.ni.add_(self.moments[1])
@@ -160,9 +161,8 @@ class BoltzmannGB300:
         """Push + collide the current particles; deposit and compaction are fused in
         (electron_kernel_numba.py:291-303 with post_processing_1D.py:40-68)."""
         self.moments.zero_()
-        self.particle_steps.add_(self.A.counts.sum(dtype=torch.int64))
         K.seg_electron_kernel(self.params(), self.A, self.B, self.E_push, self.status, self.seg_flags, self.ws,
-                              moments=self.moments)
+                              moments=self.moments, n_pushed=self.particle_steps)
         self.A, self.B = self.B, self.A
 
     def post_processing(self):
@@ -189,10 +189,9 @@ class BoltzmannGB300:
 
     def _repack_if_needed(self):
         """Spread the particles evenly again when the last push left a segment above
-        half its capacity (decided on the device; A -> B -> A so the roles stay fixed)."""
-        K.seg_repack(self.A, self.B, self.status, self.ws, only_if=self.seg_flags, clear=None, name="repack_ab")
-        K.seg_repack(self.B, self.A, self.status, self.ws, only_if=self.seg_flags, clear=self.seg_flags,
-                     name="repack_ba")
+        half its capacity (decided on the device; through B and back into A in one
+        launch, so the buffer roles stay fixed)."""
+        K.seg_rebalance(self.A, self.B, self.status, self.ws, only_if=self.seg_flags, clear=self.seg_flags)
 
     def heavies_kernel_fluid(self):
         cfg = self.cfg
@@ -200,8 +199,8 @@ class BoltzmannGB300:
 
     def EF_kernel(self):
         cfg = self.cfg
-        K.EF_kernel(self.N, cfg.dx, cfg.eps0, cfg.V0, cfg.freq, 0.0, self.moments[0], self.ni, self.chol_d,
-                    self.chol_l, self.V, self.E, self.E_push if self.dtype == torch.float32 else None, t_dev=self.t)
+        K.EF_kernel(self.N, cfg.dx, cfg.eps0, cfg.V0, cfg.freq, 0.0, self.moments[0], self.ni, self.poisson_plan,
+                    self.V, self.E, self.E_push if self.dtype == torch.float32 else None, t_dev=self.t)
         if self.dtype == torch.float64:
             self.E_push.copy_(self.E)
 
@@ -300,8 +299,7 @@ class BoltzmannGB300:
         lib = _lib.load()
         nkeys = self.nnodes * self.nb
         self.ws.get("seg_push", lib.bz_seg_push_workspace())
-        self.ws.get("repack_ab", lib.bz_seg_repack_workspace(self.A.nseg))
-        self.ws.get("repack_ba", lib.bz_seg_repack_workspace(self.A.nseg))
+        self.ws.get("seg_rebalance", lib.bz_seg_repack_workspace(self.A.nseg))
         if resample:
             self.ws.get("seg_bin", lib.bz_seg_bin_workspace(self.A.nseg, self.A.capacity))
             self.ws.get("seg_resample", lib.bz_seg_resample_workspace(self.A.nseg, self.A.capacity, nkeys))
@@ -329,14 +327,14 @@ class BoltzmannGB300:
 
     # --------------------------------------------------------------------------------- diagnostics
     def kernel_launches(self, resample):
-        """libbz kernels one step launches (torch's own memset/sum kernels not counted).
+        """libbz kernels one step launches (torch's memset of the moments not counted).
         Every step: the push, grid update, clock, ion fluid and Poisson (5); a plain step
-        adds the two conditional repacks (count, scan, scatter, set counts: 4 each); a
-        resampling step adds binning (segment totals, key offsets twice, keys, then per
-        8-bit radix pass a histogram, scan and scatter), decide + apply (2) and the repack
-        of the survivors with the appended particles (5)."""
+        adds the conditional rebalance (one cooperative kernel); a resampling step
+        adds binning (segment totals, key offsets twice, keys, then per 8-bit radix pass a
+        histogram, scan and scatter), decide + apply (2) and the repack of the survivors
+        with the appended particles (1)."""
         passes = 2 if self.nnodes * self.nb >= 256 else 1
-        return 5 + (4 + 3 * passes + 2 + 5 if resample else 8)
+        return 5 + (4 + 3 * passes + 2 + 1 if resample else 1)
 
     def n(self):
         return self.A.n()

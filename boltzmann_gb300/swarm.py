@@ -171,9 +171,8 @@ class SwarmEnsemble:
     def electron_kernel(self):
         """One push + collide of every swarm, deposit per swarm fused in."""
         self.moments.zero_()
-        self.particle_steps.add_(self.A.counts.sum(dtype=torch.int64))
         K.seg_electron_kernel(self.params(), self.A, self.B, self.E, self.status, self.seg_flags, self.ws,
-                              moments=self.moments)
+                              moments=self.moments, n_pushed=self.particle_steps)
         self.A, self.B = self.B, self.A
         # pre-push population = after-push weight minus the children (every ionization
         # adds one particle of its parent's weight; a 0-D swarm loses none)
@@ -181,9 +180,7 @@ class SwarmEnsemble:
         self.acc_pre.add_(self.moments[0] - self.moments[1])
 
     def _repack_if_needed(self):
-        K.seg_repack(self.A, self.B, self.status, self.ws, only_if=self.seg_flags, clear=None, name="repack_ab")
-        K.seg_repack(self.B, self.A, self.status, self.ws, only_if=self.seg_flags, clear=self.seg_flags,
-                     name="repack_ba")
+        K.seg_rebalance(self.A, self.B, self.status, self.ws, only_if=self.seg_flags, clear=self.seg_flags)
 
     def _resample(self):
         cfg = self.cfg
@@ -252,8 +249,7 @@ class SwarmEnsemble:
     def _capture(self, resample):
         lib = _lib.load()
         self.ws.get("seg_push", lib.bz_seg_push_workspace())
-        self.ws.get("repack_ab", lib.bz_seg_repack_workspace(self.A.nseg))
-        self.ws.get("repack_ba", lib.bz_seg_repack_workspace(self.A.nseg))
+        self.ws.get("seg_rebalance", lib.bz_seg_repack_workspace(self.A.nseg))
         self.ws.get("seg_bin", lib.bz_seg_bin_workspace(self.A.nseg, self.A.capacity))
         self.ws.get("seg_resample", lib.bz_seg_resample_workspace(self.A.nseg, self.A.capacity, self.S * self.nb))
         s = torch.cuda.Stream(device=self.device)

@@ -198,14 +198,16 @@ int bz_grid_update(int32_t n_nodes, const double *moments, double *ni, double *T
 /* heavies_kernel_fluid (heavies_kernel_1D.py:4-64), ion part; break flag -> *brk. */
 int bz_ion_fluid(int32_t N, double dx, double dt, double mu_i, double D_i, const double *E, double *ni,
                  double *Ji, int32_t *brk, void *stream);
-/* EF_kernel (EF_kernel_1D.py:7-44) with the banded Cholesky factor of boltzmann.py:744-755
- * (chol_diag[N-1], chol_lower[N-1] from bz_poisson_factor). t is read from *t_dev when
- * t_dev != NULL (graph capture), else t_host. Writes V[N-1] and E (float64 [N]);
- * E32 (optional) receives a float32 copy for the float32 push. */
-int bz_poisson_factor(int32_t N, double dx, double *chol_diag, double *chol_lower);
+/* EF_kernel (EF_kernel_1D.py:7-44) with the banded Cholesky factor of boltzmann.py:744-755.
+ * bz_poisson_factor (once per grid, synchronous) writes the factor chol_diag[N-1],
+ * chol_lower[N-1] and the solve plan[4*(N-1)]: the substitutions' prefix products and
+ * scaled reciprocals, so that each solve is two prefix sums. bz_poisson: t is read from
+ * *t_dev when t_dev != NULL (graph capture), else t_host. Writes V[N-1] and E (float64
+ * [N]); E32 (optional) receives a float32 copy for the float32 push. */
+int bz_poisson_factor(int32_t N, double dx, double *chol_diag, double *chol_lower, double *plan);
 int bz_poisson(int32_t N, double dx, double eps0, double V0, double freq, double t_host, const double *t_dev,
-               const double *ne, const double *ni, const double *chol_diag, const double *chol_lower,
-               double *V, double *E, float *E32, void *stream);
+               const double *ne, const double *ni, const double *plan, double *V, double *E, float *E32,
+               void *stream);
 /* Step clock on the device (graph-capturable): *t_dev += dt, *step_dev += 1 (either may be NULL). */
 int bz_advance_clock(double *t_dev, uint64_t *step_dev, double dt, void *stream);
 
@@ -226,15 +228,16 @@ typedef struct bz_segments_f64 { double *x, *vx, *vy, *vz, *w; int32_t *counts; 
 #define BZ_SEG_NEEDS_REPACK 0x1u
 
 /* Push + collide (+ deposit) of a segmented state into another (same nseg, half); the
- * per-particle arithmetic of bz_push_collide_*. Philox counters use the input slot. */
+ * per-particle arithmetic of bz_push_collide_*. Philox counters use the input slot.
+ * n_pushed (optional, device) accumulates the number of input particles pushed. */
 size_t bz_seg_push_workspace(void);
 int bz_seg_push_collide_f32(const bz_params *p, bz_segments_f32 in, bz_segments_f32 out, const float *E,
                             const double *replay_R, const double *replay_gas, double *moments,
-                            void *workspace, size_t workspace_bytes, uint32_t *seg_flags,
+                            uint64_t *n_pushed, void *workspace, size_t workspace_bytes, uint32_t *seg_flags,
                             uint32_t *status, void *stream);
 int bz_seg_push_collide_f64(const bz_params *p, bz_segments_f64 in, bz_segments_f64 out, const double *E,
                             const double *replay_R, const double *replay_gas, double *moments,
-                            void *workspace, size_t workspace_bytes, uint32_t *seg_flags,
+                            uint64_t *n_pushed, void *workspace, size_t workspace_bytes, uint32_t *seg_flags,
                             uint32_t *status, void *stream);
 /* CTA shapes of the float32 table + deposit segmented push (threads per CTA, particles
  * per lane per round, CTAs per SM the registers are budgeted for). Shape 0 is the
@@ -256,6 +259,13 @@ int bz_seg_repack_f32(const bz_segments_f32 *in, bz_particles_f32 app, const int
 int bz_seg_repack_f64(const bz_segments_f64 *in, bz_particles_f64 app, const int32_t *app_n,
                       int64_t app_capacity, bz_segments_f64 out, void *workspace, size_t workspace_bytes,
                       const uint32_t *only_if, uint32_t *seg_flags, uint32_t *status, void *stream);
+/* Repack s through scratch (same geometry) and back into s, in one launch: what a caller
+ * whose graph fixes the buffer roles needs after a push that filled a segment. Same
+ * workspace (bz_seg_repack_workspace(s.nseg)), only_if and seg_flags rules. */
+int bz_seg_rebalance_f32(bz_segments_f32 s, bz_segments_f32 scratch, void *workspace, size_t workspace_bytes,
+                         const uint32_t *only_if, uint32_t *seg_flags, uint32_t *status, void *stream);
+int bz_seg_rebalance_f64(bz_segments_f64 s, bz_segments_f64 scratch, void *workspace, size_t workspace_bytes,
+                         const uint32_t *only_if, uint32_t *seg_flags, uint32_t *status, void *stream);
 /* Moments (sum w, 0, 0, sum w*energy) of a segmented state (no ion flags are stored). */
 int bz_seg_deposit_f32(const bz_params *p, bz_segments_f32 s, double *moments, void *stream);
 int bz_seg_deposit_f64(const bz_params *p, bz_segments_f64 s, double *moments, void *stream);

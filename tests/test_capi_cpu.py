@@ -61,7 +61,7 @@ def test_argument_validation_without_gpu(lib):
     assert rc == _lib.BZ_ERR_ARG
     rc = lib.bz_bin_f32(ctypes.byref(p), empty, None, 10, 1, None, 0.1, None, None, None, None, None, 0, None, None)
     assert rc == _lib.BZ_ERR_ARG
-    assert lib.bz_poisson(2, 0.1, 1.0, 1.0, 1.0, 0.0, None, None, None, None, None, None, None, None, None) == \
+    assert lib.bz_poisson(2, 0.1, 1.0, 1.0, 1.0, 0.0, None, None, None, None, None, None, None, None) == \
         _lib.BZ_ERR_ARG
     assert lib.bz_push_workspace(1 << 20) >= 8 * 1024
     assert lib.bz_bin_workspace(1 << 20, 5000) > 6 * (1 << 20)

@@ -20,13 +20,14 @@ def test_poisson_and_fluid_match_reference():
     dev = "cuda"
     d = torch.zeros(N - 1, dtype=torch.float64, device=dev)
     l = torch.zeros(N - 1, dtype=torch.float64, device=dev)
-    K.poisson_factor(N, dx, d, l)
+    plan = torch.zeros(4 * (N - 1), dtype=torch.float64, device=dev)
+    K.poisson_factor(N, dx, d, l, plan)
     ne = torch.as_tensor(g["ne"], device=dev)
     ni = torch.as_tensor(g["ni"], device=dev)
     V = torch.zeros(N - 1, dtype=torch.float64, device=dev)
     E = torch.zeros(N, dtype=torch.float64, device=dev)
     E32 = torch.zeros(N, dtype=torch.float32, device=dev)
-    K.EF_kernel(N, dx, float(g["eps0"]), float(g["V0"]), float(g["freq"]), float(g["t"]), ne, ni, d, l, V, E, E32)
+    K.EF_kernel(N, dx, float(g["eps0"]), float(g["V0"]), float(g["freq"]), float(g["t"]), ne, ni, plan, V, E, E32)
     torch.cuda.synchronize()
     np.testing.assert_allclose(V.cpu().numpy(), g["V"], rtol=1e-11, atol=1e-9)
     np.testing.assert_allclose(E.cpu().numpy(), g["E"], rtol=1e-11, atol=1e-7)

@@ -151,6 +151,36 @@ def test_conditional_repack_skips_without_request():
     assert int(flags.item()) == 0 and b.n() == 28
 
 
+def test_rebalance_in_place_matches_repack():
+    """bz_seg_rebalance: repack through the scratch set and back in one launch; the
+    result equals a plain repack into a fresh set; skipped without the request."""
+    rng = np.random.default_rng(4)
+    nseg, half = 40, 512
+    a = K.SegmentSet(nseg, half)
+    c = rng.integers(0, half + 1, (nseg, 2)).astype(np.int32)
+    a.counts.copy_(torch.as_tensor(c.reshape(-1), device="cuda"))
+    for f in a.FIELDS:
+        getattr(a, f).copy_(torch.rand(a.capacity, device="cuda") + 0.5)
+    a.w[torch.rand(a.capacity, device="cuda") < 0.1] = 0.0
+    ref = K.SegmentSet(nseg, half)
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    K.seg_repack(a, ref, st, K.Workspace())
+    scratch = K.SegmentSet(nseg, half)
+    flags = torch.zeros(1, dtype=torch.int32, device="cuda")
+    before = a.counts.clone()
+    K.seg_rebalance(a, scratch, st, K.Workspace(), only_if=flags, clear=flags)
+    torch.cuda.synchronize()
+    assert torch.equal(a.counts, before)  # no request: nothing ran
+    flags.fill_(_lib.SEG_NEEDS_REPACK)
+    K.seg_rebalance(a, scratch, st, K.Workspace(), only_if=flags, clear=flags)
+    torch.cuda.synchronize()
+    assert int(st.item()) == 0 and int(flags.item()) == 0
+    np.testing.assert_array_equal(a.counts.cpu().numpy(), ref.counts.cpu().numpy())
+    got, want = a.to_numpy("segments"), ref.to_numpy("segments")
+    for f in a.FIELDS:
+        np.testing.assert_array_equal(got[f], want[f])
+
+
 @pytest.mark.parametrize("variant", ["3bin", "5bin"])
 def test_seg_bin_and_resample_match_dense(variant):
     g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", f"resample_{variant}.npz"))
@@ -216,3 +246,51 @@ def test_seg_deposit_matches_dense():
     K.deposit(p, dense, m2)
     torch.cuda.synchronize()
     np.testing.assert_allclose(m1.cpu().numpy(), m2.cpu().numpy(), rtol=1e-5, atol=1e-9)
+
+
+def test_every_cta_shape_gives_the_same_particles():
+    """The push's CTA shapes (bz_seg_push_select) change only the float summation order
+    of the moments: particles and counts are identical."""
+    rng = np.random.default_rng(19)
+    n, N, L, nseg, half = 120_000, 512, 2.54, 96, 2048
+    x = rng.uniform(1e-4, L - 1e-4, n)
+    v = rng.normal(0, 1.4e6, (n, 3))
+    w = rng.uniform(1e4, 1e5, n)
+    E = rng.uniform(-1200, 1200, N)
+    seg = K.SegmentSet(nseg, half, torch.float32)
+    seg.load(x, v[:, 0], v[:, 1], v[:, 2], w)
+    tab = xsec.analytic_argon(2000)
+    nn = 3.22e22
+    xt = torch.as_tensor(tab.nsigma(nn), device="cuda")
+    p = K.make_params(n_faces=N, n_nodes=N + 1, bnf=4, advect=1, L=L, dx=L / N, dt=1.0 / 13.56e6 / 400, nn=nn,
+                      gas_sigma=6.74e4, e_exc=tab.e_exc, xs_mode=_lib.XS_TABLE, xs_table=xt, xs_emin=tab.emin,
+                      xs_emax=tab.emax, flags=_lib.QUIRK_DEAD_IONFLAG, seed=2, step=7)
+    shapes = K.seg_push_shapes()
+    assert len(shapes) >= 2 and shapes[0] == (320, 1, 4)
+    # the push's own counter of pushed particles
+    cnt = torch.zeros(1, dtype=torch.int64, device="cuda")
+    tmp = K.SegmentSet(nseg, half, torch.float32)
+    st0 = torch.zeros(1, dtype=torch.int32, device="cuda")
+    fl0 = torch.zeros(1, dtype=torch.int32, device="cuda")
+    for _ in range(2):
+        K.seg_electron_kernel(p, seg, tmp, torch.as_tensor(E, dtype=torch.float32, device="cuda"), st0, fl0,
+                              K.Workspace(), n_pushed=cnt)
+    assert int(cnt.item()) == 2 * seg.n() == 2 * n
+    ref = None
+    try:
+        for k in range(len(shapes)):
+            K.select_seg_push_shape(k)
+            out, mom, st, fl = seg_push(seg, p, E)
+            assert st == 0
+            o = out.to_numpy("segments")
+            c = out.counts.cpu().numpy()
+            if ref is None:
+                ref = (o, c, mom)
+                continue
+            np.testing.assert_array_equal(c, ref[1])
+            for f in K.SegmentSet.FIELDS:
+                np.testing.assert_array_equal(o[f], ref[0][f])
+            for j in (0, 1, 3):
+                np.testing.assert_allclose(mom[j], ref[2][j], rtol=1e-5, atol=1e-6 * np.abs(ref[2][j]).max())
+    finally:
+        K.select_seg_push_shape(0)

@@ -1,0 +1,70 @@
+"""The GPU solver against the oracle's CPU step loop (oracle/ccp.py) on a small 1 Torr
+argon CCP: 128 cells, 1e5 electrons at 1 eV, 3-bin ES-WPNC every 50 steps, 400 steps of
+tau/4000 (a tenth of an RF cycle, while the sheaths form; at tau/400 this explicit scheme
+heats the uniform start within a cycle, which makes a poor statistical test). The two
+use different random streams, so they are compared
+statistically: the oracle run must fall within the spread of four independent GPU runs
+(4 sigma, plus 0.5% for the remaining float32 effects) for the electron count, the
+ionizations, the mean energy and the cycle-averaged density in eight regions.
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+from boltzmann_gb300 import config  # noqa: E402
+from boltzmann_gb300.solver import BoltzmannGB300  # noqa: E402
+from oracle.ccp import OracleCCP  # noqa: E402
+
+STEPS, AVG_FROM, REGIONS = 400, 200, 8
+
+
+def cfg(seed):
+    return config.CCPConfig(gridpts=129, pressure_torr=1.0, in_dt=4000.0, steps_per_cycle=4000, num_particles=100_000,
+                            Te_init_eV=1.0, ne_profile="uniform", bin_edges=(4.0, 11.5), bin_fractions=(0.7, 0.2, 0.1),
+                            xs="analytic", resample_freq=50, seed=seed, autotune=False)
+
+
+def observe(moments_per_step, final_weight):
+    m = np.array(moments_per_step)  # [steps, 4, nodes]
+    ne_avg = m[AVG_FROM:, 0].mean(axis=0)
+    reg = ne_avg[: (len(ne_avg) // REGIONS) * REGIONS].reshape(REGIONS, -1).sum(axis=1)
+    return {
+        "weight": final_weight,
+        "ionizations": m[:, 1].sum(),
+        "mean_energy": m[AVG_FROM:, 3].sum() / m[AVG_FROM:, 0].sum(),
+        **{f"region{k}": reg[k] for k in range(REGIONS)},
+    }
+
+
+def gpu_run(seed):
+    sol = BoltzmannGB300(cfg(seed), device="cuda")
+    moms = []
+    for _ in range(STEPS):
+        sol.step()
+        moms.append(sol.moments.cpu().numpy().copy())
+    assert sol.device_status() == 0
+    return sol, observe(moms, float(sol.A.to_numpy()["w"].sum()))
+
+
+def test_solver_matches_oracle_step_loop_statistically():
+    # the oracle starts from the initial state of the seed-0 GPU solver
+    s0 = BoltzmannGB300(cfg(0), device="cuda")
+    st = s0.A.to_numpy("segments")
+    orc = OracleCCP(s0.cfg, st["x"], st["vx"], st["vy"], st["vz"], st["w"], s0.ni.cpu().numpy(), s0.xs, seed=5)
+    del s0
+    moms = []
+    for _ in range(STEPS):
+        orc.step()
+        moms.append(orc.moments.copy())
+    o = observe(moms, float(orc.state()["w"].sum()))
+    runs = [gpu_run(seed)[1] for seed in (1, 2, 3, 4)]
+    for k in o:
+        g = np.array([r[k] for r in runs])
+        mu, sd = g.mean(), g.std(ddof=1)
+        lim = 4 * sd * math.sqrt(1 + 1 / len(g)) + 0.005 * abs(mu)
+        assert abs(o[k] - mu) <= lim, f"{k}: oracle {o[k]:.6g}, GPU {mu:.6g} +- {sd:.3g}"
+    assert o["ionizations"] > 0
