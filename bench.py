@@ -223,7 +223,7 @@ def run_ours(args, world, rank, local, pg):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     cfg = config.ccp_1024(num_particles=int(args.particles), gridpts=args.cells + 1, resample_freq=args.rsf,
-                          seed=1 + rank, autotune=not args.no_autotune)
+                          seed=1 + rank, autotune=not args.no_autotune, capacity_factor=4.0)
     sol = BoltzmannGB300(cfg, device=dev)
     n_start = sol.n()
     for _ in range(args.warmup):
@@ -248,32 +248,32 @@ def run_ours(args, world, rank, local, pg):
     t_max = max_over_ranks(pg, ms / 1e3, dev)
     ps_all = sum_over_ranks(pg, ps, dev)
     value = ps_all / t_max
-    status = sol.device_status()
 
-    # dominant kernel alone: the fused segmented push (ping-pong on the solver's buffers)
+    # dominant kernel alone: the fused segmented push of the current state A into the
+    # scratch buffer B, repeated (A is only read, so the solver's state is unchanged; the
+    # flag words and moments are restored afterwards)
     A, B = sol.A, sol.B
     mom = sol.moments
     prm = sol.params(step_on_device=False)
+    saved = (sol.status.clone(), sol.seg_flags.clone(), mom.clone())
     M = 20
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
 
-    def push_once(A, B):
+    def push_once():
         mom.zero_()
         K.seg_electron_kernel(prm, A, B, sol.E_push, sol.status, sol.seg_flags, sol.ws, moments=mom)
-        return B, A
 
     for i in range(3):
-        A, B = push_once(A, B)
+        push_once()
     torch.cuda.synchronize()
-    n_before = A.n()
     ev[0].record(st)
     for i in range(M):
-        A, B = push_once(A, B)
+        push_once()
     ev[1].record(st)
     torch.cuda.synchronize()
     push_ms = ev[0].elapsed_time(ev[1]) / M
-    n_after = A.n()
-    n_now = 0.5 * (n_before + n_after)
+    n_now = A.n()
+    sol.status.copy_(saved[0]); sol.seg_flags.copy_(saved[1]); mom.copy_(saved[2])
     # algorithmic bytes: read the particles pushed (20 B), write them back (20 B)
     bytes_per_launch = BYTES_PER_PARTICLE * n_now
     achieved = bytes_per_launch / (push_ms * 1e-3) / 1e9
@@ -333,13 +333,79 @@ def run_ours(args, world, rank, local, pg):
                      "traffic": traffic, "kernel": "k_seg_push (fused push+collide+deposit+compaction)",
                      "launch_ms": push_ms, "particles_per_launch": n_now, "peak_kind": kind,
                      "cta_shape": (None if sol.push_shape is None else
-                                   dict(zip(("threads", "per_lane", "min_blocks"), sol.push_shape["shape"])))},
+                                   dict(zip(("threads", "per_lane", "min_blocks", "prefetch"),
+                                            sol.push_shape["shape"])))},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": (sol.kernel_launches(False) * (args.steps - n_resample)
                          + sol.kernel_launches(True) * n_resample),
         "clocks": clk.summary(),
-        "particles_start": n_start, "particles_end": int(n_now), "device_status": status,
+        "particles_start": n_start, "particles_end": int(n_now), "device_status": sol.device_status(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_swarms(args, world, rank, local, pg):
+    """The batched 0-D swarm ensemble (512 argon swarms, 10-1000 Td, 1e4-2e5 particles
+    each, float32, 3-bin ES-WPNC every 10 steps, dt = 1 ps): particle-steps/s of whole
+    ensemble steps (push + deposit per swarm + conditional rebalance, binning and
+    resampling when due), graph replays timed with CUDA events."""
+    import numpy as np
+    import torch
+    from boltzmann_gb300 import kernels as K, swarm
+
+    torch.cuda.set_device(local)
+    cfg = swarm.ensemble_512(seed=rank)
+    ens = swarm.SwarmEnsemble(cfg, device=torch.device("cuda", local))
+    for _ in range(max(args.warmup, 10)):
+        ens.step()
+    ens.capture_all()
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    ps0 = int(ens.particle_steps.item())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(pg)
+    with ClockSampler(local) as clk:
+        e0.record(st)
+        for _ in range(args.steps):
+            ens.step()
+        e1.record(st)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    ps = int(ens.particle_steps.item()) - ps0
+    t_max = max_over_ranks(pg, ms / 1e3, ens.device)
+    value = sum_over_ranks(pg, ps, ens.device) / t_max
+    # the push alone on the current state (read only), as for the CCP
+    prm = ens.params(step_on_device=False)
+    saved = (ens.status.clone(), ens.seg_flags.clone(), ens.moments.clone())
+    for _ in range(3):
+        K.seg_electron_kernel(prm, ens.A, ens.B, ens.E, ens.status, ens.seg_flags, ens.ws, moments=ens.moments)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(st)
+    for _ in range(20):
+        K.seg_electron_kernel(prm, ens.A, ens.B, ens.E, ens.status, ens.seg_flags, ens.ws, moments=ens.moments)
+    ev1.record(st)
+    torch.cuda.synchronize()
+    push_ms = ev0.elapsed_time(ev1) / 20
+    ens.status.copy_(saved[0]); ens.seg_flags.copy_(saved[1]); ens.moments.copy_(saved[2])
+    n_now = ens.A.n()
+    achieved = BYTES_PER_PARTICLE * n_now / (push_ms * 1e-3) / 1e9
+    peak, kind = peaks()
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "batched 0-D argon swarms: 512 swarms, E/N 10-1000 Td, 1e4-2e5 particles each, "
+                               "3-bin ES-WPNC every 10 steps, dt 1 ps", "swarms": cfg.n_swarms,
+                   "particles": int(sum(cfg.counts)), "state": "float32 SoA"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "kernel": "k_seg_push (ensemble mode)", "launch_ms": push_ms,
+                     "particles_per_launch": n_now, "peak_kind": kind},
+        "cpu_baseline": None, "e2e": None,
+        "clocks": clk.summary(), "device_status": ens.device_status(),
+        "mean_energy_eV": [float(np.min(ens.mean_energy())), float(np.max(ens.mean_energy()))],
     }
     print(json.dumps(line), flush=True)
 
@@ -350,6 +416,8 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="ccp1024", choices=["ccp1024", "swarm512"],
+                    help="ccp1024: the 2e7-particle CCP (default); swarm512: the batched swarm ensemble")
     ap.add_argument("--particles", type=float, default=2e7)
     ap.add_argument("--cells", type=int, default=1024)
     ap.add_argument("--rsf", type=int, default=50)
@@ -367,6 +435,8 @@ def main():
     args.gpus = max(args.gpus, world)
     if args.impl == "reference":
         run_reference_arm(args, world, rank, pg)
+    elif args.workload == "swarm512":
+        run_swarms(args, world, rank, local, pg)
     else:
         run_ours(args, world, rank, local, pg)
     if pg is not None:

@@ -97,7 +97,7 @@ _PROTOS = {
     "bz_advance_clock": (ctypes.c_int, [_vp, _vp, _f64, _vp]),
     "bz_seg_push_workspace": (_sz, []),
     "bz_seg_push_shapes": (ctypes.c_int32, []),
-    "bz_seg_push_shape_info": (ctypes.c_int, [ctypes.c_int32, _vp, _vp, _vp]),
+    "bz_seg_push_shape_info": (ctypes.c_int, [ctypes.c_int32, _vp, _vp, _vp, _vp]),
     "bz_seg_push_select": (ctypes.c_int, [ctypes.c_int32]),
     "bz_seg_push_selected": (ctypes.c_int32, []),
     "bz_seg_push_collide_f32": (ctypes.c_int, [_P, Segments, Segments, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp,

@@ -24,15 +24,15 @@ constexpr int RADIX = 256;
 // energy as the reference holds it when binning: tosum[:,3] = ((e*w)/w) after
 // post_processing (post_processing_1D.py:53,62), e = 0.5 m_e j_ev (vx^2+vy^2+vz^2)
 template <typename T>
-__device__ __forceinline__ int energy_bin(T vx, T vy, T vz, T w, int nb, const double *edges_s, float efac_f,
-                                          double efac_d) {
+__device__ __forceinline__ int energy_bin(T vx, T vy, T vz, T w, int nb, const double *edges_s,
+                                          const float *edges_f, float efac_f, double efac_d) {
     if (nb == 1) return 0;
     if (sizeof(T) == 4) {
         float e = efac_f * (float(vx) * float(vx) + float(vy) * float(vy) + float(vz) * float(vz));
         bool safe = true;
         int b = nb - 1;
         for (int k = nb - 2; k >= 0; --k) {
-            float ed = float(edges_s[k]);
+            const float ed = edges_f[k];
             if (fabsf(e - ed) <= 1e-5f * fabsf(ed) + 1e-30f) safe = false;
             if (e < ed) b = k;
         }
@@ -47,24 +47,38 @@ __device__ __forceinline__ int energy_bin(T vx, T vy, T vz, T w, int nb, const d
     return -1;  // NaN energy: in no bin (every comparison of the reference fails)
 }
 
+// w > min_wt as the reference tests it in float64: for float32 w the same as
+// w >= wmin_f, the smallest float above min_wt (formed on the host)
+__device__ __forceinline__ bool above_min(float w, double, float wmin_f) { return w >= wmin_f; }
+__device__ __forceinline__ bool above_min(double w, double min_wt, float) { return w > min_wt; }
+
+static float float_above(double m) {
+    float t = float(m);
+    if (double(t) <= m) t = nextafterf(t, INFINITY);
+    return t;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(RB_T) k_bin_keys(bz_params p, const T *x, const T *vx, const T *vy, const T *vz,
                                                    const T *w, const int32_t *n_ptr, int64_t cap, int nb,
-                                                   const double *edges,
-                                                   double min_wt, uint16_t *keys, uint32_t *hist, int32_t *counts,
+                                                   const double *edges, double min_wt, float wmin_f,
+                                                   float inv_dx_f, uint16_t *keys, uint32_t *hist, int32_t *counts,
                                                    int32_t *hw_counts, int nkeys, uint32_t *status) {
     extern __shared__ __align__(16) unsigned char smem[];
     uint32_t *c_s = reinterpret_cast<uint32_t *>(smem);  // [nkeys] counts
     uint32_t *h_s = c_s + nkeys;                          // [nkeys] hw counts
     uint32_t *d_s = h_s + nkeys;                          // [RADIX] low-digit histogram
     __shared__ double edges_s[16];
+    __shared__ float edges_f[16];
     const int n = int(min(int64_t(max(*n_ptr, 0)), cap));
     const int ntiles = int(ceil_div(n, RB_TILE));
     if (int(blockIdx.x) >= ntiles) return;
     for (int i = threadIdx.x; i < 2 * nkeys + RADIX; i += RB_T) c_s[i] = 0;
-    if (threadIdx.x < 16) edges_s[threadIdx.x] = threadIdx.x < nb - 1 ? edges[threadIdx.x] : 0.0;
+    if (threadIdx.x < 16) {
+        edges_s[threadIdx.x] = threadIdx.x < nb - 1 ? edges[threadIdx.x] : 0.0;
+        edges_f[threadIdx.x] = float(edges_s[threadIdx.x]);
+    }
     __syncthreads();
-    const float inv_dx_f = float(1.0 / p.dx);
     const float efac_f = float(0.5 * m_e() * j_ev());
     const double efac_d = 0.5 * m_e() * j_ev();
     uint32_t err = 0;
@@ -76,11 +90,11 @@ __global__ void __launch_bounds__(RB_T) k_bin_keys(bz_params p, const T *x, cons
         int key = nkeys;  // invalid: sorted past every bin
         if (wi > T(0)) {
             int cell = bin_cell(p.advect, x[i], p.dx, inv_dx_f);
-            int b = energy_bin(vx[i], vy[i], vz[i], wi, nb, edges_s, efac_f, efac_d);
+            int b = energy_bin(vx[i], vy[i], vz[i], wi, nb, edges_s, edges_f, efac_f, efac_d);
             if (cell >= 0 && cell < p.n_nodes && b >= 0) {
                 key = cell * nb + b;
                 atomicAdd(&c_s[key], 1u);
-                if (double(wi) > min_wt) atomicAdd(&h_s[key], 1u);
+                if (above_min(wi, min_wt, wmin_f)) atomicAdd(&h_s[key], 1u);
             } else {
                 err |= BZ_DEV_BINRANGE;
             }
@@ -266,7 +280,8 @@ static int bin_entry(const bz_params *pp, P s, const int32_t *n, int64_t cap, in
     if (smem > 48 * 1024 &&
         cudaFuncSetAttribute(kk, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess)
         return BZ_ERR_UNSUPPORTED;
-    kk<<<grid, RB_T, smem, st>>>(p, s.x, s.vx, s.vy, s.vz, s.w, n, cap, nb, edges, min_wt, keys_a, hist, counts, hw_counts,
+    kk<<<grid, RB_T, smem, st>>>(p, s.x, s.vx, s.vy, s.vz, s.w, n, cap, nb, edges, min_wt, float_above(min_wt),
+                                 float(1.0 / p.dx), keys_a, hist, counts, hw_counts,
                                  nkeys, status);
     const bool two = nkeys >= RADIX;  // invalid key = nkeys must be ordered too
     k_radix_scan<<<1, 1024, 0, st>>>(hist, n, cap);
@@ -295,16 +310,20 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_seg_bin_keys(bz_params p, const T *x, const T *vx, const T *vy, const T *vz,
                                                       const T *w, const int32_t *cnt, int nseg, int half,
                                                       const int32_t *pre, int nb, const double *edges, double min_wt,
-                                                      uint16_t *keys, uint32_t *slots, int32_t *counts,
+                                                      float wmin_f, float inv_dx_f, uint16_t *keys, uint32_t *slots,
+                                                      int32_t *counts,
                                                       int32_t *hw_counts, int nkeys, uint32_t *status) {
     extern __shared__ __align__(16) unsigned char smem[];
     uint32_t *c_s = reinterpret_cast<uint32_t *>(smem);
     uint32_t *h_s = c_s + nkeys;
     __shared__ double edges_s[16];
+    __shared__ float edges_f[16];
     for (int i = threadIdx.x; i < 2 * nkeys; i += blockDim.x) c_s[i] = 0;
-    if (threadIdx.x < 16) edges_s[threadIdx.x] = threadIdx.x < nb - 1 ? edges[threadIdx.x] : 0.0;
+    if (threadIdx.x < 16) {
+        edges_s[threadIdx.x] = threadIdx.x < nb - 1 ? edges[threadIdx.x] : 0.0;
+        edges_f[threadIdx.x] = float(edges_s[threadIdx.x]);
+    }
     __syncthreads();
-    const float inv_dx_f = float(1.0 / p.dx);
     const float efac_f = float(0.5 * m_e() * j_ev());
     const double efac_d = 0.5 * m_e() * j_ev();
     const int lane = threadIdx.x & 31;
@@ -321,11 +340,11 @@ __global__ void __launch_bounds__(256) k_seg_bin_keys(bz_params p, const T *x, c
                 int key = nkeys;
                 if (wi > T(0)) {
                     int cell = bin_cell(p.advect, x[i], p.dx, inv_dx_f);
-                    int e = energy_bin(vx[i], vy[i], vz[i], wi, nb, edges_s, efac_f, efac_d);
+                    int e = energy_bin(vx[i], vy[i], vz[i], wi, nb, edges_s, edges_f, efac_f, efac_d);
                     if (cell >= 0 && cell < p.n_nodes && e >= 0) {
                         key = cell * nb + e;
                         atomicAdd(&c_s[key], 1u);
-                        if (double(wi) > min_wt) atomicAdd(&h_s[key], 1u);
+                        if (above_min(wi, min_wt, wmin_f)) atomicAdd(&h_s[key], 1u);
                     } else {
                         err |= BZ_DEV_BINRANGE;
                     }
@@ -398,7 +417,8 @@ static int seg_bin_entry(const bz_params *pp, S s, int nb, const double *edges, 
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int kb = std::max(1, std::min(sms * 4, int(ceil_div(s.nseg, 8))));
-    kk<<<kb, 256, smem, st>>>(p, s.x, s.vx, s.vy, s.vz, s.w, s.counts, s.nseg, s.half, pre, nb, edges, min_wt, keys_a,
+    kk<<<kb, 256, smem, st>>>(p, s.x, s.vx, s.vy, s.vz, s.w, s.counts, s.nseg, s.half, pre, nb, edges, min_wt,
+                              float_above(min_wt), float(1.0 / p.dx), keys_a,
                               slots, counts, hw_counts, nkeys, status);
     const int grid = int(ceil_div(cap, RB_TILE));
     const bool two = nkeys >= RADIX;

@@ -16,6 +16,9 @@ namespace bz {
 template <typename T> struct SoAR { T *x, *vx, *vy, *vz, *w; };
 
 constexpr int RS_T = 256;
+// a key's cumulative-weight table lives in shared memory when it has at most RS_CDF
+// entries (the binary searches of the draws then hit shared memory), else in the scratch
+constexpr int RS_CDF = 4096;
 enum { ACT_NONE = 0, ACT_SPLIT = 1, ACT_MERGE = 2 };
 
 struct RsWs {
@@ -200,7 +203,10 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
     const int tk = (p.flags & BZ_PER_KEY_TARGETS) ? key : b;  // target / max_ppc entry
     const int64_t T_ = targets[tk];
     const double efac = 0.5 * m_e() * j_ev();
-    double *cdf = ws_cdf + off;
+    extern __shared__ double cdf_sh[];
+    // table length: the split's candidates (at most n_k) or the merge's first max_ppc
+    const int tab_len = (a == ACT_SPLIT) ? n_k : min(n_k, int(max_ppc[tk]));
+    double *cdf = tab_len <= RS_CDF ? cdf_sh : ws_cdf + off;
     int32_t *cnt = ws_cnt + off;
     if (a == ACT_SPLIT) {
         // ---- split (boltzmann.py:806-823): candidates w > min_wt, in index order
@@ -251,17 +257,29 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
         __syncthreads();
         if (p.flags & BZ_QUIRK_SPLIT_WRAP) {
             // HW_ids[unique_ids[v]]: the drawn particle id indexes the candidate list and
-            // CuPy wraps it modulo the list length (boltzmann.py:818-823). Sequential, since
-            // two entries may land on the same particle and divide its weight twice.
-            if (threadIdx.x == 0) {
-                for (int j = 0; j < nhw; ++j) {
-                    int c = cnt[j];
-                    if (!c) continue;
-                    int t = hw_ids[hw_ids[j] % nhw];
-                    double wt = double(s.w[t]) / double(c + 1);
-                    s.w[t] = T(wt);
-                    cdf[j] = double(T(wt));  // weight of this entry's copies
-                    tgt[j] = t;
+            // CuPy wraps it modulo the list length (boltzmann.py:818-823). Two entries may
+            // land on the same particle and divide its weight twice, in entry order. Warp 0
+            // takes 32 entries at a time; lanes that share a target go one after another in
+            // lane (= entry) order, the others at once.
+            if (threadIdx.x < 32) {
+                const int lane = threadIdx.x;
+                for (int j0 = 0; j0 < nhw; j0 += 32) {
+                    const int j = j0 + lane;
+                    const int c = j < nhw ? cnt[j] : 0;
+                    const int t = c ? hw_ids[hw_ids[j] % nhw] : -1;
+                    const unsigned grp = __match_any_sync(0xffffffffu, t);
+                    unsigned pending = __ballot_sync(0xffffffffu, c != 0);
+                    while (pending) {  // at most 32 rounds: each round serves every group's first lane
+                        const bool now = ((pending >> lane) & 1u) && !(grp & pending & ((1u << lane) - 1u));
+                        if (now) {
+                            const double wt = double(s.w[t]) / double(c + 1);
+                            s.w[t] = T(wt);
+                            cdf[j] = double(T(wt));  // weight of this entry's copies
+                            tgt[j] = t;
+                        }
+                        __syncwarp();  // this round's weights are visible to the next
+                        pending &= ~__ballot_sync(0xffffffffu, now);
+                    }
                 }
             }
         } else {
@@ -533,7 +551,8 @@ static int resample_entry(const bz_params *pp, P s_, const int32_t *n, int64_t c
     if (cons_diag && cudaMemsetAsync(cons_diag, 0, sizeof(double) * 10 * nkeys, st) != cudaSuccess) return BZ_ERR_CUDA;
     SoAR<T> s{s_.x, s_.vx, s_.vy, s_.vz, s_.w};
     SoAR<T> o{out_.x, out_.vx, out_.vy, out_.vz, out_.w};
-    k_rs_apply<T><<<nkeys, RS_T, 0, st>>>(p, s, n, cap, nb, targets, max_ppc, min_wt, merge_keep, perm, offsets,
+    k_rs_apply<T><<<nkeys, RS_T, RS_CDF * sizeof(double), st>>>(p, s, n, cap, nb, targets, max_ppc, min_wt,
+                                                                merge_keep, perm, offsets,
                                           counts, act, app_off, draw_off, replay_u, cdf, cnt, cons_diag,
                                           SoAR<T>{nullptr, nullptr, nullptr, nullptr, nullptr}, 0, status);
     if (cudaGetLastError() != cudaSuccess) return BZ_ERR_CUDA;
@@ -607,7 +626,8 @@ static int seg_resample_entry(const bz_params *pp, S s_, P app_, int64_t app_cap
     if (cons_diag && cudaMemsetAsync(cons_diag, 0, sizeof(double) * 10 * nkeys, st) != cudaSuccess) return BZ_ERR_CUDA;
     SoAR<T> s{s_.x, s_.vx, s_.vy, s_.vz, s_.w};
     SoAR<T> app{app_.x, app_.vx, app_.vy, app_.vz, app_.w};
-    k_rs_apply<T><<<nkeys, RS_T, 0, st>>>(p, s, nullptr, cap, nb, targets, max_ppc, min_wt, merge_keep, perm, offsets,
+    k_rs_apply<T><<<nkeys, RS_T, RS_CDF * sizeof(double), st>>>(p, s, nullptr, cap, nb, targets, max_ppc, min_wt,
+                                                                merge_keep, perm, offsets,
                                           counts, act, app_off, draw_off, replay_u, cdf, cnt, cons_diag, app, app_cap,
                                           status);
     if (cudaGetLastError() != cudaSuccess) return BZ_ERR_CUDA;

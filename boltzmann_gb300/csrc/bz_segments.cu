@@ -24,8 +24,11 @@ namespace bz {
 // the minimum resident CTAs per SM the registers are budgeted for. Entry 0 is the
 // default; bz_seg_push_select() picks another for the float32 table + deposit push (the
 // solver's hot loop), which is what the autotuner times.
-struct SegShape { int threads, per_lane, min_blocks; };
-constexpr SegShape kSegShapes[] = {{320, 1, 4}, {256, 1, 4}, {256, 2, 4}, {512, 1, 3}, {640, 1, 2}, {256, 4, 3}};
+// prefetch: the next round's particle is loaded into registers while this round computes
+// (one particle per lane only; costs five registers, so it pairs with 64-register shapes).
+struct SegShape { int threads, per_lane, min_blocks; bool prefetch; };
+constexpr SegShape kSegShapes[] = {{512, 1, 2, true}, {320, 1, 4, true}, {640, 1, 2, true}, {384, 1, 3, true},
+                                   {448, 1, 2, true}, {320, 1, 4, false}, {256, 2, 4, false}, {256, 1, 4, true}};
 constexpr int kSegNumShapes = int(sizeof(kSegShapes) / sizeof(kSegShapes[0]));
 static int g_seg_shape = 0;
 
@@ -39,7 +42,7 @@ __device__ __forceinline__ int64_t seg_slot(int seg, int run, int half, int j) {
     return int64_t(seg) * (2 * int64_t(half)) + int64_t(run) * half + j;
 }
 
-template <typename T, bool REPLAY, int XS, bool DEPOSIT, int SG_T, int SG_I, int MINB>
+template <typename T, bool REPLAY, int XS, bool DEPOSIT, int SG_T, int SG_I, int MINB, bool PF>
 __global__ void __launch_bounds__(SG_T, MINB)
     k_seg_push(bz_params p, PushConst<T> kc, Seg<T> in, Seg<T> out, const T *E, const double *R, const double *gas,
                double *moments, unsigned long long *n_pushed, unsigned int *ticket, uint32_t *seg_flags,
@@ -81,11 +84,28 @@ __global__ void __launch_bounds__(SG_T, MINB)
             }
             if (n_pushed && lane == 0 && cnt > 0) atomicAdd(n_pushed, (unsigned long long)cnt);
             const int64_t rbase = seg_slot(seg, run, H, 0);
+            // one particle of the run (zeros past its end)
+            auto fetch = [&](int j, T &a, T &b, T &c, T &d, T &e) {
+                const bool ok = j < cnt;
+                const int64_t q = rbase + j;
+                a = ok ? in.a.x[q] : T(0);
+                b = ok ? in.a.vx[q] : T(0);
+                c = ok ? in.a.vy[q] : T(0);
+                d = ok ? in.a.vz[q] : T(0);
+                e = ok ? in.a.w[q] : T(0);
+            };
+            T px = T(0), pvx = T(0), pvy = T(0), pvz = T(0), pw = T(0);  // the next round (prefetch)
+            if constexpr (PF) fetch(lane, px, pvx, pvy, pvz, pw);
             for (int r0 = 0; r0 < cnt; r0 += SG_R) {
                 const int j0 = r0 + lane * SG_I;
                 T x[SG_I], vx[SG_I], vy[SG_I], vz[SG_I], w[SG_I];
                 bool vec = false;
-                if constexpr (SG_I == 4 && sizeof(T) == 4) {
+                if constexpr (PF) {
+                    static_assert(SG_I == 1, "prefetch takes one particle per lane");
+                    x[0] = px; vx[0] = pvx; vy[0] = pvy; vz[0] = pvz; w[0] = pw;
+                    fetch(r0 + SG_R + lane, px, pvx, pvy, pvz, pw);
+                    vec = true;
+                } else if constexpr (SG_I == 4 && sizeof(T) == 4) {
                   if (j0 + SG_I <= cnt && (H % 4) == 0) {
                     vec = true;
                     const int64_t b = rbase + j0;
@@ -403,7 +423,7 @@ template <typename T, typename S> static Seg<T> to_seg(const S &s) {
 }
 
 template <typename T, bool REPLAY, int XS, bool DEPOSIT, int SG_T = kSegShapes[0].threads,
-          int SG_I = kSegShapes[0].per_lane, int MINB = kSegShapes[0].min_blocks>
+          int SG_I = kSegShapes[0].per_lane, int MINB = kSegShapes[0].min_blocks, bool PF = kSegShapes[0].prefetch>
 static int launch_seg_push(const bz_params &p, Seg<T> in, Seg<T> out, const T *E, const double *R, const double *gas,
                            double *moments, uint64_t *n_pushed, void *ws, uint32_t *seg_flags, uint32_t *status,
                            cudaStream_t st) {
@@ -412,7 +432,7 @@ static int launch_seg_push(const bz_params &p, Seg<T> in, Seg<T> out, const T *E
     const int xsn = (XS == BZ_XS_TABLE) ? p.xs_n : 0;
     const size_t smem = size_t(xsn) * sizeof(float4) + (DEPOSIT ? size_t(3) * p.n_nodes * sizeof(A) : 0) +
                         size_t(nf) * sizeof(T);
-    auto kern = k_seg_push<T, REPLAY, XS, DEPOSIT, SG_T, SG_I, MINB>;
+    auto kern = k_seg_push<T, REPLAY, XS, DEPOSIT, SG_T, SG_I, MINB, PF>;
     if (smem > 48 * 1024 &&
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess)
         return BZ_ERR_UNSUPPORTED;
@@ -457,20 +477,22 @@ static int seg_push_entry(const bz_params *pp, S in_, S out_, const T *E, const 
 #define BZ_SEG_SHAPE(K)                                                                                            \
     case K:                                                                                                        \
         return launch_seg_push<T, false, BZ_XS_TABLE, true, kSegShapes[K].threads, kSegShapes[K].per_lane,           \
-                               kSegShapes[K].min_blocks>(p, in, out, E, R, gas, moments, n_pushed, ws, seg_flags,  \
-                                                         status, st);
+                               kSegShapes[K].min_blocks, kSegShapes[K].prefetch>(p, in, out, E, R, gas, moments,   \
+                                                                                 n_pushed, ws, seg_flags, status, st);
             switch (g_seg_shape) {
                 BZ_SEG_SHAPE(1)
                 BZ_SEG_SHAPE(2)
                 BZ_SEG_SHAPE(3)
                 BZ_SEG_SHAPE(4)
                 BZ_SEG_SHAPE(5)
+                BZ_SEG_SHAPE(6)
+                BZ_SEG_SHAPE(7)
                 default: break;
             }
 #undef BZ_SEG_SHAPE
         }
     }
-    static_assert(kSegNumShapes == 6, "one case per CTA shape");
+    static_assert(kSegNumShapes == 8, "one case per CTA shape");
 #define BZ_SEG_CASE(RP, XSM, DP)                                                                                    \
     if (replay == RP && p.xs_mode == XSM && dep == DP)                                                             \
         return launch_seg_push<T, RP, XSM, DP>(p, in, out, E, R, gas, moments, n_pushed, ws, seg_flags, status, st);
@@ -605,11 +627,13 @@ extern "C" {
 
 size_t bz_seg_push_workspace(void) { return 256; }
 int32_t bz_seg_push_shapes(void) { return bz::kSegNumShapes; }
-int bz_seg_push_shape_info(int32_t shape, int32_t *threads, int32_t *per_lane, int32_t *min_blocks) {
+int bz_seg_push_shape_info(int32_t shape, int32_t *threads, int32_t *per_lane, int32_t *min_blocks,
+                           int32_t *prefetch) {
     if (shape < 0 || shape >= bz::kSegNumShapes) return BZ_ERR_ARG;
     if (threads) *threads = bz::kSegShapes[shape].threads;
     if (per_lane) *per_lane = bz::kSegShapes[shape].per_lane;
     if (min_blocks) *min_blocks = bz::kSegShapes[shape].min_blocks;
+    if (prefetch) *prefetch = bz::kSegShapes[shape].prefetch ? 1 : 0;
     return BZ_OK;
 }
 int bz_seg_push_select(int32_t shape) {

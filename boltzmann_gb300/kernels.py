@@ -246,14 +246,14 @@ def seg_electron_kernel(params, src: SegmentSet, dst: SegmentSet, E, status, seg
 
 
 def seg_push_shapes():
-    """CTA shapes (threads, particles per lane, CTAs per SM) of the float32 table +
-    deposit segmented push; index 0 is the library default."""
+    """CTA shapes (threads, particles per lane, CTAs per SM, prefetch) of the float32
+    table + deposit segmented push; index 0 is the library default."""
     lib = _lib.load()
     out = []
     for k in range(lib.bz_seg_push_shapes()):
-        t, i, m = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
-        call("bz_seg_push_shape_info", k, ctypes.byref(t), ctypes.byref(i), ctypes.byref(m))
-        out.append((t.value, i.value, m.value))
+        t, i, m, f = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        call("bz_seg_push_shape_info", k, ctypes.byref(t), ctypes.byref(i), ctypes.byref(m), ctypes.byref(f))
+        out.append((t.value, i.value, m.value, bool(f.value)))
     return out
 
 

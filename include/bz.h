@@ -240,12 +240,13 @@ int bz_seg_push_collide_f64(const bz_params *p, bz_segments_f64 in, bz_segments_
                             uint64_t *n_pushed, void *workspace, size_t workspace_bytes, uint32_t *seg_flags,
                             uint32_t *status, void *stream);
 /* CTA shapes of the float32 table + deposit segmented push (threads per CTA, particles
- * per lane per round, CTAs per SM the registers are budgeted for). Shape 0 is the
- * default; bz_seg_push_select sets the shape later launches use (process-wide; select
- * before capturing a graph). Results do not depend on the shape except for the
- * summation order of the float moments. */
+ * per lane per round, CTAs per SM the registers are budgeted for, whether the next
+ * round is prefetched into registers). Shape 0 is the default; bz_seg_push_select sets
+ * the shape later launches use (process-wide; select before capturing a graph). Results
+ * do not depend on the shape except for the summation order of the float moments. */
 int32_t bz_seg_push_shapes(void);
-int bz_seg_push_shape_info(int32_t shape, int32_t *threads, int32_t *per_lane, int32_t *min_blocks);
+int bz_seg_push_shape_info(int32_t shape, int32_t *threads, int32_t *per_lane, int32_t *min_blocks,
+                           int32_t *prefetch);
 int bz_seg_push_select(int32_t shape);
 int32_t bz_seg_push_selected(void);
 /* All particles with w != 0 of *in (segment order, run 0 then run 1; in may be NULL)
