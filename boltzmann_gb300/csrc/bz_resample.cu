@@ -226,11 +226,14 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
         if (nhw == 0) return;
         for (int j = threadIdx.x; j < nhw; j += RS_T) W += double(s.w[cnt[j]]);
         W = block_sum<double>(W, shd);
-        // cdf = cumsum(w/W), then / cdf[-1] (CuPy RandomState.choice with p)
+        // cdf = cumsum(w/W), then / cdf[-1] (CuPy RandomState.choice with p); the
+        // divisions are multiplications by the reciprocal (within 2 ulp; float64 division
+        // is many instructions on this part's narrow float64 pipe)
+        const double inv_W = 1.0 / W;
         double carry = 0.0;
         for (int c0 = 0; c0 < nhw; c0 += RS_T) {
             int j = c0 + threadIdx.x;
-            double v = j < nhw ? double(s.w[cnt[j]]) / W : 0.0;
+            double v = j < nhw ? double(s.w[cnt[j]]) * inv_W : 0.0;
             double tot;
             double ex = block_excl_scan<double>(v, shd, &tot);
             if (j < nhw) cdf[j] = carry + ex + v;
@@ -238,7 +241,8 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
         }
         __syncthreads();
         const double last = cdf[nhw - 1];
-        for (int j = threadIdx.x; j < nhw; j += RS_T) cdf[j] = cdf[j] / last;
+        const double inv_last = 1.0 / last;
+        for (int j = threadIdx.x; j < nhw; j += RS_T) cdf[j] = cdf[j] * inv_last;
         __syncthreads();
         // scratch regions of this key: cnt = draw counts, hw_ids = candidate ids, tgt = copy targets
         int32_t *hw_ids = ws_cnt + cap + off;
@@ -339,13 +343,14 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
     py = block_sum<double>(py, shd);
     pz = block_sum<double>(pz, shd);
     ew = block_sum<double>(ew, shd);
+    const double inv_W = 1.0 / W;
     const double ux = px / W, uy = py / W, uz = pz / W;
     const double T_cell = (2.0 / 3.0) * (ew / W);
     // cdf = cumsum(w/W) (not renormalised), stratified R_k = (1/K)(u_k + k)
     double carry = 0.0;
     for (int c0 = 0; c0 < np_; c0 += RS_T) {
         int j = c0 + threadIdx.x;
-        double v = j < np_ ? double(s.w[perm[off + j]]) / W : 0.0;
+        double v = j < np_ ? double(s.w[perm[off + j]]) * inv_W : 0.0;
         double tot;
         double ex = block_excl_scan<double>(v, shd, &tot);
         if (j < np_) cdf[j] = carry + ex + v;

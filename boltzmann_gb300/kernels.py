@@ -262,7 +262,7 @@ def select_seg_push_shape(k):
 
 
 def autotune_seg_push(params, src: SegmentSet, dst: SegmentSet, E, status, seg_flags, ws: Workspace, moments,
-                      reps=5, warmup=2):
+                      reps=10, warmup=2):
     """Time every CTA shape of the float32 table + deposit push on src -> dst with CUDA
     events and select the fastest (process-wide, for later launches and captures). src
     is only read; dst, moments and the flag words are left as before the call. Returns

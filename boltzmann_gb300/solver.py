@@ -105,10 +105,8 @@ class BoltzmannGB300:
         self._grid_solves(advance=False)
         # CTA shape of the push, timed on the initial state (A is only read)
         self.push_shape = None
-        if cfg.autotune and self.dtype == torch.float32:
-            best, times = K.autotune_seg_push(self.params(step_on_device=False), self.A, self.B, self.E_push,
-                                              self.status, self.seg_flags, self.ws, self.moments)
-            self.push_shape = {"shape": K.seg_push_shapes()[best], "ms": times}
+        if cfg.autotune:
+            self.retune()
 
     # ---------------------------------------------------------------------------------
     def _ne_profile(self):
@@ -263,6 +261,16 @@ class BoltzmannGB300:
                     host_block.dtype != torch.float64:
                 raise ValueError(f"host block must be pinned float64 of {self.io.numel()} values")
         self._host_io = host_block
+        self._graphs = {}
+
+    def retune(self):
+        """Time the push's CTA shapes on the current state (A is only read) and keep the
+        fastest; the step graphs, which hold the kernel, are captured again."""
+        if self.dtype != torch.float32:
+            return
+        best, times = K.autotune_seg_push(self.params(step_on_device=False), self.A, self.B, self.E_push,
+                                          self.status, self.seg_flags, self.ws, self.moments)
+        self.push_shape = {"shape": K.seg_push_shapes()[best], "ms": times}
         self._graphs = {}
 
     def _capture_key(self, key):

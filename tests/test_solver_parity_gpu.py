@@ -3,9 +3,9 @@ argon CCP: 128 cells, 1e5 electrons at 1 eV, 3-bin ES-WPNC every 50 steps, 400 s
 tau/4000 (a tenth of an RF cycle, while the sheaths form; at tau/400 this explicit scheme
 heats the uniform start within a cycle, which makes a poor statistical test). The two
 use different random streams, so they are compared
-statistically: the oracle run must fall within the spread of four independent GPU runs
-(4 sigma, plus 0.5% for the remaining float32 effects) for the electron count, the
-ionizations, the mean energy and the cycle-averaged density in eight regions.
+statistically: the mean of two oracle runs and the mean of eight independent GPU runs must
+agree within four standard errors (plus 0.5% for the remaining float32 effects) for the
+electron count, the ionizations, the mean energy and the averaged density in eight regions.
 """
 import math
 
@@ -51,20 +51,30 @@ def gpu_run(seed):
 
 
 def test_solver_matches_oracle_step_loop_statistically():
-    # the oracle starts from the initial state of the seed-0 GPU solver
+    # two oracle runs (different random streams) from the initial state of the seed-0 GPU
+    # solver, eight GPU runs with their own seeds; the means must agree within 4 standard
+    # errors of the difference (+0.5%), the spread taken from the GPU runs and, for the
+    # ionizations (a few hundred events), never below the counting noise
     s0 = BoltzmannGB300(cfg(0), device="cuda")
     st = s0.A.to_numpy("segments")
-    orc = OracleCCP(s0.cfg, st["x"], st["vx"], st["vy"], st["vz"], st["w"], s0.ni.cpu().numpy(), s0.xs, seed=5)
+    w_mean = float(st["w"].mean())
+    oracle = []
+    for seed in (5, 6):
+        orc = OracleCCP(s0.cfg, st["x"], st["vx"], st["vy"], st["vz"], st["w"], s0.ni.cpu().numpy(), s0.xs,
+                        seed=seed)
+        moms = []
+        for _ in range(STEPS):
+            orc.step()
+            moms.append(orc.moments.copy())
+        oracle.append(observe(moms, float(orc.state()["w"].sum())))
     del s0
-    moms = []
-    for _ in range(STEPS):
-        orc.step()
-        moms.append(orc.moments.copy())
-    o = observe(moms, float(orc.state()["w"].sum()))
-    runs = [gpu_run(seed)[1] for seed in (1, 2, 3, 4)]
-    for k in o:
+    runs = [gpu_run(seed)[1] for seed in range(1, 9)]
+    for k in oracle[0]:
         g = np.array([r[k] for r in runs])
-        mu, sd = g.mean(), g.std(ddof=1)
-        lim = 4 * sd * math.sqrt(1 + 1 / len(g)) + 0.005 * abs(mu)
-        assert abs(o[k] - mu) <= lim, f"{k}: oracle {o[k]:.6g}, GPU {mu:.6g} +- {sd:.3g}"
-    assert o["ionizations"] > 0
+        o = np.array([r[k] for r in oracle])
+        sd = g.std(ddof=1)
+        if k == "ionizations":
+            sd = max(sd, w_mean * math.sqrt(g.mean() / w_mean))
+        lim = 4 * sd * math.sqrt(1 / len(g) + 1 / len(o)) + 0.005 * abs(g.mean())
+        assert abs(o.mean() - g.mean()) <= lim, f"{k}: oracle {o}, GPU {g.mean():.6g} +- {sd:.3g}"
+    assert min(r["ionizations"] for r in oracle) > 0
