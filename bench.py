@@ -102,8 +102,11 @@ def dist_setup():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     pg = None
     if world > 1:
+        import torch
         import torch.distributed as dist
-        backend = "nccl"
+        # one replica per GPU over NCCL; gloo where no GPU is visible (the reference arm,
+        # which runs on the host cores, and the CPU tests of this launch path)
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
         dist.init_process_group(backend=backend)
         pg = dist
     return world, rank, local, pg
