@@ -226,7 +226,7 @@ def run_ours(args, world, rank, local, pg):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     cfg = config.ccp_1024(num_particles=int(args.particles), gridpts=args.cells + 1, resample_freq=args.rsf,
-                          seed=1 + rank, autotune=not args.no_autotune, capacity_factor=4.0)
+                          seed=1 + rank, autotune=not args.no_autotune, capacity_factor=4.0, seg_half=args.seg_half)
     sol = BoltzmannGB300(cfg, device=dev)
     n_start = sol.n()
     for _ in range(args.warmup):
@@ -429,6 +429,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the push's default CTA shape")
+    ap.add_argument("--seg-half", type=int, default=4096, help="slots per run of a particle segment")
     ap.add_argument("--cpu-sample", type=float, default=1e6)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--ref-sample", type=float, default=2e6)

@@ -284,7 +284,12 @@ def autotune_seg_push(params, src: SegmentSet, dst: SegmentSet, E, status, seg_f
         e1.record(st)
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1) / reps)
+    # the default (shape 0) stays unless another shape is clearly faster: the ranking of
+    # close shapes moves with the state (collision rate), the default is the best measured
+    # on a heated CCP
     best = int(np.argmin(times))
+    if times[best] > 0.97 * times[0]:
+        best = 0
     select_seg_push_shape(best)
     status.copy_(saved[0]); seg_flags.copy_(saved[1]); moments.copy_(saved[2]); dst.counts.copy_(saved[3])
     return best, times
