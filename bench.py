@@ -429,7 +429,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the push's default CTA shape")
-    ap.add_argument("--seg-half", type=int, default=4096, help="slots per run of a particle segment")
+    ap.add_argument("--seg-half", type=int, default=2048, help="slots per run of a particle segment")
     ap.add_argument("--cpu-sample", type=float, default=1e6)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--ref-sample", type=float, default=2e6)

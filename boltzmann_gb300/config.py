@@ -62,7 +62,7 @@ class CCPConfig:
     # of 2*seg_half slots (one warp pushes one segment)
     num_particles: int = 200000
     capacity_factor: float = 2.5
-    seg_half: int = 4096
+    seg_half: int = 2048
     Te_init_eV: float = 0.5           # boltzmann.py:249 (the benchmark CCPs start at 1 eV)
     ne_profile: str = "reference"     # "reference" (boltzmann.py:246-247) or "uniform"
     ne_uniform: float = 1e9           # cm^-3 when ne_profile == "uniform"

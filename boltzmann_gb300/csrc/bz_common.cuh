@@ -42,6 +42,31 @@ __device__ __forceinline__ u32x4 philox(uint32_t c0, uint32_t c1, uint32_t c2, u
     return {c0, c1, c2, c3};
 }
 
+// The same generator with the ten round keys precomputed (k + r*W, r = 0..9): when they sit
+// in the kernel's parameter space the XORs read them directly and no key schedule runs.
+__device__ __forceinline__ u32x4 philox_rk(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, const uint32_t *rk0,
+                                           const uint32_t *rk1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint64_t p0 = uint64_t(0xD2511F53u) * c0;
+        const uint64_t p1 = uint64_t(0xCD9E8D57u) * c2;
+        const uint32_t hi0 = uint32_t(p0 >> 32), lo0 = uint32_t(p0);
+        const uint32_t hi1 = uint32_t(p1 >> 32), lo1 = uint32_t(p1);
+        c0 = hi1 ^ c1 ^ rk0[r];
+        c1 = lo1;
+        c2 = hi0 ^ c3 ^ rk1[r];
+        c3 = lo0;
+    }
+    return {c0, c1, c2, c3};
+}
+inline void philox_round_keys(uint64_t seed, uint32_t *rk0, uint32_t *rk1) {
+    uint32_t k0 = uint32_t(seed), k1 = uint32_t(seed >> 32);
+    for (int r = 0; r < 10; ++r, k0 += 0x9E3779B9u, k1 += 0xBB67AE85u) {
+        rk0[r] = k0;
+        rk1[r] = k1;
+    }
+}
+
 // A uniform and its complement, both exact: float path u = ((r>>9)+0.5)*2^-23;
 // double path u = ((hi26<<26 | lo26) + 0.5)*2^-52. Keeping 1-u exact lets sin(chi)
 // = 2 sqrt(u(1-u)) keep full relative accuracy near the poles.
@@ -79,6 +104,18 @@ __device__ __forceinline__ void draw4(const Rng &g, uint32_t slot, uint32_t tag,
 __device__ __forceinline__ void draw4(const Rng &g, uint32_t slot, uint32_t tag, Draw4<double> &d) {
     u32x4 a = philox(slot, g.s0, g.s1, tag, g.k0, g.k1);
     u32x4 b = philox(slot, g.s0, g.s1, tag | (1u << 8), g.k0, g.k1);
+    d.v[0] = uni_d(a.x, a.y); d.v[1] = uni_d(a.z, a.w); d.v[2] = uni_d(b.x, b.y); d.v[3] = uni_d(b.z, b.w);
+}
+// the same draws with precomputed round keys
+__device__ __forceinline__ void draw4(const Rng &g, const uint32_t *rk0, const uint32_t *rk1, uint32_t slot,
+                                      uint32_t tag, Draw4<float> &d) {
+    u32x4 r = philox_rk(slot, g.s0, g.s1, tag, rk0, rk1);
+    d.v[0] = uni_f(r.x); d.v[1] = uni_f(r.y); d.v[2] = uni_f(r.z); d.v[3] = uni_f(r.w);
+}
+__device__ __forceinline__ void draw4(const Rng &g, const uint32_t *rk0, const uint32_t *rk1, uint32_t slot,
+                                      uint32_t tag, Draw4<double> &d) {
+    u32x4 a = philox_rk(slot, g.s0, g.s1, tag, rk0, rk1);
+    u32x4 b = philox_rk(slot, g.s0, g.s1, tag | (1u << 8), rk0, rk1);
     d.v[0] = uni_d(a.x, a.y); d.v[1] = uni_d(a.z, a.w); d.v[2] = uni_d(b.x, b.y); d.v[3] = uni_d(b.z, b.w);
 }
 

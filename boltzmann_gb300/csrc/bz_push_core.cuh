@@ -67,6 +67,7 @@ template <typename T> struct PushConst {
     T inv_nu_max;
     T dt, e_exc;    // dt and the excitation threshold in the working precision
     NodeMap nm;     // deposit node map
+    uint32_t rk0[10], rk1[10];  // Philox round keys of the seed
 };
 
 template <typename T> struct Item {
@@ -132,14 +133,14 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
     } else {
         if (k.gas_sigma > T(0)) {
             Draw4<T> d;
-            draw4(rng, slot, 0u, d);
+            draw4(rng, k.rk0, k.rk1, slot, 0u, d);
             T h;
             box_muller(d.v[0].u, d.v[1].u, g0, g1);
             box_muller(d.v[2].u, d.v[3].u, g2, h);
             g0 *= k.gas_sigma; g1 *= k.gas_sigma; g2 *= k.gas_sigma;
         }
         Draw4<T> d;
-        draw4(rng, slot, 1u, d);
+        draw4(rng, k.rk0, k.rk1, slot, 1u, d);
         u0 = d.v[0]; u1 = d.v[1]; u2 = d.v[2]; u3 = d.v[3];
         r0_replay = double(u0.u);
     }
@@ -232,7 +233,7 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
                 u5 = uni_from_replay<T>(R[size_t(slot) * 7 + 5]);
             } else {
                 Draw4<T> d;
-                draw4(rng, slot, 2u, d);
+                draw4(rng, k.rk0, k.rk1, slot, 2u, d);
                 u5 = d.v[0];
             }
             iso_dir(u3, u5, vn, o.cvx, o.cvy, o.cvz);
@@ -306,6 +307,7 @@ template <typename T> inline PushConst<T> make_push_const(const bz_params &p) {
     k.dt = T(p.dt);
     k.e_exc = T(p.e_exc);
     k.nm = make_node_map(p);
+    philox_round_keys(p.seed, k.rk0, k.rk1);
     return k;
 }
 
