@@ -93,6 +93,8 @@ _PROTOS = {
     "bz_grid_update": (ctypes.c_int, [_i32, _vp, _vp, _vp, _vp, _vp]),
     "bz_ion_fluid": (ctypes.c_int, [_i32, _f64, _f64, _f64, _f64, _vp, _vp, _vp, _vp, _vp]),
     "bz_poisson_factor": (ctypes.c_int, [_i32, _f64, _vp, _vp, _vp]),
+    "bz_field_step": (ctypes.c_int, [_i32, _f64, _f64, _f64, _f64, _f64, _f64, _f64, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                     _vp, _vp, _vp, _vp, _vp, _vp]),
     "bz_poisson": (ctypes.c_int, [_i32, _f64, _f64, _f64, _f64, _f64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "bz_advance_clock": (ctypes.c_int, [_vp, _vp, _f64, _vp]),
     "bz_seg_push_workspace": (_sz, []),

@@ -6,9 +6,10 @@
 
 namespace bz {
 
-// boltzmann.py:643-647
-__global__ void k_grid_update(int nn, const double *mom, double *ni, double *Te, double *g2) {
-    for (int i = threadIdx.x + blockIdx.x * blockDim.x; i < nn; i += blockDim.x * gridDim.x) {
+// boltzmann.py:643-647, nodes i = first, first + stride, ...
+__device__ __forceinline__ void grid_update_body(int nn, const double *mom, double *ni, double *Te, double *g2,
+                                                 int first, int stride) {
+    for (int i = first; i < nn; i += stride) {
         double ne = mom[i], src = mom[nn + i], nrg = mom[3 * nn + i];
         if (ni) ni[i] = ni[i] + src;
         if (Te) {
@@ -19,11 +20,15 @@ __global__ void k_grid_update(int nn, const double *mom, double *ni, double *Te,
     }
 }
 
-// heavies_kernel_1D.py:4-64, ion part. One CTA; the boundary nodes depend on the
+__global__ void k_grid_update(int nn, const double *mom, double *ni, double *Te, double *g2) {
+    grid_update_body(nn, mom, ni, Te, g2, threadIdx.x + blockIdx.x * blockDim.x, blockDim.x * gridDim.x);
+}
+
+// heavies_kernel_1D.py:4-64, ion part, by one whole CTA; the boundary nodes depend on the
 // interior update, so the phases are separated by barriers.
-__global__ void __launch_bounds__(1024) k_ion_fluid(int N, double dx, double dt, double mu_i, double D_i,
-                                                    const double *E, double *ni, double *Ji, int32_t *brk) {
-    __shared__ int s_brk;
+__device__ void ion_fluid_body(int N, double dx, double dt, double mu_i, double D_i, const double *E, double *ni,
+                               double *Ji, int32_t *brk, int *s_brk_p) {
+    int &s_brk = *s_brk_p;
     if (threadIdx.x == 0) {
         s_brk = 0;
         double e0 = fmax(E[0], 0.0), eN = fmin(E[N - 1], 0.0);
@@ -48,6 +53,12 @@ __global__ void __launch_bounds__(1024) k_ion_fluid(int N, double dx, double dt,
         ni[N] = ni[N - 1] * ((D_i / dx + 0.5 * mu_i * eN) / (D_i / dx - 0.5 * mu_i * eN));
         if (brk) *brk = s_brk;
     }
+}
+
+__global__ void __launch_bounds__(1024) k_ion_fluid(int N, double dx, double dt, double mu_i, double D_i,
+                                                    const double *E, double *ni, double *Ji, int32_t *brk) {
+    __shared__ int s_brk;
+    ion_fluid_body(N, dx, dt, mu_i, D_i, E, ni, Ji, brk, &s_brk);
 }
 
 // banded Cholesky factor of tridiag(-1, 2, -1)/dx^2 (what boltzmann.py:744-755 gets from
@@ -115,12 +126,13 @@ __device__ double block_inclusive_sum(double v, double *sh) {
 // prefix sums of the plan), then face fields. One CTA, float64; rows in chunks of PS_T
 // with the running sum carried between chunks. y (the forward result) lives in E until
 // the faces overwrite it.
-__global__ void __launch_bounds__(PS_T) k_poisson(int N, double dx, double eps0, double V0, double freq,
-                                                  double t_host, const double *t_dev, const double *ne,
-                                                  const double *ni, const double *plan, double *V, double *E,
-                                                  float *E32, double *y) {
-    __shared__ double sh[32];
-    __shared__ double carry, vs_s;
+struct PoissonShared { double sh[32]; double carry, vs; };
+
+__device__ void poisson_body(int N, double dx, double eps0, double V0, double freq, double t_host,
+                             const double *t_dev, const double *ne, const double *ni, const double *plan, double *V,
+                             double *E, float *E32, double *y, PoissonShared &S) {
+    double *sh = S.sh;
+    double &carry = S.carry, &vs_s = S.vs;
     const int n = N - 1;
     const double *P = plan, *g = plan + n, *Q = plan + 2 * n, *h = plan + 3 * n;
     // electrode voltage, evaluated once (float64 sin is costly on this part's narrow FP64 pipe)
@@ -170,6 +182,37 @@ __global__ void __launch_bounds__(PS_T) k_poisson(int N, double dx, double eps0,
     }
 }
 
+__global__ void __launch_bounds__(PS_T) k_poisson(int N, double dx, double eps0, double V0, double freq,
+                                                  double t_host, const double *t_dev, const double *ne,
+                                                  const double *ni, const double *plan, double *V, double *E,
+                                                  float *E32, double *y) {
+    __shared__ PoissonShared S;
+    poisson_body(N, dx, eps0, V0, freq, t_host, t_dev, ne, ni, plan, V, E, E32, y, S);
+}
+
+// The whole grid part of a step in one CTA (the order of the step loop,
+// boltzmann.py:643-678): grid update, clock, ion fluid with the field of the last solve,
+// Poisson with the new time and densities. One launch instead of four.
+__global__ void __launch_bounds__(PS_T) k_field_step(int N, double dx, double dt, double mu_i, double D_i,
+                                                     double eps0, double V0, double freq, const double *mom,
+                                                     double *ni, double *Te, double *g2, double *t_dev,
+                                                     uint64_t *step_dev, const double *plan, double *V,
+                                                     double *E, float *E32, double *Ji, int32_t *brk) {
+    __shared__ PoissonShared S;
+    __shared__ int s_brk;
+    const int nn = N + 1;
+    grid_update_body(nn, mom, ni, Te, g2, threadIdx.x, blockDim.x);
+    if (threadIdx.x == 0) {
+        if (t_dev) *t_dev = *t_dev + dt;
+        if (step_dev) *step_dev = *step_dev + 1;
+    }
+    __syncthreads();
+    ion_fluid_body(N, dx, dt, mu_i, D_i, E, ni, Ji, brk, &s_brk);
+    __syncthreads();
+    // E is the forward substitution's scratch: the fluid above has read the old field
+    poisson_body(N, dx, eps0, V0, freq, 0.0, t_dev, mom, ni, plan, V, E, E32, E, S);
+}
+
 __global__ void k_advance_clock(double *t, uint64_t *step, double dt) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         if (t) *t = *t + dt;
@@ -205,6 +248,14 @@ int bz_poisson(int32_t N, double dx, double eps0, double V0, double freq, double
     // the backward substitution has consumed y (both inside the same CTA).
     bz::k_poisson<<<1, bz::PS_T, 0, bz::as_stream(stream)>>>(N, dx, eps0, V0, freq, t_host, t_dev, ne, ni, plan, V,
                                                               E, E32, E);
+    return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+}
+int bz_field_step(int32_t N, double dx, double dt, double mu_i, double D_i, double eps0, double V0, double freq,
+                  const double *moments, double *ni, double *Te, double *g2, double *t_dev, uint64_t *step_dev,
+                  const double *plan, double *V, double *E, float *E32, double *Ji, int32_t *brk, void *stream) {
+    if (N < 3 || !moments || !ni || !t_dev || !plan || !V || !E || !Ji) return BZ_ERR_ARG;
+    bz::k_field_step<<<1, bz::PS_T, 0, bz::as_stream(stream)>>>(N, dx, dt, mu_i, D_i, eps0, V0, freq, moments, ni,
+                                                                 Te, g2, t_dev, step_dev, plan, V, E, E32, Ji, brk);
     return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
 }
 int bz_advance_clock(double *t_dev, uint64_t *step_dev, double dt, void *stream) {

@@ -68,6 +68,9 @@ template <typename T> struct PushConst {
     T dt, e_exc;    // dt and the excitation threshold in the working precision
     NodeMap nm;     // deposit node map
     uint32_t rk0[10], rk1[10];  // Philox round keys of the seed
+    T wall_lo, wall_hi;         // L*1e-3, L*(1-1e-3): closer to a wall the float64 test decides
+    float xs_last;              // xs_n - 1 (float), the table's last index
+    int xs_imax, face_max;      // xs_n - 2, n_faces - 1
 };
 
 template <typename T> struct Item {
@@ -177,8 +180,8 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
     } else {
         // n*sigma table, linear in log2(e) on the log grid
         float lt = fmaf(__log2f(float(e)), k.xs_inv_d, -k.xs_off);
-        lt = fminf(fmaxf(lt, 0.0f), float(p.xs_n - 1));
-        int i = min(int(lt), p.xs_n - 2);
+        lt = fminf(fmaxf(lt, 0.0f), k.xs_last);
+        int i = min(int(lt), k.xs_imax);
         float f = lt - float(i);
         float4 a = xs_s[i], b = xs_s[i + 1];
         T s0 = T(fmaf(f, b.x - a.x, a.x));
@@ -249,12 +252,12 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
     int face = 0;
     bool valid = true;
     if (p.advect == BZ_ADVECT_ENSEMBLE) {
-        face = min(max(int(x), 0), p.n_faces - 1);
+        face = min(max(int(x), 0), k.face_max);
     } else if (p.advect) {
         xn = x + k.c100dt * nvx;
         face = face_index(x, p.dx, k.inv_dx_f);
-        face = min(max(face, 0), p.n_faces - 1);
-        if (xn < k.L * T(1e-3) || xn > k.L * T(1 - 1e-3)) {
+        face = min(max(face, 0), k.face_max);
+        if (xn < k.wall_lo || xn > k.wall_hi) {
             // near a wall: decide in float64 like the reference
             double xd = double(x) + k.c100dt_d * double(nvx);
             valid = (0.0 < xd) && (xd < p.L);
@@ -308,6 +311,11 @@ template <typename T> inline PushConst<T> make_push_const(const bz_params &p) {
     k.e_exc = T(p.e_exc);
     k.nm = make_node_map(p);
     philox_round_keys(p.seed, k.rk0, k.rk1);
+    k.wall_lo = T(p.L) * T(1e-3);
+    k.wall_hi = T(p.L) * T(1 - 1e-3);
+    k.xs_last = float(p.xs_n - 1);
+    k.xs_imax = p.xs_n - 2;
+    k.face_max = p.n_faces - 1;
     return k;
 }
 

@@ -164,9 +164,11 @@ __global__ void __launch_bounds__(SG_T, MINB)
                             if (it[k].alive) {
                                 int nd = deposit_node(p.advect, it[k].x, nm);
                                 if (nd >= 0 && nd < nnodes) {
-                                    atomicAdd(&mom_s[nd], A(w[k]));
-                                    if (it[k].ionized) atomicAdd(&mom_s[nnodes + nd], A(w[k]));
-                                    atomicAdd(&mom_s[2 * nnodes + nd], A(w[k] * it[k].e));
+                                    if (p.advect != BZ_ADVECT_ENSEMBLE) {  // ensembles: warp-summed below
+                                        atomicAdd(&mom_s[nd], A(w[k]));
+                                        if (it[k].ionized) atomicAdd(&mom_s[nnodes + nd], A(w[k]));
+                                        atomicAdd(&mom_s[2 * nnodes + nd], A(w[k] * it[k].e));
+                                    }
                                     if (it[k].excited && (p.flags & BZ_MOMENT_EXCITATION))
                                         atomicAdd(&moments[2 * nnodes + nd], double(w[k]));  // rare: straight to the grid
                                 }
@@ -180,6 +182,37 @@ __global__ void __launch_bounds__(SG_T, MINB)
                                     atomicAdd(&mom_s[2 * nnodes + nd], A(w[k] * it[k].ce));
                                 }
                             }
+                        }
+                    }
+                }
+                if (DEPOSIT && p.advect == BZ_ADVECT_ENSEMBLE) {
+                    // in an ensemble a warp's particles usually belong to one swarm: when all
+                    // lanes deposit to the same node, sum over the warp first (one atomic per
+                    // moment instead of 32 colliding ones)
+#pragma unroll
+                    for (int k = 0; k < SG_I; ++k) {
+                        int nd = it[k].alive ? int(it[k].x) : -1;
+                        if (nd >= nnodes) nd = -1;
+                        A c0 = nd >= 0 ? A(w[k]) : A(0);
+                        A c1 = (nd >= 0 && it[k].ionized) ? A(w[k]) : A(0);
+                        A c2 = nd >= 0 ? A(w[k] * it[k].e) : A(0);
+                        const int nd0 = __shfl_sync(0xffffffffu, nd, 0);
+                        if (__all_sync(0xffffffffu, nd == nd0)) {
+#pragma unroll
+                            for (int o = 16; o > 0; o >>= 1) {
+                                c0 += __shfl_xor_sync(0xffffffffu, c0, o);
+                                c1 += __shfl_xor_sync(0xffffffffu, c1, o);
+                                c2 += __shfl_xor_sync(0xffffffffu, c2, o);
+                            }
+                            if (lane == 0 && nd0 >= 0) {
+                                atomicAdd(&mom_s[nd0], c0);
+                                if (c1 != A(0)) atomicAdd(&mom_s[nnodes + nd0], c1);
+                                atomicAdd(&mom_s[2 * nnodes + nd0], c2);
+                            }
+                        } else if (nd >= 0) {
+                            atomicAdd(&mom_s[nd], c0);
+                            if (c1 != A(0)) atomicAdd(&mom_s[nnodes + nd], c1);
+                            atomicAdd(&mom_s[2 * nnodes + nd], c2);
                         }
                     }
                 }

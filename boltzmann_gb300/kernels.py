@@ -367,5 +367,13 @@ def EF_kernel(N, dx, eps0, V0, freq, t, ne, ni, plan, V, E, E32=None, t_dev=None
          _ptr(ni), _ptr(plan), _ptr(V), _ptr(E), _ptr(E32), _stream())
 
 
+def field_step(N, dx, dt, mu_i, D_i, eps0, V0, freq, moments, ni, Te, g2, t_dev, step_dev, plan, V, E, E32, Ji,
+               brk=None):
+    """Grid update, clock, ion fluid and Poisson of one step in one launch."""
+    call("bz_field_step", int(N), float(dx), float(dt), float(mu_i), float(D_i), float(eps0), float(V0), float(freq),
+         _ptr(moments), _ptr(ni), _ptr(Te), _ptr(g2), _ptr(t_dev), _ptr(step_dev), _ptr(plan), _ptr(V), _ptr(E),
+         _ptr(E32), _ptr(Ji), _ptr(brk), _stream())
+
+
 def advance_clock(t_dev, step_dev, dt):
     call("bz_advance_clock", _ptr(t_dev), _ptr(step_dev), float(dt), _stream())

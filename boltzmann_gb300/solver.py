@@ -203,12 +203,18 @@ class BoltzmannGB300:
             self.E_push.copy_(self.E)
 
     def _grid_solves(self, advance=True):
+        """Grid update, clock, ion fluid and Poisson (boltzmann.py:643-678) in one launch;
+        the first solve (advance=False) is the Poisson alone."""
         cfg = self.cfg
-        if advance:
-            K.grid_update(self.nnodes, self.moments, self.ni, self.Te, self.g2)
-            K.advance_clock(self.t, self.step_dev, cfg.dt)
-            self.heavies_kernel_fluid()
-        self.EF_kernel()
+        if not advance:
+            self.EF_kernel()
+            return
+        f32 = self.dtype == torch.float32
+        K.field_step(self.N, cfg.dx, cfg.dt, cfg.mu_i, cfg.D_i, cfg.eps0, cfg.V0, cfg.freq, self.moments, self.ni,
+                     self.Te, self.g2, self.t, self.step_dev, self.poisson_plan, self.V, self.E,
+                     self.E_push if f32 else None, self.Ji, self.brk)
+        if not f32:
+            self.E_push.copy_(self.E)
 
     # --------------------------------------------------------------------------------- stepping
     def _step_body(self, resample):
@@ -336,13 +342,13 @@ class BoltzmannGB300:
     # --------------------------------------------------------------------------------- diagnostics
     def kernel_launches(self, resample):
         """libbz kernels one step launches (torch's memset of the moments not counted).
-        Every step: the push, grid update, clock, ion fluid and Poisson (5); a plain step
-        adds the conditional rebalance (one cooperative kernel); a resampling step
-        adds binning (segment totals, key offsets twice, keys, then per 8-bit radix pass a
-        histogram, scan and scatter), decide + apply (2) and the repack of the survivors
-        with the appended particles (1)."""
+        Every step: the push and the fused grid step (grid update, clock, ion fluid,
+        Poisson) (2); a plain step adds the conditional rebalance (one cooperative
+        kernel); a resampling step adds binning (segment totals, key offsets twice, keys,
+        then per 8-bit radix pass a histogram, scan and scatter), decide + apply (2) and the
+        repack of the survivors with the appended particles (1)."""
         passes = 2 if self.nnodes * self.nb >= 256 else 1
-        return 5 + (4 + 3 * passes + 2 + 1 if resample else 1)
+        return 2 + (4 + 3 * passes + 2 + 1 if resample else 1)
 
     def n(self):
         return self.A.n()

@@ -208,6 +208,13 @@ int bz_poisson_factor(int32_t N, double dx, double *chol_diag, double *chol_lowe
 int bz_poisson(int32_t N, double dx, double eps0, double V0, double freq, double t_host, const double *t_dev,
                const double *ne, const double *ni, const double *plan, double *V, double *E, float *E32,
                void *stream);
+/* The grid part of one step in one launch, in the step loop's order (boltzmann.py:643-678):
+ * bz_grid_update (ni += ni_src, Te, g2), the clock (*t_dev += dt, *step_dev += 1),
+ * bz_ion_fluid with the field of the last solve, bz_poisson at the new time (moments row 0
+ * is ne). Te, g2, step_dev, E32 and brk may be NULL. */
+int bz_field_step(int32_t N, double dx, double dt, double mu_i, double D_i, double eps0, double V0, double freq,
+                  const double *moments, double *ni, double *Te, double *g2, double *t_dev, uint64_t *step_dev,
+                  const double *plan, double *V, double *E, float *E32, double *Ji, int32_t *brk, void *stream);
 /* Step clock on the device (graph-capturable): *t_dev += dt, *step_dev += 1 (either may be NULL). */
 int bz_advance_clock(double *t_dev, uint64_t *step_dev, double dt, void *stream);
 

@@ -62,3 +62,41 @@ def test_grid_update_and_clock():
     te[3] = 0.0  # 0/0 -> nan -> 0 (np.nan_to_num, boltzmann.py:646)
     np.testing.assert_allclose(Te.cpu().numpy(), te)
     assert float(t.item()) == 1.5 and int(step.item()) == 3
+
+
+def test_fused_field_step_equals_the_four_kernels():
+    """bz_field_step = grid update, clock, ion fluid, Poisson, bit for bit."""
+    g = np.load(os.path.join(G, "field.npz"))
+    N, dx, dev = int(g["N"]), float(g["dx"]), "cuda"
+    rng = np.random.default_rng(3)
+    nn = N + 1
+    d = torch.zeros(N - 1, dtype=torch.float64, device=dev)
+    l = torch.zeros(N - 1, dtype=torch.float64, device=dev)
+    plan = torch.zeros(4 * (N - 1), dtype=torch.float64, device=dev)
+    K.poisson_factor(N, dx, d, l, plan)
+    mom = torch.as_tensor(np.abs(rng.normal(1e9, 1e8, (4, nn))), device=dev)
+    ni0 = torch.as_tensor(g["ni"], device=dev)
+    E0 = torch.as_tensor(rng.normal(0, 50, N), device=dev)
+    out = []
+    for fused in (False, True):
+        ni, E = ni0.clone(), E0.clone()
+        Te = torch.zeros(nn, dtype=torch.float64, device=dev)
+        t = torch.full((1,), 1e-8, dtype=torch.float64, device=dev)
+        step = torch.zeros(1, dtype=torch.int64, device=dev)
+        V = torch.zeros(N - 1, dtype=torch.float64, device=dev)
+        E32 = torch.zeros(N, dtype=torch.float32, device=dev)
+        Ji = torch.zeros(N, dtype=torch.float64, device=dev)
+        args = (float(g["dt"]), float(g["mu_i"]), float(g["D_i"]))
+        if fused:
+            K.field_step(N, dx, *args, float(g["eps0"]), float(g["V0"]), float(g["freq"]), mom, ni, Te, None, t,
+                         step, plan, V, E, E32, Ji)
+        else:
+            K.grid_update(nn, mom, ni, Te, None)
+            K.advance_clock(t, step, args[0])
+            K.heavies_kernel_fluid(N, dx, *args, E, ni, Ji)
+            K.EF_kernel(N, dx, float(g["eps0"]), float(g["V0"]), float(g["freq"]), 0.0, mom[0], ni, plan, V, E, E32,
+                        t_dev=t)
+        torch.cuda.synchronize()
+        out.append([a.cpu().numpy() for a in (ni, Te, t, step, V, E, E32, Ji)])
+    for a, b in zip(*out):
+        np.testing.assert_array_equal(a, b)
