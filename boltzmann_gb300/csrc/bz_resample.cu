@@ -118,14 +118,19 @@ __device__ __forceinline__ double rs_uniform(const Rng &g, const double *replay_
     return (j & 1) ? uni_d(r.z, r.w).u : uni_d(r.x, r.y).u;
 }
 
+// Binary searches over a non-decreasing table of non-negative doubles. For non-negative
+// IEEE doubles the order of the bit patterns as integers is the order of the values, so
+// the comparisons run on the integer pipe instead of GB300's narrow float64 pipe.
 __device__ __forceinline__ int lower_bound_d(const double *a, int n, double v) {
+    const long long vb = __double_as_longlong(v);
     int lo = 0, hi = n;
-    while (lo < hi) { int m = (lo + hi) >> 1; if (a[m] < v) lo = m + 1; else hi = m; }
+    while (lo < hi) { int m = (lo + hi) >> 1; if (__double_as_longlong(a[m]) < vb) lo = m + 1; else hi = m; }
     return lo;
 }
 __device__ __forceinline__ int upper_bound_d(const double *a, int n, double v) {
+    const long long vb = __double_as_longlong(v);
     int lo = 0, hi = n;
-    while (lo < hi) { int m = (lo + hi) >> 1; if (a[m] <= v) lo = m + 1; else hi = m; }
+    while (lo < hi) { int m = (lo + hi) >> 1; if (__double_as_longlong(a[m]) <= vb) lo = m + 1; else hi = m; }
     return lo;
 }
 
@@ -174,6 +179,61 @@ template <typename V> __device__ V block_excl_scan(V v, V *sh, V *total) {
     return r;
 }
 
+// N block-wide sums with one set of barriers (sh: RS_T/32 * N doubles)
+template <int N> __device__ void block_sum_n(double (&v)[N], double *sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int i = 0; i < N; ++i) sh[warp * N + i] = v[i];
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            double t = lane < RS_T / 32 ? sh[lane * N + i] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+            v[i] = t;
+        }
+        if (lane == 0)
+#pragma unroll
+            for (int i = 0; i < N; ++i) sh[i] = v[i];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < N; ++i) v[i] = sh[i];
+    __syncthreads();
+}
+
+// cdf[j] = carry + sum_{i<=j} val(j) for j < len, RS_ITEMS consecutive entries per thread
+// and one block scan per RS_T*RS_ITEMS entries
+constexpr int RS_ITEMS = 8;
+template <typename F> __device__ void block_cumsum(int len, F val, double *cdf, double *sh) {
+    double carry = 0.0;
+    for (int c0 = 0; c0 < len; c0 += RS_T * RS_ITEMS) {
+        const int j0 = c0 + threadIdx.x * RS_ITEMS;
+        double v[RS_ITEMS];
+        double local = 0.0;
+#pragma unroll
+        for (int i = 0; i < RS_ITEMS; ++i) {
+            v[i] = j0 + i < len ? val(j0 + i) : 0.0;
+            local += v[i];
+        }
+        double tot;
+        double acc = carry + block_excl_scan<double>(local, sh, &tot);
+#pragma unroll
+        for (int i = 0; i < RS_ITEMS; ++i) {
+            acc += v[i];
+            if (j0 + i < len) cdf[j0 + i] = acc;
+        }
+        carry += tot;
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const int32_t *n_ptr, int64_t cap, int nb,
                                                    const int32_t *targets, const int32_t *max_ppc, double min_wt,
@@ -183,6 +243,7 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
                                                    int32_t *ws_cnt, double *cons_diag, SoAR<T> app, int64_t app_cap,
                                                    uint32_t *status) {
     __shared__ double shd[RS_T / 32 + 1];
+    __shared__ double shv[RS_T / 32 * 5];
     __shared__ int64_t shi[RS_T / 32 + 1];
     const int key = blockIdx.x;
     const int a = act[key];
@@ -224,21 +285,14 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
         }
         __syncthreads();
         if (nhw == 0) return;
+        #pragma unroll 4
         for (int j = threadIdx.x; j < nhw; j += RS_T) W += double(s.w[cnt[j]]);
         W = block_sum<double>(W, shd);
         // cdf = cumsum(w/W), then / cdf[-1] (CuPy RandomState.choice with p); the
         // divisions are multiplications by the reciprocal (within 2 ulp; float64 division
         // is many instructions on this part's narrow float64 pipe)
         const double inv_W = 1.0 / W;
-        double carry = 0.0;
-        for (int c0 = 0; c0 < nhw; c0 += RS_T) {
-            int j = c0 + threadIdx.x;
-            double v = j < nhw ? double(s.w[cnt[j]]) * inv_W : 0.0;
-            double tot;
-            double ex = block_excl_scan<double>(v, shd, &tot);
-            if (j < nhw) cdf[j] = carry + ex + v;
-            carry += tot;
-        }
+        block_cumsum(nhw, [&](int j) { return double(s.w[cnt[j]]) * inv_W; }, cdf, shd);
         __syncthreads();
         const double last = cdf[nhw - 1];
         const double inv_last = 1.0 / last;
@@ -329,6 +383,7 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
         return;
     }
     double W = 0, px = 0, py = 0, pz = 0, ew = 0;
+    #pragma unroll 4
     for (int j = threadIdx.x; j < np_; j += RS_T) {
         int id = perm[off + j];
         double w = s.w[id], vx = s.vx[id], vy = s.vy[id], vz = s.vz[id];
@@ -338,28 +393,21 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
         pz += vz * w;
         ew += w * (efac * (vx * vx + vy * vy + vz * vz));
     }
-    W = block_sum<double>(W, shd);
-    px = block_sum<double>(px, shd);
-    py = block_sum<double>(py, shd);
-    pz = block_sum<double>(pz, shd);
-    ew = block_sum<double>(ew, shd);
+    {
+        double m[5] = {W, px, py, pz, ew};
+        block_sum_n<5>(m, shv);
+        W = m[0]; px = m[1]; py = m[2]; pz = m[3]; ew = m[4];
+    }
     const double inv_W = 1.0 / W;
     const double ux = px / W, uy = py / W, uz = pz / W;
     const double T_cell = (2.0 / 3.0) * (ew / W);
     // cdf = cumsum(w/W) (not renormalised), stratified R_k = (1/K)(u_k + k)
-    double carry = 0.0;
-    for (int c0 = 0; c0 < np_; c0 += RS_T) {
-        int j = c0 + threadIdx.x;
-        double v = j < np_ ? double(s.w[perm[off + j]]) * inv_W : 0.0;
-        double tot;
-        double ex = block_excl_scan<double>(v, shd, &tot);
-        if (j < np_) cdf[j] = carry + ex + v;
-        carry += tot;
-    }
+    block_cumsum(np_, [&](int j) { return double(s.w[perm[off + j]]) * inv_W; }, cdf, shd);
     __syncthreads();
     const double wbar = W / double(K);
     const T wbar_t = T(wbar);
     double hx = 0, hy = 0, hz = 0, he = 0;
+    #pragma unroll 4
     for (int k = threadIdx.x; k < K; k += RS_T) {
         double u = rs_uniform(rng, replay_u, draw_off[key], key, k);
         double R = (1.0 / double(K)) * (u + double(k));
@@ -373,10 +421,11 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
         hz += vz * wbar;
         he += wbar * (efac * (vx * vx + vy * vy + vz * vz));
     }
-    hx = block_sum<double>(hx, shd) / W;
-    hy = block_sum<double>(hy, shd) / W;
-    hz = block_sum<double>(hz, shd) / W;
-    he = block_sum<double>(he, shd);
+    {
+        double m[4] = {hx, hy, hz, he};
+        block_sum_n<4>(m, shv);
+        hx = m[0] / W; hy = m[1] / W; hz = m[2] / W; he = m[3];
+    }
     const double Te_hat = (2.0 / 3.0) * he / W;
     double Tfac;
     if (p.flags & BZ_FIX_MERGE_ENERGY) {
@@ -391,6 +440,7 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
     }
     __syncthreads();  // every read of the originals is done before they are zeroed / overwritten
     double aW = 0, ax = 0, ay = 0, az = 0, ae = 0;
+    #pragma unroll 4
     for (int k = threadIdx.x; k < K; k += RS_T) {
         int id = cnt[k];
         T xx = s.x[id];
@@ -412,13 +462,12 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
         ae += wd * (efac * (dx * dx + dy * dy + dz * dz));
     }
     __syncthreads();
+    #pragma unroll 4
     for (int j = threadIdx.x; j < np_; j += RS_T) s.w[perm[off + j]] = T(0);
     if (cons_diag) {
-        aW = block_sum<double>(aW, shd);
-        ax = block_sum<double>(ax, shd);
-        ay = block_sum<double>(ay, shd);
-        az = block_sum<double>(az, shd);
-        ae = block_sum<double>(ae, shd);
+        double m[5] = {aW, ax, ay, az, ae};
+        block_sum_n<5>(m, shv);
+        aW = m[0]; ax = m[1]; ay = m[2]; az = m[3]; ae = m[4];
         if (threadIdx.x == 0) {
             double *d = cons_diag + size_t(key) * 10;
             d[0] = W; d[1] = px; d[2] = py; d[3] = pz; d[4] = ew;
