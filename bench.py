@@ -40,6 +40,17 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def peak_tensor():
+    """Dense bf16 tensor peak (TFLOP/s): the measured burst figure, else the fallback."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["bf16_tflops"]), "measured"
+    except Exception:
+        return 1900.0, "fallback"
+
+
 class ClockSampler:
     """nvidia-smi samples during the timed region (read-only)."""
 
@@ -415,14 +426,97 @@ def run_swarms(args, world, rank, local, pg):
     print(json.dumps(line), flush=True)
 
 
+def run_learned(args, world, rank, local, pg):
+    """The learned start-up (config 5's network on config 4's swarms): swarm-sweep data
+    (512 swarms, 10-1000 Td, ~2e5 snapshot samples), Adam training of the 4x128 GELU
+    network by the library's BF16 tensor-core kernels, then held-out swarms started plain
+    and learned. Reports the wall time and steps each start needs to reach its steady mean
+    energy (within 2%), the training throughput against the tensor roofline, and the
+    one-off costs (data, training, start-up)."""
+    import math
+    import time
+
+    import numpy as np
+    import torch
+    from boltzmann_gb300 import surrogate as S
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    rng = np.random.default_rng(rank)
+    t0 = time.perf_counter()
+    td = np.exp(rng.uniform(math.log(10.0), math.log(1000.0), 512))
+    X, T, info = S.swarm_dataset(td, [10_000] * 512, steps=30_000, snapshot_every=75, device=dev)
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    mlp = S.SurrogateMLP(device=dev, seed=rank)
+    xd, tdv = torch.as_tensor(X, device=dev), torch.as_tensor(T, device=dev)
+    batch = args.mlp_batch
+    mlp.train(xd, tdv, steps=20, batch=batch)  # warm-up (and workspace)
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    hist = mlp.train(xd, tdv, steps=args.train_steps, batch=batch, log_every=max(args.train_steps // 10, 1))
+    e1.record(st)
+    torch.cuda.synchronize()
+    train_s = e0.elapsed_time(e1) / 1e3
+    w_count = sum(a * b for a, b in S.LAYERS)
+    l0 = S.LAYERS[0][0] * S.LAYERS[0][1]
+    flops_step = 2.0 * batch * (3 * w_count - l0)  # forward, weight gradient, input gradient (not layer 0's)
+    tflops = flops_step * args.train_steps / train_s / 1e12
+    # held-out swarms, plain and learned start
+    td_h = np.exp(np.random.default_rng(100 + rank).uniform(math.log(150.0), math.log(1000.0), 32))
+    counts = [30_000] * len(td_h)
+    steps, chunk = 20_000, 100
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    plain, ep = S.swarm_relaxation(td_h, counts, steps, chunk, device=dev)
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t1
+    t2 = time.perf_counter()
+    learned, el = S.swarm_relaxation(td_h, counts, steps, chunk, mlp=mlp, device=dev)
+    torch.cuda.synchronize()
+    t_learned = time.perf_counter() - t2
+    tail = int(0.6 * len(plain))
+    final = 0.5 * (plain[tail:].mean(axis=0) + learned[tail:].mean(axis=0))
+    kp = S.steps_to_steady(plain, final) * chunk
+    kl = S.steps_to_steady(learned, final) * chunk
+    ms_step_p = t_plain * 1e3 / steps
+    ms_step_l = t_learned * 1e3 / steps
+    wall_p = float(np.median(kp)) * ms_step_p
+    wall_l = float(np.median(kl)) * ms_step_l
+    peak_tf = peak_tensor()
+    if rank != 0:
+        return
+    line = {
+        "metric": "wall time to steady mean energy, learned start / plain start", "value": wall_l / max(wall_p, 1e-9),
+        "unit": "ratio", "n_gpus": world, "steps": args.train_steps, "warmup": 20, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (network) / f32 (particles)", "data": "synthetic",
+        "config": {"workload": "learned start-up: 4x128 GELU network trained on 512 swarms (10-1000 Td, 1e4 "
+                               "particles, 3e4 steps, 400 snapshots each), 32 held-out swarms (150-1000 Td, "
+                               "3e4 particles, 2e4 steps)", "samples": int(len(X)), "batch": batch,
+                   "train_steps": args.train_steps},
+        "steady": {"median_steps_plain": float(np.median(kp)), "median_steps_learned": float(np.median(kl)),
+                   "median_wall_ms_plain": wall_p, "median_wall_ms_learned": wall_l,
+                   "within_5pct_at_start": float(np.mean(np.abs(learned[0] / final - 1) < 0.05))},
+        "one_off_s": {"data": t_data, "train": train_s},
+        "training": {"loss_first": hist[0], "loss_last": hist[-1], "ms_per_step": train_s * 1e3 / args.train_steps},
+        "roofline": {"bound": "tensor", "achieved": tflops, "peak": peak_tf[0], "unit": "TFLOP/s",
+                     "frac": tflops / peak_tf[0], "traffic": None, "kernel": "k_mlp_fwd + k_mlp_bwd (one step)",
+                     "peak_kind": peak_tf[1]},
+        "cpu_baseline": None, "e2e": None, "device_status": [ep.device_status(), el.device_status()],
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="ccp1024", choices=["ccp1024", "swarm512"],
-                    help="ccp1024: the 2e7-particle CCP (default); swarm512: the batched swarm ensemble")
+    ap.add_argument("--workload", default="ccp1024", choices=["ccp1024", "swarm512", "learned"],
+                    help="ccp1024: the 2e7-particle CCP (default); swarm512: the batched swarm ensemble; "
+                         "learned: the learned start-up against the plain one")
     ap.add_argument("--particles", type=float, default=2e7)
     ap.add_argument("--cells", type=int, default=1024)
     ap.add_argument("--rsf", type=int, default=50)
@@ -434,6 +528,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--ref-sample", type=float, default=2e6)
     ap.add_argument("--ref-budget", type=float, default=60.0)
+    ap.add_argument("--train-steps", type=int, default=20000, help="Adam steps of the learned workload")
+    ap.add_argument("--mlp-batch", type=int, default=2048, help="minibatch of the learned workload")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -443,6 +539,8 @@ def main():
         run_reference_arm(args, world, rank, pg)
     elif args.workload == "swarm512":
         run_swarms(args, world, rank, local, pg)
+    elif args.workload == "learned":
+        run_learned(args, world, rank, local, pg)
     else:
         run_ours(args, world, rank, local, pg)
     if pg is not None:

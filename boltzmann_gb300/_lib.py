@@ -67,6 +67,7 @@ _vp = ctypes.c_void_p
 _i32 = ctypes.c_int32
 _i64 = ctypes.c_int64
 _f64 = ctypes.c_double
+_f32 = ctypes.c_float
 _sz = ctypes.c_size_t
 _P = ctypes.POINTER(BzParams)
 
@@ -127,6 +128,17 @@ _PROTOS = {
                                            _f64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp, _vp]),
     "bz_push_collide_f32_noalloc": (ctypes.c_int, [_P, Particles, _vp, _i64, Particles, _i64, _vp, _vp, _vp, _vp,
                                                    _vp, _vp, _vp]),
+    "bz_mlp_param_count": (ctypes.c_int32, []),
+    "bz_mlp_sync": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
+    "bz_mlp_forward": (ctypes.c_int, [_vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp]),
+    "bz_mlp_backward": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp, _vp, _vp]),
+    "bz_mlp_adam": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _i64, _f32, _f32, _f32, _f32, _f32, _vp]),
+    "bz_mlp_batch": (ctypes.c_int, [_i32, _i32, ctypes.c_uint64, ctypes.c_uint64, _vp, _vp]),
+    "bz_mlp_train_workspace": (_sz, [_i32]),
+    "bz_mlp_train_step": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, ctypes.c_uint64,
+                                         _i64, _f32, _f32, _f32, _f32, _f32, _vp, _vp, _sz, _vp]),
+    "bz_seg_sample_energy_f32": (ctypes.c_int, [_P, Segments, _i32, _i32, _f64, _f64, _vp, ctypes.c_uint64, _vp]),
+    "bz_seg_sample_energy_f64": (ctypes.c_int, [_P, Segments, _i32, _i32, _f64, _f64, _vp, ctypes.c_uint64, _vp]),
 }
 
 

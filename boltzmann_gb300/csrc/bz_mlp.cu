@@ -1,0 +1,572 @@
+// Surrogate network of the learned CCP start-up: BF16 x BF16 -> FP32 tensor-core
+// products (mma.sync m16n8k16), FP32 epilogues, FP32 master weights and Adam.
+//
+// Network: BZ_MLP_IN (16) inputs -> 4 hidden layers of 128 GELU units -> BZ_MLP_OUT (80)
+// linear outputs. Every weight matrix lives in shared memory for the whole kernel, rows
+// padded by 8 BF16 (16 bytes) so that the fragment loads of a warp hit 32 different
+// banks. A warp owns 16 rows of the batch; its activations stay in a per-warp shared
+// tile between layers, so the forward pass reads x once and writes y (and, for
+// training, the FP32 pre-activations) once.
+//
+// Fragment layout of mma.sync.m16n8k16.row.col (PTX ISA, "Matrix fragments for
+// mma.m16n8k16"), g = lane/4, t = lane%4:
+//   A (16x16, row-major): a0 = A[g][2t..2t+1], a1 = A[g+8][2t..], a2 = A[g][2t+8..],
+//                         a3 = A[g+8][2t+8..]
+//   B (16x8, k x n):      b0 = B[2t..2t+1][g], b1 = B[2t+8..2t+9][g]
+//   C (16x8, FP32):       c0,c1 = C[g][2t..2t+1], c2,c3 = C[g+8][2t..2t+1]
+// B[k][n] = W[n][k] for y = x W^T, so W stored row-major (out x in) gives B fragments as
+// single 32-bit loads; the backward pass's dA = dZ W reads the transposed copy.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+
+#include "bz_common.cuh"
+
+namespace bz {
+
+constexpr int MLP_IN = BZ_MLP_IN;
+constexpr int MLP_H = BZ_MLP_HIDDEN;
+constexpr int MLP_OUT = BZ_MLP_OUT;
+constexpr int MLP_NL = BZ_MLP_LAYERS;
+
+__host__ __device__ constexpr int mlp_in(int l) { return l == 0 ? MLP_IN : MLP_H; }
+__host__ __device__ constexpr int mlp_out(int l) { return l == MLP_NL - 1 ? MLP_OUT : MLP_H; }
+__host__ __device__ constexpr int mlp_woff(int l) {
+    return l == 0 ? 0 : mlp_woff(l - 1) + mlp_in(l - 1) * mlp_out(l - 1) + mlp_out(l - 1);
+}
+__host__ __device__ constexpr int mlp_boff(int l) { return mlp_woff(l) + mlp_in(l) * mlp_out(l); }
+constexpr int MLP_NPARAM = mlp_woff(MLP_NL);
+static_assert(MLP_NPARAM == BZ_MLP_NPARAM, "parameter count");
+static_assert(MLP_IN % 16 == 0 && MLP_H % 16 == 0 && MLP_OUT % 16 == 0, "dimensions are whole k-steps");
+
+// shared-memory copies: W_l as out_l rows of in_l + 8, W_l^T as in_l rows of out_l + 8
+__host__ __device__ constexpr int ws_stride(int l) { return mlp_in(l) + 8; }
+__host__ __device__ constexpr int ws_off(int l) { return l == 0 ? 0 : ws_off(l - 1) + mlp_out(l - 1) * ws_stride(l - 1); }
+__host__ __device__ constexpr int wts_stride(int l) { return mlp_out(l) + 8; }
+__host__ __device__ constexpr int wts_off(int l) {  // layers 1.. only (layer 0's input gradient is not needed)
+    return l <= 1 ? 0 : wts_off(l - 1) + mlp_in(l - 1) * wts_stride(l - 1);
+}
+__host__ __device__ constexpr int bs_off(int l) { return l == 0 ? 0 : bs_off(l - 1) + mlp_out(l - 1); }
+constexpr int WS_TOTAL = ws_off(MLP_NL);
+constexpr int WTS_TOTAL = wts_off(MLP_NL);
+constexpr int BS_TOTAL = bs_off(MLP_NL);
+constexpr int AS = MLP_H + 8;  // row stride of a warp's activation tile (BF16)
+
+constexpr int MF_WARPS = 8;    // forward: 8 warps, 128 rows per tile
+constexpr int MB_WARPS = 4;    // backward: 4 warps, 64 rows per tile
+constexpr int MB_ROWS = 16 * MB_WARPS;
+constexpr int RS = MB_ROWS + 8;  // row stride of the transposed tiles (BF16)
+
+constexpr size_t FWD_SMEM = size_t(WS_TOTAL) * 2 + size_t(BS_TOTAL) * 4 + size_t(MF_WARPS) * 16 * AS * 2;
+constexpr size_t BWD_SMEM = size_t(WTS_TOTAL) * 2 + size_t(MB_WARPS) * 16 * AS * 2 + size_t(MLP_H) * RS * 2 * 2;
+static_assert(FWD_SMEM <= 227 * 1024 && BWD_SMEM <= 227 * 1024, "shared memory");
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t *>(&v);
+}
+__device__ __forceinline__ float bf16_to_f(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                         uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// GELU, tanh form (Hendrycks & Gimpel 2016): 0.5 z (1 + tanh(c (z + 0.044715 z^3))),
+// c = sqrt(2/pi); and its derivative
+constexpr float GELU_C = 0.7978845608028654f;
+constexpr float GELU_A = 0.044715f;
+__device__ __forceinline__ float gelu(float z) {
+    const float u = GELU_C * fmaf(GELU_A * z * z, z, z);
+    return 0.5f * z * (1.0f + tanhf(u));
+}
+__device__ __forceinline__ float gelu_grad(float z) {
+    const float u = GELU_C * fmaf(GELU_A * z * z, z, z);
+    const float th = tanhf(u);
+    return 0.5f * (1.0f + th) + 0.5f * z * (1.0f - th * th) * GELU_C * fmaf(3.0f * GELU_A, z * z, 1.0f);
+}
+
+// 16 rows x N outputs of one warp: acc = bias + A (16 x K, shared, stride AS) * W^T
+// (W: N x K in shared memory, stride K + 8)
+template <int K, int N>
+__device__ __forceinline__ void warp_gemm_bias(const __nv_bfloat16 *A, const __nv_bfloat16 *W, const float *bias,
+                                               int lane, float (&acc)[N / 8][4]) {
+    constexpr int NT = N / 8;
+    constexpr int WS32 = (K + 8) / 2;
+    constexpr int AS32 = AS / 2;
+    const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt) {
+        const int c = nt * 8 + 2 * t;
+        acc[nt][0] = bias ? bias[c] : 0.0f;
+        acc[nt][1] = bias ? bias[c + 1] : 0.0f;
+        acc[nt][2] = acc[nt][0];
+        acc[nt][3] = acc[nt][1];
+    }
+    const uint32_t *A32 = reinterpret_cast<const uint32_t *>(A);
+    const uint32_t *W32 = reinterpret_cast<const uint32_t *>(W);
+#pragma unroll
+    for (int k0 = 0; k0 < K; k0 += 16) {
+        const int kc = k0 / 2 + t;
+        const uint32_t a0 = A32[g * AS32 + kc], a1 = A32[(g + 8) * AS32 + kc];
+        const uint32_t a2 = A32[g * AS32 + kc + 4], a3 = A32[(g + 8) * AS32 + kc + 4];
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt) {
+            const int n = nt * 8 + g;
+            mma_bf16(acc[nt], a0, a1, a2, a3, W32[n * WS32 + kc], W32[n * WS32 + kc + 4]);
+        }
+    }
+}
+
+// one forward layer of a warp: pre-activations (optionally saved), then GELU into the
+// activation tile (hidden) or the output rows (last)
+template <int L, bool SAVE>
+__device__ __forceinline__ void fwd_layer(const __nv_bfloat16 *ws, const float *bs, __nv_bfloat16 *act, int lane,
+                                          int row0, int n, float *z, float *y) {
+    constexpr int K = mlp_in(L), N = mlp_out(L);
+    float acc[N / 8][4];
+    warp_gemm_bias<K, N>(act, ws + ws_off(L), bs + bs_off(L), lane, acc);
+    __syncwarp();  // every lane has read the tile before it is overwritten
+    const int g = lane >> 2, t = lane & 3;
+    const int r0 = row0 + g, r1 = row0 + g + 8;
+    uint32_t *act32 = reinterpret_cast<uint32_t *>(act);
+#pragma unroll
+    for (int nt = 0; nt < N / 8; ++nt) {
+        const int c = nt * 8 + 2 * t;
+        if (L == MLP_NL - 1) {
+            if (r0 < n) *reinterpret_cast<float2 *>(y + size_t(r0) * MLP_OUT + c) = make_float2(acc[nt][0], acc[nt][1]);
+            if (r1 < n) *reinterpret_cast<float2 *>(y + size_t(r1) * MLP_OUT + c) = make_float2(acc[nt][2], acc[nt][3]);
+        } else {
+            if (SAVE) {
+                float *zl = z + size_t(L) * n * MLP_H;
+                if (r0 < n) *reinterpret_cast<float2 *>(zl + size_t(r0) * MLP_H + c) = make_float2(acc[nt][0], acc[nt][1]);
+                if (r1 < n) *reinterpret_cast<float2 *>(zl + size_t(r1) * MLP_H + c) = make_float2(acc[nt][2], acc[nt][3]);
+            }
+            act32[g * (AS / 2) + c / 2] = pack_bf16(gelu(acc[nt][0]), gelu(acc[nt][1]));
+            act32[(g + 8) * (AS / 2) + c / 2] = pack_bf16(gelu(acc[nt][2]), gelu(acc[nt][3]));
+        }
+    }
+    __syncwarp();
+}
+
+// x rows (gathered through idx) into a warp's tile as BF16; rows past n are zero
+__device__ __forceinline__ void load_x_tile(const float *x, const int32_t *idx, int row0, int n, int lane,
+                                            __nv_bfloat16 *act) {
+    static_assert(MLP_IN == 16, "one row = two lanes of 8 features");
+    const int rr = lane >> 1, half = lane & 1;
+    const int r = row0 + rr;
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+    if (r < n) {
+        const int src = idx ? idx[r] : r;
+        const float4 *p = reinterpret_cast<const float4 *>(x + size_t(src) * MLP_IN + half * 8);
+        a = p[0];
+        b = p[1];
+    }
+    uint4 q;
+    q.x = pack_bf16(a.x, a.y);
+    q.y = pack_bf16(a.z, a.w);
+    q.z = pack_bf16(b.x, b.y);
+    q.w = pack_bf16(b.z, b.w);
+    *reinterpret_cast<uint4 *>(act + rr * AS + half * 8) = q;
+}
+
+// BF16 matrix rows x cols (row-major, global) into shared memory with a padded stride
+__device__ __forceinline__ void copy_padded(const uint16_t *src, int rows, int cols, __nv_bfloat16 *dst, int stride) {
+    const int chunks = cols / 8;
+    for (int e = threadIdx.x; e < rows * chunks; e += blockDim.x) {
+        const int r = e / chunks, c = e - r * chunks;
+        *reinterpret_cast<uint4 *>(dst + r * stride + c * 8) =
+            *reinterpret_cast<const uint4 *>(src + size_t(r) * cols + c * 8);
+    }
+}
+
+template <bool SAVE>
+__global__ void __launch_bounds__(32 * MF_WARPS, 1)
+    k_mlp_fwd(const uint16_t *wb, const float *prm, const float *x, const int32_t *idx, int n, float *y, float *z) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __nv_bfloat16 *ws = reinterpret_cast<__nv_bfloat16 *>(smem);
+    float *bs = reinterpret_cast<float *>(smem + size_t(WS_TOTAL) * 2);
+    __nv_bfloat16 *acts = reinterpret_cast<__nv_bfloat16 *>(smem + size_t(WS_TOTAL) * 2 + size_t(BS_TOTAL) * 4);
+#pragma unroll
+    for (int l = 0; l < MLP_NL; ++l) {
+        copy_padded(wb + mlp_woff(l), mlp_out(l), mlp_in(l), ws + ws_off(l), ws_stride(l));
+        for (int i = threadIdx.x; i < mlp_out(l); i += blockDim.x) bs[bs_off(l) + i] = prm[mlp_boff(l) + i];
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __nv_bfloat16 *act = acts + warp * 16 * AS;
+    const int tiles = int(ceil_div(n, 16 * MF_WARPS));
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const int row0 = tile * 16 * MF_WARPS + warp * 16;
+        if (row0 >= n) continue;  // warp-uniform; no block barrier below
+        load_x_tile(x, idx, row0, n, lane, act);
+        __syncwarp();
+        fwd_layer<0, SAVE>(ws, bs, act, lane, row0, n, z, y);
+        fwd_layer<1, SAVE>(ws, bs, act, lane, row0, n, z, y);
+        fwd_layer<2, SAVE>(ws, bs, act, lane, row0, n, z, y);
+        fwd_layer<3, SAVE>(ws, bs, act, lane, row0, n, z, y);
+        fwd_layer<4, SAVE>(ws, bs, act, lane, row0, n, z, y);
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// backward. Per tile of 64 rows, from the output layer down:
+//   dZ_4 = wcol (y - t) / n;   for l = 4..0:
+//     dW_l += dZ_l^T A_{l-1}   (A_{-1} = x; the CTA's 64 rows are the k dimension)
+//     db_l += column sums of dZ_l
+//     dZ_{l-1} = (dZ_l W_l) * gelu'(z_{l-1})   (l >= 1)
+// dZ is kept as BF16 twice: row-major per warp (A operand of dZ W) and transposed for the
+// whole tile (A operand of dZ^T A); A_{l-1} is rebuilt from the saved z as BF16, transposed
+// (B operand). Partial dW, db of a tile are added to grad with FP32 atomics.
+// ------------------------------------------------------------------------------------
+struct BwdSmem {
+    __nv_bfloat16 *wt, *dz, *dzT, *aT;
+};
+
+// dW_l += dZ^T (out x 64) * A (64 x in), partial over the tile, added to grad
+template <int L>
+__device__ __forceinline__ void bwd_weight_grad(const BwdSmem &s, int warp, int lane, float *grad) {
+    constexpr int NO = mlp_out(L), NI = mlp_in(L);
+    constexpr int MT = NO / 16, NT = NI / 8;
+    constexpr int NCH = NT < 8 ? NT : 8;  // n-tiles per pass (8 x 4 accumulators)
+    const int g = lane >> 2, t = lane & 3;
+    const uint32_t *D32 = reinterpret_cast<const uint32_t *>(s.dzT);
+    const uint32_t *X32 = reinterpret_cast<const uint32_t *>(s.aT);
+    constexpr int RS32 = RS / 2;
+    for (int m = warp; m < MT; m += MB_WARPS) {
+#pragma unroll
+        for (int n0 = 0; n0 < NT; n0 += NCH) {
+            float acc[NCH][4];
+#pragma unroll
+            for (int j = 0; j < NCH; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+#pragma unroll
+            for (int k0 = 0; k0 < MB_ROWS; k0 += 16) {
+                const int kc = k0 / 2 + t;
+                const int o = m * 16 + g;
+                const uint32_t a0 = D32[o * RS32 + kc], a1 = D32[(o + 8) * RS32 + kc];
+                const uint32_t a2 = D32[o * RS32 + kc + 4], a3 = D32[(o + 8) * RS32 + kc + 4];
+#pragma unroll
+                for (int j = 0; j < NCH; ++j) {
+                    const int i = (n0 + j) * 8 + g;
+                    mma_bf16(acc[j], a0, a1, a2, a3, X32[i * RS32 + kc], X32[i * RS32 + kc + 4]);
+                }
+            }
+            float *gw = grad + mlp_woff(L);
+#pragma unroll
+            for (int j = 0; j < NCH; ++j) {
+                const int i = (n0 + j) * 8 + 2 * t;
+                const int o = m * 16 + g;
+                atomicAdd(gw + o * NI + i, acc[j][0]);
+                atomicAdd(gw + o * NI + i + 1, acc[j][1]);
+                atomicAdd(gw + (o + 8) * NI + i, acc[j][2]);
+                atomicAdd(gw + (o + 8) * NI + i + 1, acc[j][3]);
+            }
+        }
+    }
+    // db_l: column sums of dZ over the tile's rows
+    for (int o = threadIdx.x; o < NO; o += blockDim.x) {
+        float sum = 0.f;
+        for (int r = 0; r < MB_ROWS; ++r) sum += bf16_to_f(s.dzT[o * RS + r]);
+        if (sum != 0.f) atomicAdd(grad + mlp_boff(L) + o, sum);
+    }
+}
+
+// the transposed BF16 activations A_{L-1} of the tile (B operand of the weight gradient)
+template <int L>
+__device__ __forceinline__ void bwd_build_aT(const BwdSmem &s, const float *x, const int32_t *idx, const float *z,
+                                             int n, int tile_row0) {
+    constexpr int NI = mlp_in(L);
+    for (int e = threadIdx.x; e < MB_ROWS * NI; e += blockDim.x) {
+        const int rr = e / NI, i = e - rr * NI;
+        const int r = tile_row0 + rr;
+        float v = 0.f;
+        if (r < n) {
+            if (L == 0) {
+                v = x[size_t(idx ? idx[r] : r) * MLP_IN + i];
+            } else {
+                v = gelu(z[(size_t(L - 1) * n + r) * MLP_H + i]);
+            }
+        }
+        s.aT[i * RS + rr] = __float2bfloat16_rn(v);
+    }
+}
+
+// store one warp's dZ values (accumulator layout) row-major and transposed
+__device__ __forceinline__ void put_dz(const BwdSmem &s, int warp, int lane, int c, float d00, float d01, float d10,
+                                       float d11) {
+    const int g = lane >> 2;
+    uint32_t *dz32 = reinterpret_cast<uint32_t *>(s.dz + warp * 16 * AS);
+    const uint32_t p0 = pack_bf16(d00, d01), p1 = pack_bf16(d10, d11);
+    dz32[g * (AS / 2) + c / 2] = p0;
+    dz32[(g + 8) * (AS / 2) + c / 2] = p1;
+    const __nv_bfloat162 q0 = *reinterpret_cast<const __nv_bfloat162 *>(&p0);
+    const __nv_bfloat162 q1 = *reinterpret_cast<const __nv_bfloat162 *>(&p1);
+    const int rl = warp * 16 + g;
+    s.dzT[c * RS + rl] = q0.x;
+    s.dzT[(c + 1) * RS + rl] = q0.y;
+    s.dzT[c * RS + rl + 8] = q1.x;
+    s.dzT[(c + 1) * RS + rl + 8] = q1.y;
+}
+
+// dZ_{L-1} = (dZ_L W_L) * gelu'(z_{L-1}) for one warp's 16 rows
+template <int L>
+__device__ __forceinline__ void bwd_input_grad(const BwdSmem &s, int warp, int lane, const float *z, int n,
+                                               int row0) {
+    constexpr int NO = mlp_out(L), NI = mlp_in(L);
+    float acc[NI / 8][4];
+    warp_gemm_bias<NO, NI>(s.dz + warp * 16 * AS, s.wt + wts_off(L), nullptr, lane, acc);
+    __syncthreads();  // the whole tile is done with dZ_L (weight gradient, this product)
+    const int g = lane >> 2, t = lane & 3;
+    const int r0 = row0 + g, r1 = row0 + g + 8;
+    const float *zl = z + size_t(L - 1) * n * MLP_H;
+#pragma unroll
+    for (int nt = 0; nt < NI / 8; ++nt) {
+        const int c = nt * 8 + 2 * t;
+        float2 z0 = make_float2(0.f, 0.f), z1 = z0;
+        const bool ok0 = r0 < n, ok1 = r1 < n;
+        if (ok0) z0 = *reinterpret_cast<const float2 *>(zl + size_t(r0) * MLP_H + c);
+        if (ok1) z1 = *reinterpret_cast<const float2 *>(zl + size_t(r1) * MLP_H + c);
+        put_dz(s, warp, lane, c, ok0 ? acc[nt][0] * gelu_grad(z0.x) : 0.f, ok0 ? acc[nt][1] * gelu_grad(z0.y) : 0.f,
+               ok1 ? acc[nt][2] * gelu_grad(z1.x) : 0.f, ok1 ? acc[nt][3] * gelu_grad(z1.y) : 0.f);
+    }
+}
+
+template <int L>
+__device__ __forceinline__ void bwd_layer(const BwdSmem &s, int warp, int lane, const float *x, const int32_t *idx,
+                                          const float *z, int n, int tile_row0, float *grad) {
+    bwd_build_aT<L>(s, x, idx, z, n, tile_row0);
+    __syncthreads();  // aT and dzT of the tile are complete
+    bwd_weight_grad<L>(s, warp, lane, grad);
+    if constexpr (L > 0) bwd_input_grad<L>(s, warp, lane, z, n, tile_row0 + warp * 16);
+    __syncthreads();  // dZ_{L-1} complete; aT free again
+}
+
+__global__ void __launch_bounds__(32 * MB_WARPS, 1)
+    k_mlp_bwd(const uint16_t *wt, const float *x, const float *tg, const float *wcol, const int32_t *idx, int n,
+              const float *y, const float *z, float *grad, float *loss) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    BwdSmem s;
+    s.wt = reinterpret_cast<__nv_bfloat16 *>(smem);
+    s.dz = s.wt + WTS_TOTAL;
+    s.dzT = s.dz + MB_WARPS * 16 * AS;
+    s.aT = s.dzT + MLP_H * RS;
+#pragma unroll
+    for (int l = 1; l < MLP_NL; ++l)
+        copy_padded(wt + mlp_woff(l), mlp_in(l), mlp_out(l), s.wt + wts_off(l), wts_stride(l));
+    for (int i = threadIdx.x; i < MLP_H * RS; i += blockDim.x) s.dzT[i] = __float2bfloat16_rn(0.f);
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int g = lane >> 2, t = lane & 3;
+    const float inv_n = 1.0f / float(n);
+    float lsum = 0.f;
+    const int tiles = int(ceil_div(n, MB_ROWS));
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const int tile_row0 = tile * MB_ROWS;
+        const int row0 = tile_row0 + warp * 16;
+        // dZ_4 = wcol (y - t) / n, and the loss
+        for (int nt = 0; nt < MLP_OUT / 8; ++nt) {
+            const int c = nt * 8 + 2 * t;
+            float d[4];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int r = row0 + g + 8 * h;
+                float e0 = 0.f, e1 = 0.f;
+                if (r < n) {
+                    const float *tr = tg + size_t(idx ? idx[r] : r) * MLP_OUT;
+                    e0 = (y[size_t(r) * MLP_OUT + c] - tr[c]) * wcol[c];
+                    e1 = (y[size_t(r) * MLP_OUT + c + 1] - tr[c + 1]) * wcol[c + 1];
+                    lsum += 0.5f * (e0 * (y[size_t(r) * MLP_OUT + c] - tr[c]) +
+                                    e1 * (y[size_t(r) * MLP_OUT + c + 1] - tr[c + 1]));
+                }
+                d[2 * h] = e0 * inv_n;
+                d[2 * h + 1] = e1 * inv_n;
+            }
+            put_dz(s, warp, lane, c, d[0], d[1], d[2], d[3]);
+        }
+        bwd_layer<4>(s, warp, lane, x, idx, z, n, tile_row0, grad);
+        bwd_layer<3>(s, warp, lane, x, idx, z, n, tile_row0, grad);
+        bwd_layer<2>(s, warp, lane, x, idx, z, n, tile_row0, grad);
+        bwd_layer<1>(s, warp, lane, x, idx, z, n, tile_row0, grad);
+        bwd_layer<0>(s, warp, lane, x, idx, z, n, tile_row0, grad);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+    if (lane == 0 && lsum != 0.f) atomicAdd(loss, lsum * inv_n);
+}
+
+// ------------------------------------------------------------------------------------
+// parameters: BF16 copies, Adam, minibatch indices
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ void put_bf16_copies(int i, float p, uint16_t *wb, uint16_t *wt) {
+    int l = 0;
+#pragma unroll
+    for (int k = 1; k < MLP_NL; ++k) l += (i >= mlp_woff(k));
+    const int e = i - mlp_woff(l);
+    const int ni = mlp_in(l), no = mlp_out(l);
+    if (e >= ni * no) return;  // a bias
+    const int o = e / ni, c = e - o * ni;
+    const __nv_bfloat16 b = __float2bfloat16_rn(p);
+    const uint16_t u = *reinterpret_cast<const uint16_t *>(&b);
+    wb[i] = u;
+    wt[mlp_woff(l) + c * no + o] = u;
+}
+
+__global__ void k_mlp_sync(const float *prm, uint16_t *wb, uint16_t *wt) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < MLP_NPARAM; i += gridDim.x * blockDim.x)
+        put_bf16_copies(i, prm[i], wb, wt);
+}
+
+__global__ void k_mlp_adam(float *prm, float *grad, float *m, float *v, uint16_t *wb, uint16_t *wt, float lr_c1,
+                           float b1, float b2, float c2, float eps, float lr_wd) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < MLP_NPARAM; i += gridDim.x * blockDim.x) {
+        const float gi = grad[i];
+        grad[i] = 0.f;
+        const float mi = fmaf(b1, m[i], (1.f - b1) * gi);
+        const float vi = fmaf(b2, v[i], (1.f - b2) * gi * gi);
+        m[i] = mi;
+        v[i] = vi;
+        int l = 0;
+#pragma unroll
+        for (int k = 1; k < MLP_NL; ++k) l += (i >= mlp_woff(k));
+        const bool is_w = i < mlp_boff(l);
+        float p = prm[i];
+        if (is_w) p -= lr_wd * p;  // decoupled weight decay (Loshchilov & Hutter 2019)
+        p -= lr_c1 * mi / (sqrtf(vi * c2) + eps);
+        prm[i] = p;
+        put_bf16_copies(i, p, wb, wt);
+    }
+}
+
+__global__ void k_mlp_batch(int n_rows, int n, Rng g, int32_t *idx) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        const u32x4 q = philox(uint32_t(r), g.s0, g.s1, 0x6d6c7000u, g.k0, g.k1);
+        idx[r] = int32_t((uint64_t(q.x) * uint64_t(uint32_t(n_rows))) >> 32);  // Lemire's multiply-shift
+    }
+}
+
+static int num_sms_mlp() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+static bool al16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+static int mlp_forward(const uint16_t *wb, const float *prm, const float *x, const int32_t *idx, int n, float *y,
+                       float *z, cudaStream_t st) {
+    if (n == 0) return BZ_OK;
+    if (!wb || !prm || !x || !y || n < 0 || !al16(wb) || !al16(x) || !al16(y) || (z && !al16(z))) return BZ_ERR_ARG;
+    auto run = [&](auto kern) -> int {
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(FWD_SMEM)) != cudaSuccess)
+            return BZ_ERR_UNSUPPORTED;
+        const int tiles = int(ceil_div(n, 16 * MF_WARPS));
+        kern<<<std::min(tiles, num_sms_mlp()), 32 * MF_WARPS, FWD_SMEM, st>>>(wb, prm, x, idx, n, y, z);
+        return cudaGetLastError() == cudaSuccess ? int(BZ_OK) : int(BZ_ERR_CUDA);
+    };
+    return z ? run(k_mlp_fwd<true>) : run(k_mlp_fwd<false>);
+}
+
+static int mlp_backward(const uint16_t *wt, const float *x, const float *t, const float *wcol, const int32_t *idx,
+                        int n, const float *y, const float *z, float *grad, float *loss, cudaStream_t st) {
+    if (n == 0) return BZ_OK;
+    if (!wt || !x || !t || !wcol || !y || !z || !grad || !loss || n < 0 || !al16(wt) || !al16(y) || !al16(z))
+        return BZ_ERR_ARG;
+    if (cudaFuncSetAttribute(k_mlp_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, int(BWD_SMEM)) != cudaSuccess)
+        return BZ_ERR_UNSUPPORTED;
+    const int tiles = int(ceil_div(n, MB_ROWS));
+    k_mlp_bwd<<<std::min(tiles, num_sms_mlp()), 32 * MB_WARPS, BWD_SMEM, st>>>(wt, x, t, wcol, idx, n, y, z, grad,
+                                                                                loss);
+    return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+}
+
+static int mlp_adam(float *prm, float *grad, float *m, float *v, uint16_t *wb, uint16_t *wt, int64_t step, float lr,
+                    float b1, float b2, float eps, float wd, cudaStream_t st) {
+    if (!prm || !grad || !m || !v || !wb || !wt || step < 1 || !(b1 >= 0.f && b1 < 1.f) || !(b2 >= 0.f && b2 < 1.f))
+        return BZ_ERR_ARG;
+    const double c1 = 1.0 - std::pow(double(b1), double(step));
+    const double c2 = 1.0 - std::pow(double(b2), double(step));
+    k_mlp_adam<<<int(ceil_div(MLP_NPARAM, 256)), 256, 0, st>>>(prm, grad, m, v, wb, wt, float(lr / c1), b1, b2,
+                                                               float(1.0 / c2), eps, lr * wd);
+    return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+}
+
+static int mlp_batch(int n_rows, int n, uint64_t seed, uint64_t step, int32_t *idx, cudaStream_t st) {
+    if (n == 0) return BZ_OK;
+    if (!idx || n < 0 || n_rows < 1) return BZ_ERR_ARG;
+    const Rng g{uint32_t(seed), uint32_t(seed >> 32), uint32_t(step), uint32_t(step >> 32)};
+    k_mlp_batch<<<int(std::min<int64_t>(ceil_div(n, 256), 1024)), 256, 0, st>>>(n_rows, n, g, idx);
+    return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+}
+
+// training workspace: idx (n int32, padded to 256 B), y (n x OUT), z ((NL-1) x n x H)
+static size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+static size_t mlp_train_ws(int n) {
+    return align256(size_t(n) * 4) + align256(size_t(n) * MLP_OUT * 4) + align256(size_t(MLP_NL - 1) * n * MLP_H * 4);
+}
+
+}  // namespace bz
+
+using namespace bz;
+
+extern "C" {
+
+int32_t bz_mlp_param_count(void) { return MLP_NPARAM; }
+
+int bz_mlp_sync(const float *params, uint16_t *wb, uint16_t *wt, void *stream) {
+    if (!params || !wb || !wt) return BZ_ERR_ARG;
+    k_mlp_sync<<<int(ceil_div(MLP_NPARAM, 256)), 256, 0, as_stream(stream)>>>(params, wb, wt);
+    return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+}
+
+int bz_mlp_forward(const uint16_t *wb, const float *params, const float *x, const int32_t *idx, int32_t n, float *y,
+                   float *z, void *stream) {
+    return mlp_forward(wb, params, x, idx, n, y, z, as_stream(stream));
+}
+
+int bz_mlp_backward(const uint16_t *wb, const uint16_t *wt, const float *params, const float *x, const float *t,
+                    const float *wcol, const int32_t *idx, int32_t n, const float *y, const float *z, float *grad,
+                    float *loss, void *stream) {
+    (void)wb;
+    (void)params;  // the output layer's bias and the weights enter through y and z
+    return mlp_backward(wt, x, t, wcol, idx, n, y, z, grad, loss, as_stream(stream));
+}
+
+int bz_mlp_adam(float *params, float *grad, float *m, float *v, uint16_t *wb, uint16_t *wt, int64_t step, float lr,
+                float beta1, float beta2, float eps, float weight_decay, void *stream) {
+    return mlp_adam(params, grad, m, v, wb, wt, step, lr, beta1, beta2, eps, weight_decay, as_stream(stream));
+}
+
+int bz_mlp_batch(int32_t n_rows, int32_t n, uint64_t seed, uint64_t step, int32_t *idx, void *stream) {
+    return mlp_batch(n_rows, n, seed, step, idx, as_stream(stream));
+}
+
+size_t bz_mlp_train_workspace(int32_t n) { return n > 0 ? mlp_train_ws(n) : 0; }
+
+int bz_mlp_train_step(float *params, float *grad, float *m, float *v, uint16_t *wb, uint16_t *wt, const float *x,
+                      const float *t, const float *wcol, int32_t n_rows, int32_t n, uint64_t seed, int64_t step,
+                      float lr, float beta1, float beta2, float eps, float weight_decay, float *loss, void *workspace,
+                      size_t workspace_bytes, void *stream) {
+    if (n < 1 || n_rows < 1 || !workspace || !al16(workspace)) return BZ_ERR_ARG;
+    if (workspace_bytes < mlp_train_ws(n)) return BZ_ERR_WORKSPACE;
+    cudaStream_t st = as_stream(stream);
+    unsigned char *w = static_cast<unsigned char *>(workspace);
+    int32_t *idx = reinterpret_cast<int32_t *>(w);
+    float *y = reinterpret_cast<float *>(w + align256(size_t(n) * 4));
+    float *z = reinterpret_cast<float *>(w + align256(size_t(n) * 4) + align256(size_t(n) * MLP_OUT * 4));
+    int rc = mlp_batch(n_rows, n, seed, uint64_t(step), idx, st);
+    if (rc == BZ_OK) rc = mlp_forward(wb, params, x, idx, n, y, z, st);
+    if (rc == BZ_OK) rc = mlp_backward(wt, x, t, wcol, idx, n, y, z, grad, loss, st);
+    if (rc == BZ_OK) rc = mlp_adam(params, grad, m, v, wb, wt, step, lr, beta1, beta2, eps, weight_decay, st);
+    return rc;
+}
+
+}  // extern "C"

@@ -639,6 +639,61 @@ static int seg_eedf_entry(const bz_params *pp, S s_, int nbins, double emin, dou
     return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
 }
 
+// velocities drawn from a tabulated energy distribution per key (the learned start-up):
+// bin by inverse CDF, energy log-uniform within the bin, isotropic direction
+template <typename T>
+__global__ void __launch_bounds__(256) k_seg_sample_energy(bz_params p, NodeMap nm, Seg<T> s, int nkeys, int nbins,
+                                                           double lemin, double dle, const double *cdf, Rng g) {
+    const double e2v = 2.0 / (j_ev() * m_e());  // eV -> (m/s)^2
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int seg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; seg < s.nseg; seg += warps) {
+        for (int run = 0; run < 2; ++run) {
+            const int cnt = min(max(s.cnt[2 * seg + run], 0), s.half);
+            const int64_t b = seg_slot(seg, run, s.half, 0);
+            for (int j = lane; j < cnt; j += 32) {
+                if (!(s.a.w[b + j] > T(0))) continue;
+                const int key = deposit_node(p.advect, s.a.x[b + j], nm);
+                if (key < 0 || key >= nkeys) continue;
+                const double *c = cdf + int64_t(key) * nbins;
+                const double tot = c[nbins - 1];
+                if (!(tot > 0.0)) continue;
+                const uint32_t slot = uint32_t(b + j);
+                const u32x4 q = philox(slot, g.s0, g.s1, 0x65656400u, g.k0, g.k1);
+                const u32x4 r = philox(slot, g.s0, g.s1, 0x65656401u, g.k0, g.k1);
+                const double ub = uni_d(q.x, q.y).u * tot;
+                int lo = 0, hi = nbins - 1;  // first bin whose cumulative fraction exceeds ub
+                while (lo < hi) {
+                    const int m = (lo + hi) >> 1;
+                    if (c[m] > ub) hi = m; else lo = m + 1;
+                }
+                const double e = exp(lemin + (double(lo) + uni_d(q.z, q.w).u) * dle);
+                const double sp = sqrt(e * e2v);
+                const Uni<double> a = uni_d(r.x, r.y), bb = uni_d(r.z, r.w);
+                const double cc = a.u - a.c, sc = 2.0 * sqrt(a.u * a.c);
+                double sph, cph;
+                sincospi(2.0 * bb.u, &sph, &cph);
+                s.a.vx[b + j] = T(sp * sc * cph);
+                s.a.vy[b + j] = T(sp * sc * sph);
+                s.a.vz[b + j] = T(sp * cc);
+            }
+        }
+    }
+}
+
+template <typename T, typename S>
+static int seg_sample_energy_entry(const bz_params *pp, S s_, int nkeys, int nbins, double emin, double emax,
+                                   const double *cdf, uint64_t seed, void *stream) {
+    if (!pp || !cdf || !seg_ok<T>(s_) || nkeys < 1 || nbins < 1 || !(emin > 0) || !(emax > emin)) return BZ_ERR_ARG;
+    const bz_params &p = *pp;
+    if (p.advect == BZ_ADVECT_1D && (p.dx <= 0 || p.L <= 0 || p.bnf < 1 || p.n_nodes < 1)) return BZ_ERR_ARG;
+    const int blocks = std::max(1, std::min(num_sms() * 8, int(ceil_div(s_.nseg, 8))));
+    const Rng g{uint32_t(seed), uint32_t(seed >> 32), 0u, 0u};
+    k_seg_sample_energy<T><<<blocks, 256, 0, as_stream(stream)>>>(p, make_node_map(p), to_seg<T>(s_), nkeys, nbins,
+                                                                  log(emin), log(emax / emin) / nbins, cdf, g);
+    return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+}
+
 template <typename T, typename S>
 static int seg_deposit_entry(const bz_params *pp, S s_, double *moments, void *stream) {
     if (!pp || !moments || !seg_ok<T>(s_)) return BZ_ERR_ARG;
@@ -726,6 +781,14 @@ int bz_seg_eedf_f32(const bz_params *p, bz_segments_f32 s, int32_t nbins, double
 int bz_seg_eedf_f64(const bz_params *p, bz_segments_f64 s, int32_t nbins, double emin, double emax, double *hist,
                     void *stream) {
     return bz::seg_eedf_entry<double>(p, s, nbins, emin, emax, hist, stream);
+}
+int bz_seg_sample_energy_f32(const bz_params *p, bz_segments_f32 s, int32_t n_keys, int32_t nbins, double emin,
+                             double emax, const double *cdf, uint64_t seed, void *stream) {
+    return bz::seg_sample_energy_entry<float>(p, s, n_keys, nbins, emin, emax, cdf, seed, stream);
+}
+int bz_seg_sample_energy_f64(const bz_params *p, bz_segments_f64 s, int32_t n_keys, int32_t nbins, double emin,
+                             double emax, const double *cdf, uint64_t seed, void *stream) {
+    return bz::seg_sample_energy_entry<double>(p, s, n_keys, nbins, emin, emax, cdf, seed, stream);
 }
 
 }  // extern "C"

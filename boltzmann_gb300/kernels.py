@@ -377,3 +377,41 @@ def field_step(N, dx, dt, mu_i, D_i, eps0, V0, freq, moments, ni, Te, g2, t_dev,
 
 def advance_clock(t_dev, step_dev, dt):
     call("bz_advance_clock", _ptr(t_dev), _ptr(step_dev), float(dt), _stream())
+
+
+# ------------------------------------------------------------------------------------ surrogate network
+def seg_sample_energy(params, s: SegmentSet, cdf, emin, emax, seed):
+    """Velocities of every live particle drawn from cdf [n_keys, nbins] (float64, cumulative
+    weight fractions of log bins over [emin, emax) eV) of its key (deposit node / swarm)."""
+    call(f"bz_seg_sample_energy_{s.suffix}", ctypes.byref(params), s.struct(), int(cdf.shape[0]), int(cdf.shape[1]),
+         float(emin), float(emax), _ptr(cdf), int(seed), _stream())
+
+
+def mlp_sync(prm, wb, wt):
+    call("bz_mlp_sync", _ptr(prm), _ptr(wb), _ptr(wt), _stream())
+
+
+def mlp_forward(wb, prm, x, y, idx=None, z=None):
+    call("bz_mlp_forward", _ptr(wb), _ptr(prm), _ptr(x), _ptr(idx), int(y.shape[0]), _ptr(y), _ptr(z), _stream())
+
+
+def mlp_backward(wb, wt, prm, x, t, wcol, y, z, grad, loss, idx=None):
+    call("bz_mlp_backward", _ptr(wb), _ptr(wt), _ptr(prm), _ptr(x), _ptr(t), _ptr(wcol), _ptr(idx), int(y.shape[0]),
+         _ptr(y), _ptr(z), _ptr(grad), _ptr(loss), _stream())
+
+
+def mlp_adam(prm, grad, m, v, wb, wt, step, lr, beta1=0.9, beta2=0.999, eps=1e-8, weight_decay=0.0):
+    call("bz_mlp_adam", _ptr(prm), _ptr(grad), _ptr(m), _ptr(v), _ptr(wb), _ptr(wt), int(step), float(lr),
+         float(beta1), float(beta2), float(eps), float(weight_decay), _stream())
+
+
+def mlp_batch(n_rows, idx, seed, step):
+    call("bz_mlp_batch", int(n_rows), int(idx.numel()), int(seed), int(step), _ptr(idx), _stream())
+
+
+def mlp_train_step(prm, grad, m, v, wb, wt, x, t, wcol, batch, seed, step, lr, loss, ws: Workspace, beta1=0.9,
+                   beta2=0.999, eps=1e-8, weight_decay=0.0):
+    w = ws.get("mlp_train", _lib.load().bz_mlp_train_workspace(int(batch)))
+    call("bz_mlp_train_step", _ptr(prm), _ptr(grad), _ptr(m), _ptr(v), _ptr(wb), _ptr(wt), _ptr(x), _ptr(t),
+         _ptr(wcol), int(x.shape[0]), int(batch), int(seed), int(step), float(lr), float(beta1), float(beta2),
+         float(eps), float(weight_decay), _ptr(loss), _ptr(w), w.numel(), _stream())

@@ -339,6 +339,41 @@ class BoltzmannGB300:
                     v.zero_()
         return self
 
+    # --------------------------------------------------------------------------------- learned start-up
+    def node_state(self):
+        """Per deposit node: reduced field E/N (Td, from the face fields next to the node),
+        mean electron energy (eV, from the last deposit), weight fractions in the 64 log
+        energy bins of the learned start-up, and the RF phase."""
+        from . import surrogate as S
+        cfg = self.cfg
+        E = np.abs(self.E.detach().cpu().numpy())  # V/cm at the N faces
+        En = np.empty(self.nnodes)
+        En[0], En[-1] = E[0], E[-1]
+        En[1:-1] = 0.5 * (E[:-1] + E[1:])
+        td = En * 100.0 / cfg.nn_m3 / 1e-21
+        mom = self.moments.detach().cpu().numpy()
+        mean = np.where(mom[0] > 0, mom[3] / np.maximum(mom[0], 1e-300), 0.0)
+        h = torch.zeros(self.nnodes, S.EEDF_BINS, dtype=torch.float64, device=self.device)
+        K.seg_eedf(self.params(step_on_device=False), self.A, h, S.EEDF_EMIN, S.EEDF_EMAX)
+        h = h.cpu().numpy()
+        f = h / np.maximum(h.sum(axis=1, keepdims=True), 1e-300)
+        phase = 2.0 * math.pi * ((cfg.freq * float(self.t.item())) % 1.0)
+        return td, mean, f, phase
+
+    def learned_start(self, mlp, seed=None):
+        """Redraw every electron's velocity from the surrogate network's steady-state energy
+        distribution for its node (features from ``node_state``), then refresh the
+        moments. Positions, weights and the field are unchanged; the plain step loop
+        continues from here. Returns the network's per-node (eedf, k_exc, k_ion)."""
+        from . import surrogate as S
+        td, mean, f, phase = self.node_state()
+        out = S.learned_start(mlp, self.params(step_on_device=False), self.A, td, np.maximum(mean, 1e-3),
+                              S.bin_fractions(f), phase, seed=self.cfg.seed + 7 if seed is None else seed,
+                              device=self.device)
+        self.moments.zero_()
+        K.seg_deposit(self.params(step_on_device=False), self.A, self.moments)
+        return out
+
     # --------------------------------------------------------------------------------- diagnostics
     def kernel_launches(self, resample):
         """libbz kernels one step launches (torch's memset of the moments not counted).

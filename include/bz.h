@@ -338,6 +338,63 @@ int bz_push_collide_f32_noalloc(const bz_params *p, bz_particles_f32 in, const i
                                 const double *replay_gas, double *moments, uint32_t *status,
                                 void *stream);
 
+/* ---------------------------------------------------------------------------------------
+ * Surrogate network of the learned CCP start-up (no counterpart in the reference: its
+ * runs always start from the plain initial state, boltzmann.py:271-312). A fully
+ * connected network of BZ_MLP_LAYERS weight layers: BZ_MLP_IN inputs (the features,
+ * zero-padded), BZ_MLP_LAYERS-1 hidden layers of BZ_MLP_HIDDEN GELU units (tanh form),
+ * BZ_MLP_OUT linear outputs (zero-padded). Matrix products take BF16 operands and
+ * accumulate in FP32 on the tensor cores; biases, pre-activations, outputs, gradients
+ * and the Adam state are FP32.
+ *
+ * Parameters: one FP32 array of BZ_MLP_NPARAM values, layer by layer: W_l (out_l x in_l,
+ * row-major) followed by b_l (out_l). The BF16 copies `wb` (same layout, the bias slots
+ * unused) and `wt` (each W_l transposed, in_l x out_l, at W_l's offset) are what the
+ * kernels read; bz_mlp_sync and bz_mlp_adam keep them equal to round(W) in BF16.
+ * Rows: x is n x BZ_MLP_IN FP32 (16-byte aligned), y n x BZ_MLP_OUT FP32; the saved
+ * pre-activations z are (BZ_MLP_LAYERS-1) x n x BZ_MLP_HIDDEN FP32.
+ * ------------------------------------------------------------------------------------- */
+#define BZ_MLP_IN 16
+#define BZ_MLP_HIDDEN 128
+#define BZ_MLP_OUT 80
+#define BZ_MLP_LAYERS 5
+#define BZ_MLP_NPARAM 62032 /* 16*128+128 + 3*(128*128+128) + 128*80+80 */
+int32_t bz_mlp_param_count(void);
+/* wb/wt from the FP32 parameters */
+int bz_mlp_sync(const float *params, uint16_t *wb, uint16_t *wt, void *stream);
+/* y = f(x[idx[r]]) for r < n (idx NULL: row r); z (NULL: not kept) receives the hidden
+ * layers' pre-activations for a following bz_mlp_backward */
+int bz_mlp_forward(const uint16_t *wb, const float *params, const float *x, const int32_t *idx, int32_t n,
+                   float *y, float *z, void *stream);
+/* loss = sum_r sum_c wcol[c] (y - t[idx[r]])^2 / (2 n) added to *loss; its gradient with
+ * respect to every parameter added to grad (FP32, BZ_MLP_NPARAM) */
+int bz_mlp_backward(const uint16_t *wb, const uint16_t *wt, const float *params, const float *x,
+                    const float *t, const float *wcol, const int32_t *idx, int32_t n, const float *y,
+                    const float *z, float *grad, float *loss, void *stream);
+/* one Adam step (Kingma & Ba 2015) with bias correction for step `step` (1-based) and
+ * decoupled weight decay on the weights; clears grad and refreshes wb/wt */
+int bz_mlp_adam(float *params, float *grad, float *m, float *v, uint16_t *wb, uint16_t *wt, int64_t step,
+                float lr, float beta1, float beta2, float eps, float weight_decay, void *stream);
+/* n indices uniform in [0, n_rows) from Philox (seed, step): a training minibatch */
+int bz_mlp_batch(int32_t n_rows, int32_t n, uint64_t seed, uint64_t step, int32_t *idx, void *stream);
+/* batch + forward (z kept) + backward + Adam: one training step (four launches);
+ * ws: bz_mlp_train_workspace(n) bytes */
+size_t bz_mlp_train_workspace(int32_t n);
+int bz_mlp_train_step(float *params, float *grad, float *m, float *v, uint16_t *wb, uint16_t *wt,
+                      const float *x, const float *t, const float *wcol, int32_t n_rows, int32_t n,
+                      uint64_t seed, int64_t step, float lr, float beta1, float beta2, float eps,
+                      float weight_decay, float *loss, void *workspace, size_t workspace_bytes, void *stream);
+
+/* Sets every live particle's velocity from a tabulated energy distribution of its key (its
+ * deposit node; in an ensemble its swarm): cdf is n_keys x nbins FP64, the cumulative
+ * weight fractions of nbins log-spaced bins over [emin, emax) eV (last entry 1; a key
+ * whose last entry is not positive keeps its particles as they are). Energy: the bin by
+ * inverse CDF, log-uniform within it; direction isotropic; Philox (seed, slot). */
+int bz_seg_sample_energy_f32(const bz_params *p, bz_segments_f32 s, int32_t n_keys, int32_t nbins, double emin,
+                             double emax, const double *cdf, uint64_t seed, void *stream);
+int bz_seg_sample_energy_f64(const bz_params *p, bz_segments_f64 s, int32_t n_keys, int32_t nbins, double emin,
+                             double emax, const double *cdf, uint64_t seed, void *stream);
+
 /* library identification */
 const char *bz_version(void);
 
