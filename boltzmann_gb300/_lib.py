@@ -129,6 +129,9 @@ _PROTOS = {
     "bz_push_collide_f32_noalloc": (ctypes.c_int, [_P, Particles, _vp, _i64, Particles, _i64, _vp, _vp, _vp, _vp,
                                                    _vp, _vp, _vp]),
     "bz_mlp_param_count": (ctypes.c_int32, []),
+    "bz_mlp_select": (ctypes.c_int, [_i32]),
+    "bz_mlp_selected": (ctypes.c_int32, []),
+    "bz_mlp_status": (ctypes.c_int, [_vp]),
     "bz_mlp_sync": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
     "bz_mlp_forward": (ctypes.c_int, [_vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp]),
     "bz_mlp_backward": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp, _vp, _vp]),

@@ -174,13 +174,21 @@ __device__ __forceinline__ void load_x_tile(const float *x, const int32_t *idx, 
     *reinterpret_cast<uint4 *>(act + rr * AS + half * 8) = q;
 }
 
-// BF16 matrix rows x cols (row-major, global) into shared memory with a padded stride
+// BF16 matrix rows x cols (row-major, global) into shared memory with a padded stride:
+// 16-byte asynchronous copies (cp.async), all in flight at once; the caller waits
+// (cp_async_wait_all) and synchronises the block before reading
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc) {
+    const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(smem_dst));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
 __device__ __forceinline__ void copy_padded(const uint16_t *src, int rows, int cols, __nv_bfloat16 *dst, int stride) {
     const int chunks = cols / 8;
     for (int e = threadIdx.x; e < rows * chunks; e += blockDim.x) {
         const int r = e / chunks, c = e - r * chunks;
-        *reinterpret_cast<uint4 *>(dst + r * stride + c * 8) =
-            *reinterpret_cast<const uint4 *>(src + size_t(r) * cols + c * 8);
+        cp_async16(dst + r * stride + c * 8, src + size_t(r) * cols + c * 8);
     }
 }
 
@@ -196,6 +204,7 @@ __global__ void __launch_bounds__(32 * MF_WARPS, 1)
         copy_padded(wb + mlp_woff(l), mlp_out(l), mlp_in(l), ws + ws_off(l), ws_stride(l));
         for (int i = threadIdx.x; i < mlp_out(l); i += blockDim.x) bs[bs_off(l) + i] = prm[mlp_boff(l) + i];
     }
+    cp_async_wait_all();
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     __nv_bfloat16 *act = acts + warp * 16 * AS;
@@ -211,6 +220,218 @@ __global__ void __launch_bounds__(32 * MF_WARPS, 1)
         fwd_layer<3, SAVE>(ws, bs, act, lane, row0, n, z, y);
         fwd_layer<4, SAVE>(ws, bs, act, lane, row0, n, z, y);
     }
+}
+
+// ------------------------------------------------------------------------------------
+// forward on the 5th-generation tensor cores (tcgen05): one CTA of 4 warps per tile of 128
+// rows. The weights sit in shared memory in the canonical K-major layout without swizzle
+// (8-row x 16-byte core matrices; element (r, k) at (r/8)*SBO + (k/8)*128 + (r%8)*16 +
+// (k%8)*2 bytes, SBO = 16*K), the tile's activations likewise; one thread issues the
+// layer's K/16 tcgen05.mma (M = 128, N = 128 or 80, BF16 x BF16 -> FP32) into a
+// 128-column TMEM accumulator and commits them to an mbarrier; every warp then reads its
+// 32 TMEM lanes (= its 32 rows) with tcgen05.ld, adds the bias, applies GELU and writes the
+// next layer's operand back to shared memory (or the output rows). Waits are bounded: on
+// a timeout the kernel raises a status bit and stops.
+// ------------------------------------------------------------------------------------
+constexpr int TC_ROWS = 128;
+constexpr int TC_THREADS = 128;
+constexpr uint32_t TC_WAIT_LIMIT = 1u << 24;
+__host__ __device__ constexpr int wc_off(int l) { return l == 0 ? 0 : wc_off(l - 1) + mlp_out(l - 1) * mlp_in(l - 1) * 2; }
+constexpr int WC_BYTES = wc_off(MLP_NL);
+constexpr int TC_ACT_BYTES = TC_ROWS * MLP_H * 2;
+constexpr size_t TC_SMEM = 1024 + size_t(WC_BYTES) + TC_ACT_BYTES + BS_TOTAL * 4 + 64;
+static_assert(TC_SMEM <= 227 * 1024, "shared memory");
+
+__device__ uint32_t g_mlp_status = 0;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return uint32_t(__cvta_generic_to_shared(p)); }
+// shared-memory matrix descriptor: start address, leading (K-direction) and stride
+// (8-row direction) byte offsets, descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return uint64_t((saddr & 0x3FFFFu) >> 4) | (uint64_t(lbo >> 4) << 16) | (uint64_t(sbo >> 4) << 32) |
+           (1ull << 46);
+}
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(M >> 4) << 24);
+}
+__device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+                 : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase) {
+    for (uint32_t it = 0; it < TC_WAIT_LIMIT; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(phase)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+// 16 consecutive FP32 accumulator columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// byte offset of the 16-byte chunk (row r, k = 8*c8 .. 8*c8+7) in the canonical layout of a
+// matrix with K columns
+__device__ __forceinline__ int canon_off(int r, int c8, int K) { return (r >> 3) * (16 * K) + c8 * 128 + (r & 7) * 16; }
+
+template <int L, bool SAVE>
+__device__ __forceinline__ bool tc_layer(unsigned char *wc, unsigned char *act, const float *bs, uint32_t tmem,
+                                         uint32_t mbar, uint32_t &phase, int row0, int n, float *z, float *y) {
+    constexpr int K = mlp_in(L), N = mlp_out(L);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    // every thread's operand writes are complete and visible to the tensor core
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0) {
+        tc_fence_after();
+        const uint32_t a0 = smem_u32(act), b0 = smem_u32(wc + wc_off(L));
+        constexpr uint32_t idesc = idesc_bf16(TC_ROWS, N);
+#pragma unroll
+        for (int kk = 0; kk < K / 16; ++kk)
+            tc_mma(tmem, umma_desc(a0 + kk * 256, 128, 16 * K), umma_desc(b0 + kk * 256, 128, 16 * K), idesc,
+                   kk > 0 ? 1u : 0u);
+        tc_commit(mbar);
+    }
+    // one decision for the whole block (every thread reaches this barrier)
+    const bool ok = __syncthreads_and(mbar_wait(mbar, phase)) != 0;
+    phase ^= 1u;
+    if (!ok) return false;
+    tc_fence_after();
+    // epilogue: this thread owns row tid (TMEM lane tid)
+    float v[N];
+#pragma unroll
+    for (int c = 0; c < N; c += 16) tmem_ld16(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c), v + c);
+    tmem_wait_ld();
+    const int r = row0 + tid;
+    const float *b = bs + bs_off(L);
+#pragma unroll
+    for (int c = 0; c < N; ++c) v[c] += b[c];
+    if (L == MLP_NL - 1) {
+        if (r < n) {
+            float4 *yr = reinterpret_cast<float4 *>(y + size_t(r) * MLP_OUT);
+#pragma unroll
+            for (int c = 0; c < N; c += 4) yr[c / 4] = make_float4(v[c], v[c + 1], v[c + 2], v[c + 3]);
+        }
+    } else {
+        if (SAVE && r < n) {
+            float4 *zr = reinterpret_cast<float4 *>(z + (size_t(L) * n + r) * MLP_H);
+#pragma unroll
+            for (int c = 0; c < N; c += 4) zr[c / 4] = make_float4(v[c], v[c + 1], v[c + 2], v[c + 3]);
+        }
+        // the next layer's A operand (K = 128): 16-byte chunks of 8 activations
+#pragma unroll
+        for (int c8 = 0; c8 < N / 8; ++c8) {
+            uint4 q;
+            q.x = pack_bf16(gelu(v[8 * c8 + 0]), gelu(v[8 * c8 + 1]));
+            q.y = pack_bf16(gelu(v[8 * c8 + 2]), gelu(v[8 * c8 + 3]));
+            q.z = pack_bf16(gelu(v[8 * c8 + 4]), gelu(v[8 * c8 + 5]));
+            q.w = pack_bf16(gelu(v[8 * c8 + 6]), gelu(v[8 * c8 + 7]));
+            *reinterpret_cast<uint4 *>(act + canon_off(tid, c8, MLP_H)) = q;
+        }
+    }
+    return true;
+}
+
+template <bool SAVE>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_mlp_fwd_tc(const uint16_t *wb, const float *prm, const float *x, const int32_t *idx, int n, float *y, float *z) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // 1024-byte aligned operand region
+    unsigned char *base = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023u)) & 1023u);
+    unsigned char *wc = base;
+    unsigned char *act = wc + WC_BYTES;
+    float *bs = reinterpret_cast<float *>(act + TC_ACT_BYTES);
+    uint64_t *mbar_p = reinterpret_cast<uint64_t *>(bs + BS_TOTAL + (BS_TOTAL & 1));
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar_p + 1);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    // weights into the canonical layout (asynchronous 16-byte copies), biases
+#pragma unroll
+    for (int l = 0; l < MLP_NL; ++l) {
+        const int K = mlp_in(l), N = mlp_out(l), chunks = K / 8;
+        for (int e = tid; e < N * chunks; e += TC_THREADS) {
+            const int r = e / chunks, c8 = e - r * chunks;
+            cp_async16(wc + wc_off(l) + canon_off(r, c8, K), wb + mlp_woff(l) + size_t(r) * K + c8 * 8);
+        }
+        for (int i = tid; i < N; i += TC_THREADS) bs[bs_off(l) + i] = prm[mlp_boff(l) + i];
+    }
+    const uint32_t mbar = smem_u32(mbar_p);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(smem_u32(tmem_slot))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    cp_async_wait_all();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    uint32_t phase = 0;
+    bool ok = true;
+    const int tiles = int(ceil_div(n, TC_ROWS));
+    for (int tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+        const int row0 = tile * TC_ROWS;
+        // the tile's inputs (K = 16): this thread's row, two 16-byte chunks
+        {
+            const int r = row0 + tid;
+            float4 q[4] = {};
+            if (r < n) {
+                const float4 *p = reinterpret_cast<const float4 *>(x + size_t(idx ? idx[r] : r) * MLP_IN);
+                q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; q[3] = p[3];
+            }
+#pragma unroll
+            for (int c8 = 0; c8 < 2; ++c8) {
+                uint4 u;
+                u.x = pack_bf16(q[2 * c8].x, q[2 * c8].y);
+                u.y = pack_bf16(q[2 * c8].z, q[2 * c8].w);
+                u.z = pack_bf16(q[2 * c8 + 1].x, q[2 * c8 + 1].y);
+                u.w = pack_bf16(q[2 * c8 + 1].z, q[2 * c8 + 1].w);
+                *reinterpret_cast<uint4 *>(act + canon_off(tid, c8, MLP_IN)) = u;
+            }
+        }
+        ok = tc_layer<0, SAVE>(wc, act, bs, tmem, mbar, phase, row0, n, z, y) &&
+             tc_layer<1, SAVE>(wc, act, bs, tmem, mbar, phase, row0, n, z, y) &&
+             tc_layer<2, SAVE>(wc, act, bs, tmem, mbar, phase, row0, n, z, y) &&
+             tc_layer<3, SAVE>(wc, act, bs, tmem, mbar, phase, row0, n, z, y) &&
+             tc_layer<4, SAVE>(wc, act, bs, tmem, mbar, phase, row0, n, z, y);
+        // every TMEM read and shared write of this tile is done before the next one
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+    }
+    if (!ok && tid == 0) atomicOr(&g_mlp_status, BZ_DEV_LOOKBACK);
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem) : "memory");
 }
 
 // ------------------------------------------------------------------------------------
@@ -275,23 +496,39 @@ __device__ __forceinline__ void bwd_weight_grad(const BwdSmem &s, int warp, int 
     }
 }
 
-// the transposed BF16 activations A_{L-1} of the tile (B operand of the weight gradient)
+// the transposed BF16 activations A_{L-1} of the tile (B operand of the weight gradient):
+// four consecutive features per thread and item, four items in flight per thread
 template <int L>
 __device__ __forceinline__ void bwd_build_aT(const BwdSmem &s, const float *x, const int32_t *idx, const float *z,
                                              int n, int tile_row0) {
-    constexpr int NI = mlp_in(L);
-    for (int e = threadIdx.x; e < MB_ROWS * NI; e += blockDim.x) {
-        const int rr = e / NI, i = e - rr * NI;
-        const int r = tile_row0 + rr;
-        float v = 0.f;
-        if (r < n) {
-            if (L == 0) {
-                v = x[size_t(idx ? idx[r] : r) * MLP_IN + i];
-            } else {
-                v = gelu(z[(size_t(L - 1) * n + r) * MLP_H + i]);
+    constexpr int NI = mlp_in(L), NI4 = NI / 4, TOT = MB_ROWS * NI4, U = 4;
+    for (int e0 = threadIdx.x; e0 < TOT; e0 += U * blockDim.x) {
+        float4 v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int e = e0 + u * blockDim.x;
+            const int rr = e / NI4, i4 = e - rr * NI4;
+            const int r = tile_row0 + rr;
+            v[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (e < TOT && r < n) {
+                const float *src = (L == 0) ? x + size_t(idx ? idx[r] : r) * MLP_IN + 4 * i4
+                                            : z + (size_t(L > 0 ? L - 1 : 0) * n + r) * MLP_H + 4 * i4;
+                v[u] = *reinterpret_cast<const float4 *>(src);
             }
         }
-        s.aT[i * RS + rr] = __float2bfloat16_rn(v);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int e = e0 + u * blockDim.x;
+            if (e >= TOT) break;
+            const int rr = e / NI4, i4 = e - rr * NI4;
+            const bool ok = tile_row0 + rr < n;
+            float a0 = v[u].x, a1 = v[u].y, a2 = v[u].z, a3 = v[u].w;
+            if (L > 0 && ok) { a0 = gelu(a0); a1 = gelu(a1); a2 = gelu(a2); a3 = gelu(a3); }
+            s.aT[(4 * i4 + 0) * RS + rr] = __float2bfloat16_rn(a0);
+            s.aT[(4 * i4 + 1) * RS + rr] = __float2bfloat16_rn(a1);
+            s.aT[(4 * i4 + 2) * RS + rr] = __float2bfloat16_rn(a2);
+            s.aT[(4 * i4 + 3) * RS + rr] = __float2bfloat16_rn(a3);
+        }
     }
 }
 
@@ -358,6 +595,7 @@ __global__ void __launch_bounds__(32 * MB_WARPS, 1)
     for (int l = 1; l < MLP_NL; ++l)
         copy_padded(wt + mlp_woff(l), mlp_in(l), mlp_out(l), s.wt + wts_off(l), wts_stride(l));
     for (int i = threadIdx.x; i < MLP_H * RS; i += blockDim.x) s.dzT[i] = __float2bfloat16_rn(0.f);
+    cp_async_wait_all();
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int g = lane >> 2, t = lane & 3;
@@ -461,10 +699,22 @@ static int num_sms_mlp() {
 
 static bool al16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
+static int g_mlp_path = 0;  // 0: mma.sync, 1: tcgen05
+
 static int mlp_forward(const uint16_t *wb, const float *prm, const float *x, const int32_t *idx, int n, float *y,
                        float *z, cudaStream_t st) {
     if (n == 0) return BZ_OK;
     if (!wb || !prm || !x || !y || n < 0 || !al16(wb) || !al16(x) || !al16(y) || (z && !al16(z))) return BZ_ERR_ARG;
+    if (g_mlp_path == 1) {
+        auto run_tc = [&](auto kern) -> int {
+            if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TC_SMEM)) != cudaSuccess)
+                return BZ_ERR_UNSUPPORTED;
+            const int tiles = int(ceil_div(n, TC_ROWS));
+            kern<<<std::min(tiles, num_sms_mlp()), TC_THREADS, TC_SMEM, st>>>(wb, prm, x, idx, n, y, z);
+            return cudaGetLastError() == cudaSuccess ? int(BZ_OK) : int(BZ_ERR_CUDA);
+        };
+        return z ? run_tc(k_mlp_fwd_tc<true>) : run_tc(k_mlp_fwd_tc<false>);
+    }
     auto run = [&](auto kern) -> int {
         if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(FWD_SMEM)) != cudaSuccess)
             return BZ_ERR_UNSUPPORTED;
@@ -520,6 +770,22 @@ using namespace bz;
 extern "C" {
 
 int32_t bz_mlp_param_count(void) { return MLP_NPARAM; }
+
+int bz_mlp_select(int32_t path) {
+    if (path < 0 || path > 1) return BZ_ERR_ARG;
+    g_mlp_path = path;
+    return BZ_OK;
+}
+int32_t bz_mlp_selected(void) { return g_mlp_path; }
+
+int bz_mlp_status(uint32_t *out) {
+    if (!out) return BZ_ERR_ARG;
+    uint32_t v = 0, zero = 0;
+    if (cudaMemcpyFromSymbol(&v, g_mlp_status, sizeof(v)) != cudaSuccess) return BZ_ERR_CUDA;
+    if (v && cudaMemcpyToSymbol(g_mlp_status, &zero, sizeof(zero)) != cudaSuccess) return BZ_ERR_CUDA;
+    *out = v;
+    return BZ_OK;
+}
 
 int bz_mlp_sync(const float *params, uint16_t *wb, uint16_t *wt, void *stream) {
     if (!params || !wb || !wt) return BZ_ERR_ARG;

@@ -18,7 +18,7 @@ the hybrid CCP that the benchmark asks for, built on the same kernels:
 
 Features (9 of BZ_MLP_IN = 16, the rest zero):
   0: log10(E/N in Td) / 3          1: log10(mean energy in eV) / 2
-  2, 3: sin and cos of the RF phase
+  2, 3: sin and cos of the RF phase (both 0 for a DC field: swarms)
   4..8: weight fractions in the energy bins [0,2), [2,6), [6,11.5), [11.5,15.76), >= 15.76 eV
 Outputs (66 of BZ_MLP_OUT = 80):
   0..63: (log10(f_k + 1e-6) + 3) / 3, f_k the weight fraction in log bin k of 64 over
@@ -66,9 +66,10 @@ def features(td, mean_e, phase, fr5):
     x = np.zeros((n, NIN), dtype=np.float32)
     x[:, 0] = np.log10(np.maximum(td, 1e-3)) / 3.0
     x[:, 1] = np.log10(np.maximum(np.broadcast_to(mean_e, (n,)), 1e-3)) / 2.0
-    ph = np.broadcast_to(np.asarray(phase, dtype=np.float64), (n,))
-    x[:, 2] = np.sin(ph)
-    x[:, 3] = np.cos(ph)
+    if phase is not None:  # DC (phase None): the zero vector
+        ph = np.broadcast_to(np.asarray(phase, dtype=np.float64), (n,))
+        x[:, 2] = np.sin(ph)
+        x[:, 3] = np.cos(ph)
     x[:, 4:9] = np.broadcast_to(fr5, (n, 5))
     return x
 
@@ -200,7 +201,7 @@ def swarm_dataset(td, counts, steps, snapshot_every, settle_fraction=0.5, seed=1
             ens.reset_averages()
         ens.run(snapshot_every)
         mean, f = swarm_state(ens)
-        feats.append(features(td, mean, 0.0, bin_fractions(f)))
+        feats.append(features(td, mean, None, bin_fractions(f)))
         means.append(mean)
         eedfs.append(f)
     f_ss = np.mean(eedfs[settle:], axis=0)
@@ -210,7 +211,7 @@ def swarm_dataset(td, counts, steps, snapshot_every, settle_fraction=0.5, seed=1
     T = np.concatenate([tg] * n_snap)
     # the initial state is a sample too (what the start-up sees)
     f0 = initial_eedf(cfg.Te_init_eV)
-    X = np.concatenate([features(td, 1.5 * cfg.Te_init_eV, 0.0, bin_fractions(f0[None, :])), X])
+    X = np.concatenate([features(td, 1.5 * cfg.Te_init_eV, None, bin_fractions(f0[None, :])), X])
     T = np.concatenate([tg, T])
     info = {"td": td, "mean_series": np.array(means), "eedf_ss": f_ss, "k_exc": kexc, "k_ion": kion,
             "mean_ss": np.mean(means[settle:], axis=0), "status": ens.device_status()}
@@ -235,9 +236,10 @@ def eedf_cdf(eedf):
     return c
 
 
-def learned_start(mlp: SurrogateMLP, params, segs, td, mean_e, fr5, phase=0.0, seed=11, device="cuda"):
+def learned_start(mlp: SurrogateMLP, params, segs, td, mean_e, fr5, phase=None, seed=11, device="cuda"):
     """Redraw the velocities of every particle from the network's steady-state EEDF for
-    its key (swarm / deposit node): features per key from (td, mean_e, fr5, phase)."""
+    its key (swarm / deposit node): features per key from (td, mean_e, fr5, phase; phase
+    None for a DC field)."""
     x = features(td, mean_e, phase, fr5)
     f, kx, ki = mlp.predict(x)
     cdf = torch.as_tensor(eedf_cdf(f), dtype=torch.float64, device=device)
@@ -325,3 +327,35 @@ def ccp_dataset(cfg, cycles, snaps_per_cycle=8, settle_cycles=None, min_density=
     info = {"nodes": np.nonzero(keep)[0], "eedf_ss": f_ss, "k_ion": k_ion, "k_exc": k_exc,
             "status": sv.device_status(), "n_end": sv.n()}
     return X, T, info
+
+
+def steps_to_periodic(series, period, tol=0.02, window=5):
+    """Index of the first sample of the first period of ``series`` (1-D, at least two
+    periods long) from which the moving average (``window`` samples) of the ratio to the
+    same phase one period later is within tol of 1; ``period`` when it never is."""
+    s = np.asarray(series, dtype=np.float64)
+    r = s[:period] / s[period:2 * period]
+    ma = np.convolve(r, np.ones(window) / window, mode="valid")
+    ok = np.nonzero(np.abs(ma - 1.0) <= tol)[0]
+    return int(ok[0] + window - 1) if len(ok) else period
+
+
+def ccp_relaxation(cfg, steps, chunk, mlp: Optional[SurrogateMLP] = None, device="cuda"):
+    """Mean electron energy of a CCP (weight-averaged over the whole gap) per chunk of
+    ``chunk`` steps, from the plain start or, with ``mlp``, the learned start; also returns
+    the solver."""
+    from .solver import BoltzmannGB300
+    sv = BoltzmannGB300(cfg, device=device)
+    if mlp is not None:
+        sv.learned_start(mlp)
+    acc = torch.zeros(2, dtype=torch.float64, device=device)
+    out = []
+    for _ in range(steps // chunk):
+        acc.zero_()
+        for _ in range(chunk):
+            sv.step()
+            acc[0].add_(sv.moments[0].sum())
+            acc[1].add_(sv.moments[3].sum())
+        a = acc.cpu().numpy()
+        out.append(a[1] / max(a[0], 1e-300))
+    return np.array(out), sv

@@ -43,3 +43,31 @@ def test_learned_start_reaches_steady_state_sooner():
     assert np.median(kl) <= 0.3 * np.median(kp), (kp, kl)
     # the learned start is already within 5% for most swarms
     assert np.mean(np.abs(learned[0] / final - 1) < 0.05) >= 0.75
+
+
+def test_learned_start_of_the_ccp():
+    """A network trained on a plain CCP run (and the swarm sweep) starts a new CCP run
+    (another seed) at its periodic electron energy: the plain 1 eV start needs a quarter
+    of an RF cycle to heat up."""
+    from boltzmann_gb300 import config as C
+    kw = dict(ne_uniform=1e9, in_dt=4000.0, steps_per_cycle=4000, num_particles=1_000_000)
+    Xc, Tc, info = S.ccp_dataset(C.ccp_256(**kw), cycles=2, snaps_per_cycle=16, settle_cycles=1)
+    assert info["status"] == 0 and len(Xc) > 0
+    rng = np.random.default_rng(0)
+    td = np.exp(rng.uniform(math.log(30.0), math.log(1000.0), 128))
+    Xs, Ts, _ = S.swarm_dataset(td, [10_000] * 128, steps=12_000, snapshot_every=300)
+    mlp = S.SurrogateMLP(seed=0)
+    mlp.train(torch.as_tensor(np.concatenate([Xs, Xc])), torch.as_tensor(np.concatenate([Ts, Tc])), steps=3000,
+              batch=4096)
+    cfg = C.ccp_256(**dict(kw, seed=9))
+    per, chunk = 4000 // 50, 50
+    plain, sp = S.ccp_relaxation(cfg, 8000, chunk)
+    learned, sl = S.ccp_relaxation(cfg, 8000, chunk, mlp=mlp)
+    assert sp.device_status() == 0 and sl.device_status() == 0
+    # the same periodic state in the second cycle
+    np.testing.assert_allclose(learned[per:].mean(), plain[per:].mean(), rtol=0.03)
+    kp = S.steps_to_periodic(plain, per)
+    kl = S.steps_to_periodic(learned, per)
+    assert kl <= 0.6 * kp, (kp, kl)
+    assert abs(learned[0] / plain[per] - 1) < 0.15  # within 15% of the periodic value at once
+    assert abs(plain[0] / plain[per] - 1) > 0.5     # the plain start is far from it

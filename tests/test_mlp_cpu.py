@@ -95,6 +95,7 @@ def test_features_and_bin_fractions():
     np.testing.assert_allclose(x[:, 0], [2 / 3, 1 / 3], rtol=1e-6)
     np.testing.assert_allclose(x[:, 2:4], [[1, 0], [1, 0]], atol=1e-7)
     assert np.all(x[:, 9:] == 0)
+    assert np.all(S.features([50.0], 3.0, None, fr)[:, 2:4] == 0)  # DC: no phase
     cdf = S.eedf_cdf(np.vstack([f0, f0]))
     assert np.all(np.diff(cdf, axis=1) >= 0) and np.all(cdf[:, -1] == 1.0)
 
@@ -112,3 +113,14 @@ def test_steps_to_steady():
     assert s5[0] == 4 and 37 < s5[1] < 42
     never = S.steps_to_steady(np.stack([slow], 1), np.array([7.0]), tol=0.02)
     assert never[0] == n
+
+
+def test_steps_to_periodic():
+    p = 40
+    k = np.arange(3 * p)
+    periodic = 5.0 + 0.5 * np.sin(2 * np.pi * k / p)
+    assert S.steps_to_periodic(periodic, p, window=1) == 0
+    relax = periodic - 4.0 * np.exp(-k / 5.0)
+    s = S.steps_to_periodic(relax, p, window=1)
+    assert 10 < s < 25
+    assert S.steps_to_periodic(periodic * (1 + 0.5 * (k < p)), p) == p

@@ -171,3 +171,70 @@ def test_training_fits_a_smooth_map():
     after = net.evaluate(xd, td)
     assert hist[-1] < hist[0]
     assert after < 0.05 * before
+
+
+@pytest.fixture
+def tcgen05_path():
+    from boltzmann_gb300 import _lib
+    lib = _lib.load()
+    old = lib.bz_mlp_selected()
+    yield lib
+    lib.bz_mlp_select(old)
+
+
+def mlp_status(lib):
+    import ctypes
+    v = ctypes.c_uint32(0)
+    assert lib.bz_mlp_status(ctypes.byref(v)) == 0
+    return v.value
+
+
+@pytest.mark.parametrize("n", [1, 100, 128, 300, 2000])
+def test_tcgen05_forward_matches_mma_sync_and_oracle(n, tcgen05_path):
+    """The tcgen05 forward (TMEM accumulator, canonical shared-memory operands) computes
+    the same network as the mma.sync one: identical BF16 operands, FP32 accumulation in
+    another order (single activations may round to the neighbouring BF16 value)."""
+    lib = tcgen05_path
+    p, x, _ = rand_case(n, 50 + n)
+    net = S.SurrogateMLP(params=p)
+    xd = dev(x)
+    lib.bz_mlp_select(0)
+    y0 = torch.zeros(n, 80, device="cuda")
+    z0 = torch.zeros(4, n, 128, device="cuda")
+    K.mlp_forward(net.wb, net.prm, xd, y0, z=z0)
+    lib.bz_mlp_select(1)
+    y1 = torch.zeros(n, 80, device="cuda")
+    z1 = torch.zeros(4, n, 128, device="cuda")
+    K.mlp_forward(net.wb, net.prm, xd, y1, z=z1)
+    y2 = net.forward(xd)  # inference path (no saved pre-activations)
+    torch.cuda.synchronize()
+    assert mlp_status(lib) == 0
+    a, b = y0.cpu().numpy(), y1.cpu().numpy()
+    assert rel(b, a) < 1e-3
+    assert np.median(np.abs(b - a)) <= 1e-5 * np.abs(a).max()
+    assert torch.equal(y1, y2)
+    for l in range(4):
+        assert rel(z1[l].cpu().numpy(), z0[l].cpu().numpy()) < 1e-3
+    y_o, _ = O.forward(net.params(), x.astype(np.float32))
+    assert rel(b, y_o) < 2e-3
+
+
+def test_tcgen05_training_step_matches(tcgen05_path):
+    """One training step with the tcgen05 forward gives the gradient of the oracle."""
+    lib = tcgen05_path
+    lib.bz_mlp_select(1)
+    n = 512
+    p, x, t = rand_case(n, 91)
+    net = S.SurrogateMLP(params=p)
+    w = S.output_weights()
+    y = torch.zeros(n, 80, device="cuda")
+    z = torch.zeros(4, n, 128, device="cuda")
+    K.mlp_forward(net.wb, net.prm, dev(x), y, z=z)
+    grad = torch.zeros(S.NPARAM, device="cuda")
+    loss = torch.zeros(1, device="cuda")
+    K.mlp_backward(net.wb, net.wt, net.prm, dev(x), dev(t), dev(w), y, z, grad, loss)
+    torch.cuda.synchronize()
+    assert mlp_status(lib) == 0
+    L_o, g_o = O.backward(net.params(), x.astype(np.float32), t.astype(np.float32), w)
+    assert abs(float(loss.item()) - L_o) <= 1e-3 * L_o
+    assert rel(grad.cpu().numpy(), g_o) < 1e-2
