@@ -1,5 +1,7 @@
 // Surrogate network of the learned CCP start-up: BF16 x BF16 -> FP32 tensor-core
-// products (mma.sync m16n8k16), FP32 epilogues, FP32 master weights and Adam.
+// products, FP32 epilogues, FP32 master weights and Adam. The forward pass runs on
+// tcgen05.mma with a TMEM accumulator (k_mlp_fwd_tc, the default) or on warp-level
+// mma.sync m16n8k16 (k_mlp_fwd); the backward pass uses mma.sync.
 //
 // Network: BZ_MLP_IN (16) inputs -> 4 hidden layers of 128 GELU units -> BZ_MLP_OUT (80)
 // linear outputs. Every weight matrix lives in shared memory for the whole kernel, rows
@@ -77,16 +79,22 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], uint32_t a0, uint32_t a1
 }
 
 // GELU, tanh form (Hendrycks & Gimpel 2016): 0.5 z (1 + tanh(c (z + 0.044715 z^3))),
-// c = sqrt(2/pi); and its derivative
+// c = sqrt(2/pi); and its derivative. tanh is the hardware approximation (tanh.approx.f32,
+// relative error about 2^-11, below the BF16 rounding that every activation gets next).
 constexpr float GELU_C = 0.7978845608028654f;
 constexpr float GELU_A = 0.044715f;
+__device__ __forceinline__ float tanh_hw(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 __device__ __forceinline__ float gelu(float z) {
     const float u = GELU_C * fmaf(GELU_A * z * z, z, z);
-    return 0.5f * z * (1.0f + tanhf(u));
+    return 0.5f * z * (1.0f + tanh_hw(u));
 }
 __device__ __forceinline__ float gelu_grad(float z) {
     const float u = GELU_C * fmaf(GELU_A * z * z, z, z);
-    const float th = tanhf(u);
+    const float th = tanh_hw(u);
     return 0.5f * (1.0f + th) + 0.5f * z * (1.0f - th * th) * GELU_C * fmaf(3.0f * GELU_A, z * z, 1.0f);
 }
 
@@ -234,13 +242,14 @@ __global__ void __launch_bounds__(32 * MF_WARPS, 1)
 // a timeout the kernel raises a status bit and stops.
 // ------------------------------------------------------------------------------------
 constexpr int TC_ROWS = 128;
-constexpr int TC_THREADS = 128;
+constexpr int TC_THREADS = 256;  // warps w and w+4 share TMEM lanes 32*(w%4).. and split the columns
 constexpr uint32_t TC_WAIT_LIMIT = 1u << 24;
 __host__ __device__ constexpr int wc_off(int l) { return l == 0 ? 0 : wc_off(l - 1) + mlp_out(l - 1) * mlp_in(l - 1) * 2; }
 constexpr int WC_BYTES = wc_off(MLP_NL);
 constexpr int TC_ACT_BYTES = TC_ROWS * MLP_H * 2;
 constexpr size_t TC_SMEM = 1024 + size_t(WC_BYTES) + TC_ACT_BYTES + BS_TOTAL * 4 + 64;
 static_assert(TC_SMEM <= 227 * 1024, "shared memory");
+static_assert(TC_THREADS == 2 * TC_ROWS && MLP_IN == 16, "two threads per row: the 16 inputs as two 16-byte chunks");
 
 __device__ uint32_t g_mlp_status = 0;
 
@@ -324,36 +333,50 @@ __device__ __forceinline__ bool tc_layer(unsigned char *wc, unsigned char *act, 
     phase ^= 1u;
     if (!ok) return false;
     tc_fence_after();
-    // epilogue: this thread owns row tid (TMEM lane tid)
-    float v[N];
+    // epilogue: this thread owns row 32*(warp%4) + lane (its TMEM lane) and half of the
+    // 16-column chunks (warps 0-3 the first, 4-7 the second)
+    constexpr int NCH = N / 16, HALF = (NCH + 1) / 2;
+    const int lo = (warp >> 2) ? HALF : 0, hi = (warp >> 2) ? NCH : HALF;
+    const int rl = 32 * (warp & 3) + (tid & 31);
+    const uint32_t tl = tmem + (uint32_t(32 * (warp & 3)) << 16);
+    float v[HALF * 16];
 #pragma unroll
-    for (int c = 0; c < N; c += 16) tmem_ld16(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c), v + c);
+    for (int j = 0; j < HALF; ++j)
+        if (lo + j < hi) tmem_ld16(tl + uint32_t((lo + j) * 16), v + 16 * j);
     tmem_wait_ld();
-    const int r = row0 + tid;
+    const int r = row0 + rl;
     const float *b = bs + bs_off(L);
 #pragma unroll
-    for (int c = 0; c < N; ++c) v[c] += b[c];
-    if (L == MLP_NL - 1) {
-        if (r < n) {
-            float4 *yr = reinterpret_cast<float4 *>(y + size_t(r) * MLP_OUT);
+    for (int j = 0; j < HALF; ++j) {
+        if (lo + j >= hi) break;
+        const int c0 = (lo + j) * 16;
 #pragma unroll
-            for (int c = 0; c < N; c += 4) yr[c / 4] = make_float4(v[c], v[c + 1], v[c + 2], v[c + 3]);
-        }
-    } else {
-        if (SAVE && r < n) {
-            float4 *zr = reinterpret_cast<float4 *>(z + (size_t(L) * n + r) * MLP_H);
+        for (int c = 0; c < 16; ++c) v[16 * j + c] += b[c0 + c];
+        if (L == MLP_NL - 1) {
+            if (r < n) {
+                float4 *yr = reinterpret_cast<float4 *>(y + size_t(r) * MLP_OUT + c0);
 #pragma unroll
-            for (int c = 0; c < N; c += 4) zr[c / 4] = make_float4(v[c], v[c + 1], v[c + 2], v[c + 3]);
-        }
-        // the next layer's A operand (K = 128): 16-byte chunks of 8 activations
+                for (int c = 0; c < 16; c += 4)
+                    yr[c / 4] = make_float4(v[16 * j + c], v[16 * j + c + 1], v[16 * j + c + 2], v[16 * j + c + 3]);
+            }
+        } else {
+            if (SAVE && r < n) {
+                float4 *zr = reinterpret_cast<float4 *>(z + (size_t(L) * n + r) * MLP_H + c0);
 #pragma unroll
-        for (int c8 = 0; c8 < N / 8; ++c8) {
-            uint4 q;
-            q.x = pack_bf16(gelu(v[8 * c8 + 0]), gelu(v[8 * c8 + 1]));
-            q.y = pack_bf16(gelu(v[8 * c8 + 2]), gelu(v[8 * c8 + 3]));
-            q.z = pack_bf16(gelu(v[8 * c8 + 4]), gelu(v[8 * c8 + 5]));
-            q.w = pack_bf16(gelu(v[8 * c8 + 6]), gelu(v[8 * c8 + 7]));
-            *reinterpret_cast<uint4 *>(act + canon_off(tid, c8, MLP_H)) = q;
+                for (int c = 0; c < 16; c += 4)
+                    zr[c / 4] = make_float4(v[16 * j + c], v[16 * j + c + 1], v[16 * j + c + 2], v[16 * j + c + 3]);
+            }
+            // the next layer's A operand (K = 128): two 16-byte chunks of 8 activations
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const float *a = v + 16 * j + 8 * h;
+                uint4 q;
+                q.x = pack_bf16(gelu(a[0]), gelu(a[1]));
+                q.y = pack_bf16(gelu(a[2]), gelu(a[3]));
+                q.z = pack_bf16(gelu(a[4]), gelu(a[5]));
+                q.w = pack_bf16(gelu(a[6]), gelu(a[7]));
+                *reinterpret_cast<uint4 *>(act + canon_off(rl, c0 / 8 + h, MLP_H)) = q;
+            }
         }
     }
     return true;
@@ -401,23 +424,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int tiles = int(ceil_div(n, TC_ROWS));
     for (int tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
         const int row0 = tile * TC_ROWS;
-        // the tile's inputs (K = 16): this thread's row, two 16-byte chunks
+        // the tile's inputs (K = 16): one 16-byte chunk (8 features) per thread
         {
-            const int r = row0 + tid;
-            float4 q[4] = {};
+            const int rl = tid & (TC_ROWS - 1), c8 = tid / TC_ROWS;
+            const int r = row0 + rl;
+            float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0;
             if (r < n) {
-                const float4 *p = reinterpret_cast<const float4 *>(x + size_t(idx ? idx[r] : r) * MLP_IN);
-                q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; q[3] = p[3];
+                const float4 *p = reinterpret_cast<const float4 *>(x + size_t(idx ? idx[r] : r) * MLP_IN + 8 * c8);
+                q0 = p[0];
+                q1 = p[1];
             }
-#pragma unroll
-            for (int c8 = 0; c8 < 2; ++c8) {
-                uint4 u;
-                u.x = pack_bf16(q[2 * c8].x, q[2 * c8].y);
-                u.y = pack_bf16(q[2 * c8].z, q[2 * c8].w);
-                u.z = pack_bf16(q[2 * c8 + 1].x, q[2 * c8 + 1].y);
-                u.w = pack_bf16(q[2 * c8 + 1].z, q[2 * c8 + 1].w);
-                *reinterpret_cast<uint4 *>(act + canon_off(tid, c8, MLP_IN)) = u;
-            }
+            uint4 u;
+            u.x = pack_bf16(q0.x, q0.y);
+            u.y = pack_bf16(q0.z, q0.w);
+            u.z = pack_bf16(q1.x, q1.y);
+            u.w = pack_bf16(q1.z, q1.w);
+            *reinterpret_cast<uint4 *>(act + canon_off(rl, c8, MLP_IN)) = u;
         }
         ok = tc_layer<0, SAVE>(wc, act, bs, tmem, mbar, phase, row0, n, z, y) &&
              tc_layer<1, SAVE>(wc, act, bs, tmem, mbar, phase, row0, n, z, y) &&
@@ -699,7 +721,7 @@ static int num_sms_mlp() {
 
 static bool al16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
-static int g_mlp_path = 0;  // 0: mma.sync, 1: tcgen05
+static int g_mlp_path = 1;  // 0: mma.sync, 1: tcgen05 (default)
 
 static int mlp_forward(const uint16_t *wb, const float *prm, const float *x, const int32_t *idx, int n, float *y,
                        float *z, cudaStream_t st) {

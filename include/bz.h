@@ -361,7 +361,7 @@ int bz_push_collide_f32_noalloc(const bz_params *p, bz_particles_f32 in, const i
 #define BZ_MLP_NPARAM 62032 /* 16*128+128 + 3*(128*128+128) + 128*80+80 */
 int32_t bz_mlp_param_count(void);
 /* forward kernel of bz_mlp_forward / bz_mlp_train_step: 0 = warp-level mma.sync
- * (m16n8k16, default), 1 = tcgen05.mma with a TMEM accumulator (one CTA per 128 rows) */
+ * (m16n8k16), 1 = tcgen05.mma with a TMEM accumulator (one CTA per 128 rows, default) */
 int bz_mlp_select(int32_t path);
 int32_t bz_mlp_selected(void);
 /* device-side conditions of the network kernels since the last call (BZ_DEV_LOOKBACK: a

@@ -11,6 +11,8 @@ kernels compute, in float64:
   GPU rounds them: x and every a_l before a product, the weights, and the loss gradient
   dZ_l before both products of the backward pass (dW_l = dZ_l^T a_{l-1}, dA = dZ_l W_l)
   and the bias sums;
+* GELU with the exact tanh (the GPU uses the hardware tanh approximation, relative error
+  about 2^-11, below the BF16 rounding of every activation that follows);
 * loss = sum_r sum_c wcol_c (y_rc - t_rc)^2 / (2 n);
 * Adam (Kingma & Ba 2015) with bias correction and decoupled weight decay on the
   weights (Loshchilov & Hutter 2019).
