@@ -536,15 +536,75 @@ def run_learned(args, world, rank, local, pg):
     print(json.dumps(line), flush=True)
 
 
+def run_mlp(args, world, rank, local, pg):
+    """The surrogate network's kernels alone: Adam training steps on a fixed synthetic
+    set (2e5 rows, the learned workload's size) and inference over all rows, timed with
+    CUDA events; FLOPs against the measured bf16 tensor peak."""
+    import numpy as np
+    import torch
+    from boltzmann_gb300 import _lib, kernels as K, surrogate as S
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    rng = np.random.default_rng(rank)
+    n = 200_000
+    X = np.zeros((n, 16), np.float32)
+    X[:, :9] = rng.uniform(-1, 1, (n, 9))
+    T = np.zeros((n, 80), np.float32)
+    T[:, :66] = rng.normal(0, 1, (n, 66))
+    xd, td = torch.as_tensor(X, device=dev), torch.as_tensor(T, device=dev)
+    mlp = S.SurrogateMLP(device=dev, seed=rank)
+    batch = args.mlp_batch
+    mlp.train(xd, td, steps=max(args.warmup, 3), batch=batch)
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    mlp.train(xd, td, steps=args.steps, batch=batch)
+    e1.record(st)
+    torch.cuda.synchronize()
+    train_ms = e0.elapsed_time(e1) / args.steps
+    y = torch.empty(n, 80, device=dev)
+    for _ in range(3):
+        K.mlp_forward(mlp.wb, mlp.prm, xd, y)
+    e0.record(st)
+    for _ in range(20):
+        K.mlp_forward(mlp.wb, mlp.prm, xd, y)
+    e1.record(st)
+    torch.cuda.synchronize()
+    inf_ms = e0.elapsed_time(e1) / 20
+    w_count = sum(a * b for a, b in S.LAYERS)
+    l0 = S.LAYERS[0][0] * S.LAYERS[0][1]
+    train_tf = 2.0 * batch * (3 * w_count - l0) / (train_ms * 1e-3) / 1e12
+    inf_tf = 2.0 * n * w_count / (inf_ms * 1e-3) / 1e12
+    peak_tf = peak_tensor()
+    if rank != 0:
+        return
+    path = ["mma.sync", "tcgen05"][_lib.load().bz_mlp_selected()]
+    line = {
+        "metric": "surrogate network inference throughput", "value": n / (inf_ms * 1e-3), "unit": "rows/s",
+        "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": train_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+        "config": {"workload": "4x128 GELU network, 16 inputs, 80 outputs; inference over 2e5 rows, Adam steps "
+                               "on minibatches of %d" % batch, "forward": path},
+        "training": {"ms_per_step": train_ms, "tflops": train_tf},
+        "roofline": {"bound": "tensor", "achieved": inf_tf, "peak": peak_tf[0], "unit": "TFLOP/s",
+                     "frac": inf_tf / peak_tf[0], "traffic": None, "kernel": "k_mlp_fwd_tc (inference)",
+                     "launch_ms": inf_ms, "peak_kind": peak_tf[1]},
+        "cpu_baseline": None, "e2e": None,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="ccp1024", choices=["ccp1024", "swarm512", "learned"],
+    ap.add_argument("--workload", default="ccp1024", choices=["ccp1024", "swarm512", "learned", "mlp"],
                     help="ccp1024: the 2e7-particle CCP (default); swarm512: the batched swarm ensemble; "
-                         "learned: the learned start-up against the plain one")
+                         "learned: the learned start-up against the plain one; mlp: the network's kernels")
     ap.add_argument("--particles", type=float, default=2e7)
     ap.add_argument("--cells", type=int, default=1024)
     ap.add_argument("--rsf", type=int, default=50)
@@ -569,6 +629,8 @@ def main():
         run_swarms(args, world, rank, local, pg)
     elif args.workload == "learned":
         run_learned(args, world, rank, local, pg)
+    elif args.workload == "mlp":
+        run_mlp(args, world, rank, local, pg)
     else:
         run_ours(args, world, rank, local, pg)
     if pg is not None:

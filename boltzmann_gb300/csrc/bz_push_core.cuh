@@ -209,28 +209,31 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
     o.ionized = false;
     o.excited = (proc == P_EXCITE);
     T nvx = vx, nvy = vy, nvz = vz;
-    if (proc == P_ELASTIC) {
-        // |v| (1 - 2 m_e/m_n)^1/2, isotropic (electron_kernel_numba.py:197-209)
-        iso_dir(u1, u2, vmag * k.f_el, nvx, nvy, nvz);
-    } else if (proc != P_NONE) {
-        // energy left after the threshold: in the working precision when e - threshold
-        // keeps at least a quarter of e, else in float64 (the subtraction cancels)
-        const double thr = (proc == P_EXCITE) ? p.e_exc : E_ION;
+    if (proc != P_NONE) {
+        // speed after the collision; one isotropic redirection for every process (warps
+        // whose lanes collide differently run it once)
         T vn;
-        if (sizeof(T) == 8 || e - T(thr) >= T(0.25) * e) {
-            T en = (proc == P_EXCITE) ? (e - T(thr)) : T(0.5) * (e - T(thr));
-            vn = sqrt_pos(en * k.e2v);
+        if (proc == P_ELASTIC) {
+            // |v| (1 - 2 m_e/m_n)^1/2 (electron_kernel_numba.py:197-209)
+            vn = vmag * k.f_el;
         } else {
-            double ed = k.efac_d * (double(ax) * double(ax) + double(ay) * double(ay) + double(az) * double(az));
-            double en = (proc == P_EXCITE) ? fabs(ed - thr) : fabs(0.5 * (ed - thr));
-            vn = T(sqrt(en * k.e2v_d));
+            // energy left after the threshold: in the working precision when e - threshold
+            // keeps at least a quarter of e, else in float64 (the subtraction cancels);
+            // excitation loses e_exc (the reference has no excitation: sigma_g1 = 0),
+            // ionization shares e - 15.76 equally (electron_kernel_numba.py:211-255)
+            const double thr = (proc == P_EXCITE) ? p.e_exc : E_ION;
+            if (sizeof(T) == 8 || e - T(thr) >= T(0.25) * e) {
+                T en = (proc == P_EXCITE) ? (e - T(thr)) : T(0.5) * (e - T(thr));
+                vn = sqrt_pos(en * k.e2v);
+            } else {
+                double ed = k.efac_d * (double(ax) * double(ax) + double(ay) * double(ay) + double(az) * double(az));
+                double en = (proc == P_EXCITE) ? fabs(ed - thr) : fabs(0.5 * (ed - thr));
+                vn = T(sqrt(en * k.e2v_d));
+            }
         }
-        if (proc == P_EXCITE) {
-            // lose e_exc, isotropic (the reference has no excitation: sigma_g1 = 0)
-            iso_dir(u1, u2, vn, nvx, nvy, nvz);
-        } else {
-            // ionization, equal sharing of e - 15.76 (electron_kernel_numba.py:211-255)
-            iso_dir(u1, u2, vn, nvx, nvy, nvz);
+        iso_dir(u1, u2, vn, nvx, nvy, nvz);
+        if (proc == P_IONIZE) {
+            // the new electron: same position and weight, its own isotropic direction
             Uni<T> u5;
             if (REPLAY) {
                 u5 = uni_from_replay<T>(R[size_t(slot) * 7 + 5]);

@@ -41,6 +41,11 @@ template <typename T> struct Seg {
 __device__ __forceinline__ int64_t seg_slot(int seg, int run, int half, int j) {
     return int64_t(seg) * (2 * int64_t(half)) + int64_t(run) * half + j;
 }
+// the same slot as a 32-bit index: the push's launcher checks that every slot fits (an
+// unsigned 32-bit index lets each array access be one wide multiply-add on its base)
+__device__ __forceinline__ uint32_t seg_slot32(int seg, int run, int half, int j) {
+    return uint32_t(seg) * (2u * uint32_t(half)) + uint32_t(run) * uint32_t(half) + uint32_t(j);
+}
 
 template <typename T, bool REPLAY, int XS, bool DEPOSIT, int SG_T, int SG_I, int MINB, bool PF>
 __global__ void __launch_bounds__(SG_T, MINB)
@@ -83,11 +88,11 @@ __global__ void __launch_bounds__(SG_T, MINB)
                 cnt = cnt < 0 ? 0 : H;
             }
             if (n_pushed && lane == 0 && cnt > 0) atomicAdd(n_pushed, (unsigned long long)cnt);
-            const int64_t rbase = seg_slot(seg, run, H, 0);
+            const uint32_t rbase = seg_slot32(seg, run, H, 0);
             // one particle of the run (zeros past its end)
             auto fetch = [&](int j, T &a, T &b, T &c, T &d, T &e) {
                 const bool ok = j < cnt;
-                const int64_t q = rbase + j;
+                const uint32_t q = rbase + uint32_t(j);
                 a = ok ? in.a.x[q] : T(0);
                 b = ok ? in.a.vx[q] : T(0);
                 c = ok ? in.a.vy[q] : T(0);
@@ -108,7 +113,7 @@ __global__ void __launch_bounds__(SG_T, MINB)
                 } else if constexpr (SG_I == 4 && sizeof(T) == 4) {
                   if (j0 + SG_I <= cnt && (H % 4) == 0) {
                     vec = true;
-                    const int64_t b = rbase + j0;
+                    const uint32_t b = rbase + uint32_t(j0);
                     float4 qa = *reinterpret_cast<const float4 *>(in.a.x + b);
                     float4 qb = *reinterpret_cast<const float4 *>(in.a.vx + b);
                     float4 qc = *reinterpret_cast<const float4 *>(in.a.vy + b);
@@ -123,7 +128,7 @@ __global__ void __launch_bounds__(SG_T, MINB)
                 } else if constexpr (SG_I == 2 && sizeof(T) == 4) {
                   if (j0 + SG_I <= cnt && (H % 2) == 0) {
                     vec = true;
-                    const int64_t b = rbase + j0;
+                    const uint32_t b = rbase + uint32_t(j0);
                     float2 qa = *reinterpret_cast<const float2 *>(in.a.x + b);
                     float2 qb = *reinterpret_cast<const float2 *>(in.a.vx + b);
                     float2 qc = *reinterpret_cast<const float2 *>(in.a.vy + b);
@@ -140,7 +145,7 @@ __global__ void __launch_bounds__(SG_T, MINB)
 #pragma unroll
                     for (int k = 0; k < SG_I; ++k) {
                         const bool ok = j0 + k < cnt;
-                        const int64_t b = rbase + j0 + k;
+                        const uint32_t b = rbase + uint32_t(j0 + k);
                         x[k] = ok ? in.a.x[b] : T(0);
                         vx[k] = ok ? in.a.vx[b] : T(0);
                         vy[k] = ok ? in.a.vy[b] : T(0);
@@ -156,7 +161,7 @@ __global__ void __launch_bounds__(SG_T, MINB)
                     it[k].ionized = false;
                     it[k].excited = false;
                     if (w[k] > T(0)) {
-                        push_item<T, REPLAY, XS>(p, kc, rng, uint32_t(rbase + j0 + k), x[k], vx[k], vy[k], vz[k], E_s,
+                        push_item<T, REPLAY, XS>(p, kc, rng, rbase + uint32_t(j0 + k), x[k], vx[k], vy[k], vz[k], E_s,
                                                  xs_s, R, gas, it[k]);
                         // one test for the three components (a sum of finite speeds stays finite)
                         if (!isfinite(it[k].vx + it[k].vy + it[k].vz)) err |= BZ_DEV_NONFINITE;
@@ -233,7 +238,7 @@ __global__ void __launch_bounds__(SG_T, MINB)
                 for (int k = 0; k < SG_I; ++k) {
                     if (it[k].alive) {
                         if (ps < uint32_t(H)) {
-                            const int64_t q = seg_slot(seg, 0, H, int(ps));
+                            const uint32_t q = seg_slot32(seg, 0, H, int(ps));
                             out.a.x[q] = it[k].x; out.a.vx[q] = it[k].vx; out.a.vy[q] = it[k].vy;
                             out.a.vz[q] = it[k].vz; out.a.w[q] = w[k];
                         } else {
@@ -243,7 +248,7 @@ __global__ void __launch_bounds__(SG_T, MINB)
                     }
                     if (it[k].child) {
                         if (pc < uint32_t(H)) {
-                            const int64_t q = seg_slot(seg, 1, H, int(pc));
+                            const uint32_t q = seg_slot32(seg, 1, H, int(pc));
                             out.a.x[q] = it[k].cx; out.a.vx[q] = it[k].cvx; out.a.vy[q] = it[k].cvy;
                             out.a.vz[q] = it[k].cvz; out.a.w[q] = w[k];
                         } else {
@@ -489,6 +494,7 @@ static int seg_push_entry(const bz_params *pp, S in_, S out_, const T *E, const 
                           void *stream) {
     if (!pp || !E || !ws || !status || !seg_flags || !seg_ok<T>(in_) || !seg_ok<T>(out_)) return BZ_ERR_ARG;
     if (in_.nseg != out_.nseg || in_.half != out_.half) return BZ_ERR_ARG;
+    if (int64_t(in_.nseg) * 2 * in_.half > int64_t(UINT32_MAX)) return BZ_ERR_TOO_LARGE;  // 32-bit slot indices
     if (ws_bytes < 256) return BZ_ERR_WORKSPACE;
     if ((R == nullptr) != (gas == nullptr)) return BZ_ERR_ARG;
     const bz_params &p = *pp;

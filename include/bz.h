@@ -236,7 +236,8 @@ typedef struct bz_segments_f64 { double *x, *vx, *vy, *vz, *w; int32_t *counts; 
 
 /* Push + collide (+ deposit) of a segmented state into another (same nseg, half); the
  * per-particle arithmetic of bz_push_collide_*. Philox counters use the input slot.
- * n_pushed (optional, device) accumulates the number of input particles pushed. */
+ * n_pushed (optional, device) accumulates the number of input particles pushed. Slots are
+ * indexed with 32 bits: nseg * 2 * half above 2^32 - 1 returns BZ_ERR_TOO_LARGE. */
 size_t bz_seg_push_workspace(void);
 int bz_seg_push_collide_f32(const bz_params *p, bz_segments_f32 in, bz_segments_f32 out, const float *E,
                             const double *replay_R, const double *replay_gas, double *moments,
