@@ -237,7 +237,8 @@ def run_ours(args, world, rank, local, pg):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     cfg = config.ccp_1024(num_particles=int(args.particles), gridpts=args.cells + 1, resample_freq=args.rsf,
-                          seed=1 + rank, autotune=not args.no_autotune, capacity_factor=4.0, seg_half=args.seg_half)
+                          seed=1 + rank, autotune=not args.no_autotune, capacity_factor=4.0, seg_half=args.seg_half,
+                          Te_init_eV=args.te_init)
     sol = BoltzmannGB300(cfg, device=dev)
     n_start = sol.n()
     for _ in range(args.warmup):
@@ -612,6 +613,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the push's default CTA shape")
     ap.add_argument("--seg-half", type=int, default=2048, help="slots per run of a particle segment")
+    ap.add_argument("--te-init", type=float, default=1.0,
+                    help="initial electron temperature, eV (the benchmark starts at 1; a hotter start profiles the "
+                         "collision-heavy state the run reaches after ~100 steps)")
     ap.add_argument("--cpu-sample", type=float, default=1e6)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--ref-sample", type=float, default=2e6)
