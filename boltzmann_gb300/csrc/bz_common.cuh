@@ -59,6 +59,25 @@ __device__ __forceinline__ u32x4 philox_rk(uint32_t c0, uint32_t c1, uint32_t c2
     }
     return {c0, c1, c2, c3};
 }
+// Two independent counters (differing only in the last word) through the same rounds, one
+// round of each after the other: the two dependency chains interleave, so a warp has a
+// second multiply to issue while the first one's result is pending.
+__device__ __forceinline__ void philox_rk_x2(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3a, uint32_t c3b,
+                                             const uint32_t *rk0, const uint32_t *rk1, u32x4 &ra, u32x4 &rb) {
+    uint32_t a0 = c0, a1 = c1, a2 = c2, a3 = c3a;
+    uint32_t b0 = c0, b1 = c1, b2 = c2, b3 = c3b;
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint64_t pa0 = uint64_t(0xD2511F53u) * a0, pa1 = uint64_t(0xCD9E8D57u) * a2;
+        const uint64_t pb0 = uint64_t(0xD2511F53u) * b0, pb1 = uint64_t(0xCD9E8D57u) * b2;
+        const uint32_t na0 = uint32_t(pa1 >> 32) ^ a1 ^ rk0[r], na2 = uint32_t(pa0 >> 32) ^ a3 ^ rk1[r];
+        const uint32_t nb0 = uint32_t(pb1 >> 32) ^ b1 ^ rk0[r], nb2 = uint32_t(pb0 >> 32) ^ b3 ^ rk1[r];
+        a1 = uint32_t(pa1); a3 = uint32_t(pa0); a0 = na0; a2 = na2;
+        b1 = uint32_t(pb1); b3 = uint32_t(pb0); b0 = nb0; b2 = nb2;
+    }
+    ra = {a0, a1, a2, a3};
+    rb = {b0, b1, b2, b3};
+}
 inline void philox_round_keys(uint64_t seed, uint32_t *rk0, uint32_t *rk1) {
     uint32_t k0 = uint32_t(seed), k1 = uint32_t(seed >> 32);
     for (int r = 0; r < 10; ++r, k0 += 0x9E3779B9u, k1 += 0xBB67AE85u) {
@@ -107,6 +126,13 @@ __device__ __forceinline__ void draw4(const Rng &g, uint32_t slot, uint32_t tag,
     d.v[0] = uni_d(a.x, a.y); d.v[1] = uni_d(a.z, a.w); d.v[2] = uni_d(b.x, b.y); d.v[3] = uni_d(b.z, b.w);
 }
 // the same draws with precomputed round keys
+__device__ __forceinline__ void draw4x2(const Rng &g, const uint32_t *rk0, const uint32_t *rk1, uint32_t slot,
+                                        uint32_t tag_a, uint32_t tag_b, Draw4<float> &da, Draw4<float> &db) {
+    u32x4 a, b;
+    philox_rk_x2(slot, g.s0, g.s1, tag_a, tag_b, rk0, rk1, a, b);
+    da.v[0] = uni_f(a.x); da.v[1] = uni_f(a.y); da.v[2] = uni_f(a.z); da.v[3] = uni_f(a.w);
+    db.v[0] = uni_f(b.x); db.v[1] = uni_f(b.y); db.v[2] = uni_f(b.z); db.v[3] = uni_f(b.w);
+}
 __device__ __forceinline__ void draw4(const Rng &g, const uint32_t *rk0, const uint32_t *rk1, uint32_t slot,
                                       uint32_t tag, Draw4<float> &d) {
     u32x4 r = philox_rk(slot, g.s0, g.s1, tag, rk0, rk1);

@@ -134,16 +134,20 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
         u2 = uni_from_replay<T>(R[size_t(slot) * 7 + 2]);
         u3 = uni_from_replay<T>(R[size_t(slot) * 7 + 3]);
     } else {
+        Draw4<T> dg, d;
+        if constexpr (sizeof(T) == 4) {
+            // gas-velocity and collision uniforms from one interleaved pair of Philox calls
+            draw4x2(rng, k.rk0, k.rk1, slot, 0u, 1u, dg, d);
+        } else {
+            draw4(rng, k.rk0, k.rk1, slot, 0u, dg);
+            draw4(rng, k.rk0, k.rk1, slot, 1u, d);
+        }
         if (k.gas_sigma > T(0)) {
-            Draw4<T> d;
-            draw4(rng, k.rk0, k.rk1, slot, 0u, d);
             T h;
-            box_muller(d.v[0].u, d.v[1].u, g0, g1);
-            box_muller(d.v[2].u, d.v[3].u, g2, h);
+            box_muller(dg.v[0].u, dg.v[1].u, g0, g1);
+            box_muller(dg.v[2].u, dg.v[3].u, g2, h);
             g0 *= k.gas_sigma; g1 *= k.gas_sigma; g2 *= k.gas_sigma;
         }
-        Draw4<T> d;
-        draw4(rng, k.rk0, k.rk1, slot, 1u, d);
         u0 = d.v[0]; u1 = d.v[1]; u2 = d.v[2]; u3 = d.v[3];
         r0_replay = double(u0.u);
     }
