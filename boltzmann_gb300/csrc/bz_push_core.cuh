@@ -151,6 +151,16 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
         u0 = d.v[0]; u1 = d.v[1]; u2 = d.v[2]; u3 = d.v[3];
         r0_replay = double(u0.u);
     }
+    // the field at the pre-push face (electron_kernel_numba.py:257-263), read first: it
+    // depends on x only, and its shared-memory load overlaps the collision arithmetic
+    int face = 0;
+    if (p.advect == BZ_ADVECT_ENSEMBLE) {
+        face = min(max(int(x), 0), k.face_max);
+    } else if (p.advect) {
+        face = face_index(x, p.dx, k.inv_dx_f);
+        face = min(max(face, 0), k.face_max);
+    }
+    const T Ef = E_s[face];
     // energy of the gas-relative velocity (electron_kernel_numba.py:55-63)
     T ax = vx - g0, ay = vy - g1, az = vz - g2;
     T v2 = ax * ax + ay * ay + az * az;
@@ -256,14 +266,9 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
     // drift with the post-collision velocity, kick with E at the pre-push face,
     // absorbing walls (electron_kernel_numba.py:257-276)
     T xn = x;
-    int face = 0;
     bool valid = true;
-    if (p.advect == BZ_ADVECT_ENSEMBLE) {
-        face = min(max(int(x), 0), k.face_max);
-    } else if (p.advect) {
+    if (p.advect == BZ_ADVECT_1D) {
         xn = x + k.c100dt * nvx;
-        face = face_index(x, p.dx, k.inv_dx_f);
-        face = min(max(face, 0), k.face_max);
         if (xn < k.wall_lo || xn > k.wall_hi) {
             // near a wall: decide in float64 like the reference
             double xd = double(x) + k.c100dt_d * double(nvx);
@@ -271,7 +276,7 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
             xn = T(xd);
         }
     }
-    nvx -= k.kick * E_s[face];
+    nvx -= k.kick * Ef;
     o.alive = valid;
     o.x = xn; o.vx = nvx; o.vy = nvy; o.vz = nvz;
     o.e = k.efac * (nvx * nvx + nvy * nvy + nvz * nvz);
