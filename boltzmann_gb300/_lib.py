@@ -134,7 +134,8 @@ _PROTOS = {
     "bz_mlp_status": (ctypes.c_int, [_vp]),
     "bz_mlp_sync": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
     "bz_mlp_forward": (ctypes.c_int, [_vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp]),
-    "bz_mlp_backward": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp, _vp, _vp]),
+    "bz_mlp_backward_workspace": (_sz, [_i32]),
+    "bz_mlp_backward": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "bz_mlp_adam": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _i64, _f32, _f32, _f32, _f32, _f32, _vp]),
     "bz_mlp_batch": (ctypes.c_int, [_i32, _i32, ctypes.c_uint64, ctypes.c_uint64, _vp, _vp]),
     "bz_mlp_train_workspace": (_sz, [_i32]),

@@ -659,6 +659,261 @@ __global__ void __launch_bounds__(32 * MB_WARPS, 1)
 }
 
 // ------------------------------------------------------------------------------------
+// backward on tcgen05: one CTA of 8 warps per tile of 128 rows, from the output layer down.
+// Per layer l two products into TMEM (one thread issues both, one commit):
+//   dW_l | db_l = dZ_l^T [A_{l-1} | 1]   M = 128 (out_l rows, zero-padded), N = in_l + 16,
+//                                         K = the tile's 128 rows; column in_l of the
+//                                         accumulator is the bias gradient
+//   dA_{l-1}    = dZ_l W_l               M = 128 rows, N = in_l, K = out_l   (l >= 1)
+// Operands in shared memory in the canonical K-major layout: dZ row-major and transposed,
+// [A_{l-1} | 1] transposed (rebuilt from the saved pre-activations), W_l^T (all layers,
+// staged once). dZ_{l-1} = dA_{l-1} gelu'(z_{l-1}) stays in the registers of the thread that
+// owns the row. The tile's dW, db go to the CTA's own FP32 slice of a partial buffer (no
+// atomics: the sum over slices is taken afterwards, in a fixed order).
+// ------------------------------------------------------------------------------------
+__host__ __device__ constexpr int wtc_off(int l) {  // W_l^T, layers 1..
+    return l <= 1 ? 0 : wtc_off(l - 1) + mlp_in(l - 1) * mlp_out(l - 1) * 2;
+}
+constexpr int WTC_BYTES = wtc_off(MLP_NL);
+constexpr int TB_DZ = TC_ROWS * MLP_H * 2;          // dZ, rows x out (K = out)
+constexpr int TB_DZT = 128 * TC_ROWS * 2;           // dZ^T, out (padded to 128) x rows
+constexpr int TB_AT = (MLP_H + 16) * TC_ROWS * 2;   // [A | 1]^T, (in + 16) x rows
+constexpr size_t TCB_SMEM = 1024 + size_t(WTC_BYTES) + TB_DZ + TB_DZT + TB_AT + 64;
+static_assert(TCB_SMEM <= 227 * 1024, "shared memory");
+constexpr uint32_t TCB_COL_DA = 256;  // TMEM column of the dA accumulator (dW | db at 0)
+
+// bf16 of v at (row r, column k) of a canonical K-major matrix with K columns
+__device__ __forceinline__ void put_canon(unsigned char *base, int r, int k, int K, float v) {
+    *reinterpret_cast<__nv_bfloat16 *>(base + (r >> 3) * (16 * K) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2) =
+        __float2bfloat16_rn(v);
+}
+
+// 16 values (columns c0 .. c0+15 of row rl) as two 16-byte chunks of a canonical K-major
+// matrix with C columns
+__device__ __forceinline__ void put_row16(unsigned char *base, int rl, int c0, int C, const float *v) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const float *a = v + 8 * h;
+        uint4 q;
+        q.x = pack_bf16(a[0], a[1]);
+        q.y = pack_bf16(a[2], a[3]);
+        q.z = pack_bf16(a[4], a[5]);
+        q.w = pack_bf16(a[6], a[7]);
+        *reinterpret_cast<uint4 *>(base + canon_off(rl, c0 / 8 + h, C)) = q;
+    }
+}
+
+// [A_{L-1} | 1]^T of the tile: this thread's row (a column of the operand), its half of
+// the inputs
+template <int L>
+__device__ __forceinline__ void tcb_put_at(unsigned char *at, int rl, int half, int row0, int n, const float *x,
+                                           const int32_t *idx, const float *z) {
+    constexpr int NI = mlp_in(L);
+    const int r = row0 + rl;
+    const float *src = nullptr;
+    if (r < n) src = (L == 0) ? x + size_t(idx ? idx[r] : r) * MLP_IN : z + (size_t(L > 0 ? L - 1 : 0) * n + r) * MLP_H;
+    const int c_lo = half * (NI / 2);
+#pragma unroll
+    for (int c = 0; c < NI / 2; c += 4) {
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (src) {
+            v = *reinterpret_cast<const float4 *>(src + c_lo + c);
+            if (L > 0) { v.x = gelu(v.x); v.y = gelu(v.y); v.z = gelu(v.z); v.w = gelu(v.w); }
+        }
+        put_canon(at, c_lo + c + 0, rl, TC_ROWS, v.x);
+        put_canon(at, c_lo + c + 1, rl, TC_ROWS, v.y);
+        put_canon(at, c_lo + c + 2, rl, TC_ROWS, v.z);
+        put_canon(at, c_lo + c + 3, rl, TC_ROWS, v.w);
+    }
+    if (half) {  // the ones row (bias gradient) and 15 zero rows
+#pragma unroll
+        for (int j = 0; j < 16; ++j) put_canon(at, NI + j, rl, TC_ROWS, (j == 0 && r < n) ? 1.f : 0.f);
+    }
+}
+
+template <int L>
+__device__ __forceinline__ bool tcb_layer(unsigned char *wtc, unsigned char *dz, unsigned char *dzt,
+                                          unsigned char *at, uint32_t tmem, uint32_t mbar, uint32_t &phase,
+                                          int row0, int n, const float *x, const int32_t *idx, const float *z,
+                                          float *part, bool first, float (&d)[64]) {
+    constexpr int NO = mlp_out(L), NI = mlp_in(L);
+    const int tid = threadIdx.x, warp = tid >> 5, half = warp >> 2;
+    const int rl = 32 * (warp & 3) + (tid & 31);
+    // operands: dZ_L (from d: this half's 16-column chunks) row-major and transposed
+    {
+        constexpr int NCH = NO / 16, H0 = (NCH + 1) / 2;
+        const int lo = half ? H0 : 0, hi = half ? NCH : H0;
+#pragma unroll
+        for (int j = 0; j < H0; ++j) {
+            if (lo + j < hi) {
+                const int c0 = (lo + j) * 16;
+                put_row16(dz, rl, c0, NO, d + 16 * j);
+#pragma unroll
+                for (int c = 0; c < 16; ++c) put_canon(dzt, c0 + c, rl, TC_ROWS, d[16 * j + c]);
+            }
+        }
+        if (NO < 128 && half)  // zero rows of the padded dZ^T
+            for (int o = NO; o < 128; ++o) put_canon(dzt, o, rl, TC_ROWS, 0.f);
+    }
+    tcb_put_at<L>(at, rl, half, row0, n, x, idx, z);
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0) {
+        tc_fence_after();
+        const uint32_t a_dzt = smem_u32(dzt), b_at = smem_u32(at);
+        constexpr uint32_t id_w = idesc_bf16(128, NI + 16);
+#pragma unroll
+        for (int kk = 0; kk < TC_ROWS / 16; ++kk)
+            tc_mma(tmem, umma_desc(a_dzt + kk * 256, 128, 16 * TC_ROWS), umma_desc(b_at + kk * 256, 128, 16 * TC_ROWS),
+                   id_w, kk > 0 ? 1u : 0u);
+        if constexpr (L > 0) {
+            const uint32_t a_dz = smem_u32(dz), b_w = smem_u32(wtc + wtc_off(L));
+            constexpr uint32_t id_a = idesc_bf16(TC_ROWS, NI);
+#pragma unroll
+            for (int kk = 0; kk < NO / 16; ++kk)
+                tc_mma(tmem + TCB_COL_DA, umma_desc(a_dz + kk * 256, 128, 16 * NO), umma_desc(b_w + kk * 256, 128, 16 * NO),
+                       id_a, kk > 0 ? 1u : 0u);
+        }
+        tc_commit(mbar);
+    }
+    const bool ok = __syncthreads_and(mbar_wait(mbar, phase)) != 0;
+    phase ^= 1u;
+    if (!ok) return false;
+    tc_fence_after();
+    const uint32_t tl = tmem + (uint32_t(32 * (warp & 3)) << 16);
+    // dW | db: lane = output unit o, columns = inputs (+ the ones column)
+    {
+        constexpr int NCH = (NI + 16) / 16, H0 = (NCH + 1) / 2;
+        const int lo = half ? H0 : 0, hi = half ? NCH : H0;
+        const int o = rl;
+#pragma unroll
+        for (int j = 0; j < H0; ++j) {
+            if (lo + j >= hi) break;
+            float v[16];
+            tmem_ld16(tl + uint32_t((lo + j) * 16), v);
+            tmem_wait_ld();
+            if (o < NO) {
+                float *pw = part + mlp_woff(L) + size_t(o) * NI;
+#pragma unroll
+                for (int c = 0; c < 16; ++c) {
+                    const int i = (lo + j) * 16 + c;
+                    if (i < NI) pw[i] = first ? v[c] : pw[i] + v[c];
+                    else if (i == NI) part[mlp_boff(L) + o] = first ? v[c] : part[mlp_boff(L) + o] + v[c];
+                }
+            }
+        }
+    }
+    if constexpr (L > 0) {
+        // dZ_{L-1} = dA gelu'(z_{L-1}): this thread's row, its half of the columns
+        const int r = row0 + rl;
+        const float *zr = z + (size_t(L - 1) * n + (r < n ? r : 0)) * MLP_H;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int c0 = half * 64 + j * 16;
+            float v[16];
+            tmem_ld16(tl + TCB_COL_DA + uint32_t(c0), v);
+            tmem_wait_ld();
+#pragma unroll
+            for (int c = 0; c < 16; ++c) d[16 * j + c] = (r < n) ? v[c] * gelu_grad(zr[c0 + c]) : 0.f;
+        }
+    }
+    // every TMEM read and operand read of this layer is done before the next one writes
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    return true;
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_mlp_bwd_tc(const uint16_t *wt, const float *x, const float *tg, const float *wcol, const int32_t *idx, int n,
+                 const float *y, const float *z, float *partials, float *loss) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *base = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023u)) & 1023u);
+    unsigned char *wtc = base;
+    unsigned char *dz = wtc + WTC_BYTES;
+    unsigned char *dzt = dz + TB_DZ;
+    unsigned char *at = dzt + TB_DZT;
+    uint64_t *mbar_p = reinterpret_cast<uint64_t *>(at + TB_AT);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar_p + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, half = warp >> 2;
+    const int rl = 32 * (warp & 3) + (tid & 31);
+    // W_l^T (in_l x out_l, K = out_l) of layers 1..4 into the canonical layout
+#pragma unroll
+    for (int l = 1; l < MLP_NL; ++l) {
+        const int K = mlp_out(l), N = mlp_in(l), chunks = K / 8;
+        for (int e = tid; e < N * chunks; e += TC_THREADS) {
+            const int r = e / chunks, c8 = e - r * chunks;
+            cp_async16(wtc + wtc_off(l) + canon_off(r, c8, K), wt + mlp_woff(l) + size_t(r) * K + c8 * 8);
+        }
+    }
+    float *part = partials + size_t(blockIdx.x) * MLP_NPARAM;
+    const uint32_t mbar = smem_u32(mbar_p);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tmem_slot))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    cp_async_wait_all();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    uint32_t phase = 0;
+    bool ok = true;
+    const float inv_n = 1.0f / float(n);
+    float lsum = 0.f;
+    const int tiles = int(ceil_div(n, TC_ROWS));
+    for (int tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+        const int row0 = tile * TC_ROWS;
+        const int r = row0 + rl;
+        const bool first = tile == int(blockIdx.x);
+        // dZ_4 = wcol (y - t) / n for this thread's row and half of the 80 outputs
+        float d[64];
+        {
+            constexpr int NCH = MLP_OUT / 16, H0 = (NCH + 1) / 2;
+            const int c_lo = half ? H0 * 16 : 0, c_hi = half ? MLP_OUT : H0 * 16;
+            const float *tr = (r < n) ? tg + size_t(idx ? idx[r] : r) * MLP_OUT : nullptr;
+#pragma unroll
+            for (int j = 0; j < H0 * 16; ++j) {
+                const int c = c_lo + j;
+                float e = 0.f;
+                if (tr && c < c_hi) {
+                    const float dy = y[size_t(r) * MLP_OUT + c] - tr[c];
+                    e = dy * wcol[c];
+                    lsum += 0.5f * e * dy;
+                }
+                d[j] = e * inv_n;
+            }
+        }
+        ok = tcb_layer<4>(wtc, dz, dzt, at, tmem, mbar, phase, row0, n, x, idx, z, part, first, d) &&
+             tcb_layer<3>(wtc, dz, dzt, at, tmem, mbar, phase, row0, n, x, idx, z, part, first, d) &&
+             tcb_layer<2>(wtc, dz, dzt, at, tmem, mbar, phase, row0, n, x, idx, z, part, first, d) &&
+             tcb_layer<1>(wtc, dz, dzt, at, tmem, mbar, phase, row0, n, x, idx, z, part, first, d) &&
+             tcb_layer<0>(wtc, dz, dzt, at, tmem, mbar, phase, row0, n, x, idx, z, part, first, d);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+    if ((tid & 31) == 0 && lsum != 0.f) atomicAdd(loss, lsum * inv_n);
+    if (!ok && tid == 0) atomicOr(&g_mlp_status, BZ_DEV_LOOKBACK);
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+}
+
+// grad += sum over the CTAs' slices, in slice order
+__global__ void k_mlp_reduce(const float *partials, int slices, float *grad) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < MLP_NPARAM; i += gridDim.x * blockDim.x) {
+        float s = 0.f;
+        for (int c = 0; c < slices; ++c) s += partials[size_t(c) * MLP_NPARAM + i];
+        grad[i] += s;
+    }
+}
+
+// ------------------------------------------------------------------------------------
 // parameters: BF16 copies, Adam, minibatch indices
 // ------------------------------------------------------------------------------------
 __device__ __forceinline__ void put_bf16_copies(int i, float p, uint16_t *wb, uint16_t *wt) {
@@ -721,13 +976,13 @@ static int num_sms_mlp() {
 
 static bool al16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
-static int g_mlp_path = 1;  // 0: mma.sync, 1: tcgen05 (default)
+static int g_mlp_path = 1;  // 0: mma.sync; 1: tcgen05 forward (default); 2: tcgen05 forward and backward
 
 static int mlp_forward(const uint16_t *wb, const float *prm, const float *x, const int32_t *idx, int n, float *y,
                        float *z, cudaStream_t st) {
     if (n == 0) return BZ_OK;
     if (!wb || !prm || !x || !y || n < 0 || !al16(wb) || !al16(x) || !al16(y) || (z && !al16(z))) return BZ_ERR_ARG;
-    if (g_mlp_path == 1) {
+    if (g_mlp_path >= 1) {
         auto run_tc = [&](auto kern) -> int {
             if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TC_SMEM)) != cudaSuccess)
                 return BZ_ERR_UNSUPPORTED;
@@ -747,11 +1002,30 @@ static int mlp_forward(const uint16_t *wb, const float *prm, const float *x, con
     return z ? run(k_mlp_fwd<true>) : run(k_mlp_fwd<false>);
 }
 
+// slices of the tcgen05 backward's partial gradient for n rows
+static int mlp_bwd_slices(int n) { return std::max(1, std::min(int(ceil_div(n, TC_ROWS)), num_sms_mlp())); }
+static size_t mlp_bwd_ws(int n) { return size_t(mlp_bwd_slices(n)) * MLP_NPARAM * sizeof(float); }
+
 static int mlp_backward(const uint16_t *wt, const float *x, const float *t, const float *wcol, const int32_t *idx,
-                        int n, const float *y, const float *z, float *grad, float *loss, cudaStream_t st) {
+                        int n, const float *y, const float *z, float *grad, float *loss, void *ws, size_t ws_bytes,
+                        cudaStream_t st) {
     if (n == 0) return BZ_OK;
-    if (!wt || !x || !t || !wcol || !y || !z || !grad || !loss || n < 0 || !al16(wt) || !al16(y) || !al16(z))
+    if (!wt || !x || !t || !wcol || !y || !z || !grad || !loss || n < 0 || !al16(wt) || !al16(y) || !al16(z) ||
+        !al16(x))
         return BZ_ERR_ARG;
+    if (ws) {  // tcgen05, per-CTA slices summed in a fixed order (deterministic)
+        if (!al16(ws)) return BZ_ERR_ARG;
+        if (ws_bytes < mlp_bwd_ws(n)) return BZ_ERR_WORKSPACE;
+        if (cudaFuncSetAttribute(k_mlp_bwd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TCB_SMEM)) !=
+            cudaSuccess)
+            return BZ_ERR_UNSUPPORTED;
+        const int slices = mlp_bwd_slices(n);
+        float *part = static_cast<float *>(ws);
+        k_mlp_bwd_tc<<<slices, TC_THREADS, TCB_SMEM, st>>>(wt, x, t, wcol, idx, n, y, z, part, loss);
+        if (cudaGetLastError() != cudaSuccess) return BZ_ERR_CUDA;
+        k_mlp_reduce<<<int(ceil_div(MLP_NPARAM, 256)), 256, 0, st>>>(part, slices, grad);
+        return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+    }
     if (cudaFuncSetAttribute(k_mlp_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, int(BWD_SMEM)) != cudaSuccess)
         return BZ_ERR_UNSUPPORTED;
     const int tiles = int(ceil_div(n, MB_ROWS));
@@ -779,10 +1053,12 @@ static int mlp_batch(int n_rows, int n, uint64_t seed, uint64_t step, int32_t *i
     return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
 }
 
-// training workspace: idx (n int32, padded to 256 B), y (n x OUT), z ((NL-1) x n x H)
+// training workspace: idx (n int32, padded to 256 B), y (n x OUT), z ((NL-1) x n x H), and
+// the tcgen05 backward's partial gradients
 static size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 static size_t mlp_train_ws(int n) {
-    return align256(size_t(n) * 4) + align256(size_t(n) * MLP_OUT * 4) + align256(size_t(MLP_NL - 1) * n * MLP_H * 4);
+    return align256(size_t(n) * 4) + align256(size_t(n) * MLP_OUT * 4) +
+           align256(size_t(MLP_NL - 1) * n * MLP_H * 4) + align256(mlp_bwd_ws(n));
 }
 
 }  // namespace bz
@@ -794,7 +1070,7 @@ extern "C" {
 int32_t bz_mlp_param_count(void) { return MLP_NPARAM; }
 
 int bz_mlp_select(int32_t path) {
-    if (path < 0 || path > 1) return BZ_ERR_ARG;
+    if (path < 0 || path > 2) return BZ_ERR_ARG;
     g_mlp_path = path;
     return BZ_OK;
 }
@@ -820,12 +1096,14 @@ int bz_mlp_forward(const uint16_t *wb, const float *params, const float *x, cons
     return mlp_forward(wb, params, x, idx, n, y, z, as_stream(stream));
 }
 
+size_t bz_mlp_backward_workspace(int32_t n) { return n > 0 ? mlp_bwd_ws(n) : 0; }
+
 int bz_mlp_backward(const uint16_t *wb, const uint16_t *wt, const float *params, const float *x, const float *t,
                     const float *wcol, const int32_t *idx, int32_t n, const float *y, const float *z, float *grad,
-                    float *loss, void *stream) {
+                    float *loss, void *workspace, size_t workspace_bytes, void *stream) {
     (void)wb;
     (void)params;  // the output layer's bias and the weights enter through y and z
-    return mlp_backward(wt, x, t, wcol, idx, n, y, z, grad, loss, as_stream(stream));
+    return mlp_backward(wt, x, t, wcol, idx, n, y, z, grad, loss, workspace, workspace_bytes, as_stream(stream));
 }
 
 int bz_mlp_adam(float *params, float *grad, float *m, float *v, uint16_t *wb, uint16_t *wt, int64_t step, float lr,
@@ -850,9 +1128,13 @@ int bz_mlp_train_step(float *params, float *grad, float *m, float *v, uint16_t *
     int32_t *idx = reinterpret_cast<int32_t *>(w);
     float *y = reinterpret_cast<float *>(w + align256(size_t(n) * 4));
     float *z = reinterpret_cast<float *>(w + align256(size_t(n) * 4) + align256(size_t(n) * MLP_OUT * 4));
+    void *part = w + align256(size_t(n) * 4) + align256(size_t(n) * MLP_OUT * 4) +
+                 align256(size_t(MLP_NL - 1) * n * MLP_H * 4);
     int rc = mlp_batch(n_rows, n, seed, uint64_t(step), idx, st);
     if (rc == BZ_OK) rc = mlp_forward(wb, params, x, idx, n, y, z, st);
-    if (rc == BZ_OK) rc = mlp_backward(wt, x, t, wcol, idx, n, y, z, grad, loss, st);
+    if (rc == BZ_OK)
+        rc = mlp_backward(wt, x, t, wcol, idx, n, y, z, grad, loss, g_mlp_path == 2 ? part : nullptr,
+                          mlp_bwd_ws(n), st);
     if (rc == BZ_OK) rc = mlp_adam(params, grad, m, v, wb, wt, step, lr, beta1, beta2, eps, weight_decay, st);
     return rc;
 }

@@ -395,9 +395,13 @@ def mlp_forward(wb, prm, x, y, idx=None, z=None):
     call("bz_mlp_forward", _ptr(wb), _ptr(prm), _ptr(x), _ptr(idx), int(y.shape[0]), _ptr(y), _ptr(z), _stream())
 
 
-def mlp_backward(wb, wt, prm, x, t, wcol, y, z, grad, loss, idx=None):
-    call("bz_mlp_backward", _ptr(wb), _ptr(wt), _ptr(prm), _ptr(x), _ptr(t), _ptr(wcol), _ptr(idx), int(y.shape[0]),
-         _ptr(y), _ptr(z), _ptr(grad), _ptr(loss), _stream())
+def mlp_backward(wb, wt, prm, x, t, wcol, y, z, grad, loss, idx=None, ws: "Workspace" = None):
+    """Loss and its gradient (added to grad). With a workspace the tcgen05 backward runs
+    (deterministic per-CTA partial sums); without one the mma.sync backward (atomics)."""
+    n = int(y.shape[0])
+    w = None if ws is None else ws.get("mlp_bwd", _lib.load().bz_mlp_backward_workspace(n))
+    call("bz_mlp_backward", _ptr(wb), _ptr(wt), _ptr(prm), _ptr(x), _ptr(t), _ptr(wcol), _ptr(idx), n, _ptr(y),
+         _ptr(z), _ptr(grad), _ptr(loss), _ptr(w), 0 if w is None else w.numel(), _stream())
 
 
 def mlp_adam(prm, grad, m, v, wb, wt, step, lr, beta1=0.9, beta2=0.999, eps=1e-8, weight_decay=0.0):

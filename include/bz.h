@@ -361,8 +361,10 @@ int bz_push_collide_f32_noalloc(const bz_params *p, bz_particles_f32 in, const i
 #define BZ_MLP_LAYERS 5
 #define BZ_MLP_NPARAM 62032 /* 16*128+128 + 3*(128*128+128) + 128*80+80 */
 int32_t bz_mlp_param_count(void);
-/* forward kernel of bz_mlp_forward / bz_mlp_train_step: 0 = warp-level mma.sync
- * (m16n8k16), 1 = tcgen05.mma with a TMEM accumulator (one CTA per 128 rows, default) */
+/* kernels of bz_mlp_forward / bz_mlp_train_step: 0 = warp-level mma.sync (m16n8k16)
+ * throughout; 1 = forward on tcgen05.mma with a TMEM accumulator (one CTA per 128 rows),
+ * backward on mma.sync (default: the faster training step); 2 = forward and backward on
+ * tcgen05 (deterministic gradients) */
 int bz_mlp_select(int32_t path);
 int32_t bz_mlp_selected(void);
 /* device-side conditions of the network kernels since the last call (BZ_DEV_LOOKBACK: a
@@ -375,10 +377,15 @@ int bz_mlp_sync(const float *params, uint16_t *wb, uint16_t *wt, void *stream);
 int bz_mlp_forward(const uint16_t *wb, const float *params, const float *x, const int32_t *idx, int32_t n,
                    float *y, float *z, void *stream);
 /* loss = sum_r sum_c wcol[c] (y - t[idx[r]])^2 / (2 n) added to *loss; its gradient with
- * respect to every parameter added to grad (FP32, BZ_MLP_NPARAM) */
+ * respect to every parameter added to grad (FP32, BZ_MLP_NPARAM). With a workspace of
+ * bz_mlp_backward_workspace(n) bytes the products run on tcgen05 and every CTA writes its
+ * own partial gradient, summed in a fixed order (deterministic); without one (NULL), on
+ * mma.sync with FP32 atomics. */
+size_t bz_mlp_backward_workspace(int32_t n);
 int bz_mlp_backward(const uint16_t *wb, const uint16_t *wt, const float *params, const float *x,
                     const float *t, const float *wcol, const int32_t *idx, int32_t n, const float *y,
-                    const float *z, float *grad, float *loss, void *stream);
+                    const float *z, float *grad, float *loss, void *workspace, size_t workspace_bytes,
+                    void *stream);
 /* one Adam step (Kingma & Ba 2015) with bias correction for step `step` (1-based) and
  * decoupled weight decay on the weights; clears grad and refreshes wb/wt */
 int bz_mlp_adam(float *params, float *grad, float *m, float *v, uint16_t *wb, uint16_t *wt, int64_t step,
