@@ -98,6 +98,9 @@ _PROTOS = {
                                      _vp, _vp, _vp, _vp, _vp, _vp]),
     "bz_poisson": (ctypes.c_int, [_i32, _f64, _f64, _f64, _f64, _f64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "bz_advance_clock": (ctypes.c_int, [_vp, _vp, _f64, _vp]),
+    "bz_field_step_coop_workspace": (_sz, [_i32]),
+    "bz_field_step_coop": (ctypes.c_int, [_i32, _f64, _f64, _f64, _f64, _f64, _f64, _f64, _vp, _vp, _vp, _vp, _vp, _vp,
+                                          _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "bz_seg_push_workspace": (_sz, []),
     "bz_seg_push_shapes": (ctypes.c_int32, []),
     "bz_seg_push_shape_info": (ctypes.c_int, [ctypes.c_int32, _vp, _vp, _vp, _vp]),

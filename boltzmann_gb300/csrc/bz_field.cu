@@ -2,6 +2,8 @@
 // diffusion and Poisson solve, all float64, so that a CCP step needs no host round trip.
 // This file is compiled without FMA contraction so the float64 operation order of the
 // reference's numba code (EF_kernel_1D.py, heavies_kernel_1D.py) is kept.
+#include <cooperative_groups.h>
+
 #include "bz_common.cuh"
 
 namespace bz {
@@ -213,6 +215,113 @@ __global__ void __launch_bounds__(PS_T) k_field_step(int N, double dx, double dt
     poisson_body(N, dx, eps0, V0, freq, 0.0, t_dev, mom, ni, plan, V, E, E32, E, S);
 }
 
+// The same grid step spread over G CTAs (one cooperative launch, phases separated by
+// grid-wide barriers): float64 throughput is per SM on this part, and one CTA spent most of
+// its time waiting on its SM's narrow float64 pipe. CTA b owns Poisson rows
+// [b*FM_T, (b+1)*FM_T); each substitution is a CTA-local scan plus the sum of the other
+// CTAs' totals (in CTA order), so the result equals the one-CTA kernel's up to the
+// association of the float64 sums.
+constexpr int FM_T = 64;
+
+__device__ double cta64_inclusive_sum(double v, double *sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        double t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    if (lane == 31) sh[warp] = v;
+    __syncthreads();
+    if (warp == 1) v += sh[0];
+    __syncthreads();
+    return v;
+}
+
+__global__ void __launch_bounds__(FM_T) k_field_step_mc(int N, double dx, double dt, double mu_i, double D_i,
+                                                        double eps0, double V0, double freq, const double *mom,
+                                                        double *ni, double *Te, double *g2, double *t_dev,
+                                                        uint64_t *step_dev, const double *plan, double *V, double *E,
+                                                        float *E32, double *Ji, int32_t *brk, double *tot,
+                                                        int32_t *flag) {
+    cooperative_groups::grid_group grid = cooperative_groups::this_grid();
+    __shared__ double sh[2];
+    __shared__ double s_vs;
+    __shared__ double s_c[FM_T];
+    const int G = gridDim.x, b = blockIdx.x, t = threadIdx.x;
+    const int gt = b * FM_T + t, GT = G * FM_T;
+    const int nn = N + 1, n = N - 1;
+    const double tnew = *t_dev + dt;  // every thread reads the clock before it is advanced
+    // grid update (boltzmann.py:643-647)
+    grid_update_body(nn, mom, ni, Te, g2, gt, GT);
+    if (gt == 0) *flag = 0;
+    grid.sync();
+    if (gt == 0) {
+        *t_dev = tnew;
+        if (step_dev) *step_dev = *step_dev + 1;
+    }
+    // ion fluid (heavies_kernel_1D.py:4-64): fluxes with the boundary densities formed where
+    // they are needed, then the interior, then the boundaries again
+    const double e0 = fmax(E[0], 0.0), eN = fmin(E[N - 1], 0.0);
+    for (int i = gt; i < N; i += GT) {
+        const double a = (i == 0) ? ni[1] * ((D_i / dx - 0.5 * mu_i * e0) / (D_i / dx + 0.5 * mu_i * e0)) : ni[i];
+        const double c = (i + 1 == N) ? ni[N - 1] * ((D_i / dx + 0.5 * mu_i * eN) / (D_i / dx - 0.5 * mu_i * eN))
+                                      : ni[i + 1];
+        Ji[i] = (mu_i * (0.5 * (a + c)) * E[i] - D_i * (c - a) / dx);
+    }
+    grid.sync();
+    int bf = 0;
+    for (int i = 1 + gt; i < N; i += GT) {
+        double r = ni[i] - dt * (Ji[i] - Ji[i - 1]) / dx;
+        if (r < 0 && ni[i] > 0) bf = 1;
+        ni[i] = r;
+    }
+    if (bf) atomicOr(flag, 1);
+    if (t == 0) s_vs = V0 * sin(2 * 3.141592653589793 * freq * tnew);
+    grid.sync();
+    if (gt == 0) {
+        ni[0] = ni[1] * ((D_i / dx - 0.5 * mu_i * e0) / (D_i / dx + 0.5 * mu_i * e0));
+        ni[N] = ni[N - 1] * ((D_i / dx + 0.5 * mu_i * eN) / (D_i / dx - 0.5 * mu_i * eN));
+        if (brk) *brk = *flag;
+    }
+    const double vs = s_vs;
+    const double *P = plan, *g = plan + n, *Q = plan + 2 * n, *h = plan + 3 * n;
+    const double *ne = mom;
+    // forward substitution: y_i = P_i sum_{k<=i} r_k g_k (EF_kernel_1D.py:26-42)
+    const int i = b * FM_T + t;
+    double c = 0.0;
+    if (i < n) {
+        double r = (1.0 / eps0) * (ni[i + 1] - ne[i + 1]);
+        if (i == 0) r = r + (1.0 / (dx * dx)) * vs;
+        c = r * g[i];
+    }
+    const double sf = cta64_inclusive_sum(c, sh);
+    if (t == FM_T - 1) tot[b] = sf;
+    grid.sync();
+    double carry = 0.0;
+    for (int k = 0; k < b; ++k) carry += tot[k];
+    const double y = (i < n) ? P[i] * (sf + carry) : 0.0;
+    // backward: V_i = Q_i sum_{k>=i} y_k h_k, the CTA's rows scanned from the end
+    s_c[t] = (i < n) ? y * h[i] : 0.0;
+    __syncthreads();
+    const int tr = FM_T - 1 - t, ir = b * FM_T + tr;  // this thread's row in the backward scan
+    const double sb = cta64_inclusive_sum(s_c[tr], sh);
+    if (t == FM_T - 1) tot[G + b] = sb;
+    grid.sync();
+    double carry_b = 0.0;
+    for (int k = G - 1; k > b; --k) carry_b += tot[G + k];
+    if (ir < n) V[ir] = Q[ir] * (sb + carry_b);
+    grid.sync();
+    // faces (EF_kernel_1D.py:39-42)
+    for (int f = gt; f < N; f += GT) {
+        double e;
+        if (f == 0) e = -(V[0] - vs) / dx;
+        else if (f == N - 1) e = -(0 - V[N - 2]) / dx;
+        else e = -(V[f] - V[f - 1]) / dx;
+        E[f] = e;
+        if (E32) E32[f] = float(e);
+    }
+}
+
 __global__ void k_advance_clock(double *t, uint64_t *step, double dt) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         if (t) *t = *t + dt;
@@ -257,6 +366,32 @@ int bz_field_step(int32_t N, double dx, double dt, double mu_i, double D_i, doub
     bz::k_field_step<<<1, bz::PS_T, 0, bz::as_stream(stream)>>>(N, dx, dt, mu_i, D_i, eps0, V0, freq, moments, ni,
                                                                  Te, g2, t_dev, step_dev, plan, V, E, E32, Ji, brk);
     return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+}
+size_t bz_field_step_coop_workspace(int32_t N) {
+    if (N < 3) return 0;
+    const int G = int(bz::ceil_div(N - 1, bz::FM_T));
+    return size_t(2 * G + 2) * sizeof(double);
+}
+int bz_field_step_coop(int32_t N, double dx, double dt, double mu_i, double D_i, double eps0, double V0, double freq,
+                       const double *moments, double *ni, double *Te, double *g2, double *t_dev, uint64_t *step_dev,
+                       const double *plan, double *V, double *E, float *E32, double *Ji, int32_t *brk,
+                       void *workspace, size_t workspace_bytes, void *stream) {
+    if (N < 3 || !moments || !ni || !t_dev || !plan || !V || !E || !Ji || !workspace) return BZ_ERR_ARG;
+    if (workspace_bytes < bz_field_step_coop_workspace(N)) return BZ_ERR_WORKSPACE;
+    int G = int(bz::ceil_div(N - 1, bz::FM_T));
+    int dev = 0, per_sm = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bz::k_field_step_mc, bz::FM_T, 0) != cudaSuccess ||
+        G > per_sm * sms)
+        return BZ_ERR_TOO_LARGE;  // every CTA must be resident for the grid-wide barriers
+    double *tot = static_cast<double *>(workspace);
+    int32_t *flag = reinterpret_cast<int32_t *>(tot + 2 * G);
+    void *args[] = {&N, &dx, &dt, &mu_i, &D_i, &eps0, &V0, &freq, (void *)&moments, &ni, &Te, &g2, &t_dev,
+                    &step_dev, (void *)&plan, &V, &E, &E32, &Ji, &brk, &tot, &flag};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)bz::k_field_step_mc, dim3(G), dim3(bz::FM_T), args, 0,
+                                                bz::as_stream(stream));
+    return e == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
 }
 int bz_advance_clock(double *t_dev, uint64_t *step_dev, double dt, void *stream) {
     if (!t_dev && !step_dev) return BZ_ERR_ARG;

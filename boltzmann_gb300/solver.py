@@ -203,16 +203,17 @@ class BoltzmannGB300:
             self.E_push.copy_(self.E)
 
     def _grid_solves(self, advance=True):
-        """Grid update, clock, ion fluid and Poisson (boltzmann.py:643-678) in one launch;
-        the first solve (advance=False) is the Poisson alone."""
+        """Grid update, clock, ion fluid and Poisson (boltzmann.py:643-678) in one
+        cooperative launch over ceil((N-1)/64) CTAs; the first solve (advance=False) is the
+        Poisson alone."""
         cfg = self.cfg
         if not advance:
             self.EF_kernel()
             return
         f32 = self.dtype == torch.float32
-        K.field_step(self.N, cfg.dx, cfg.dt, cfg.mu_i, cfg.D_i, cfg.eps0, cfg.V0, cfg.freq, self.moments, self.ni,
-                     self.Te, self.g2, self.t, self.step_dev, self.poisson_plan, self.V, self.E,
-                     self.E_push if f32 else None, self.Ji, self.brk)
+        K.field_step_coop(self.N, cfg.dx, cfg.dt, cfg.mu_i, cfg.D_i, cfg.eps0, cfg.V0, cfg.freq, self.moments,
+                          self.ni, self.Te, self.g2, self.t, self.step_dev, self.poisson_plan, self.V, self.E,
+                          self.E_push if f32 else None, self.Ji, self.brk, ws=self.ws)
         if not f32:
             self.E_push.copy_(self.E)
 
@@ -314,6 +315,7 @@ class BoltzmannGB300:
         nkeys = self.nnodes * self.nb
         self.ws.get("seg_push", lib.bz_seg_push_workspace())
         self.ws.get("seg_rebalance", lib.bz_seg_repack_workspace(self.A.nseg))
+        self.ws.get("field_coop", lib.bz_field_step_coop_workspace(self.N))
         if resample:
             self.ws.get("seg_bin", lib.bz_seg_bin_workspace(self.A.nseg, self.A.capacity))
             self.ws.get("seg_resample", lib.bz_seg_resample_workspace(self.A.nseg, self.A.capacity, nkeys))

@@ -100,3 +100,44 @@ def test_fused_field_step_equals_the_four_kernels():
         out.append([a.cpu().numpy() for a in (ni, Te, t, step, V, E, E32, Ji)])
     for a, b in zip(*out):
         np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("N", [None, 130, 1024, 4096])
+def test_cooperative_field_step_equals_the_one_cta_kernel(N):
+    """bz_field_step_coop (the float64 work over ceil((N-1)/64) CTAs) against bz_field_step:
+    the densities, the clock and the ion fluxes bit for bit, the Poisson solution to the
+    association of its float64 sums."""
+    g = np.load(os.path.join(G, "field.npz"))
+    N = int(g["N"]) if N is None else N
+    dx, dev = 2.54 / N if N != int(g["N"]) else float(g["dx"]), "cuda"
+    rng = np.random.default_rng(N)
+    nn = N + 1
+    d = torch.zeros(N - 1, dtype=torch.float64, device=dev)
+    l = torch.zeros(N - 1, dtype=torch.float64, device=dev)
+    plan = torch.zeros(4 * (N - 1), dtype=torch.float64, device=dev)
+    K.poisson_factor(N, dx, d, l, plan)
+    mom = torch.as_tensor(np.abs(rng.normal(1e9, 1e8, (4, nn))), device=dev)
+    ni0 = torch.as_tensor(np.abs(rng.normal(1e9, 2e8, nn)), device=dev)
+    E0 = torch.as_tensor(rng.normal(0, 50, N), device=dev)
+    out = []
+    for coop in (False, True):
+        ni, E = ni0.clone(), E0.clone()
+        Te = torch.zeros(nn, dtype=torch.float64, device=dev)
+        g2 = torch.zeros(nn, dtype=torch.float64, device=dev)
+        t = torch.full((1,), 1.23e-8, dtype=torch.float64, device=dev)
+        step = torch.zeros(1, dtype=torch.int64, device=dev)
+        V = torch.zeros(N - 1, dtype=torch.float64, device=dev)
+        E32 = torch.zeros(N, dtype=torch.float32, device=dev)
+        Ji = torch.zeros(N, dtype=torch.float64, device=dev)
+        brk = torch.zeros(1, dtype=torch.int32, device=dev)
+        args = (N, dx, float(g["dt"]), float(g["mu_i"]), float(g["D_i"]), float(g["eps0"]), float(g["V0"]),
+                float(g["freq"]), mom, ni, Te, g2, t, step, plan, V, E, E32, Ji, brk)
+        (K.field_step_coop if coop else K.field_step)(*args)
+        torch.cuda.synchronize()
+        out.append({k: a.cpu().numpy() for k, a in zip(("ni", "Te", "g2", "t", "step", "V", "E", "E32", "Ji", "brk"),
+                                                       (ni, Te, g2, t, step, V, E, E32, Ji, brk))})
+    a, b = out
+    for k in ("ni", "Te", "g2", "t", "step", "Ji", "brk"):
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    for k in ("V", "E"):
+        np.testing.assert_allclose(b[k], a[k], rtol=1e-11, atol=1e-11 * np.abs(a[k]).max(), err_msg=k)
