@@ -13,8 +13,8 @@ the hybrid CCP that the benchmark asks for, built on the same kernels:
   (csrc/bz_mlp.cu), one C call per training step;
 * the start-up: ``learned_start`` evaluates the network for every key (swarm or deposit
   node) and redraws the particles' velocities from the predicted distribution
-  (``bz_seg_sample_energy``); the plain PIC-MCC run then continues from there and is the
-  judge of the surrogate.
+  (``bz_seg_sample_energy``); the plain PIC-MCC run then continues from there and
+  checks the surrogate.
 
 Features (9 of BZ_MLP_IN = 16, the rest zero):
   0: log10(E/N in Td) / 3          1: log10(mean energy in eV) / 2

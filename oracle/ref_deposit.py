@@ -10,8 +10,8 @@ reduction/__init__.py:12-16).
 
 ``build()`` compiles that file, where it lies in the reference tree, for sm_103a into
 ``oracle/_ref/kernels_new.sm_103a.cubin`` (device code only; its pybind11 wrapper is not
-used), when the reference tree is present. The cubin travels with the repository to the
-GPU machine. ``ReferenceDeposit`` loads it into the current CUDA context through the driver API
+used), when the reference tree is present; the cubin is kept with the repository copy, so
+machines without the reference sources run it too. ``ReferenceDeposit`` loads it into the current CUDA context through the driver API
 (ctypes on libcuda) and launches the two kernels exactly as ``calls`` does, on float64
 device buffers in the reference's layout: v [ptcl][4] (w, w*ionflag, w*0, w*energy) and the
 normalised positions (x + dx/2)/(L + dx).

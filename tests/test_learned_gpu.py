@@ -2,7 +2,7 @@
 library's own BF16 training kernels) proposes each swarm's steady-state energy
 distribution; swarms started from it reach their steady mean energy (within 2%) in a
 fraction of the steps the plain 1 eV start needs. Held-out reduced fields, same seeds and
-particle counts for both starts; the plain run judges the steady state."""
+particle counts for both starts; the plain run defines the steady state."""
 import math
 
 import numpy as np

@@ -1,7 +1,7 @@
 """GPU parity of the 0-D swarm ensemble (BZ_ADVECT_ENSEMBLE: x holds the swarm index).
 
 The push, binning, per-(swarm, bin) resampling and the energy distribution are checked
-against the oracle's ensemble mode on the same inputs; the driver is checked for graph
+against the oracle's ensemble mode on the same inputs; SwarmEnsemble is checked for graph
 replay = eager stepping, for its bookkeeping, and statistically against an ensemble of
 independent oracle swarms (mean energy, ionization rate coefficient and energy
 distribution).
