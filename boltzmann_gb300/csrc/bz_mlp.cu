@@ -688,6 +688,17 @@ __device__ __forceinline__ void put_canon(unsigned char *base, int r, int k, int
         __float2bfloat16_rn(v);
 }
 
+// Transposed writes in pairs: lanes 2m and 2m+1 hold rows r and r+1 (adjacent in the
+// transposed matrix's K), so for the columns c, c+1 one shuffle lets the even lane write
+// (row c: r, r+1) and the odd lane (row c+1: r, r+1) as one 32-bit word each
+__device__ __forceinline__ void put_canon_t2(unsigned char *base, int rl, int c, int K, float vc, float vc1) {
+    const bool odd = rl & 1;
+    const float recv = __shfl_xor_sync(0xffffffffu, odd ? vc : vc1, 1);
+    const int row = odd ? c + 1 : c, k = rl & ~1;
+    const uint32_t w = odd ? pack_bf16(recv, vc1) : pack_bf16(vc, recv);
+    *reinterpret_cast<uint32_t *>(base + (row >> 3) * (16 * K) + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2) = w;
+}
+
 // 16 values (columns c0 .. c0+15 of row rl) as two 16-byte chunks of a canonical K-major
 // matrix with C columns
 __device__ __forceinline__ void put_row16(unsigned char *base, int rl, int c0, int C, const float *v) {
@@ -720,14 +731,12 @@ __device__ __forceinline__ void tcb_put_at(unsigned char *at, int rl, int half, 
             v = *reinterpret_cast<const float4 *>(src + c_lo + c);
             if (L > 0) { v.x = gelu(v.x); v.y = gelu(v.y); v.z = gelu(v.z); v.w = gelu(v.w); }
         }
-        put_canon(at, c_lo + c + 0, rl, TC_ROWS, v.x);
-        put_canon(at, c_lo + c + 1, rl, TC_ROWS, v.y);
-        put_canon(at, c_lo + c + 2, rl, TC_ROWS, v.z);
-        put_canon(at, c_lo + c + 3, rl, TC_ROWS, v.w);
+        put_canon_t2(at, rl, c_lo + c + 0, TC_ROWS, v.x, v.y);
+        put_canon_t2(at, rl, c_lo + c + 2, TC_ROWS, v.z, v.w);
     }
     if (half) {  // the ones row (bias gradient) and 15 zero rows
 #pragma unroll
-        for (int j = 0; j < 16; ++j) put_canon(at, NI + j, rl, TC_ROWS, (j == 0 && r < n) ? 1.f : 0.f);
+        for (int j = 0; j < 16; j += 2) put_canon_t2(at, rl, NI + j, TC_ROWS, (j == 0 && r < n) ? 1.f : 0.f, 0.f);
     }
 }
 
@@ -749,11 +758,11 @@ __device__ __forceinline__ bool tcb_layer(unsigned char *wtc, unsigned char *dz,
                 const int c0 = (lo + j) * 16;
                 put_row16(dz, rl, c0, NO, d + 16 * j);
 #pragma unroll
-                for (int c = 0; c < 16; ++c) put_canon(dzt, c0 + c, rl, TC_ROWS, d[16 * j + c]);
+                for (int c = 0; c < 16; c += 2) put_canon_t2(dzt, rl, c0 + c, TC_ROWS, d[16 * j + c], d[16 * j + c + 1]);
             }
         }
         if (NO < 128 && half)  // zero rows of the padded dZ^T
-            for (int o = NO; o < 128; ++o) put_canon(dzt, o, rl, TC_ROWS, 0.f);
+            for (int o = NO; o < 128; o += 2) put_canon_t2(dzt, rl, o, TC_ROWS, 0.f, 0.f);
     }
     tcb_put_at<L>(at, rl, half, row0, n, x, idx, z);
     fence_async_smem();
