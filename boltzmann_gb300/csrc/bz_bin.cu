@@ -163,18 +163,31 @@ __global__ void __launch_bounds__(1024) k_radix_scan(uint32_t *hist, const int32
 }
 
 // Stable scatter by the digit at ``shift``. vals_in == nullptr means identity values.
+// The tile is first sorted by digit in shared memory (each warp ranks its contiguous run
+// with __match_any_sync), then written out digit run by digit run, so that consecutive
+// threads write consecutive addresses (runs of ~tile/256 items) instead of scattering
+// every item to its own sector.
+constexpr size_t RB_SCATTER_SMEM = sizeof(uint32_t) * (RB_W * RADIX + 2 * RADIX) + RB_TILE * (2 + 4);
+
 __global__ void __launch_bounds__(RB_T) k_radix_scatter(const uint16_t *keys_in, const uint32_t *vals_in,
                                                         const int32_t *n_ptr, int64_t cap, int shift,
                                                         const uint32_t *offsets, uint16_t *keys_out,
                                                         uint32_t *vals_out) {
-    __shared__ uint32_t cnt[RB_W][RADIX];
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint32_t (*cnt)[RADIX] = reinterpret_cast<uint32_t (*)[RADIX]>(smem);
+    uint32_t *lbase = reinterpret_cast<uint32_t *>(smem) + RB_W * RADIX;  // tile-local start of each digit
+    uint32_t *gshift = lbase + RADIX;                                      // global start - local start
+    uint32_t *v_s = gshift + RADIX;
+    uint16_t *k_s = reinterpret_cast<uint16_t *>(v_s + RB_TILE);
     const int n = int(min(int64_t(max(*n_ptr, 0)), cap));
     const int ntiles = int(ceil_div(n, RB_TILE));
     if (int(blockIdx.x) >= ntiles) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int i = threadIdx.x; i < RB_W * RADIX; i += RB_T) (&cnt[0][0])[i] = 0;
     __syncthreads();
-    const int64_t seg0 = int64_t(blockIdx.x) * RB_TILE + int64_t(warp) * RB_SEG;
+    const int64_t tile0 = int64_t(blockIdx.x) * RB_TILE;
+    const int tile_n = int(min(int64_t(RB_TILE), int64_t(n) - tile0));
+    const int64_t seg0 = tile0 + int64_t(warp) * RB_SEG;
     uint16_t k[RB_I];
     uint32_t v[RB_I];
     const unsigned lt_mask = (1u << lane) - 1u;
@@ -193,9 +206,28 @@ __global__ void __launch_bounds__(RB_T) k_radix_scatter(const uint16_t *keys_in,
         __syncwarp();
     }
     __syncthreads();
-    // exclusive over warps per digit, plus the tile's global offset
+    // per digit: the tile's total, its local start (exclusive scan over digits, one warp),
+    // and the warps' local starts
+    if (warp == 0) {
+        uint32_t carry = 0;
+        for (int d0 = 0; d0 < RADIX; d0 += 32) {
+            const int dg = d0 + lane;
+            uint32_t tot = 0;
+            for (int ww = 0; ww < RB_W; ++ww) tot += cnt[ww][dg];
+            uint32_t incl = tot;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            lbase[dg] = carry + incl - tot;
+            carry += __shfl_sync(0xffffffffu, incl, 31);
+        }
+    }
+    __syncthreads();
     for (int dg = threadIdx.x; dg < RADIX; dg += RB_T) {
-        uint32_t run = offsets[size_t(blockIdx.x) * RADIX + dg];
+        uint32_t run = lbase[dg];
+        gshift[dg] = offsets[size_t(blockIdx.x) * RADIX + dg] - run;
         for (int ww = 0; ww < RB_W; ++ww) {
             uint32_t t = cnt[ww][dg];
             cnt[ww][dg] = run;
@@ -203,6 +235,7 @@ __global__ void __launch_bounds__(RB_T) k_radix_scatter(const uint16_t *keys_in,
         }
     }
     __syncthreads();
+    // the tile sorted by digit, in shared memory
 #pragma unroll
     for (int r = 0; r < RB_I; ++r) {
         int64_t i = seg0 + r * 32 + lane;
@@ -212,13 +245,27 @@ __global__ void __launch_bounds__(RB_T) k_radix_scatter(const uint16_t *keys_in,
             int dg = (k[r] >> shift) & 0xff;
             unsigned peers = __match_any_sync(act, dg);
             uint32_t pos = cnt[warp][dg] + __popc(peers & lt_mask);
-            keys_out[pos] = k[r];
-            vals_out[pos] = v[r];
+            k_s[pos] = k[r];
+            v_s[pos] = v[r];
             __syncwarp(act);
             if (lane == __ffs(peers) - 1) cnt[warp][dg] += __popc(peers);
         }
         __syncwarp();
     }
+    __syncthreads();
+    // out, in tile order: each digit's run lands contiguously at its global position
+    for (int p = threadIdx.x; p < tile_n; p += RB_T) {
+        const uint16_t key = k_s[p];
+        const uint32_t g = gshift[(key >> shift) & 0xff] + uint32_t(p);
+        keys_out[g] = key;
+        vals_out[g] = v_s[p];
+    }
+}
+
+// the scatter's dynamic shared memory is above the default 48 KB limit
+static bool scatter_smem_ok() {
+    return cudaFuncSetAttribute(k_radix_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(RB_SCATTER_SMEM)) == cudaSuccess;
 }
 
 // offsets[k] = exclusive scan of counts[0..nkeys), offsets[nkeys] = live total.
@@ -285,13 +332,14 @@ static int bin_entry(const bz_params *pp, P s, const int32_t *n, int64_t cap, in
                                  nkeys, status);
     const bool two = nkeys >= RADIX;  // invalid key = nkeys must be ordered too
     k_radix_scan<<<1, 1024, 0, st>>>(hist, n, cap);
-    k_radix_scatter<<<grid, RB_T, 0, st>>>(keys_a, nullptr, n, cap, 0, hist, keys_b,
-                                           two ? vals_a : reinterpret_cast<uint32_t *>(perm));
+    if (!scatter_smem_ok()) return BZ_ERR_UNSUPPORTED;
+    k_radix_scatter<<<grid, RB_T, RB_SCATTER_SMEM, st>>>(keys_a, nullptr, n, cap, 0, hist, keys_b,
+                                                         two ? vals_a : reinterpret_cast<uint32_t *>(perm));
     if (two) {
         k_radix_hist<<<grid, RB_T, 0, st>>>(keys_b, n, cap, 8, hist);
         k_radix_scan<<<1, 1024, 0, st>>>(hist, n, cap);
-        k_radix_scatter<<<grid, RB_T, 0, st>>>(keys_b, vals_a, n, cap, 8, hist, keys_a,
-                                               reinterpret_cast<uint32_t *>(perm));
+        k_radix_scatter<<<grid, RB_T, RB_SCATTER_SMEM, st>>>(keys_b, vals_a, n, cap, 8, hist, keys_a,
+                                                             reinterpret_cast<uint32_t *>(perm));
     }
     k_key_offsets<<<1, 1024, 0, st>>>(counts, nkeys, offsets);
     return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
@@ -424,13 +472,14 @@ static int seg_bin_entry(const bz_params *pp, S s, int nb, const double *edges, 
     const bool two = nkeys >= RADIX;
     k_radix_hist<<<grid, RB_T, 0, st>>>(keys_a, n, cap, 0, hist);
     k_radix_scan<<<1, 1024, 0, st>>>(hist, n, cap);
-    k_radix_scatter<<<grid, RB_T, 0, st>>>(keys_a, slots, n, cap, 0, hist, keys_b,
-                                           two ? vals_a : reinterpret_cast<uint32_t *>(perm));
+    if (!scatter_smem_ok()) return BZ_ERR_UNSUPPORTED;
+    k_radix_scatter<<<grid, RB_T, RB_SCATTER_SMEM, st>>>(keys_a, slots, n, cap, 0, hist, keys_b,
+                                                         two ? vals_a : reinterpret_cast<uint32_t *>(perm));
     if (two) {
         k_radix_hist<<<grid, RB_T, 0, st>>>(keys_b, n, cap, 8, hist);
         k_radix_scan<<<1, 1024, 0, st>>>(hist, n, cap);
-        k_radix_scatter<<<grid, RB_T, 0, st>>>(keys_b, vals_a, n, cap, 8, hist, keys_a,
-                                               reinterpret_cast<uint32_t *>(perm));
+        k_radix_scatter<<<grid, RB_T, RB_SCATTER_SMEM, st>>>(keys_b, vals_a, n, cap, 8, hist, keys_a,
+                                                             reinterpret_cast<uint32_t *>(perm));
     }
     k_key_offsets<<<1, 1024, 0, st>>>(counts, nkeys, offsets);
     return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
