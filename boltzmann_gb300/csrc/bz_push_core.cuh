@@ -68,6 +68,8 @@ template <typename T> struct PushConst {
     T dt, e_exc;    // dt and the excitation threshold in the working precision
     NodeMap nm;     // deposit node map
     uint32_t rk0[10], rk1[10];  // Philox round keys of the seed
+    float efac_h, efac_l;       // 0.5 m_e j_ev as an unevaluated sum of two floats
+    float exc_h, exc_l, ion_h, ion_l;  // the excitation and ionization thresholds, likewise
     T wall_lo, wall_hi;         // L*1e-3, L*(1-1e-3): closer to a wall the float64 test decides
     float xs_last;              // xs_n - 1 (float), the table's last index
     int xs_imax, face_max;      // xs_n - 2, n_faces - 1
@@ -90,6 +92,26 @@ __device__ __forceinline__ void iso_dir(Uni<T> a, Uni<T> b, T vn, T &vx, T &vy, 
     vx = vn * sc * cp;
     vy = vn * sc * sp;
     vz = vn * cc;
+}
+
+// e - thr for a float32 relative velocity (ax, ay, az) without the cancellation of a float
+// subtraction: the squared speed and the energy as unevaluated sums of two floats (exact
+// products by fma and exact sums, Dekker 1971 / Knuth TAOCP 4.2.2), then the threshold's
+// high part subtracted exactly (both within a factor of two: Sterbenz). Absolute error
+// about 1e-14 e. The rounded operations are spelled out so that none is contracted.
+__device__ __forceinline__ float excess_energy_f(float ax, float ay, float az, float efh, float efl, float th,
+                                                 float tl) {
+    const float p1 = __fmul_rn(ax, ax), e1 = fmaf(ax, ax, -p1);
+    const float p2 = __fmul_rn(ay, ay), e2 = fmaf(ay, ay, -p2);
+    const float p3 = __fmul_rn(az, az), e3 = fmaf(az, az, -p3);
+    const float s1 = __fadd_rn(p1, p2), b1 = __fsub_rn(s1, p1);
+    const float t1 = __fadd_rn(__fsub_rn(p1, __fsub_rn(s1, b1)), __fsub_rn(p2, b1));
+    const float s2 = __fadd_rn(s1, p3), b2 = __fsub_rn(s2, s1);
+    const float t2 = __fadd_rn(__fsub_rn(s1, __fsub_rn(s2, b2)), __fsub_rn(p3, b2));
+    const float vh = s2, vl = __fadd_rn(__fadd_rn(__fadd_rn(t1, t2), __fadd_rn(e1, e2)), e3);
+    const float eh = __fmul_rn(efh, vh);
+    const float el = __fadd_rn(fmaf(efh, vh, -eh), fmaf(efh, vl, __fmul_rn(efl, vh)));
+    return __fadd_rn(__fsub_rn(eh, th), __fsub_rn(el, tl));
 }
 
 // 1 - exp(-x), x >= 0. float: the hardware exponential, absolute error ~2e-7 (the
@@ -232,17 +254,20 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
             vn = vmag * k.f_el;
         } else {
             // energy left after the threshold: in the working precision when e - threshold
-            // keeps at least a quarter of e, else in float64 (the subtraction cancels);
+            // keeps at least a quarter of e, else without the subtraction's cancellation
+            // (float32: two-float arithmetic; float64: the float64 expression);
             // excitation loses e_exc (the reference has no excitation: sigma_g1 = 0),
             // ionization shares e - 15.76 equally (electron_kernel_numba.py:211-255)
             const double thr = (proc == P_EXCITE) ? p.e_exc : E_ION;
             if (sizeof(T) == 8 || e - T(thr) >= T(0.25) * e) {
                 T en = (proc == P_EXCITE) ? (e - T(thr)) : T(0.5) * (e - T(thr));
                 vn = sqrt_pos(en * k.e2v);
-            } else {
-                double ed = k.efac_d * (double(ax) * double(ax) + double(ay) * double(ay) + double(az) * double(az));
-                double en = (proc == P_EXCITE) ? fabs(ed - thr) : fabs(0.5 * (ed - thr));
-                vn = T(sqrt(en * k.e2v_d));
+            } else if constexpr (sizeof(T) == 4) {
+                const bool ex = proc == P_EXCITE;
+                float d = fabsf(excess_energy_f(ax, ay, az, k.efac_h, k.efac_l, ex ? k.exc_h : k.ion_h,
+                                                ex ? k.exc_l : k.ion_l));
+                if (!ex) d = 0.5f * d;
+                vn = sqrt_pos(d * k.e2v);
             }
         }
         iso_dir(u1, u2, vn, nvx, nvy, nvz);
@@ -306,6 +331,10 @@ template <typename T> inline PushConst<T> make_push_const(const bz_params &p) {
     k.f_el = T(sqrt(1 - (2 * me / mn)));
     k.e2v = T(2.0 / (jev * me));
     k.e2v_d = 2.0 / (jev * me);
+    auto split = [](double v, float &h, float &l) { h = float(v); l = float(v - double(h)); };
+    split(k.efac_d, k.efac_h, k.efac_l);
+    split(p.e_exc, k.exc_h, k.exc_l);
+    split(E_ION, k.ion_h, k.ion_l);
     k.gas_sigma = T(p.gas_sigma);
     k.L = T(p.L);
     k.inv_dx_f = float(1.0 / p.dx);
