@@ -144,8 +144,8 @@ _PROTOS = {
     "bz_mlp_train_workspace": (_sz, [_i32]),
     "bz_mlp_train_step": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, ctypes.c_uint64,
                                          _i64, _f32, _f32, _f32, _f32, _f32, _vp, _vp, _sz, _vp]),
-    "bz_seg_sample_energy_f32": (ctypes.c_int, [_P, Segments, _i32, _i32, _f64, _f64, _vp, ctypes.c_uint64, _vp]),
-    "bz_seg_sample_energy_f64": (ctypes.c_int, [_P, Segments, _i32, _i32, _f64, _f64, _vp, ctypes.c_uint64, _vp]),
+    "bz_seg_sample_energy_f32": (ctypes.c_int, [_P, Segments, _i32, _i32, _f64, _f64, _vp, _vp, ctypes.c_uint64, _vp]),
+    "bz_seg_sample_energy_f64": (ctypes.c_int, [_P, Segments, _i32, _i32, _f64, _f64, _vp, _vp, ctypes.c_uint64, _vp]),
 }
 
 

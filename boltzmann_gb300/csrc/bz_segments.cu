@@ -649,7 +649,8 @@ static int seg_eedf_entry(const bz_params *pp, S s_, int nbins, double emin, dou
 // bin by inverse CDF, energy log-uniform within the bin, isotropic direction
 template <typename T>
 __global__ void __launch_bounds__(256) k_seg_sample_energy(bz_params p, NodeMap nm, Seg<T> s, int nkeys, int nbins,
-                                                           double lemin, double dle, const double *cdf, Rng g) {
+                                                           double lemin, double dle, const double *cdf,
+                                                           const double *escale, Rng g) {
     const double e2v = 2.0 / (j_ev() * m_e());  // eV -> (m/s)^2
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
@@ -673,7 +674,8 @@ __global__ void __launch_bounds__(256) k_seg_sample_energy(bz_params p, NodeMap 
                     const int m = (lo + hi) >> 1;
                     if (c[m] > ub) hi = m; else lo = m + 1;
                 }
-                const double e = exp(lemin + (double(lo) + uni_d(q.z, q.w).u) * dle);
+                double e = exp(lemin + (double(lo) + uni_d(q.z, q.w).u) * dle);
+                if (escale) e *= escale[key];
                 const double sp = sqrt(e * e2v);
                 const Uni<double> a = uni_d(r.x, r.y), bb = uni_d(r.z, r.w);
                 const double cc = a.u - a.c, sc = 2.0 * sqrt(a.u * a.c);
@@ -689,14 +691,15 @@ __global__ void __launch_bounds__(256) k_seg_sample_energy(bz_params p, NodeMap 
 
 template <typename T, typename S>
 static int seg_sample_energy_entry(const bz_params *pp, S s_, int nkeys, int nbins, double emin, double emax,
-                                   const double *cdf, uint64_t seed, void *stream) {
+                                   const double *cdf, const double *escale, uint64_t seed, void *stream) {
     if (!pp || !cdf || !seg_ok<T>(s_) || nkeys < 1 || nbins < 1 || !(emin > 0) || !(emax > emin)) return BZ_ERR_ARG;
     const bz_params &p = *pp;
     if (p.advect == BZ_ADVECT_1D && (p.dx <= 0 || p.L <= 0 || p.bnf < 1 || p.n_nodes < 1)) return BZ_ERR_ARG;
     const int blocks = std::max(1, std::min(num_sms() * 8, int(ceil_div(s_.nseg, 8))));
     const Rng g{uint32_t(seed), uint32_t(seed >> 32), 0u, 0u};
     k_seg_sample_energy<T><<<blocks, 256, 0, as_stream(stream)>>>(p, make_node_map(p), to_seg<T>(s_), nkeys, nbins,
-                                                                  log(emin), log(emax / emin) / nbins, cdf, g);
+                                                                  log(emin), log(emax / emin) / nbins, cdf, escale,
+                                                                  g);
     return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
 }
 
@@ -789,12 +792,14 @@ int bz_seg_eedf_f64(const bz_params *p, bz_segments_f64 s, int32_t nbins, double
     return bz::seg_eedf_entry<double>(p, s, nbins, emin, emax, hist, stream);
 }
 int bz_seg_sample_energy_f32(const bz_params *p, bz_segments_f32 s, int32_t n_keys, int32_t nbins, double emin,
-                             double emax, const double *cdf, uint64_t seed, void *stream) {
-    return bz::seg_sample_energy_entry<float>(p, s, n_keys, nbins, emin, emax, cdf, seed, stream);
+                             double emax, const double *cdf, const double *energy_scale, uint64_t seed,
+                             void *stream) {
+    return bz::seg_sample_energy_entry<float>(p, s, n_keys, nbins, emin, emax, cdf, energy_scale, seed, stream);
 }
 int bz_seg_sample_energy_f64(const bz_params *p, bz_segments_f64 s, int32_t n_keys, int32_t nbins, double emin,
-                             double emax, const double *cdf, uint64_t seed, void *stream) {
-    return bz::seg_sample_energy_entry<double>(p, s, n_keys, nbins, emin, emax, cdf, seed, stream);
+                             double emax, const double *cdf, const double *energy_scale, uint64_t seed,
+                             void *stream) {
+    return bz::seg_sample_energy_entry<double>(p, s, n_keys, nbins, emin, emax, cdf, energy_scale, seed, stream);
 }
 
 }  // extern "C"

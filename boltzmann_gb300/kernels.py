@@ -389,11 +389,12 @@ def advance_clock(t_dev, step_dev, dt):
 
 
 # ------------------------------------------------------------------------------------ surrogate network
-def seg_sample_energy(params, s: SegmentSet, cdf, emin, emax, seed):
+def seg_sample_energy(params, s: SegmentSet, cdf, emin, emax, seed, scale=None):
     """Velocities of every live particle drawn from cdf [n_keys, nbins] (float64, cumulative
-    weight fractions of log bins over [emin, emax) eV) of its key (deposit node / swarm)."""
+    weight fractions of log bins over [emin, emax) eV) of its key (deposit node / swarm);
+    the energies times scale[key] when given."""
     call(f"bz_seg_sample_energy_{s.suffix}", ctypes.byref(params), s.struct(), int(cdf.shape[0]), int(cdf.shape[1]),
-         float(emin), float(emax), _ptr(cdf), int(seed), _stream())
+         float(emin), float(emax), _ptr(cdf), _ptr(scale), int(seed), _stream())
 
 
 def mlp_sync(prm, wb, wt):

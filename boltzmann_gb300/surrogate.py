@@ -94,6 +94,15 @@ def decode(y):
     return f, kx, ki
 
 
+def eedf_mean(eedf):
+    """Mean energy (eV) of weight fractions in the 64 log bins, each bin log-uniform (the
+    start-up's draw): sum_k f_k (e_k+1 - e_k) / ln(e_k+1 / e_k)."""
+    le = np.linspace(math.log(EEDF_EMIN), math.log(EEDF_EMAX), EEDF_BINS + 1)
+    e = np.exp(le)
+    mk = (e[1:] - e[:-1]) / (le[1:] - le[:-1])
+    return np.asarray(eedf, dtype=np.float64) @ mk
+
+
 def output_weights(eedf_weight=1.0, rate_weight=1.0):
     w = np.zeros(NOUT, dtype=np.float32)
     w[:EEDF_BINS] = eedf_weight
@@ -286,12 +295,13 @@ def swarm_relaxation(td, counts, steps, chunk, mlp: Optional[SurrogateMLP] = Non
 
 
 # ------------------------------------------------------------------------------------ data from plain CCP runs
-def ccp_dataset(cfg, cycles, snaps_per_cycle=8, settle_cycles=None, min_density=1e-3, device="cuda"):
+def ccp_dataset(cfg, cycles, snaps_per_cycle=8, settle_cycles=None, min_density=1e-3, density_repeat=8,
+                device="cuda"):
     """Runs a plain CCP (``BoltzmannGB300``) for ``cycles`` RF cycles and returns (X, T, info):
     per deposit node and snapshot (``snaps_per_cycle`` per cycle), the features of the
-    current state; as targets, the node's energy distribution at the same RF phase
-    averaged over the last ``settle_cycles`` cycles, and its ionization and excitation
-    rate coefficients averaged over those cycles. Nodes whose settled density is below
+    current state; as targets, the node's energy distribution at the same RF phase averaged
+    over the last ``settle_cycles`` cycles, and its ionization and excitation rate
+    coefficients averaged over those cycles. Nodes whose settled density is below
     ``min_density`` of the largest are left out."""
     import dataclasses
     from .solver import BoltzmannGB300
@@ -322,8 +332,11 @@ def ccp_dataset(cfg, cycles, snaps_per_cycle=8, settle_cycles=None, min_density=
     den = np.maximum(e[2], 1e-300) * cfg.nn_m3 * cfg.dt
     k_ion, k_exc = e[0] / den, e[1] / den
     keep = e[2] >= min_density * e[2].max()
-    X = np.concatenate([x[keep] for _, x in snaps])
-    T = np.concatenate([targets(f_ss[k][keep], k_exc[keep], k_ion[keep]) for k, _ in snaps])
+    # each node's rows repeated in proportion to its electron density (1 .. density_repeat):
+    # the fit then weighs nodes as the gap's energy balance does
+    rep = np.maximum(1, np.round(density_repeat * e[2] / e[2].max())).astype(int)[keep]
+    X = np.concatenate([np.repeat(x[keep], rep, axis=0) for _, x in snaps])
+    T = np.concatenate([np.repeat(targets(f_ss[k][keep], k_exc[keep], k_ion[keep]), rep, axis=0) for k, _ in snaps])
     info = {"nodes": np.nonzero(keep)[0], "eedf_ss": f_ss, "k_ion": k_ion, "k_exc": k_exc,
             "status": sv.device_status(), "n_end": sv.n()}
     return X, T, info

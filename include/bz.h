@@ -413,11 +413,14 @@ int bz_mlp_train_step(float *params, float *grad, float *m, float *v, uint16_t *
  * deposit node; in an ensemble its swarm): cdf is n_keys x nbins FP64, the cumulative
  * weight fractions of nbins log-spaced bins over [emin, emax) eV (last entry 1; a key
  * whose last entry is not positive keeps its particles as they are). Energy: the bin by
- * inverse CDF, log-uniform within it; direction isotropic; Philox (seed, slot). */
+ * inverse CDF, log-uniform within it, times energy_scale[key] (optional, n_keys FP64);
+ * direction isotropic; Philox (seed, slot). */
 int bz_seg_sample_energy_f32(const bz_params *p, bz_segments_f32 s, int32_t n_keys, int32_t nbins, double emin,
-                             double emax, const double *cdf, uint64_t seed, void *stream);
+                             double emax, const double *cdf, const double *energy_scale, uint64_t seed,
+                             void *stream);
 int bz_seg_sample_energy_f64(const bz_params *p, bz_segments_f64 s, int32_t n_keys, int32_t nbins, double emin,
-                             double emax, const double *cdf, uint64_t seed, void *stream);
+                             double emax, const double *cdf, const double *energy_scale, uint64_t seed,
+                             void *stream);
 
 /* library identification */
 const char *bz_version(void);

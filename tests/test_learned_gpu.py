@@ -71,3 +71,34 @@ def test_learned_start_of_the_ccp():
     assert kl <= 0.6 * kp, (kp, kl)
     assert abs(learned[0] / plain[per] - 1) < 0.15  # within 15% of the periodic value at once
     assert abs(plain[0] / plain[per] - 1) > 0.5     # the plain start is far from it
+
+
+def test_energy_redraw_follows_the_tabulated_distribution():
+    """bz_seg_sample_energy: per key, the drawn energies follow the tabulated distribution
+    (the log-bin fractions to sampling error) times the key's scale; isotropic directions;
+    positions and weights untouched."""
+    from boltzmann_gb300 import _lib, kernels as K
+    nk, per = 4, 100_000
+    n = nk * per
+    x = np.repeat(np.arange(nk, dtype=np.float64), per)
+    w = np.full(n, 2.0)
+    seg = K.SegmentSet(-(-n // 2048), 2048, torch.float32)
+    seg.load(x, np.zeros(n), np.zeros(n), np.zeros(n), w)
+    f = np.stack([S.initial_eedf(1.0), S.initial_eedf(3.0), S.initial_eedf(10.0), np.full(64, 1 / 64)])
+    scale = np.array([1.0, 2.0, 0.5, 1.0])
+    p = K.make_params(n_faces=nk, n_nodes=nk, bnf=1, advect=_lib.ADVECT_ENSEMBLE, L=float(nk), dx=1.0, dt=1e-12,
+                      nn=3.22e22)
+    K.seg_sample_energy(p, seg, torch.as_tensor(S.eedf_cdf(f), device="cuda"), S.EEDF_EMIN, S.EEDF_EMAX, 5,
+                        scale=torch.as_tensor(scale, device="cuda"))
+    o = seg.to_numpy()
+    assert np.array_equal(np.sort(o["x"]), x) and np.all(o["w"] == 2.0)
+    e = 0.5 * 9.10938e-31 * 6.241509e18 * (o["vx"] ** 2 + o["vy"] ** 2 + o["vz"] ** 2)
+    key = o["x"].astype(int)
+    for k in range(nk):
+        ek = e[key == k]
+        np.testing.assert_allclose(ek.mean(), S.eedf_mean(f[k:k + 1])[0] * scale[k], rtol=0.01)
+        # the bin fractions of the unscaled energies
+        h = np.histogram(np.log(ek / scale[k]), bins=np.linspace(np.log(S.EEDF_EMIN), np.log(S.EEDF_EMAX), 65))[0]
+        assert 0.5 * np.abs(h / len(ek) - f[k]).sum() < 0.03  # sampling noise of 1e5 draws in 64 bins: ~0.01
+        sp = np.sqrt(o["vx"] ** 2 + o["vy"] ** 2 + o["vz"] ** 2)[key == k]
+        assert abs((o["vz"][key == k] / sp).mean()) < 0.01

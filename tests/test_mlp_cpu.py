@@ -87,6 +87,7 @@ def test_features_and_bin_fractions():
     assert abs(f0.sum() - 1) < 1e-12
     c = S.eedf_centres()
     assert abs((f0 * c).sum() - 1.5) < 0.05  # <e> = 3/2 Te
+    assert abs(S.eedf_mean(f0[None, :])[0] - 1.5) < 0.02
     fr = S.bin_fractions(f0[None, :])
     assert fr.shape == (1, 5) and abs(fr.sum() - 1) < 1e-12
     assert fr[0, 0] > 0.7  # most of a 1 eV Maxwellian is below 2 eV
