@@ -28,6 +28,12 @@ METRIC = "electron particle-steps/s"
 UNIT = "particle-steps/s"
 BYTES_PER_PARTICLE = 40  # float32 SoA x, vx, vy, vz, w read + written by the push
 BYTES_PER_CHILD = 20
+# The tau/400 CCP stays numerically sound for about 320 steps from its uniform 1 eV start:
+# electrons cross up to ~7 of the 1024 cells per step, so the sheaths it forms are not
+# resolved; the ion density and the fields then grow until the explicit ion fluid breaks
+# (its break flag, heavies_kernel_1D.py:44-46, rises near step 325) and the fields diverge
+# by step 350. Steps beyond this index run from a snapshot of the early warm-up instead.
+CCP_HORIZON = 240
 
 
 def peaks():
@@ -52,33 +58,48 @@ def peak_tensor():
 
 
 class ClockSampler:
-    """nvidia-smi samples during the timed region (read-only)."""
+    """nvidia-smi samples during the timed region (read-only). Sampling starts, and its
+    first line is awaited, before the region opens; only the samples that arrive while the
+    region is open (plus one interval after it) are summarised."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
+    INTERVAL_MS = 25
 
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
-        self.lines = []
+        self.lines = []  # (arrival time, csv line)
+        self.t_open = self.t_close = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", str(self.INTERVAL_MS)],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            deadline = time.perf_counter() + 15.0
+            while not self.lines and time.perf_counter() < deadline and self.proc.poll() is None:
+                time.sleep(0.01)
         except Exception:
             self.proc = None
+        self.t_open = time.perf_counter()
         return self
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+
+    def close_region(self):
+        """Marks the end of the timed region (after its closing synchronisation)."""
+        self.t_close = time.perf_counter()
+        time.sleep(1.5 * self.INTERVAL_MS / 1e3)  # the sample in flight at the close
 
     def __exit__(self, *a):
+        if self.t_close is None:
+            self.close_region()
         if self.proc is not None:
             self.proc.terminate()
             try:
@@ -87,8 +108,10 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        hi = self.t_close + 1.5 * self.INTERVAL_MS / 1e3 if self.t_close is not None else float("inf")
+        inside = [ln for t, ln in self.lines if self.t_open is not None and self.t_open <= t <= hi]
         sm, mx, reasons = [], None, set()
-        for ln in self.lines:
+        for ln in inside:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -104,7 +127,8 @@ class ClockSampler:
         if not sm:
             return None
         sm.sort()
-        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm),
+                "interval_ms": self.INTERVAL_MS}
 
 
 def dist_setup():
@@ -241,14 +265,38 @@ def run_ours(args, world, rank, local, pg):
                           Te_init_eV=args.te_init)
     sol = BoltzmannGB300(cfg, device=dev)
     n_start = sol.n()
-    for _ in range(args.warmup):
+    # episodes: from step CCP_HORIZON on, the state goes back to a snapshot taken early in
+    # the warm-up (the restore, a device copy, runs inside the timed region when it falls
+    # there), so that every timed step is a step of a numerically sound state whatever K is
+    snap_at = min(args.warmup, 10)
+    for _ in range(snap_at):
         sol.step()
+    snap = sol.snapshot()
+    restores = {"warmup": 0, "timed": 0, "e2e": 0}
+
+    def advance(leg):
+        if sol.bigstep >= CCP_HORIZON:
+            sol.restore(snap)
+            restores[leg] += 1
+        sol.step()
+
+    def schedule(b, n):
+        out = []
+        for _ in range(n):
+            if b >= CCP_HORIZON:
+                b = snap["bigstep"]
+            out.append(b)
+            b += 1
+        return out
+
+    for _ in range(args.warmup - snap_at):
+        advance("warmup")
     if not args.no_autotune:
         sol.retune()  # on the warmed-up state, which is closer to the timed one
     sol.capture_all()  # no graph capture inside the timed loop
     torch.cuda.synchronize()
     ps0 = int(sol.particle_steps.item())
-    n_resample = sum(1 for s in range(sol.bigstep, sol.bigstep + args.steps) if s % cfg.resample_freq == 0)
+    n_resample = sum(1 for s in schedule(sol.bigstep, args.steps) if s % cfg.resample_freq == 0)
     st = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier(pg)
@@ -256,9 +304,10 @@ def run_ours(args, world, rank, local, pg):
     with ClockSampler(local) as clk:
         e0.record(st)
         for _ in range(args.steps):
-            sol.step()
+            advance("timed")
         e1.record(st)
         torch.cuda.synchronize()
+        clk.close_region()
     barrier(pg)
     ms = e0.elapsed_time(e1)
     ps = int(sol.particle_steps.item()) - ps0
@@ -310,18 +359,29 @@ def run_ours(args, world, rank, local, pg):
     # before the host may read the result; the copies are part of each step's graph
     e2e = None
     if not args.no_e2e:
+        sol.restore(snap)
         io_h = torch.empty(sol.io.numel(), dtype=torch.float64, pin_memory=True)
         io_h.copy_(sol.io)
         n_in = sol.io_in
         sol.attach_host_io(io_h)
         sol.capture_all()
         K2 = max(10, args.steps // 2)
+        # warm-up: every re-captured graph replayed once (the first replay uploads it),
+        # which takes the steps past the next resampling steps; then back to the snapshot
+        # (same buffers, so the graphs stay valid)
+        for _ in range(2 * cfg.resample_freq + 3):
+            if sol.graphs_warm():
+                break
+            advance("warmup")
+            torch.cuda.synchronize()
+        sol.restore(snap)
+        io_h.copy_(sol.io)
         torch.cuda.synchronize()
         ps_e0 = int(sol.particle_steps.item())
         t0 = time.perf_counter()
         marks = []
         for _ in range(K2):
-            sol.step()
+            advance("e2e")
             torch.cuda.synchronize()
             marks.append(time.perf_counter())
         el = time.perf_counter() - t0
@@ -358,6 +418,7 @@ def run_ours(args, world, rank, local, pg):
                          + sol.kernel_launches(True) * n_resample),
         "clocks": clk.summary(),
         "particles_start": n_start, "particles_end": int(n_now), "device_status": sol.device_status(),
+        "episodes": {"horizon_step": CCP_HORIZON, "snapshot_step": snap["bigstep"], "restores": restores},
     }
     print(json.dumps(line), flush=True)
 
@@ -388,6 +449,7 @@ def run_swarms(args, world, rank, local, pg):
             ens.step()
         e1.record(st)
         torch.cuda.synchronize()
+        clk.close_region()
     ms = e0.elapsed_time(e1)
     ps = int(ens.particle_steps.item()) - ps0
     t_max = max_over_ranks(pg, ms / 1e3, ens.device)

@@ -11,6 +11,7 @@ step is captured once into a CUDA graph and replayed.
 from __future__ import annotations
 
 import math
+import warnings
 import os
 
 import numpy as np
@@ -95,8 +96,10 @@ class BoltzmannGB300:
         self.bigstep = 0
         self.particle_steps = torch.zeros(1, dtype=torch.int64, device=dev)
         self._graphs = {}
+        self._replayed = set()  # graph keys replayed at least once since their capture
         self._kinds = set()
         self._host_io = None
+        self._brk_warned = False
         if N >= 3:
             K.poisson_factor(N, cfg.dx, self.chol_d, self.chol_l, self.poisson_plan)
         # first deposit and field solve (boltzmann.py:363-399)
@@ -241,6 +244,7 @@ class BoltzmannGB300:
         if use_graph and resample in self._kinds:
             gr = self._graphs.get(key) or self._capture_key(key)
             gr.replay()
+            self._replayed.add(key)
             # the graph swaps A and B internally; mirror the swaps on the host side
             for _ in range(2 if resample else 1):
                 self.A, self.B = self.B, self.A
@@ -257,6 +261,11 @@ class BoltzmannGB300:
             for first in (True, False):
                 if (resample, first) not in self._graphs:
                     self._capture_key((resample, first))
+
+    def graphs_warm(self):
+        """True once every captured step graph has been replayed (a graph's first replay
+        also uploads it to the device, a one-off cost)."""
+        return all(k in self._replayed for k in self._graphs)
 
     def attach_host_io(self, host_block):
         """Make every step copy the first ``io_in`` values of a pinned host block (the
@@ -289,6 +298,7 @@ class BoltzmannGB300:
         if swap:
             self.A, self.B = self.B, self.A
         self._graphs[key] = g
+        self._replayed.discard(key)
         return g
 
     def _first_A(self):
@@ -334,6 +344,11 @@ class BoltzmannGB300:
                 acc["Te"].add_(self.Te); acc["E"].add_(self.E)
             else:
                 ca = {k: (v / spc) for k, v in acc.items()}
+                if not self._brk_warned and int(self.brk.item()):
+                    # the reference prints a warning and runs on (heavies_kernel_1D.py:44-46)
+                    self._brk_warned = True
+                    warnings.warn("an ion density went negative in the fluid update (break flag); the "
+                                  "time step is too large for the densities and fields reached", RuntimeWarning)
                 if write:
                     from . import io as bzio
                     bzio.data_write(self, name, self.bigstep // spc + restart_cyclenum, ca)
@@ -386,6 +401,27 @@ class BoltzmannGB300:
         repack of the survivors with the appended particles (1)."""
         passes = 2 if self.nnodes * self.nb >= 256 else 1
         return 2 + (4 + 3 * passes + 2 + 1 if resample else 1)
+
+    def snapshot(self):
+        """A device copy of the simulation state: the particles (the buffer that holds
+        them and its counts), the grid block, the ion fluxes, the potential, the clock, the
+        status words and the step index. The Philox step counter and the particle-step
+        total are not part of it: a run restored from a snapshot draws new random numbers."""
+        return {"first": self.A is self._first_A(), "bigstep": self.bigstep,
+                "tensors": [t.clone() for t in self._state_tensors()]}
+
+    def restore(self, snap):
+        """Copy a snapshot back into the same device buffers (captured step graphs stay
+        valid: their pointers do not change)."""
+        if (self.A is self._first_A()) != snap["first"]:
+            self.A, self.B = self.B, self.A
+        for dst, src in zip(self._state_tensors(), snap["tensors"]):
+            dst.copy_(src)
+        self.bigstep = snap["bigstep"]
+
+    def _state_tensors(self):
+        return [self.A._buf, self.A.counts, self.io, self.E_push, self.V, self.Ji, self.g2, self.t, self.brk,
+                self.status, self.seg_flags]
 
     def n(self):
         return self.A.n()

@@ -61,3 +61,31 @@ def test_reference_format_roundtrip(tmp_path):
     np.testing.assert_array_equal(w, s["w"])
     ne = bzio.read_grid(name, 1, "ne")
     np.testing.assert_array_equal(ne, sol.moments[0].cpu().numpy())
+
+
+def test_snapshot_restore_returns_the_state():
+    """restore(snapshot()) puts the particles, the grid block, the clock, the status words
+    and the step index back into the same buffers, across both buffer roles and a
+    resampling step, and the captured step graphs keep running from there."""
+    sol = BoltzmannGB300(small_cfg())
+    for _ in range(3):
+        sol.step()
+    sol.capture_all()
+    snap = sol.snapshot()
+    s0, io0, t0, b0 = state(sol), sol.io.clone(), float(sol.t.item()), sol.bigstep
+    for _ in range(5):  # passes a resampling step (every 4) and swaps the buffer roles
+        sol.step()
+    assert sol.bigstep == b0 + 5 and float(sol.t.item()) != t0
+    sol.restore(snap)
+    torch.cuda.synchronize()
+    assert sol.bigstep == b0 and float(sol.t.item()) == t0
+    s1 = state(sol)
+    for f in s0:
+        np.testing.assert_array_equal(s0[f], s1[f], err_msg=f)
+    assert torch.equal(io0, sol.io)
+    ps = int(sol.particle_steps.item())
+    for _ in range(5):
+        sol.step()
+    torch.cuda.synchronize()
+    assert sol.device_status() == 0 and int(sol.particle_steps.item()) > ps
+    assert torch.isfinite(sol.E).all()
