@@ -101,6 +101,8 @@ _PROTOS = {
     "bz_field_step_coop_workspace": (_sz, [_i32]),
     "bz_field_step_coop": (ctypes.c_int, [_i32, _f64, _f64, _f64, _f64, _f64, _f64, _f64, _vp, _vp, _vp, _vp, _vp, _vp,
                                           _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "bz_field_step_select": (ctypes.c_int, [_i32]),
+    "bz_field_step_selected": (ctypes.c_int, []),
     "bz_seg_push_workspace": (_sz, []),
     "bz_seg_push_shapes": (ctypes.c_int32, []),
     "bz_seg_push_shape_info": (ctypes.c_int, [ctypes.c_int32, _vp, _vp, _vp, _vp]),

@@ -215,12 +215,14 @@ __global__ void __launch_bounds__(PS_T) k_field_step(int N, double dx, double dt
     poisson_body(N, dx, eps0, V0, freq, 0.0, t_dev, mom, ni, plan, V, E, E32, E, S);
 }
 
-// The same grid step spread over G CTAs (one cooperative launch, phases separated by
-// grid-wide barriers): float64 throughput is per SM on this part, and one CTA spent most of
-// its time waiting on its SM's narrow float64 pipe. CTA b owns Poisson rows
-// [b*FM_T, (b+1)*FM_T); each substitution is a CTA-local scan plus the sum of the other
-// CTAs' totals (in CTA order), so the result equals the one-CTA kernel's up to the
-// association of the float64 sums.
+// The same grid step spread over G CTAs, phases separated by barriers over all G CTAs:
+// float64 throughput is per SM on this part, and one CTA spent most of its time waiting on
+// its SM's narrow float64 pipe. CTA b owns Poisson rows [b*FM_T, (b+1)*FM_T); each
+// substitution is a CTA-local scan plus the sum of the other CTAs' totals (in CTA order),
+// so the result equals the one-CTA kernel's up to the association of the float64 sums.
+// CLUSTER: the G CTAs form one thread-block cluster (G <= 16, i.e. up to 1025 nodes) and
+// the barriers are the cluster's hardware barrier, whose release/acquire at cluster scope
+// orders the global-memory phases; otherwise a cooperative launch and grid-wide barriers.
 constexpr int FM_T = 64;
 
 __device__ double cta64_inclusive_sum(double v, double *sh) {
@@ -237,13 +239,19 @@ __device__ double cta64_inclusive_sum(double v, double *sh) {
     return v;
 }
 
+template <bool CLUSTER>
+__device__ __forceinline__ void phase_sync() {
+    if constexpr (CLUSTER) cooperative_groups::this_cluster().sync();
+    else cooperative_groups::this_grid().sync();
+}
+
+template <bool CLUSTER>
 __global__ void __launch_bounds__(FM_T) k_field_step_mc(int N, double dx, double dt, double mu_i, double D_i,
                                                         double eps0, double V0, double freq, const double *mom,
                                                         double *ni, double *Te, double *g2, double *t_dev,
                                                         uint64_t *step_dev, const double *plan, double *V, double *E,
                                                         float *E32, double *Ji, int32_t *brk, double *tot,
                                                         int32_t *flag) {
-    cooperative_groups::grid_group grid = cooperative_groups::this_grid();
     __shared__ double sh[2];
     __shared__ double s_vs;
     __shared__ double s_c[FM_T];
@@ -254,7 +262,7 @@ __global__ void __launch_bounds__(FM_T) k_field_step_mc(int N, double dx, double
     // grid update (boltzmann.py:643-647)
     grid_update_body(nn, mom, ni, Te, g2, gt, GT);
     if (gt == 0) *flag = 0;
-    grid.sync();
+    phase_sync<CLUSTER>();
     if (gt == 0) {
         *t_dev = tnew;
         if (step_dev) *step_dev = *step_dev + 1;
@@ -268,7 +276,7 @@ __global__ void __launch_bounds__(FM_T) k_field_step_mc(int N, double dx, double
                                       : ni[i + 1];
         Ji[i] = (mu_i * (0.5 * (a + c)) * E[i] - D_i * (c - a) / dx);
     }
-    grid.sync();
+    phase_sync<CLUSTER>();
     int bf = 0;
     for (int i = 1 + gt; i < N; i += GT) {
         double r = ni[i] - dt * (Ji[i] - Ji[i - 1]) / dx;
@@ -277,7 +285,7 @@ __global__ void __launch_bounds__(FM_T) k_field_step_mc(int N, double dx, double
     }
     if (bf) atomicOr(flag, 1);
     if (t == 0) s_vs = V0 * sin(2 * 3.141592653589793 * freq * tnew);
-    grid.sync();
+    phase_sync<CLUSTER>();
     if (gt == 0) {
         ni[0] = ni[1] * ((D_i / dx - 0.5 * mu_i * e0) / (D_i / dx + 0.5 * mu_i * e0));
         ni[N] = ni[N - 1] * ((D_i / dx + 0.5 * mu_i * eN) / (D_i / dx - 0.5 * mu_i * eN));
@@ -296,7 +304,7 @@ __global__ void __launch_bounds__(FM_T) k_field_step_mc(int N, double dx, double
     }
     const double sf = cta64_inclusive_sum(c, sh);
     if (t == FM_T - 1) tot[b] = sf;
-    grid.sync();
+    phase_sync<CLUSTER>();
     double carry = 0.0;
     for (int k = 0; k < b; ++k) carry += tot[k];
     const double y = (i < n) ? P[i] * (sf + carry) : 0.0;
@@ -306,11 +314,11 @@ __global__ void __launch_bounds__(FM_T) k_field_step_mc(int N, double dx, double
     const int tr = FM_T - 1 - t, ir = b * FM_T + tr;  // this thread's row in the backward scan
     const double sb = cta64_inclusive_sum(s_c[tr], sh);
     if (t == FM_T - 1) tot[G + b] = sb;
-    grid.sync();
+    phase_sync<CLUSTER>();
     double carry_b = 0.0;
     for (int k = G - 1; k > b; --k) carry_b += tot[G + k];
     if (ir < n) V[ir] = Q[ir] * (sb + carry_b);
-    grid.sync();
+    phase_sync<CLUSTER>();
     // faces (EF_kernel_1D.py:39-42)
     for (int f = gt; f < N; f += GT) {
         double e;
@@ -320,6 +328,46 @@ __global__ void __launch_bounds__(FM_T) k_field_step_mc(int N, double dx, double
         E[f] = e;
         if (E32) E32[f] = float(e);
     }
+}
+
+// 0: the cluster form where it fits, else the cooperative one; 1: cooperative; 2: cluster
+static int g_field_mode = 0;
+
+// Can G CTAs of the cluster form run as one cluster on the current device? (G <= 8 is
+// portable; up to 16 needs the non-portable size, granted per kernel.) Cached per
+// (device, G).
+static bool field_cluster_ok(int G) {
+    static int cached_dev = -1, cached_G = -1;
+    static bool cached = false;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev == cached_dev && G == cached_G) return cached;
+    cached_dev = dev;
+    cached_G = G;
+    cached = false;
+    if (G < 1 || G > 16) return false;
+    if (G > 8 && cudaFuncSetAttribute(k_field_step_mc<true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                     cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = unsigned(G);
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(G);
+    cfg.blockDim = dim3(FM_T);
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, k_field_step_mc<true>, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    cached = nclusters > 0;
+    return cached;
 }
 
 __global__ void k_advance_clock(double *t, uint64_t *step, double dt) {
@@ -379,20 +427,44 @@ int bz_field_step_coop(int32_t N, double dx, double dt, double mu_i, double D_i,
     if (N < 3 || !moments || !ni || !t_dev || !plan || !V || !E || !Ji || !workspace) return BZ_ERR_ARG;
     if (workspace_bytes < bz_field_step_coop_workspace(N)) return BZ_ERR_WORKSPACE;
     int G = int(bz::ceil_div(N - 1, bz::FM_T));
-    int dev = 0, per_sm = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bz::k_field_step_mc, bz::FM_T, 0) != cudaSuccess ||
-        G > per_sm * sms)
-        return BZ_ERR_TOO_LARGE;  // every CTA must be resident for the grid-wide barriers
     double *tot = static_cast<double *>(workspace);
     int32_t *flag = reinterpret_cast<int32_t *>(tot + 2 * G);
     void *args[] = {&N, &dx, &dt, &mu_i, &D_i, &eps0, &V0, &freq, (void *)&moments, &ni, &Te, &g2, &t_dev,
                     &step_dev, (void *)&plan, &V, &E, &E32, &Ji, &brk, &tot, &flag};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void *)bz::k_field_step_mc, dim3(G), dim3(bz::FM_T), args, 0,
-                                                bz::as_stream(stream));
+    if (bz::g_field_mode != 1 && bz::field_cluster_ok(G)) {
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = unsigned(G);
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3(G);
+        cfg.blockDim = dim3(bz::FM_T);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = bz::as_stream(stream);
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        cudaError_t e = cudaLaunchKernelExC(&cfg, (const void *)bz::k_field_step_mc<true>, args);
+        return e == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+    }
+    if (bz::g_field_mode == 2) return BZ_ERR_UNSUPPORTED;  // the cluster form was asked for and is not possible
+    int dev = 0, per_sm = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bz::k_field_step_mc<false>, bz::FM_T, 0) !=
+            cudaSuccess ||
+        G > per_sm * sms)
+        return BZ_ERR_TOO_LARGE;  // every CTA must be resident for the grid-wide barriers
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)bz::k_field_step_mc<false>, dim3(G), dim3(bz::FM_T),
+                                                args, 0, bz::as_stream(stream));
     return e == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
 }
+int bz_field_step_select(int32_t mode) {
+    if (mode < 0 || mode > 2) return BZ_ERR_ARG;
+    bz::g_field_mode = mode;
+    return BZ_OK;
+}
+int bz_field_step_selected(void) { return bz::g_field_mode; }
 int bz_advance_clock(double *t_dev, uint64_t *step_dev, double dt, void *stream) {
     if (!t_dev && !step_dev) return BZ_ERR_ARG;
     bz::k_advance_clock<<<1, 32, 0, bz::as_stream(stream)>>>(t_dev, step_dev, dt);

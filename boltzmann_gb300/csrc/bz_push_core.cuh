@@ -258,12 +258,16 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
             // (float32: two-float arithmetic; float64: the float64 expression);
             // excitation loses e_exc (the reference has no excitation: sigma_g1 = 0),
             // ionization shares e - 15.76 equally (electron_kernel_numba.py:211-255)
-            const double thr = (proc == P_EXCITE) ? p.e_exc : E_ION;
-            if (sizeof(T) == 8 || e - T(thr) >= T(0.25) * e) {
-                T en = (proc == P_EXCITE) ? (e - T(thr)) : T(0.5) * (e - T(thr));
+            // (the float thresholds are the float64 ones rounded on the host, so no float64
+            // conversion runs here)
+            const bool ex = proc == P_EXCITE;
+            T thr;
+            if constexpr (sizeof(T) == 4) thr = ex ? k.exc_h : k.ion_h;
+            else thr = ex ? p.e_exc : E_ION;
+            if (sizeof(T) == 8 || e - thr >= T(0.25) * e) {
+                T en = ex ? (e - thr) : T(0.5) * (e - thr);
                 vn = sqrt_pos(en * k.e2v);
             } else if constexpr (sizeof(T) == 4) {
-                const bool ex = proc == P_EXCITE;
                 float d = fabsf(excess_energy_f(ax, ay, az, k.efac_h, k.efac_l, ex ? k.exc_h : k.ion_h,
                                                 ex ? k.exc_l : k.ion_l));
                 if (!ex) d = 0.5f * d;

@@ -377,11 +377,21 @@ def field_step(N, dx, dt, mu_i, D_i, eps0, V0, freq, moments, ni, Te, g2, t_dev,
 
 def field_step_coop(N, dx, dt, mu_i, D_i, eps0, V0, freq, moments, ni, Te, g2, t_dev, step_dev, plan, V, E, E32, Ji,
                     brk=None, ws: "Workspace" = None):
-    """field_step spread over ceil((N-1)/64) CTAs (one cooperative launch)."""
+    """field_step spread over ceil((N-1)/64) CTAs: one thread-block cluster where it fits,
+    else one cooperative launch."""
     w = (ws or Workspace(moments.device)).get("field_coop", _lib.load().bz_field_step_coop_workspace(int(N)))
     call("bz_field_step_coop", int(N), float(dx), float(dt), float(mu_i), float(D_i), float(eps0), float(V0),
          float(freq), _ptr(moments), _ptr(ni), _ptr(Te), _ptr(g2), _ptr(t_dev), _ptr(step_dev), _ptr(plan), _ptr(V),
          _ptr(E), _ptr(E32), _ptr(Ji), _ptr(brk), _ptr(w), w.numel(), _stream())
+
+
+def field_step_select(mode):
+    """Form of field_step_coop: 0 cluster where it fits (default), 1 cooperative, 2 cluster."""
+    call("bz_field_step_select", int(mode))
+
+
+def field_step_selected():
+    return int(_lib.load().bz_field_step_selected())
 
 
 def advance_clock(t_dev, step_dev, dt):

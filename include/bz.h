@@ -217,15 +217,23 @@ int bz_field_step(int32_t N, double dx, double dt, double mu_i, double D_i, doub
                   const double *plan, double *V, double *E, float *E32, double *Ji, int32_t *brk, void *stream);
 /* Step clock on the device (graph-capturable): *t_dev += dt, *step_dev += 1 (either may be NULL). */
 int bz_advance_clock(double *t_dev, uint64_t *step_dev, double dt, void *stream);
-/* bz_field_step over ceil((N-1)/64) CTAs of one cooperative launch (grid-wide barriers
- * between the phases): the float64 work is spread over that many SMs. Same results up to
- * the association of the Poisson substitution sums. workspace: bz_field_step_coop_workspace(N)
- * bytes; BZ_ERR_TOO_LARGE when the CTAs cannot all be resident. */
+/* bz_field_step over G = ceil((N-1)/64) CTAs with barriers over all of them between the
+ * phases: the float64 work is spread over G SMs. Where G <= 16 (N <= 1025) and the device
+ * can form such a cluster, the CTAs are one thread-block cluster and the barriers are the
+ * cluster's hardware barrier; otherwise one cooperative launch with grid-wide barriers.
+ * Same results up to the association of the Poisson substitution sums. workspace:
+ * bz_field_step_coop_workspace(N) bytes; BZ_ERR_TOO_LARGE when the cooperative CTAs cannot
+ * all be resident. */
 size_t bz_field_step_coop_workspace(int32_t N);
 int bz_field_step_coop(int32_t N, double dx, double dt, double mu_i, double D_i, double eps0, double V0,
                        double freq, const double *moments, double *ni, double *Te, double *g2, double *t_dev,
                        uint64_t *step_dev, const double *plan, double *V, double *E, float *E32, double *Ji,
                        int32_t *brk, void *workspace, size_t workspace_bytes, void *stream);
+/* Which form bz_field_step_coop takes: 0 the cluster form where it fits, else the
+ * cooperative one (default); 1 always cooperative; 2 always the cluster form
+ * (BZ_ERR_UNSUPPORTED where it does not fit). Process-wide. */
+int bz_field_step_select(int32_t mode);
+int bz_field_step_selected(void);
 
 /* ---------------------------------------------------------------------------------- */
 /* segmented particle state (the solver's hot loop)                                      */

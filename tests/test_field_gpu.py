@@ -8,7 +8,7 @@ import torch
 
 pytestmark = pytest.mark.gpu
 
-from boltzmann_gb300 import kernels as K  # noqa: E402
+from boltzmann_gb300 import _lib, kernels as K  # noqa: E402
 
 G = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
@@ -102,11 +102,14 @@ def test_fused_field_step_equals_the_four_kernels():
         np.testing.assert_array_equal(a, b)
 
 
+@pytest.mark.parametrize("mode", [1, 2])
 @pytest.mark.parametrize("N", [None, 130, 1024, 4096])
-def test_cooperative_field_step_equals_the_one_cta_kernel(N):
-    """bz_field_step_coop (the float64 work over ceil((N-1)/64) CTAs) against bz_field_step:
-    the densities, the clock and the ion fluxes bit for bit, the Poisson solution to the
-    association of its float64 sums."""
+def test_cooperative_field_step_equals_the_one_cta_kernel(N, mode):
+    """bz_field_step_coop (the float64 work over ceil((N-1)/64) CTAs; mode 1 a cooperative
+    launch with grid-wide barriers, mode 2 one thread-block cluster with its hardware
+    barrier) against bz_field_step: the densities, the clock and the ion fluxes bit for bit,
+    the Poisson solution to the association of its float64 sums. The cluster form takes at
+    most 16 CTAs (1025 nodes) and refuses more."""
     g = np.load(os.path.join(G, "field.npz"))
     N = int(g["N"]) if N is None else N
     dx, dev = 2.54 / N if N != int(g["N"]) else float(g["dx"]), "cuda"
@@ -132,7 +135,18 @@ def test_cooperative_field_step_equals_the_one_cta_kernel(N):
         brk = torch.zeros(1, dtype=torch.int32, device=dev)
         args = (N, dx, float(g["dt"]), float(g["mu_i"]), float(g["D_i"]), float(g["eps0"]), float(g["V0"]),
                 float(g["freq"]), mom, ni, Te, g2, t, step, plan, V, E, E32, Ji, brk)
-        (K.field_step_coop if coop else K.field_step)(*args)
+        if coop:
+            K.field_step_select(mode)
+            try:
+                if mode == 2 and N > 1025:
+                    with pytest.raises(_lib.BzError):
+                        K.field_step_coop(*args)
+                    return
+                K.field_step_coop(*args)
+            finally:
+                K.field_step_select(0)
+        else:
+            K.field_step(*args)
         torch.cuda.synchronize()
         out.append({k: a.cpu().numpy() for k, a in zip(("ni", "Te", "g2", "t", "step", "V", "E", "E32", "Ji", "brk"),
                                                        (ni, Te, g2, t, step, V, E, E32, Ji, brk))})
