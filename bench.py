@@ -245,7 +245,10 @@ def run_reference_arm(args, world, rank, pg):
 def workload_config(args):
     return {"workload": f"argon CCP 1 Torr, {args.cells} cells, {args.particles:.3g} electrons, 5-bin ES-WPNC",
             "cells": args.cells, "particles": int(args.particles), "bins": 5, "resample_every": args.rsf,
-            "dt": "tau/400", "state": "float32 SoA", "l2": "inputs larger than L2 (particle state 400 MB)",
+            "dt": "tau/400", "state": "float32 SoA",
+            "l2": (f"inputs larger than L2 (particle state {20 * args.particles / 1e6:.0f} MB at the start)"
+                   if 20 * args.particles > 129e6 else
+                   f"inputs smaller than L2 ({20 * args.particles / 1e6:.0f} MB): not a throughput configuration"),
             "parallelism": "replicas" if args.gpus > 1 else "1 GPU"}
 
 
