@@ -173,7 +173,7 @@ def sum_over_ranks(pg, v, device):
 # --------------------------------------------------------------------------------------
 # CPU baseline: the reference algorithm (oracle port) on the host cores
 # --------------------------------------------------------------------------------------
-def cpu_reference_rate(sample_particles, steps, cells, seed=0, threads=None, time_budget=20.0):
+def cpu_reference_rate(sample_particles, steps, cells, seed=0, threads=None, time_budget=20.0, warmup=0):
     import numpy as np
     from oracle import oracle as O
     from boltzmann_gb300 import xsec
@@ -204,39 +204,53 @@ def cpu_reference_rate(sample_particles, steps, cells, seed=0, threads=None, tim
     E = np.ascontiguousarray(E)
     import ctypes
     lib = O.lib()
+    step_no = 0
+
+    def one_step():
+        nonlocal n, step_no
+        if 2 * n > cap:  # the sample has no resampling: restart it before it outgrows its buffers
+            data[:], tosum[:] = data0, tosum0
+            n = n0
+        p.step = step_no
+        nn_ = lib.orc_step_omp(ctypes.byref(p), n, cap, data, tosum, dtmp, ttmp, E, mom, threads)
+        if nn_ < 0:
+            raise RuntimeError("oracle step refused: sample outgrew its buffers")
+        pushed = n
+        n = int(nn_)
+        step_no += 1
+        return pushed
+
+    for _ in range(warmup):  # untimed
+        one_step()
     done = 0
     t0 = time.perf_counter()
     k = 0
     while k < steps:
-        if 2 * n > cap:  # the sample has no resampling: restart it before it outgrows its buffers
-            data[:], tosum[:] = data0, tosum0
-            n = n0
-        p.step = k
-        nn_ = lib.orc_step_omp(ctypes.byref(p), n, cap, data, tosum, dtmp, ttmp, E, mom, threads)
-        if nn_ < 0:
-            raise RuntimeError("oracle step refused: sample outgrew its buffers")
-        done += n
-        n = int(nn_)
+        done += one_step()
         k += 1
         if time.perf_counter() - t0 > time_budget:
             break
     el = time.perf_counter() - t0
-    return done / el, threads, k, int(sample_particles)
+    return done / el, threads, k, int(sample_particles), el
 
 
 def run_reference_arm(args, world, rank, pg):
     if rank != 0:
         return
     sample = int(args.ref_sample)
-    rate, threads, k, n = cpu_reference_rate(sample, args.steps + args.warmup, args.cells, time_budget=args.ref_budget)
+    t0 = time.perf_counter()
+    rate, threads, k, n, el = cpu_reference_rate(sample, args.steps, args.cells, time_budget=args.ref_budget,
+                                                 warmup=args.warmup)
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": k, "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "steps": k, "warmup": args.warmup, "ms_per_step": el / max(k, 1) * 1e3, "higher_is_better": True,
+        "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": workload_config(args),
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{n} particles x {k} steps of the {args.cells}-cell CCP step "
-                                   "(push+collide+deposit+compaction), float64 AoS, OpenMP"},
+                         "sample": f"{n} particles x {k} timed steps (after {args.warmup} untimed) of the "
+                                   f"{args.cells}-cell CCP step (push+collide+deposit+compaction), float64 AoS, "
+                                   f"OpenMP {threads} threads; {time.perf_counter() - t0:.1f} s in all"},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -401,7 +415,7 @@ def run_ours(args, world, rank, local, pg):
         return
     cpu = None
     if not args.no_cpu:
-        rate, threads, k, n = cpu_reference_rate(args.cpu_sample, 1000, args.cells, time_budget=args.cpu_budget)
+        rate, threads, k, n, _ = cpu_reference_rate(args.cpu_sample, 1000, args.cells, time_budget=args.cpu_budget)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{n} particles x {k} steps of the same CCP step, float64 AoS (reference layout), "
                          f"OpenMP {threads} threads"}
