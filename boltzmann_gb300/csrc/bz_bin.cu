@@ -116,17 +116,20 @@ __global__ void __launch_bounds__(RB_T) k_radix_hist(const uint16_t *keys, const
     __shared__ uint32_t d_s[RADIX];
     const int n = int(min(int64_t(max(*n_ptr, 0)), cap));
     const int ntiles = int(ceil_div(n, RB_TILE));
-    if (int(blockIdx.x) >= ntiles) return;
-    for (int i = threadIdx.x; i < RADIX; i += RB_T) d_s[i] = 0;
-    __syncthreads();
-    const int64_t t0 = int64_t(blockIdx.x) * RB_TILE;
-    for (int j = threadIdx.x; j < RB_TILE; j += RB_T) {
-        int64_t i = t0 + j;
-        if (i >= n) break;
-        atomicAdd(&d_s[(keys[i] >> shift) & 0xff], 1u);
+    // the live tile count is known only here: a grid of a few CTAs per SM loops over them
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        for (int i = threadIdx.x; i < RADIX; i += RB_T) d_s[i] = 0;
+        __syncthreads();
+        const int64_t t0 = int64_t(tile) * RB_TILE;
+        for (int j = threadIdx.x; j < RB_TILE; j += RB_T) {
+            int64_t i = t0 + j;
+            if (i >= n) break;
+            atomicAdd(&d_s[(keys[i] >> shift) & 0xff], 1u);
+        }
+        __syncthreads();
+        for (int d = threadIdx.x; d < RADIX; d += RB_T) hist[size_t(tile) * RADIX + d] = d_s[d];
+        __syncthreads();
     }
-    __syncthreads();
-    for (int d = threadIdx.x; d < RADIX; d += RB_T) hist[size_t(blockIdx.x) * RADIX + d] = d_s[d];
 }
 
 // hist[t][d] -> global exclusive offset of (digit d, tile t) in (digit, tile) order.
@@ -181,84 +184,87 @@ __global__ void __launch_bounds__(RB_T) k_radix_scatter(const uint16_t *keys_in,
     uint16_t *k_s = reinterpret_cast<uint16_t *>(v_s + RB_TILE);
     const int n = int(min(int64_t(max(*n_ptr, 0)), cap));
     const int ntiles = int(ceil_div(n, RB_TILE));
-    if (int(blockIdx.x) >= ntiles) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int i = threadIdx.x; i < RB_W * RADIX; i += RB_T) (&cnt[0][0])[i] = 0;
-    __syncthreads();
-    const int64_t tile0 = int64_t(blockIdx.x) * RB_TILE;
-    const int tile_n = int(min(int64_t(RB_TILE), int64_t(n) - tile0));
-    const int64_t seg0 = tile0 + int64_t(warp) * RB_SEG;
-    uint16_t k[RB_I];
-    uint32_t v[RB_I];
-    const unsigned lt_mask = (1u << lane) - 1u;
+    // a grid of a few CTAs per SM loops over the live tiles (their count is known only here)
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        for (int i = threadIdx.x; i < RB_W * RADIX; i += RB_T) (&cnt[0][0])[i] = 0;
+        __syncthreads();
+        const int64_t tile0 = int64_t(tile) * RB_TILE;
+        const int tile_n = int(min(int64_t(RB_TILE), int64_t(n) - tile0));
+        const int64_t seg0 = tile0 + int64_t(warp) * RB_SEG;
+        uint16_t k[RB_I];
+        uint32_t v[RB_I];
+        const unsigned lt_mask = (1u << lane) - 1u;
 #pragma unroll
-    for (int r = 0; r < RB_I; ++r) {
-        int64_t i = seg0 + r * 32 + lane;
-        bool ok = i < n;
-        k[r] = ok ? keys_in[i] : uint16_t(0);
-        v[r] = ok ? (vals_in ? vals_in[i] : uint32_t(i)) : 0u;
-        unsigned act = __ballot_sync(0xffffffffu, ok);
-        if (ok) {
-            int dg = (k[r] >> shift) & 0xff;
-            unsigned peers = __match_any_sync(act, dg);
-            if (lane == __ffs(peers) - 1) cnt[warp][dg] += __popc(peers);
-        }
-        __syncwarp();
-    }
-    __syncthreads();
-    // per digit: the tile's total, its local start (exclusive scan over digits, one warp),
-    // and the warps' local starts
-    if (warp == 0) {
-        uint32_t carry = 0;
-        for (int d0 = 0; d0 < RADIX; d0 += 32) {
-            const int dg = d0 + lane;
-            uint32_t tot = 0;
-            for (int ww = 0; ww < RB_W; ++ww) tot += cnt[ww][dg];
-            uint32_t incl = tot;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += t;
+        for (int r = 0; r < RB_I; ++r) {
+            int64_t i = seg0 + r * 32 + lane;
+            bool ok = i < n;
+            k[r] = ok ? keys_in[i] : uint16_t(0);
+            v[r] = ok ? (vals_in ? vals_in[i] : uint32_t(i)) : 0u;
+            unsigned act = __ballot_sync(0xffffffffu, ok);
+            if (ok) {
+                int dg = (k[r] >> shift) & 0xff;
+                unsigned peers = __match_any_sync(act, dg);
+                if (lane == __ffs(peers) - 1) cnt[warp][dg] += __popc(peers);
             }
-            lbase[dg] = carry + incl - tot;
-            carry += __shfl_sync(0xffffffffu, incl, 31);
+            __syncwarp();
         }
-    }
-    __syncthreads();
-    for (int dg = threadIdx.x; dg < RADIX; dg += RB_T) {
-        uint32_t run = lbase[dg];
-        gshift[dg] = offsets[size_t(blockIdx.x) * RADIX + dg] - run;
-        for (int ww = 0; ww < RB_W; ++ww) {
-            uint32_t t = cnt[ww][dg];
-            cnt[ww][dg] = run;
-            run += t;
-        }
-    }
-    __syncthreads();
-    // the tile sorted by digit, in shared memory
+        __syncthreads();
+        // per digit: the tile's total, its local start (exclusive scan over digits, one warp),
+        // and the warps' local starts
+        if (warp == 0) {
+            uint32_t carry = 0;
+            for (int d0 = 0; d0 < RADIX; d0 += 32) {
+                const int dg = d0 + lane;
+                uint32_t tot = 0;
+                for (int ww = 0; ww < RB_W; ++ww) tot += cnt[ww][dg];
+                uint32_t incl = tot;
 #pragma unroll
-    for (int r = 0; r < RB_I; ++r) {
-        int64_t i = seg0 + r * 32 + lane;
-        bool ok = i < n;
-        unsigned act = __ballot_sync(0xffffffffu, ok);
-        if (ok) {
-            int dg = (k[r] >> shift) & 0xff;
-            unsigned peers = __match_any_sync(act, dg);
-            uint32_t pos = cnt[warp][dg] + __popc(peers & lt_mask);
-            k_s[pos] = k[r];
-            v_s[pos] = v[r];
-            __syncwarp(act);
-            if (lane == __ffs(peers) - 1) cnt[warp][dg] += __popc(peers);
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += t;
+                }
+                lbase[dg] = carry + incl - tot;
+                carry += __shfl_sync(0xffffffffu, incl, 31);
+            }
         }
-        __syncwarp();
-    }
-    __syncthreads();
-    // out, in tile order: each digit's run lands contiguously at its global position
-    for (int p = threadIdx.x; p < tile_n; p += RB_T) {
-        const uint16_t key = k_s[p];
-        const uint32_t g = gshift[(key >> shift) & 0xff] + uint32_t(p);
-        keys_out[g] = key;
-        vals_out[g] = v_s[p];
+        __syncthreads();
+        for (int dg = threadIdx.x; dg < RADIX; dg += RB_T) {
+            uint32_t run = lbase[dg];
+            gshift[dg] = offsets[size_t(tile) * RADIX + dg] - run;
+            for (int ww = 0; ww < RB_W; ++ww) {
+                uint32_t t = cnt[ww][dg];
+                cnt[ww][dg] = run;
+                run += t;
+            }
+        }
+        __syncthreads();
+        // the tile sorted by digit, in shared memory
+#pragma unroll
+        for (int r = 0; r < RB_I; ++r) {
+            int64_t i = seg0 + r * 32 + lane;
+            bool ok = i < n;
+            unsigned act = __ballot_sync(0xffffffffu, ok);
+            if (ok) {
+                int dg = (k[r] >> shift) & 0xff;
+                unsigned peers = __match_any_sync(act, dg);
+                uint32_t pos = cnt[warp][dg] + __popc(peers & lt_mask);
+                k_s[pos] = k[r];
+                v_s[pos] = v[r];
+                __syncwarp(act);
+                if (lane == __ffs(peers) - 1) cnt[warp][dg] += __popc(peers);
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+        // out, in tile order: each digit's run lands contiguously at its global position
+        for (int p = threadIdx.x; p < tile_n; p += RB_T) {
+            const uint16_t key = k_s[p];
+            const uint32_t g = gshift[(key >> shift) & 0xff] + uint32_t(p);
+            keys_out[g] = key;
+            vals_out[g] = v_s[p];
+        }
+        __syncthreads();  // the next tile reuses the shared arrays
     }
 }
 
@@ -266,6 +272,25 @@ __global__ void __launch_bounds__(RB_T) k_radix_scatter(const uint16_t *keys_in,
 static bool scatter_smem_ok() {
     return cudaFuncSetAttribute(k_radix_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 int(RB_SCATTER_SMEM)) == cudaSuccess;
+}
+
+// Grids of the histogram and scatter passes: as many CTAs as can be resident at once
+// (they loop over the live tiles), never more than the tiles of the capacity.
+static int radix_grid(int64_t cap, bool scatter) {
+    static int per_sm[2] = {0, 0};
+    int &k = per_sm[scatter ? 1 : 0];
+    if (k == 0) {
+        int b = 0;
+        cudaError_t e = scatter ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_radix_scatter, RB_T,
+                                                                                int(RB_SCATTER_SMEM))
+                                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_radix_hist, RB_T, 0);
+        if (e != cudaSuccess) cudaGetLastError();
+        k = std::max(1, b);
+    }
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return int(std::max<int64_t>(1, std::min<int64_t>(ceil_div(cap, RB_TILE), int64_t(sms) * k)));
 }
 
 // offsets[k] = exclusive scan of counts[0..nkeys), offsets[nkeys] = live total.
@@ -333,12 +358,12 @@ static int bin_entry(const bz_params *pp, P s, const int32_t *n, int64_t cap, in
     const bool two = nkeys >= RADIX;  // invalid key = nkeys must be ordered too
     k_radix_scan<<<1, 1024, 0, st>>>(hist, n, cap);
     if (!scatter_smem_ok()) return BZ_ERR_UNSUPPORTED;
-    k_radix_scatter<<<grid, RB_T, RB_SCATTER_SMEM, st>>>(keys_a, nullptr, n, cap, 0, hist, keys_b,
+    k_radix_scatter<<<radix_grid(cap, true), RB_T, RB_SCATTER_SMEM, st>>>(keys_a, nullptr, n, cap, 0, hist, keys_b,
                                                          two ? vals_a : reinterpret_cast<uint32_t *>(perm));
     if (two) {
-        k_radix_hist<<<grid, RB_T, 0, st>>>(keys_b, n, cap, 8, hist);
+        k_radix_hist<<<radix_grid(cap, false), RB_T, 0, st>>>(keys_b, n, cap, 8, hist);
         k_radix_scan<<<1, 1024, 0, st>>>(hist, n, cap);
-        k_radix_scatter<<<grid, RB_T, RB_SCATTER_SMEM, st>>>(keys_b, vals_a, n, cap, 8, hist, keys_a,
+        k_radix_scatter<<<radix_grid(cap, true), RB_T, RB_SCATTER_SMEM, st>>>(keys_b, vals_a, n, cap, 8, hist, keys_a,
                                                              reinterpret_cast<uint32_t *>(perm));
     }
     k_key_offsets<<<1, 1024, 0, st>>>(counts, nkeys, offsets);
@@ -470,15 +495,15 @@ static int seg_bin_entry(const bz_params *pp, S s, int nb, const double *edges, 
                               slots, counts, hw_counts, nkeys, status);
     const int grid = int(ceil_div(cap, RB_TILE));
     const bool two = nkeys >= RADIX;
-    k_radix_hist<<<grid, RB_T, 0, st>>>(keys_a, n, cap, 0, hist);
+    k_radix_hist<<<radix_grid(cap, false), RB_T, 0, st>>>(keys_a, n, cap, 0, hist);
     k_radix_scan<<<1, 1024, 0, st>>>(hist, n, cap);
     if (!scatter_smem_ok()) return BZ_ERR_UNSUPPORTED;
-    k_radix_scatter<<<grid, RB_T, RB_SCATTER_SMEM, st>>>(keys_a, slots, n, cap, 0, hist, keys_b,
+    k_radix_scatter<<<radix_grid(cap, true), RB_T, RB_SCATTER_SMEM, st>>>(keys_a, slots, n, cap, 0, hist, keys_b,
                                                          two ? vals_a : reinterpret_cast<uint32_t *>(perm));
     if (two) {
-        k_radix_hist<<<grid, RB_T, 0, st>>>(keys_b, n, cap, 8, hist);
+        k_radix_hist<<<radix_grid(cap, false), RB_T, 0, st>>>(keys_b, n, cap, 8, hist);
         k_radix_scan<<<1, 1024, 0, st>>>(hist, n, cap);
-        k_radix_scatter<<<grid, RB_T, RB_SCATTER_SMEM, st>>>(keys_b, vals_a, n, cap, 8, hist, keys_a,
+        k_radix_scatter<<<radix_grid(cap, true), RB_T, RB_SCATTER_SMEM, st>>>(keys_b, vals_a, n, cap, 8, hist, keys_a,
                                                              reinterpret_cast<uint32_t *>(perm));
     }
     k_key_offsets<<<1, 1024, 0, st>>>(counts, nkeys, offsets);

@@ -296,3 +296,99 @@ def test_every_cta_shape_gives_the_same_particles():
                 np.testing.assert_allclose(mom[j], ref[2][j], rtol=1e-5, atol=1e-6 * np.abs(ref[2][j]).max())
     finally:
         K.select_seg_push_shape(0)
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_ragged_segments_match_oracle_philox(prec):
+    """Segments filled unevenly — empty, run 0 full, run 1 full, one particle, both runs
+    partly filled — push like the oracle on the slot-indexed array (holes are w = 0)."""
+    rng = np.random.default_rng(23)
+    N, L, half = 128, 2.54, 256
+    pattern = [(0, 0), (half, 0), (0, half), (half - 1, 1), (1, 0), (0, 1), (100, 100), (0, 0), (37, 0),
+               (half // 2, half // 2)]
+    nseg = len(pattern)
+    seg = K.SegmentSet(nseg, half, DT[prec])
+    cap = seg.capacity
+    cnt = np.array(pattern, dtype=np.int32).reshape(-1)
+    seg.counts.copy_(torch.as_tensor(cnt, device="cuda"))
+    xs_, vxs, vys, vzs, ws_ = (np.zeros(cap) for _ in range(5))
+    for s, (a, b) in enumerate(pattern):
+        for run, c in ((0, a), (1, b)):
+            lo = s * 2 * half + run * half
+            sl = slice(lo, lo + c)
+            xs_[sl] = rng.uniform(1e-4, L - 1e-4, c)
+            vxs[sl], vys[sl], vzs[sl] = rng.normal(0, 1.3e6, (3, c))
+            ws_[sl] = rng.uniform(1e4, 1e5, c)
+    f32 = lambda a: a.astype(np.float32).astype(np.float64)
+    xs_, vxs, vys, vzs, ws_ = (f32(a) for a in (xs_, vxs, vys, vzs, ws_))
+    E = f32(rng.uniform(-1500, 1500, N))
+    tab = xsec.analytic_argon(2000)
+    nn, dt, gas_sigma = 3.22e22, 1.0 / 13.56e6 / 400, 6.74e4
+    op = O.make_params(N, L=L, dt=dt, nn=nn, rng_mode=1, precision=64 if prec == "f64" else 32, seed=6, step=2,
+                       gas_sigma=gas_sigma, xs_table=tab.nsigma(nn), xs_emin=tab.emin, xs_emax=tab.emax,
+                       e_exc=tab.e_exc)
+    data, tosum = O.soa_to_aos(xs_, vxs, vys, vzs, ws_, cap=2 * cap)
+    _, margin = O.push_margin(op, data.copy(), tosum.copy(), cap, E)
+    ws_[(margin < 1e-5) & (ws_ > 0)] = 0.0  # too close to a decision boundary to compare
+    for f, a in zip(seg.FIELDS, (xs_, vxs, vys, vzs, ws_)):
+        getattr(seg, f).copy_(torch.as_tensor(a, dtype=DT[prec], device="cuda"))
+    data, tosum = O.soa_to_aos(xs_, vxs, vys, vzs, ws_, cap=2 * cap)
+    nni = O.push(op, data, tosum, cap, E)
+    vs = velocity_scale(xs_, np.stack([vxs, vys, vzs], 1), ws_, tosum[:cap, 0] > 0, E, dt, L, N,
+                        data[cap:cap + nni, 3:6])
+    mom_o, nnew = O.post(op, data, tosum, cap + nni)
+    xt = torch.as_tensor(tab.nsigma(nn), device="cuda")
+    p = K.make_params(n_faces=N, n_nodes=N + 1, bnf=4, advect=1, L=L, dx=L / N, dt=dt, nn=nn, gas_sigma=gas_sigma,
+                      e_exc=tab.e_exc, xs_mode=_lib.XS_TABLE, xs_table=xt, xs_emin=tab.emin, xs_emax=tab.emax,
+                      flags=_lib.QUIRK_DEAD_IONFLAG, seed=6, step=2)
+    out, mom, st, fl = seg_push(seg, p, E)
+    assert st == 0
+    o = out.to_numpy("runs")
+    assert len(o["x"]) == nnew
+    assert int(out.counts.cpu().numpy()[1::2].sum()) == nni
+    oc = out.counts.cpu().numpy().reshape(-1, 2)
+    assert np.all(oc[[0, 7], :] == 0)  # empty segments stay empty
+    rtol = 1e-10 if prec == "f64" else 1e-6
+    check_state(o, data[:nnew, 0], data[:nnew, 3:6], tosum[:nnew, 0], rtol, dt=dt, vscale=vs)
+    col = {0: tosum[:nnew, 0], 1: tosum[:nnew, 0], 3: tosum[:nnew, 0] * tosum[:nnew, 3]}
+    for j in (0, 1, 3):
+        allow = node_allowance(data[:nnew, 0], col[j], L, N, 4, prec == "f32")
+        check_moments(mom[j], mom_o[j], 1e-10 if prec == "f64" else 1e-5, allow)
+
+
+def test_empty_state_through_push_bin_resample_deposit():
+    """No particle at all: every stage runs, reports no error and leaves everything empty."""
+    N, L, nseg, half, nb = 64, 2.54, 6, 128, 3
+    seg = K.SegmentSet(nseg, half)
+    tab = xsec.analytic_argon(2000)
+    xt = torch.as_tensor(tab.nsigma(3.22e22), device="cuda")
+    p = K.make_params(n_faces=N, n_nodes=N + 1, bnf=4, advect=1, L=L, dx=L / N, dt=1e-12, nn=3.22e22,
+                      gas_sigma=6.74e4, e_exc=tab.e_exc, xs_mode=_lib.XS_TABLE, xs_table=xt, xs_emin=tab.emin,
+                      xs_emax=tab.emax, seed=1, step=1)
+    out, mom, st, fl = seg_push(seg, p, np.zeros(N))
+    assert st == 0 and out.n() == 0 and not np.any(mom)
+    nkeys = (N + 1) * nb
+    ed = torch.as_tensor(np.array([4.0, 11.5]), device="cuda")
+    perm = torch.full((seg.capacity,), -1, dtype=torch.int32, device="cuda")
+    offs = torch.full((nkeys + 1,), -1, dtype=torch.int32, device="cuda")
+    cnts = torch.full((nkeys,), -1, dtype=torch.int32, device="cuda")
+    hw = torch.full((nkeys,), -1, dtype=torch.int32, device="cuda")
+    sts = torch.zeros(1, dtype=torch.int32, device="cuda")
+    ws = K.Workspace()
+    K.seg_bin_particles(p, out, ed, 0.1, perm, offs, cnts, hw, sts, ws)
+    torch.cuda.synchronize()
+    assert int(sts.item()) == 0
+    assert not cnts.any() and not hw.any() and not offs.any()
+    app = K.ParticleSet(16)
+    res = K.SegmentSet(nseg, half)
+    tg = torch.full((nb,), 100, dtype=torch.int32, device="cuda")
+    mp = torch.full((nb,), 1000, dtype=torch.int32, device="cuda")
+    need = torch.full((1,), -1, dtype=torch.int32, device="cuda")
+    fl2 = torch.zeros(1, dtype=torch.int32, device="cuda")
+    K.seg_resample(p, out, app, res, nb, tg, mp, 0.1, 0.5, 3.0, 0.6, perm, offs, cnts, hw, sts, fl2, ws, need=need)
+    torch.cuda.synchronize()
+    assert int(sts.item()) == 0 and int(need.item()) == 0 and res.n() == 0
+    m = torch.zeros(4, N + 1, dtype=torch.float64, device="cuda")
+    K.seg_deposit(p, res, m)
+    torch.cuda.synchronize()
+    assert not m.any()
