@@ -102,6 +102,7 @@ _PROTOS = {
     "bz_field_step_coop": (ctypes.c_int, [_i32, _f64, _f64, _f64, _f64, _f64, _f64, _f64, _vp, _vp, _vp, _vp, _vp, _vp,
                                           _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "bz_field_step_select": (ctypes.c_int, [_i32]),
+    "bz_philox4x32_10": (ctypes.c_int, [_vp, _vp, _i32, _i32, _vp, _vp]),
     "bz_field_step_selected": (ctypes.c_int, []),
     "bz_seg_push_workspace": (_sz, []),
     "bz_seg_push_shapes": (ctypes.c_int32, []),

@@ -308,6 +308,30 @@ static int push_entry(const bz_params *pp, P in_, const int32_t *n_in, int64_t i
     return BZ_ERR_ARG;
 }
 
+// Philox4x32-10 of n (counter, key) pairs through the device code the kernels use:
+// variant 0 the plain rounds, 1 and 2 the two halves of the interleaved pair with round
+// keys (philox_rk_x2, whose second counter differs in word 3: here the same counter).
+__global__ void k_philox(const uint32_t *ctr, const uint32_t *key, int n, int variant, uint32_t *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t *c = ctr + 4 * size_t(i), *k = key + 2 * size_t(i);
+    u32x4 r;
+    if (variant == 0) {
+        r = philox(c[0], c[1], c[2], c[3], k[0], k[1]);
+    } else {
+        uint32_t rk0[10], rk1[10];
+        for (int j = 0; j < 10; ++j) {
+            rk0[j] = k[0] + uint32_t(j) * 0x9E3779B9u;
+            rk1[j] = k[1] + uint32_t(j) * 0xBB67AE85u;
+        }
+        u32x4 a, b;
+        philox_rk_x2(c[0], c[1], c[2], c[3], c[3], rk0, rk1, a, b);
+        r = variant == 1 ? a : b;
+    }
+    uint32_t *o = out + 4 * size_t(i);
+    o[0] = r.x; o[1] = r.y; o[2] = r.z; o[3] = r.w;
+}
+
 }  // namespace bz
 
 extern "C" {
@@ -328,6 +352,14 @@ int bz_push_collide_f64(const bz_params *p, bz_particles_f64 in, const int32_t *
                         uint32_t *status, void *stream) {
     return bz::push_entry<double>(p, in, n_in, in_capacity, out, out_capacity, counts, E, replay_R, replay_gas, moments, workspace,
                                   workspace_bytes, status, stream);
+}
+
+int bz_philox4x32_10(const uint32_t *ctr, const uint32_t *key, int32_t n, int32_t variant, uint32_t *out,
+                     void *stream) {
+    if (n < 0 || variant < 0 || variant > 2 || (n > 0 && (!ctr || !key || !out))) return BZ_ERR_ARG;
+    if (n == 0) return BZ_OK;
+    bz::k_philox<<<int(bz::ceil_div(n, 256)), 256, 0, bz::as_stream(stream)>>>(ctr, key, n, variant, out);
+    return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
 }
 
 const char *bz_version(void) { return "libbz 0.1 sm_103a"; }

@@ -385,6 +385,17 @@ def field_step_coop(N, dx, dt, mu_i, D_i, eps0, V0, freq, moments, ni, Te, g2, t
          _ptr(E), _ptr(E32), _ptr(Ji), _ptr(brk), _ptr(w), w.numel(), _stream())
 
 
+def philox(ctr, key, variant=0):
+    """Philox4x32-10 on the device: ctr [n, 4] and key [n, 2] int64 tensors holding uint32
+    values (or numpy arrays); returns [n, 4] int64 (uint32 values)."""
+    c = torch.as_tensor(np.asarray(ctr, dtype=np.uint32).view(np.int32), device="cuda").contiguous()
+    k = torch.as_tensor(np.asarray(key, dtype=np.uint32).view(np.int32), device="cuda").contiguous()
+    n = c.shape[0]
+    out = torch.zeros(n, 4, dtype=torch.int32, device="cuda")
+    call("bz_philox4x32_10", _ptr(c), _ptr(k), int(n), int(variant), _ptr(out), _stream())
+    return out.cpu().numpy().view(np.uint32).astype(np.int64)
+
+
 def field_step_select(mode):
     """Form of field_step_coop: 0 cluster where it fits (default), 1 cooperative, 2 cluster."""
     call("bz_field_step_select", int(mode))

@@ -430,6 +430,13 @@ int bz_seg_sample_energy_f64(const bz_params *p, bz_segments_f64 s, int32_t n_ke
                              double emax, const double *cdf, const double *energy_scale, uint64_t seed,
                              void *stream);
 
+/* Philox4x32-10 (Salmon et al. 2011) of n counters ctr[n][4] under keys key[n][2] into
+ * out[n][4], all device pointers, through the device code the kernels draw from: variant 0
+ * the plain rounds, 1 and 2 the two outputs of the interleaved pair with precomputed round
+ * keys (both given the same counter). For known-answer checks of the generator. */
+int bz_philox4x32_10(const uint32_t *ctr, const uint32_t *key, int32_t n, int32_t variant, uint32_t *out,
+                     void *stream);
+
 /* library identification */
 const char *bz_version(void);
 
