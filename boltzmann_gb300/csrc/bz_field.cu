@@ -239,6 +239,16 @@ __device__ double cta64_inclusive_sum(double v, double *sh) {
     return v;
 }
 
+// The ion flux through face i (heavies_kernel_1D.py:36-37) with the boundary densities of
+// faces 0 and N-1 formed where they are needed (heavies_kernel_1D.py:22-33).
+__device__ __forceinline__ double face_flux(int i, int N, double dx, double mu_i, double D_i, double e0, double eN,
+                                            const double *ni, const double *E) {
+    const double a = (i == 0) ? ni[1] * ((D_i / dx - 0.5 * mu_i * e0) / (D_i / dx + 0.5 * mu_i * e0)) : ni[i];
+    const double c = (i + 1 == N) ? ni[N - 1] * ((D_i / dx + 0.5 * mu_i * eN) / (D_i / dx - 0.5 * mu_i * eN))
+                                  : ni[i + 1];
+    return (mu_i * (0.5 * (a + c)) * E[i] - D_i * (c - a) / dx);
+}
+
 template <bool CLUSTER>
 __device__ __forceinline__ void phase_sync() {
     if constexpr (CLUSTER) cooperative_groups::this_cluster().sync();
@@ -262,49 +272,51 @@ __global__ void __launch_bounds__(FM_T) k_field_step_mc(int N, double dx, double
     // grid update (boltzmann.py:643-647)
     grid_update_body(nn, mom, ni, Te, g2, gt, GT);
     if (gt == 0) *flag = 0;
+    if (t == 0) s_vs = V0 * sin(2 * 3.141592653589793 * freq * tnew);
     phase_sync<CLUSTER>();
     if (gt == 0) {
         *t_dev = tnew;
         if (step_dev) *step_dev = *step_dev + 1;
     }
-    // ion fluid (heavies_kernel_1D.py:4-64): fluxes with the boundary densities formed where
-    // they are needed, then the interior, then the boundaries again
+    // ion fluid (heavies_kernel_1D.py:4-64). G*FM_T >= N-1, so thread gt owns at most one
+    // interior node j = gt+1: it forms both fluxes of that node itself (the left one is also
+    // its left neighbour's right flux, the same arithmetic on the same operands), writes
+    // face j (and face 0 for j = 1) and keeps the new density in a register — the Poisson
+    // row j-1 below is this thread's too. The densities reach memory only after the next
+    // barrier, when no thread reads the old ones any more; the boundary densities are
+    // formed by the threads that own nodes 1 and N-1.
     const double e0 = fmax(E[0], 0.0), eN = fmin(E[N - 1], 0.0);
-    for (int i = gt; i < N; i += GT) {
-        const double a = (i == 0) ? ni[1] * ((D_i / dx - 0.5 * mu_i * e0) / (D_i / dx + 0.5 * mu_i * e0)) : ni[i];
-        const double c = (i + 1 == N) ? ni[N - 1] * ((D_i / dx + 0.5 * mu_i * eN) / (D_i / dx - 0.5 * mu_i * eN))
-                                      : ni[i + 1];
-        Ji[i] = (mu_i * (0.5 * (a + c)) * E[i] - D_i * (c - a) / dx);
-    }
-    phase_sync<CLUSTER>();
-    int bf = 0;
-    for (int i = 1 + gt; i < N; i += GT) {
-        double r = ni[i] - dt * (Ji[i] - Ji[i - 1]) / dx;
-        if (r < 0 && ni[i] > 0) bf = 1;
-        ni[i] = r;
-    }
-    if (bf) atomicOr(flag, 1);
-    if (t == 0) s_vs = V0 * sin(2 * 3.141592653589793 * freq * tnew);
-    phase_sync<CLUSTER>();
-    if (gt == 0) {
-        ni[0] = ni[1] * ((D_i / dx - 0.5 * mu_i * e0) / (D_i / dx + 0.5 * mu_i * e0));
-        ni[N] = ni[N - 1] * ((D_i / dx + 0.5 * mu_i * eN) / (D_i / dx - 0.5 * mu_i * eN));
-        if (brk) *brk = *flag;
+    const int j = 1 + gt;
+    double nj = 0.0;
+    if (j < N) {
+        const double JL = face_flux(j - 1, N, dx, mu_i, D_i, e0, eN, ni, E);
+        const double JR = face_flux(j, N, dx, mu_i, D_i, e0, eN, ni, E);
+        if (j == 1) Ji[0] = JL;
+        Ji[j] = JR;
+        const double old = ni[j];
+        nj = old - dt * (JR - JL) / dx;
+        if (nj < 0 && old > 0) atomicOr(flag, 1);
     }
     const double vs = s_vs;
     const double *P = plan, *g = plan + n, *Q = plan + 2 * n, *h = plan + 3 * n;
     const double *ne = mom;
     // forward substitution: y_i = P_i sum_{k<=i} r_k g_k (EF_kernel_1D.py:26-42)
-    const int i = b * FM_T + t;
+    const int i = b * FM_T + t;  // = gt: row i uses node i+1 = j
     double c = 0.0;
     if (i < n) {
-        double r = (1.0 / eps0) * (ni[i + 1] - ne[i + 1]);
+        double r = (1.0 / eps0) * (nj - ne[i + 1]);
         if (i == 0) r = r + (1.0 / (dx * dx)) * vs;
         c = r * g[i];
     }
     const double sf = cta64_inclusive_sum(c, sh);
     if (t == FM_T - 1) tot[b] = sf;
     phase_sync<CLUSTER>();
+    if (j < N) {
+        ni[j] = nj;
+        if (j == 1) ni[0] = nj * ((D_i / dx - 0.5 * mu_i * e0) / (D_i / dx + 0.5 * mu_i * e0));
+        if (j == N - 1) ni[N] = nj * ((D_i / dx + 0.5 * mu_i * eN) / (D_i / dx - 0.5 * mu_i * eN));
+    }
+    if (gt == 0 && brk) *brk = *flag;
     double carry = 0.0;
     for (int k = 0; k < b; ++k) carry += tot[k];
     const double y = (i < n) ? P[i] * (sf + carry) : 0.0;
