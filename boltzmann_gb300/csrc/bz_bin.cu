@@ -47,16 +47,6 @@ __device__ __forceinline__ int energy_bin(T vx, T vy, T vz, T w, int nb, const d
     return -1;  // NaN energy: in no bin (every comparison of the reference fails)
 }
 
-// w > min_wt as the reference tests it in float64: for float32 w the same as
-// w >= wmin_f, the smallest float above min_wt (formed on the host)
-__device__ __forceinline__ bool above_min(float w, double, float wmin_f) { return w >= wmin_f; }
-__device__ __forceinline__ bool above_min(double w, double min_wt, float) { return w > min_wt; }
-
-static float float_above(double m) {
-    float t = float(m);
-    if (double(t) <= m) t = nextafterf(t, INFINITY);
-    return t;
-}
 
 template <typename T>
 __global__ void __launch_bounds__(RB_T) k_bin_keys(bz_params p, const T *x, const T *vx, const T *vy, const T *vz,

@@ -160,6 +160,17 @@ __device__ __forceinline__ void sincos2pi(float u, float *s, float *c) {
 }
 __device__ __forceinline__ void sincos2pi(double u, double *s, double *c) { sincospi(2.0 * u, s, c); }
 
+// w > min_wt as the reference tests it in float64: for float32 w the same as
+// w >= wmin_f, the smallest float above min_wt (formed on the host)
+__device__ __forceinline__ bool above_min(float w, double, float wmin_f) { return w >= wmin_f; }
+__device__ __forceinline__ bool above_min(double w, double min_wt, float) { return w > min_wt; }
+
+static inline float float_above(double m) {
+    float t = float(m);
+    if (double(t) <= m) t = nextafterf(t, INFINITY);
+    return t;
+}
+
 // square root of a positive argument: x * rsqrt(x) in float (relative error ~1e-7),
 // correctly rounded in double
 __device__ __forceinline__ float sqrt_pos(float x) { return x * rsqrtf(x); }

@@ -237,7 +237,7 @@ template <typename F> __device__ void block_cumsum(int len, F val, double *cdf, 
 template <typename T>
 __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const int32_t *n_ptr, int64_t cap, int nb,
                                                    const int32_t *targets, const int32_t *max_ppc, double min_wt,
-                                                   double merge_keep, const int32_t *perm, const int32_t *offsets,
+                                                   float wmin_f, double merge_keep, const int32_t *perm, const int32_t *offsets,
                                                    const int32_t *counts, const int32_t *act, const int32_t *app_off,
                                                    const int32_t *draw_off, const double *replay_u, double *ws_cdf,
                                                    int32_t *ws_cnt, double *cons_diag, SoAR<T> app, int64_t app_cap,
@@ -277,7 +277,7 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
         for (int c0 = 0; c0 < n_k; c0 += RS_T) {
             int j = c0 + threadIdx.x;
             int id = j < n_k ? perm[off + j] : -1;
-            bool hw = id >= 0 && double(s.w[id]) > min_wt;
+            bool hw = id >= 0 && above_min(s.w[id], min_wt, wmin_f);
             int64_t tot;
             int64_t pos = block_excl_scan<int64_t>(hw ? 1 : 0, shi, &tot);
             if (hw) cnt[nhw + pos] = id;
@@ -286,13 +286,17 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
         __syncthreads();
         if (nhw == 0) return;
         #pragma unroll 4
-        for (int j = threadIdx.x; j < nhw; j += RS_T) W += double(s.w[cnt[j]]);
+        for (int j = threadIdx.x; j < nhw; j += RS_T) {  // the weights in float64, kept for the cumsum
+            const double wd = double(s.w[cnt[j]]);
+            cdf[j] = wd;
+            W += wd;
+        }
         W = block_sum<double>(W, shd);
         // cdf = cumsum(w/W), then / cdf[-1] (CuPy RandomState.choice with p); the
         // divisions are multiplications by the reciprocal (within 2 ulp; float64 division
         // is many instructions on this part's narrow float64 pipe)
         const double inv_W = 1.0 / W;
-        block_cumsum(nhw, [&](int j) { return double(s.w[cnt[j]]) * inv_W; }, cdf, shd);
+        block_cumsum(nhw, [&](int j) { return cdf[j] * inv_W; }, cdf, shd);  // in place
         __syncthreads();
         const double last = cdf[nhw - 1];
         const double inv_last = 1.0 / last;
@@ -387,6 +391,7 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
     for (int j = threadIdx.x; j < np_; j += RS_T) {
         int id = perm[off + j];
         double w = s.w[id], vx = s.vx[id], vy = s.vy[id], vz = s.vz[id];
+        cdf[j] = w;  // kept for the cumsum
         W += w;
         px += vx * w;
         py += vy * w;
@@ -402,7 +407,7 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
     const double ux = px / W, uy = py / W, uz = pz / W;
     const double T_cell = (2.0 / 3.0) * (ew / W);
     // cdf = cumsum(w/W) (not renormalised), stratified R_k = (1/K)(u_k + k)
-    block_cumsum(np_, [&](int j) { return double(s.w[perm[off + j]]) * inv_W; }, cdf, shd);
+    block_cumsum(np_, [&](int j) { return cdf[j] * inv_W; }, cdf, shd);  // in place
     __syncthreads();
     const double wbar = W / double(K);
     const T wbar_t = T(wbar);
@@ -606,7 +611,7 @@ static int resample_entry(const bz_params *pp, P s_, const int32_t *n, int64_t c
     SoAR<T> s{s_.x, s_.vx, s_.vy, s_.vz, s_.w};
     SoAR<T> o{out_.x, out_.vx, out_.vy, out_.vz, out_.w};
     k_rs_apply<T><<<nkeys, RS_T, RS_CDF * sizeof(double), st>>>(p, s, n, cap, nb, targets, max_ppc, min_wt,
-                                                                merge_keep, perm, offsets,
+                                                                float_above(min_wt), merge_keep, perm, offsets,
                                           counts, act, app_off, draw_off, replay_u, cdf, cnt, cons_diag,
                                           SoAR<T>{nullptr, nullptr, nullptr, nullptr, nullptr}, 0, status);
     if (cudaGetLastError() != cudaSuccess) return BZ_ERR_CUDA;
@@ -681,7 +686,7 @@ static int seg_resample_entry(const bz_params *pp, S s_, P app_, int64_t app_cap
     SoAR<T> s{s_.x, s_.vx, s_.vy, s_.vz, s_.w};
     SoAR<T> app{app_.x, app_.vx, app_.vy, app_.vz, app_.w};
     k_rs_apply<T><<<nkeys, RS_T, RS_CDF * sizeof(double), st>>>(p, s, nullptr, cap, nb, targets, max_ppc, min_wt,
-                                                                merge_keep, perm, offsets,
+                                                                float_above(min_wt), merge_keep, perm, offsets,
                                           counts, act, app_off, draw_off, replay_u, cdf, cnt, cons_diag, app, app_cap,
                                           status);
     if (cudaGetLastError() != cudaSuccess) return BZ_ERR_CUDA;
