@@ -450,7 +450,7 @@ def run_swarms(args, world, rank, local, pg):
     from boltzmann_gb300 import kernels as K, swarm
 
     torch.cuda.set_device(local)
-    cfg = swarm.ensemble_512(seed=rank)
+    cfg = swarm.ensemble_512(seed=rank, n_swarms=args.swarms)
     ens = swarm.SwarmEnsemble(cfg, device=torch.device("cuda", local))
     for _ in range(max(args.warmup, 10)):
         ens.step()
@@ -493,7 +493,7 @@ def run_swarms(args, world, rank, local, pg):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "batched 0-D argon swarms: 512 swarms, E/N 10-1000 Td, 1e4-2e5 particles each, "
+        "config": {"workload": f"batched 0-D argon swarms: {cfg.n_swarms} swarms, E/N 10-1000 Td, 1e4-2e5 particles each, "
                                "3-bin ES-WPNC every 10 steps, dt 1 ps", "swarms": cfg.n_swarms,
                    "particles": int(sum(cfg.counts)), "state": "float32 SoA"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -707,6 +707,7 @@ def main():
     ap.add_argument("--ref-sample", type=float, default=2e6)
     ap.add_argument("--ref-budget", type=float, default=60.0)
     ap.add_argument("--train-steps", type=int, default=20000, help="Adam steps of the learned workload")
+    ap.add_argument("--swarms", type=int, default=512, help="swarms of the swarm512 workload (fewer: a small case)")
     ap.add_argument("--mlp-batch", type=int, default=8192, help="minibatch of the learned workload")
     args = ap.parse_args()
     if args.warmup < 3:
