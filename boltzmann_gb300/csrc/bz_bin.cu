@@ -133,7 +133,15 @@ __global__ void __launch_bounds__(1024) k_radix_scan(uint32_t *hist, const int32
     const int per = (ntiles + 3) / 4;
     const int lo = q * per, hi = min(ntiles, lo + per);
     uint32_t s = 0;
-    for (int t = lo; t < hi; ++t) s += hist[size_t(t) * RADIX + d];
+    int t = lo;
+    for (; t + 8 <= hi; t += 8) {  // eight independent loads in flight per thread
+        uint32_t v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = hist[size_t(t + u) * RADIX + d];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) s += v[u];
+    }
+    for (; t < hi; ++t) s += hist[size_t(t) * RADIX + d];
     part[q][d] = s;
     __syncthreads();
     if (threadIdx.x < RADIX) {
@@ -148,7 +156,18 @@ __global__ void __launch_bounds__(1024) k_radix_scan(uint32_t *hist, const int32
     __syncthreads();
     uint32_t run = dig_base[d];
     for (int k = 0; k < q; ++k) run += part[k][d];
-    for (int t = lo; t < hi; ++t) {
+    t = lo;
+    for (; t + 8 <= hi; t += 8) {  // each entry is read, then overwritten with its offset
+        uint32_t v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = hist[size_t(t + u) * RADIX + d];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            hist[size_t(t + u) * RADIX + d] = run;
+            run += v[u];
+        }
+    }
+    for (; t < hi; ++t) {
         uint32_t v = hist[size_t(t) * RADIX + d];
         hist[size_t(t) * RADIX + d] = run;
         run += v;
@@ -288,8 +307,18 @@ __global__ void __launch_bounds__(1024) k_key_offsets(const int32_t *counts, int
     __shared__ int32_t part[1024];
     const int per = (nkeys + 1023) / 1024;
     const int lo = threadIdx.x * per, hi = min(nkeys, lo + per);
+    // each thread's span is read in batches of eight independent loads (the sums and the
+    // running offsets only depend on the values, not on the loads' order)
     int32_t s = 0;
-    for (int k = lo; k < hi; ++k) s += counts[k];
+    int k = lo;
+    for (; k + 8 <= hi; k += 8) {
+        int32_t v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = counts[k + u];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) s += v[u];
+    }
+    for (; k < hi; ++k) s += counts[k];
     part[threadIdx.x] = s;
     __syncthreads();
     for (int o = 1; o < 1024; o <<= 1) {
@@ -299,7 +328,18 @@ __global__ void __launch_bounds__(1024) k_key_offsets(const int32_t *counts, int
         __syncthreads();
     }
     int32_t run = part[threadIdx.x] - s;
-    for (int k = lo; k < hi; ++k) { offsets[k] = run; run += counts[k]; }
+    k = lo;
+    for (; k + 8 <= hi; k += 8) {
+        int32_t v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = counts[k + u];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            offsets[k + u] = run;
+            run += v[u];
+        }
+    }
+    for (; k < hi; ++k) { offsets[k] = run; run += counts[k]; }
     if (threadIdx.x == 1023) offsets[nkeys] = part[1023];
 }
 

@@ -298,7 +298,13 @@ __device__ __forceinline__ bool repack_skip(const uint32_t *only_if) {
 template <typename T>
 __device__ __forceinline__ void repack_put(Seg<T> &out, int64_t v, int fill, T x, T vx, T vy, T vz, T w,
                                            uint32_t &err) {
-    const int seg = int(v / fill), j = int(v - int64_t(seg) * fill);
+    if (v < 0 || v > int64_t(UINT32_MAX)) {  // slot indices fit 32 bits (checked at the entry points)
+        err |= BZ_DEV_CAPACITY;
+        return;
+    }
+    const uint32_t vv = uint32_t(v), f = uint32_t(fill);
+    const uint32_t sq = vv / f;  // 32-bit division: a fraction of the 64-bit one's instructions
+    const int seg = int(sq), j = int(vv - sq * f);
     if (seg < out.nseg && j < out.half) {
         const int64_t q = seg_slot(seg, 0, out.half, j);
         out.a.x[q] = x; out.a.vx[q] = vx; out.a.vy[q] = vy; out.a.vz[q] = vz; out.a.w[q] = w;
@@ -328,6 +334,7 @@ __global__ void __launch_bounds__(RP_T) k_seg_repack(Seg<T> in, SoA<T> app, cons
         for (int run = 0; run < 2; ++run) {
             const int cnt = min(max(in.cnt[2 * seg + run], 0), in.half);
             const int64_t b = seg_slot(seg, run, in.half, 0);
+#pragma unroll 8
             for (int j = lane; j < cnt; j += 32) c += (in.a.w[b + j] != T(0));
         }
 #pragma unroll
@@ -340,7 +347,15 @@ __global__ void __launch_bounds__(RP_T) k_seg_repack(Seg<T> in, SoA<T> app, cons
         const int per = (m + RP_T - 1) / RP_T;
         const int lo = threadIdx.x * per, hi = min(m, lo + per);
         int64_t sum = 0;
-        for (int k = lo; k < hi; ++k) sum += live[k];
+        int k = lo;
+        for (; k + 8 <= hi; k += 8) {  // eight independent loads in flight
+            int32_t v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) v[u] = live[k + u];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) sum += v[u];
+        }
+        for (; k < hi; ++k) sum += live[k];
         part[threadIdx.x] = sum;
         __syncthreads();
         for (int o = 1; o < RP_T; o <<= 1) {
@@ -350,7 +365,18 @@ __global__ void __launch_bounds__(RP_T) k_seg_repack(Seg<T> in, SoA<T> app, cons
             __syncthreads();
         }
         int64_t run = part[threadIdx.x] - sum;
-        for (int k = lo; k < hi; ++k) { pre[k] = int32_t(run); run += live[k]; }
+        k = lo;
+        for (; k + 8 <= hi; k += 8) {
+            int32_t v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) v[u] = live[k + u];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                pre[k + u] = int32_t(run);
+                run += v[u];
+            }
+        }
+        for (; k < hi; ++k) { pre[k] = int32_t(run); run += live[k]; }
         if (threadIdx.x == RP_T - 1) {
             const int64_t a = app_n ? min(int64_t(max(*app_n, 0)), app_cap) : 0;
             pre[m] = int32_t(part[RP_T - 1]);
@@ -367,17 +393,36 @@ __global__ void __launch_bounds__(RP_T) k_seg_repack(Seg<T> in, SoA<T> app, cons
         for (int run = 0; run < 2; ++run) {
             const int cnt = min(max(in.cnt[2 * seg + run], 0), in.half);
             const int64_t b = seg_slot(seg, run, in.half, 0);
-            for (int j0 = 0; j0 < cnt; j0 += 32) {
-                const int j = j0 + lane;
-                const bool ok = j < cnt;
-                const T w = ok ? in.a.w[b + j] : T(0);
-                const bool keep = ok && w != T(0);
-                const unsigned mk = __ballot_sync(0xffffffffu, keep);
-                if (keep) {
-                    const int64_t v = off + __popc(mk & ((1u << lane) - 1u));
-                    repack_put(out, v, fill, in.a.x[b + j], in.a.vx[b + j], in.a.vy[b + j], in.a.vz[b + j], w, err);
+            // four rounds of 32 at a time: their weights, then the kept particles' other
+            // columns, are loaded together (independent loads in flight), then written in
+            // round order
+            for (int j0 = 0; j0 < cnt; j0 += 4 * 32) {
+                T wv[4], xx[4], a1[4], a2[4], a3[4];
+                bool keep[4];
+                unsigned mk[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int j = j0 + u * 32 + lane;
+                    wv[u] = j < cnt ? in.a.w[b + j] : T(0);
                 }
-                off += __popc(mk);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int j = j0 + u * 32 + lane;
+                    keep[u] = j < cnt && wv[u] != T(0);
+                    mk[u] = __ballot_sync(0xffffffffu, keep[u]);
+                    xx[u] = keep[u] ? in.a.x[b + j] : T(0);
+                    a1[u] = keep[u] ? in.a.vx[b + j] : T(0);
+                    a2[u] = keep[u] ? in.a.vy[b + j] : T(0);
+                    a3[u] = keep[u] ? in.a.vz[b + j] : T(0);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    if (keep[u]) {
+                        const int64_t v = off + __popc(mk[u] & ((1u << lane) - 1u));
+                        repack_put(out, v, fill, xx[u], a1[u], a2[u], a3[u], wv[u], err);
+                    }
+                    off += __popc(mk[u]);
+                }
             }
         }
     }
