@@ -437,23 +437,41 @@ __global__ void __launch_bounds__(256) k_seg_bin_keys(bz_params p, const T *x, c
         for (int run = 0; run < 2; ++run) {
             const int c = min(max(cnt[2 * seg + run], 0), half);
             const int64_t b = int64_t(seg) * 2 * half + int64_t(run) * half;
-            for (int j = lane; j < c; j += 32) {
-                const int64_t i = b + j;
-                const T wi = w[i];
-                int key = nkeys;
-                if (wi > T(0)) {
-                    int cell = bin_cell(p.advect, x[i], p.dx, inv_dx_f);
-                    int e = energy_bin(vx[i], vy[i], vz[i], wi, nb, edges_s, edges_f, efac_f, efac_d);
-                    if (cell >= 0 && cell < p.n_nodes && e >= 0) {
-                        key = cell * nb + e;
-                        atomicAdd(&c_s[key], 1u);
-                        if (above_min(wi, min_wt, wmin_f)) atomicAdd(&h_s[key], 1u);
-                    } else {
-                        err |= BZ_DEV_BINRANGE;
+            // four rounds of 32 particles at a time, all five columns loaded together (the
+            // loads do not wait on the weight test), then keyed in order
+            for (int j0 = 0; j0 < c; j0 += 4 * 32) {
+                T wv[4], xv[4], ux[4], uy[4], uz[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int j = j0 + u * 32 + lane;
+                    const bool ok = j < c;
+                    const int64_t i = b + j;
+                    wv[u] = ok ? w[i] : T(0);
+                    xv[u] = ok ? x[i] : T(0);
+                    ux[u] = ok ? vx[i] : T(0);
+                    uy[u] = ok ? vy[i] : T(0);
+                    uz[u] = ok ? vz[i] : T(0);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int j = j0 + u * 32 + lane;
+                    if (j < c) {
+                        int key = nkeys;
+                        if (wv[u] > T(0)) {
+                            int cell = bin_cell(p.advect, xv[u], p.dx, inv_dx_f);
+                            int e = energy_bin(ux[u], uy[u], uz[u], wv[u], nb, edges_s, edges_f, efac_f, efac_d);
+                            if (cell >= 0 && cell < p.n_nodes && e >= 0) {
+                                key = cell * nb + e;
+                                atomicAdd(&c_s[key], 1u);
+                                if (above_min(wv[u], min_wt, wmin_f)) atomicAdd(&h_s[key], 1u);
+                            } else {
+                                err |= BZ_DEV_BINRANGE;
+                            }
+                        }
+                        keys[v0 + j] = uint16_t(key);
+                        slots[v0 + j] = uint32_t(b + j);
                     }
                 }
-                keys[v0 + j] = uint16_t(key);
-                slots[v0 + j] = uint32_t(i);
             }
             v0 += c;
         }
