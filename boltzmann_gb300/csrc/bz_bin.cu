@@ -122,55 +122,75 @@ __global__ void __launch_bounds__(RB_T) k_radix_hist(const uint16_t *keys, const
     }
 }
 
-// hist[t][d] -> global exclusive offset of (digit d, tile t) in (digit, tile) order.
-// One CTA of 1024 threads: 4 threads per digit, each owning a quarter of the tiles.
-__global__ void __launch_bounds__(1024) k_radix_scan(uint32_t *hist, const int32_t *n_ptr, int64_t cap) {
-    __shared__ uint32_t part[4][RADIX];
-    __shared__ uint32_t dig_base[RADIX];
+// hist[t][d] -> global exclusive offset of (digit d, tile t) in (digit, tile) order, in two
+// passes of one CTA per digit: the column totals, then each column's exclusive scan plus
+// the totals of the digits below it (integer sums: the result does not depend on the order).
+constexpr int RS_COL_T = 256;
+
+__device__ __forceinline__ uint32_t cta_sum_u32(uint32_t v, uint32_t *sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    uint32_t t = 0;
+    for (int w = 0; w < RS_COL_T / 32; ++w) t += sh[w];
+    __syncthreads();
+    return t;
+}
+
+__global__ void __launch_bounds__(RS_COL_T) k_radix_colsum(const uint32_t *hist, const int32_t *n_ptr, int64_t cap,
+                                                          uint32_t *totals) {
+    __shared__ uint32_t sh[RS_COL_T / 32];
     const int n = int(min(int64_t(max(*n_ptr, 0)), cap));
     const int ntiles = int(ceil_div(n, RB_TILE));
-    const int d = threadIdx.x & (RADIX - 1), q = threadIdx.x >> 8;
-    const int per = (ntiles + 3) / 4;
-    const int lo = q * per, hi = min(ntiles, lo + per);
+    const int d = blockIdx.x;
     uint32_t s = 0;
-    int t = lo;
-    for (; t + 8 <= hi; t += 8) {  // eight independent loads in flight per thread
-        uint32_t v[8];
+    for (int t = threadIdx.x; t < ntiles; t += RS_COL_T) s += hist[size_t(t) * RADIX + d];
+    s = cta_sum_u32(s, sh);
+    if (threadIdx.x == 0) totals[d] = s;
+}
+
+__global__ void __launch_bounds__(RS_COL_T) k_radix_colscan(uint32_t *hist, const int32_t *n_ptr, int64_t cap,
+                                                           const uint32_t *totals) {
+    __shared__ uint32_t sh[RS_COL_T / 32];
+    const int n = int(min(int64_t(max(*n_ptr, 0)), cap));
+    const int ntiles = int(ceil_div(n, RB_TILE));
+    const int d = blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t b = 0;
+    for (int k = threadIdx.x; k < d; k += RS_COL_T) b += totals[k];
+    uint32_t carry = cta_sum_u32(b, sh);  // the digits below d
+    constexpr int PER = 8;                // consecutive tiles per thread in a chunk
+    for (int c0 = 0; c0 < ntiles; c0 += RS_COL_T * PER) {
+        const int t0 = c0 + threadIdx.x * PER;
+        uint32_t v[PER], local = 0;
 #pragma unroll
-        for (int u = 0; u < 8; ++u) v[u] = hist[size_t(t + u) * RADIX + d];
+        for (int u = 0; u < PER; ++u) {
+            v[u] = t0 + u < ntiles ? hist[size_t(t0 + u) * RADIX + d] : 0u;
+            local += v[u];
+        }
+        uint32_t incl = local;
 #pragma unroll
-        for (int u = 0; u < 8; ++u) s += v[u];
-    }
-    for (; t < hi; ++t) s += hist[size_t(t) * RADIX + d];
-    part[q][d] = s;
-    __syncthreads();
-    if (threadIdx.x < RADIX) {
-        uint32_t tot = part[0][d] + part[1][d] + part[2][d] + part[3][d];
-        dig_base[d] = tot;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t run = 0;
-        for (int k = 0; k < RADIX; ++k) { uint32_t v = dig_base[k]; dig_base[k] = run; run += v; }
-    }
-    __syncthreads();
-    uint32_t run = dig_base[d];
-    for (int k = 0; k < q; ++k) run += part[k][d];
-    t = lo;
-    for (; t + 8 <= hi; t += 8) {  // each entry is read, then overwritten with its offset
-        uint32_t v[8];
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (lane == 31) sh[warp] = incl;
+        __syncthreads();
+        uint32_t before = 0, chunk = 0;
+        for (int w = 0; w < RS_COL_T / 32; ++w) {
+            if (w < warp) before += sh[w];
+            chunk += sh[w];
+        }
+        uint32_t run = carry + before + incl - local;
 #pragma unroll
-        for (int u = 0; u < 8; ++u) v[u] = hist[size_t(t + u) * RADIX + d];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            hist[size_t(t + u) * RADIX + d] = run;
+        for (int u = 0; u < PER; ++u) {
+            if (t0 + u < ntiles) hist[size_t(t0 + u) * RADIX + d] = run;
             run += v[u];
         }
-    }
-    for (; t < hi; ++t) {
-        uint32_t v = hist[size_t(t) * RADIX + d];
-        hist[size_t(t) * RADIX + d] = run;
-        run += v;
+        carry += chunk;
+        __syncthreads();  // sh is rewritten by the next chunk
     }
 }
 
@@ -352,7 +372,7 @@ struct BinWs {
         keys_b = keys_a + ((c * 2 + 255) & ~size_t(255));
         vals_a = keys_b + ((c * 2 + 255) & ~size_t(255));
         hist = vals_a + ((c * 4 + 255) & ~size_t(255));
-        total = hist + nt * RADIX * 4;
+        total = hist + (nt + 1) * RADIX * 4;  // the tiles' digit counts, then the digit totals
     }
 };
 
@@ -373,6 +393,7 @@ static int bin_entry(const bz_params *pp, P s, const int32_t *n, int64_t cap, in
     uint16_t *keys_b = reinterpret_cast<uint16_t *>(b + L.keys_b);
     uint32_t *vals_a = reinterpret_cast<uint32_t *>(b + L.vals_a);
     uint32_t *hist = reinterpret_cast<uint32_t *>(b + L.hist);
+    uint32_t *dig_tot = hist + size_t(ceil_div(std::max<int64_t>(cap, 1), RB_TILE)) * RADIX;
     cudaStream_t st = as_stream(stream);
     const int grid = int(ceil_div(cap, RB_TILE));
     if (cudaMemsetAsync(counts, 0, sizeof(int32_t) * nkeys, st) != cudaSuccess) return BZ_ERR_CUDA;
@@ -386,13 +407,15 @@ static int bin_entry(const bz_params *pp, P s, const int32_t *n, int64_t cap, in
                                  float(1.0 / p.dx), keys_a, hist, counts, hw_counts,
                                  nkeys, status);
     const bool two = nkeys >= RADIX;  // invalid key = nkeys must be ordered too
-    k_radix_scan<<<1, 1024, 0, st>>>(hist, n, cap);
+    k_radix_colsum<<<RADIX, RS_COL_T, 0, st>>>(hist, n, cap, dig_tot);
+    k_radix_colscan<<<RADIX, RS_COL_T, 0, st>>>(hist, n, cap, dig_tot);
     if (!scatter_smem_ok()) return BZ_ERR_UNSUPPORTED;
     k_radix_scatter<<<radix_grid(cap, true), RB_T, RB_SCATTER_SMEM, st>>>(keys_a, nullptr, n, cap, 0, hist, keys_b,
                                                          two ? vals_a : reinterpret_cast<uint32_t *>(perm));
     if (two) {
         k_radix_hist<<<radix_grid(cap, false), RB_T, 0, st>>>(keys_b, n, cap, 8, hist);
-        k_radix_scan<<<1, 1024, 0, st>>>(hist, n, cap);
+        k_radix_colsum<<<RADIX, RS_COL_T, 0, st>>>(hist, n, cap, dig_tot);
+    k_radix_colscan<<<RADIX, RS_COL_T, 0, st>>>(hist, n, cap, dig_tot);
         k_radix_scatter<<<radix_grid(cap, true), RB_T, RB_SCATTER_SMEM, st>>>(keys_b, vals_a, n, cap, 8, hist, keys_a,
                                                              reinterpret_cast<uint32_t *>(perm));
     }
@@ -495,7 +518,7 @@ struct SegBinWs {
         vals_a = keys_b + al(2 * c);
         slots = vals_a + al(4 * c);
         hist = slots + al(4 * c);
-        tot = hist + al(nt * RADIX * 4);
+        tot = hist + al((nt + 1) * RADIX * 4);  // the tiles' digit counts, then the digit totals
         pre = tot + al(4 * size_t(nseg));
         total = pre + al(4 * (size_t(nseg) + 1));
     }
@@ -521,6 +544,7 @@ static int seg_bin_entry(const bz_params *pp, S s, int nb, const double *edges, 
     uint32_t *vals_a = reinterpret_cast<uint32_t *>(b + L.vals_a);
     uint32_t *slots = reinterpret_cast<uint32_t *>(b + L.slots);
     uint32_t *hist = reinterpret_cast<uint32_t *>(b + L.hist);
+    uint32_t *dig_tot = hist + size_t(ceil_div(std::max<int64_t>(cap, 1), RB_TILE)) * RADIX;
     int32_t *tot = reinterpret_cast<int32_t *>(b + L.tot);
     int32_t *pre = reinterpret_cast<int32_t *>(b + L.pre);
     cudaStream_t st = as_stream(stream);
@@ -544,13 +568,15 @@ static int seg_bin_entry(const bz_params *pp, S s, int nb, const double *edges, 
     const int grid = int(ceil_div(cap, RB_TILE));
     const bool two = nkeys >= RADIX;
     k_radix_hist<<<radix_grid(cap, false), RB_T, 0, st>>>(keys_a, n, cap, 0, hist);
-    k_radix_scan<<<1, 1024, 0, st>>>(hist, n, cap);
+    k_radix_colsum<<<RADIX, RS_COL_T, 0, st>>>(hist, n, cap, dig_tot);
+    k_radix_colscan<<<RADIX, RS_COL_T, 0, st>>>(hist, n, cap, dig_tot);
     if (!scatter_smem_ok()) return BZ_ERR_UNSUPPORTED;
     k_radix_scatter<<<radix_grid(cap, true), RB_T, RB_SCATTER_SMEM, st>>>(keys_a, slots, n, cap, 0, hist, keys_b,
                                                          two ? vals_a : reinterpret_cast<uint32_t *>(perm));
     if (two) {
         k_radix_hist<<<radix_grid(cap, false), RB_T, 0, st>>>(keys_b, n, cap, 8, hist);
-        k_radix_scan<<<1, 1024, 0, st>>>(hist, n, cap);
+        k_radix_colsum<<<RADIX, RS_COL_T, 0, st>>>(hist, n, cap, dig_tot);
+    k_radix_colscan<<<RADIX, RS_COL_T, 0, st>>>(hist, n, cap, dig_tot);
         k_radix_scatter<<<radix_grid(cap, true), RB_T, RB_SCATTER_SMEM, st>>>(keys_b, vals_a, n, cap, 8, hist, keys_a,
                                                              reinterpret_cast<uint32_t *>(perm));
     }
