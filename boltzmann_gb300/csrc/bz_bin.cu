@@ -15,10 +15,10 @@
 namespace bz {
 
 constexpr int RB_T = 512;               // threads per tile CTA
-constexpr int RB_I = 16;                // items per thread
-constexpr int RB_TILE = RB_T * RB_I;    // 8192 items per tile
+constexpr int RB_I = 8;                 // items per thread
+constexpr int RB_TILE = RB_T * RB_I;    // 4096 items per tile
 constexpr int RB_W = RB_T / 32;         // warps
-constexpr int RB_SEG = RB_TILE / RB_W;  // items per warp segment (512)
+constexpr int RB_SEG = RB_TILE / RB_W;  // items per warp segment (256)
 constexpr int RADIX = 256;
 
 // energy as the reference holds it when binning: tosum[:,3] = ((e*w)/w) after
