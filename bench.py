@@ -259,6 +259,8 @@ def run_reference_arm(args, world, rank, pg):
 def workload_config(args):
     return {"workload": f"argon CCP 1 Torr, {args.cells} cells, {args.particles:.3g} electrons, 5-bin ES-WPNC",
             "cells": args.cells, "particles": int(args.particles), "bins": 5, "resample_every": args.rsf,
+            "merge": "energy-conserving (thermal part rescaled), reference split indexing and trigger",
+            "timed_window": "starts on a resampling step (binning + split/merge + repack inside it)",
             "dt": "tau/400", "state": "float32 SoA",
             "l2": (f"inputs larger than L2 (particle state {20 * args.particles / 1e6:.0f} MB at the start)"
                    if 20 * args.particles > 129e6 else
@@ -269,6 +271,53 @@ def workload_config(args):
 # --------------------------------------------------------------------------------------
 # our arm
 # --------------------------------------------------------------------------------------
+def dense_push_leg(sol, prm, reps, peak):
+    """The drop-in dense push (bz_push_collide_f32: the reference's global order, decoupled
+    look-back between tiles) on the solver's current particles, gathered into one dense
+    list on the device: launch time and algorithmic bandwidth (40 B per particle)."""
+    import torch
+    from boltzmann_gb300 import kernels as K
+    A = sol.A
+    cnt = A.counts.long()
+    n = int(cnt.sum().item())
+    if n == 0:
+        return None
+    dev = A.counts.device
+    seg = torch.arange(A.nseg, device=dev).repeat_interleave(2)
+    run = torch.arange(2, device=dev).repeat(A.nseg)
+    start = seg * 2 * A.half + run * A.half
+    excl = torch.cumsum(cnt, 0) - cnt
+    idx = torch.repeat_interleave(start - excl, cnt) + torch.arange(n, device=dev)
+    src, dst = K.ParticleSet(n, A.dtype, dev), K.ParticleSet(2 * n, A.dtype, dev)
+    for f in K.ParticleSet.FIELDS:
+        getattr(src, f).copy_(getattr(A, f)[idx])
+    src.cnt.zero_()
+    src.cnt[2] = n
+    del idx
+    st = torch.zeros(1, dtype=torch.int32, device=dev)
+    mom = torch.zeros_like(sol.moments)
+    ws = K.Workspace(dev)
+    stream = torch.cuda.current_stream()
+
+    def once():
+        K.electron_kernel(prm, src, dst, sol.E_push, st, ws, moments=mom)
+
+    for _ in range(3):
+        once()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        once()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    gbs = BYTES_PER_PARTICLE * n / (ms * 1e-3) / 1e9
+    return {"kernel": "k_push + k_append_children (bz_push_collide_f32: dense reference order, decoupled "
+                      "look-back)", "launch_ms": ms, "particles": n, "achieved_gbs": gbs, "frac": gbs / peak,
+            "device_status": int(st.item())}
+
+
 def run_ours(args, world, rank, local, pg):
     import numpy as np
     import torch
@@ -306,31 +355,51 @@ def run_ours(args, world, rank, local, pg):
             b += 1
         return out
 
-    for _ in range(args.warmup - snap_at):
+    # at least W warm-up steps, then on to the next resampling step: the timed window starts
+    # with binning + resampling, so every window of K steps holds ceil(K / rsf) of them
+    n_warm = snap_at
+    while n_warm < args.warmup or sol.bigstep % cfg.resample_freq != 0:
         advance("warmup")
+        n_warm += 1
     if not args.no_autotune:
         sol.retune()  # on the warmed-up state, which is closer to the timed one
     sol.capture_all()  # no graph capture inside the timed loop
     torch.cuda.synchronize()
     ps0 = int(sol.particle_steps.item())
-    n_resample = sum(1 for s in schedule(sol.bigstep, args.steps) if s % cfg.resample_freq == 0)
+    first_step = sol.bigstep
+    kinds = [s % cfg.resample_freq == 0 for s in schedule(sol.bigstep, args.steps)]
+    n_resample = sum(kinds)
     st = torch.cuda.current_stream()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev_steps = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     barrier(pg)
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        e0.record(st)
-        for _ in range(args.steps):
+        ev_steps[0].record(st)
+        for k in range(args.steps):
             advance("timed")
-        e1.record(st)
+            ev_steps[k + 1].record(st)
         torch.cuda.synchronize()
         clk.close_region()
     barrier(pg)
-    ms = e0.elapsed_time(e1)
+    ms = ev_steps[0].elapsed_time(ev_steps[-1])
+    per_step = np.array([ev_steps[k].elapsed_time(ev_steps[k + 1]) for k in range(args.steps)])
     ps = int(sol.particle_steps.item()) - ps0
     t_max = max_over_ranks(pg, ms / 1e3, dev)
     ps_all = sum_over_ranks(pg, ps, dev)
     value = ps_all / t_max
+    rs_ms = per_step[np.array(kinds, bool)]
+    pl_ms = per_step[~np.array(kinds, bool)]
+    step_kinds = {
+        "resampling": {"steps": int(len(rs_ms)), "ms_mean": float(rs_ms.mean()) if len(rs_ms) else None},
+        "plain": {"steps": int(len(pl_ms)), "ms_median": float(np.median(pl_ms)) if len(pl_ms) else None,
+                  "ms_mean": float(pl_ms.mean()) if len(pl_ms) else None},
+        "first_timed_step": first_step,
+    }
+    if len(rs_ms) and len(pl_ms):
+        # the same steps with resampling at its configured share (one step in rsf)
+        amort = (rs_ms.mean() + (cfg.resample_freq - 1) * pl_ms.mean()) / cfg.resample_freq
+        step_kinds["ms_per_step_at_configured_share"] = float(amort)
+        step_kinds["value_at_configured_share"] = float(ps_all / args.steps / (amort * 1e-3))
 
     # dominant kernel alone: the fused segmented push of the current state A into the
     # scratch buffer B, repeated (A is only read, so the solver's state is unchanged; the
@@ -361,6 +430,7 @@ def run_ours(args, world, rank, local, pg):
     bytes_per_launch = BYTES_PER_PARTICLE * n_now
     achieved = bytes_per_launch / (push_ms * 1e-3) / 1e9
     peak, kind = peaks()
+    dense = dense_push_leg(sol, prm, M, peaks()[0]) if not args.no_dense else None
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "push_traffic.json")
     if os.path.exists(tpath):
@@ -392,6 +462,9 @@ def run_ours(args, world, rank, local, pg):
             advance("warmup")
             torch.cuda.synchronize()
         sol.restore(snap)
+        while sol.bigstep % cfg.resample_freq != 0:  # the timed steps start on a resampling step
+            advance("warmup")
+        torch.cuda.synchronize()
         io_h.copy_(sol.io)
         torch.cuda.synchronize()
         ps_e0 = int(sol.particle_steps.item())
@@ -422,7 +495,8 @@ def run_ours(args, world, rank, local, pg):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic", "config": workload_config(args),
+        "dtype": "f32", "data": "synthetic", "config": dict(workload_config(args), warmup_steps_run=n_warm),
+        "step_kinds": step_kinds,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "kernel": "k_seg_push (fused push+collide+deposit+compaction)",
                      "launch_ms": push_ms, "particles_per_launch": n_now, "peak_kind": kind,
@@ -431,6 +505,7 @@ def run_ours(args, world, rank, local, pg):
                                             sol.push_shape["shape"])))},
         "cpu_baseline": cpu,
         "e2e": e2e,
+        "dense_push": dense,
         "gpu_launches": (sol.kernel_launches(False) * (args.steps - n_resample)
                          + sol.kernel_launches(True) * n_resample),
         "clocks": clk.summary(),
@@ -504,6 +579,139 @@ def run_swarms(args, world, rank, local, pg):
         "mean_energy_eV": [float(np.min(ens.mean_energy())), float(np.max(ens.mean_energy()))],
     }
     print(json.dumps(line), flush=True)
+
+
+def run_swarm100(args, world, rank, local, pg):
+    """The single FP64 argon swarm of the benchmark list: 100 Td, 1e5 particles from a 1 eV
+    Maxwellian, dt = 1 ps, 1e4 steps in all (W warm-up, the rest timed), one energy bin
+    merged back to 1e5 past 2e5 (checked every 10 steps). Whole steps (push + deposit +
+    the conditional rebalance, binning and resampling check when due) are graph replays
+    timed with CUDA events; the push alone gives the roofline at 80 B per particle-step
+    (float64 x, vx, vy, vz, w read and written)."""
+    import ctypes
+
+    import numpy as np
+    import torch
+    from boltzmann_gb300 import kernels as K, swarm, xsec
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    cfg = swarm.swarm_100td(seed=1 + rank)
+    ens = swarm.SwarmEnsemble(cfg, device=dev)
+    total = args.swarm_steps
+    for _ in range(args.warmup):
+        ens.step()
+    ens.capture_all()
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    ps0 = int(ens.particle_steps.item())
+    timed = total - args.warmup
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(pg)
+    with ClockSampler(local) as clk:
+        e0.record(st)
+        for _ in range(timed):
+            ens.step()
+        e1.record(st)
+        torch.cuda.synchronize()
+        clk.close_region()
+    ms = e0.elapsed_time(e1)
+    ps = int(ens.particle_steps.item()) - ps0
+    t_max = max_over_ranks(pg, ms / 1e3, ens.device)
+    value = sum_over_ranks(pg, ps, ens.device) / t_max
+    mean_e = float(ens.mean_energy()[0])
+    # the push alone on the current state (read only)
+    prm = ens.params(step_on_device=False)
+    saved = (ens.status.clone(), ens.seg_flags.clone(), ens.moments.clone())
+    for _ in range(3):
+        K.seg_electron_kernel(prm, ens.A, ens.B, ens.E, ens.status, ens.seg_flags, ens.ws, moments=ens.moments)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(st)
+    for _ in range(200):
+        K.seg_electron_kernel(prm, ens.A, ens.B, ens.E, ens.status, ens.seg_flags, ens.ws, moments=ens.moments)
+    ev1.record(st)
+    torch.cuda.synchronize()
+    push_ms = ev0.elapsed_time(ev1) / 200
+    ens.status.copy_(saved[0]); ens.seg_flags.copy_(saved[1]); ens.moments.copy_(saved[2])
+    n_now = ens.A.n()
+    achieved = 80 * n_now / (push_ms * 1e-3) / 1e9
+    peak, kind = peaks()
+    # e2e through the ensemble's step with a swarm caller's per-step host traffic: the field
+    # (one float64 per swarm) from pinned memory before the step, the moments (4 float64 per
+    # swarm) back after it, then a synchronisation
+    E_h = torch.empty(ens.E.numel(), dtype=ens.E.dtype, pin_memory=True)
+    E_h.copy_(ens.E)
+    m_h = torch.empty(ens.moments.numel(), dtype=torch.float64, pin_memory=True)
+    K2 = 1000
+    ps_e0 = int(ens.particle_steps.item())
+    t0 = time.perf_counter()
+    for _ in range(K2):
+        ens.E.copy_(E_h, non_blocking=True)
+        ens.step()
+        m_h.copy_(ens.moments.view(-1), non_blocking=True)
+        torch.cuda.synchronize()
+    el = max_over_ranks(pg, time.perf_counter() - t0, ens.device)
+    ps_e = sum_over_ranks(pg, int(ens.particle_steps.item()) - ps_e0, ens.device)
+    e2e = {"value": ps_e / el, "unit": UNIT, "h2d_bytes_per_step": int(E_h.numel() * E_h.element_size()),
+           "d2h_bytes_per_step": int(m_h.numel() * 8), "steps": K2}
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu:
+        cpu = cpu_swarm100_rate(args.cpu_budget)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": timed, "warmup": args.warmup,
+        "ms_per_step": t_max * 1e3 / timed, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "0-D argon swarm, 100 Td, 1e5 particles from a 1 eV Maxwellian, dt 1 ps, 1e4 steps, "
+                               "float64, 1-bin ES-WPNC merge back to 1e5 past 2e5",
+                   "particles": int(sum(cfg.counts)), "state": "float64 SoA",
+                   "l2": "inputs smaller than L2 (4 MB of particle state): a latency configuration"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "kernel": "k_seg_push<double> (ensemble mode, 80 B per particle-step)",
+                     "launch_ms": push_ms, "particles_per_launch": n_now, "peak_kind": kind},
+        "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(), "device_status": ens.device_status(),
+        "mean_energy_eV": mean_e,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_swarm100_rate(budget):
+    """The oracle's float64 step (push + collide + deposit) on the host cores for the same
+    swarm: 1e5 particles, 100 Td, as many steps as fit the time budget."""
+    import ctypes
+
+    import numpy as np
+    from oracle import oracle as O
+    from boltzmann_gb300 import xsec
+    NN = 3.22e22
+    tab = xsec.analytic_argon(2000)
+    E = np.array([100.0 * 1e-21 * NN / 100.0])
+    per = 100_000
+    rng = np.random.default_rng(0)
+    v = rng.normal(0, math.sqrt(1.0 * 1.5 * 1.17255e11), (per, 3))
+    cap = 2 * per
+    d, t = O.soa_to_aos(np.zeros(per), v[:, 0], v[:, 1], v[:, 2], np.ones(per), cap=cap)
+    dtmp, ttmp = np.zeros((2 * cap, 6)), np.zeros((2 * cap, 4))
+    p = O.make_params(1, L=1.0, bnf=1, dt=1e-12, nn=NN, advect=0, rng_mode=1, precision=64, seed=5,
+                      gas_sigma=math.sqrt(1.380649e-23 * 300.0 / 6.6e-26), xs_table=tab.nsigma(NN), xs_emin=tab.emin,
+                      xs_emax=tab.emax, e_exc=tab.e_exc)
+    p.n_nodes = 1
+    mom = np.zeros((4, 1))
+    lib = O.lib()
+    threads = os.cpu_count() or 1
+    n, done, k = per, 0, 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < budget and k < 10_000:
+        p.step = k
+        nn_ = lib.orc_step_omp(ctypes.byref(p), n, cap, d, t, dtmp, ttmp, E, mom, threads)
+        done += n
+        n = int(nn_)
+        k += 1
+    el = time.perf_counter() - t0
+    return {"value": done / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{per} particles x {k} steps of the same swarm, float64 AoS (reference layout), "
+                      f"OpenMP {threads} threads"}
 
 
 def run_learned(args, world, rank, local, pg):
@@ -689,14 +897,17 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="ccp1024", choices=["ccp1024", "swarm512", "learned", "mlp"],
+    ap.add_argument("--workload", default="ccp1024", choices=["ccp1024", "swarm512", "swarm100", "learned", "mlp"],
                     help="ccp1024: the 2e7-particle CCP (default); swarm512: the batched swarm ensemble; "
-                         "learned: the learned start-up against the plain one; mlp: the network's kernels")
+                         "swarm100: the single FP64 swarm at 100 Td; learned: the learned start-up against the "
+                         "plain one; mlp: the network's kernels")
+    ap.add_argument("--swarm-steps", type=int, default=10_000, help="steps of the swarm100 run, warm-up included")
     ap.add_argument("--particles", type=float, default=2e7)
     ap.add_argument("--cells", type=int, default=1024)
     ap.add_argument("--rsf", type=int, default=50)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-dense", action="store_true", help="skip the dense drop-in push leg")
     ap.add_argument("--no-autotune", action="store_true", help="keep the push's default CTA shape")
     ap.add_argument("--seg-half", type=int, default=2048, help="slots per run of a particle segment")
     ap.add_argument("--te-init", type=float, default=1.0,
@@ -718,6 +929,8 @@ def main():
         run_reference_arm(args, world, rank, pg)
     elif args.workload == "swarm512":
         run_swarms(args, world, rank, local, pg)
+    elif args.workload == "swarm100":
+        run_swarm100(args, world, rank, local, pg)
     elif args.workload == "learned":
         run_learned(args, world, rank, local, pg)
     elif args.workload == "mlp":

@@ -14,7 +14,7 @@ LIB_PATH = os.path.join(PKG, "libbz.so")
 BZ_OK, BZ_ERR_ARG, BZ_ERR_CUDA, BZ_ERR_WORKSPACE, BZ_ERR_UNSUPPORTED, BZ_ERR_TOO_LARGE = 0, 1, 2, 3, 4, 5
 DEV_CAPACITY, DEV_LOOKBACK, DEV_NONFINITE, DEV_BINRANGE = 0x1, 0x2, 0x4, 0x8
 QUIRK_SPLIT_WRAP, QUIRK_DEAD_IONFLAG, QUIRK_TRIGGER_LAST, FIX_MERGE_ENERGY = 0x1, 0x2, 0x4, 0x8
-PER_KEY_TARGETS, MOMENT_EXCITATION = 0x10, 0x20
+PER_KEY_TARGETS, MOMENT_EXCITATION, CLEAR_MOMENTS = 0x10, 0x20, 0x40
 ADVECT_NONE, ADVECT_1D, ADVECT_ENSEMBLE = 0, 1, 2
 XS_TABLE, XS_REF_FITS = 0, 1
 COLL_DIRECT, COLL_NULL = 0, 1
@@ -60,6 +60,7 @@ class Segments(ctypes.Structure):
 
 
 SEG_NEEDS_REPACK = 0x1
+CONS_DIAG_STRIDE = 15  # float64 values per key of the resampling diagnostics
 
 _lib = None
 
@@ -134,6 +135,12 @@ _PROTOS = {
                                            _f64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp, _vp]),
     "bz_push_collide_f32_noalloc": (ctypes.c_int, [_P, Particles, _vp, _i64, Particles, _i64, _vp, _vp, _vp, _vp,
                                                    _vp, _vp, _vp]),
+    "bz_push_noalloc_scratch_address": (ctypes.c_int, [_vp]),
+    "bz_set_wait_limit": (ctypes.c_int, [ctypes.c_uint32]),
+    "bz_wait_limit": (ctypes.c_uint32, []),
+    "bz_lookback_selftest_workspace": (_sz, [_i32]),
+    "bz_lookback_selftest": (ctypes.c_int, [_i32, _i32, _vp, _vp, _sz, _vp, _vp]),
+    "bz_mlp_wait_selftest": (ctypes.c_int, [_i32, _vp, _vp]),
     "bz_mlp_param_count": (ctypes.c_int32, []),
     "bz_mlp_select": (ctypes.c_int, [_i32]),
     "bz_mlp_selected": (ctypes.c_int32, []),

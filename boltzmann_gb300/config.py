@@ -151,21 +151,28 @@ def reference(variant_bins=1, **kw):
     return CCPConfig(bin_edges=edges, bin_fractions=fr, **kw)
 
 
+# The benchmark CCPs resample with the reference's split indexing and trigger but with the
+# energy-conserving merge: the reference's rescale (boltzmann.py:861-869) loses the drift
+# part of the energy, and these runs are to conserve weight, momentum and energy per bin.
+BENCH_QUIRKS = (_lib.QUIRK_SPLIT_WRAP | _lib.QUIRK_DEAD_IONFLAG | _lib.QUIRK_TRIGGER_LAST
+                | _lib.FIX_MERGE_ENERGY)
+
+
 def ccp_256(**kw):
     """1 Torr argon CCP: 256 cells, 2e6 particles at 1 eV, dt = tau/400, 3 bins with
-    edges 4 and 11.5 eV, analytic cross sections."""
+    edges 4 and 11.5 eV, analytic cross sections, energy-conserving merge."""
     base = dict(gridpts=257, pressure_torr=1.0, in_dt=400.0, steps_per_cycle=400, num_particles=2_000_000,
                 Te_init_eV=1.0, ne_profile="uniform", bin_edges=(4.0, 11.5), bin_fractions=(0.7, 0.2, 0.1),
-                xs="analytic", resample_freq=50)
+                xs="analytic", resample_freq=50, quirks=BENCH_QUIRKS)
     base.update(kw)
     return CCPConfig(**base)
 
 
 def ccp_1024(**kw):
     """1 Torr argon CCP scale-up: 1024 cells, 2e7 particles, 5 bins with edges 2, 6,
-    11.5, 15.76 eV, analytic cross sections, float32 state."""
+    11.5, 15.76 eV, analytic cross sections, float32 state, energy-conserving merge."""
     base = dict(gridpts=1025, pressure_torr=1.0, in_dt=400.0, steps_per_cycle=400, num_particles=20_000_000,
                 Te_init_eV=1.0, ne_profile="uniform", bin_edges=(2.0, 6.0, 11.5, 15.76),
-                bin_fractions=(0.4, 0.3, 0.2, 0.07, 0.03), xs="analytic", resample_freq=50)
+                bin_fractions=(0.4, 0.3, 0.2, 0.07, 0.03), xs="analytic", resample_freq=50, quirks=BENCH_QUIRKS)
     base.update(kw)
     return CCPConfig(**base)

@@ -276,11 +276,17 @@ __device__ __forceinline__ uint64_t lb_pack(uint64_t flag, uint32_t s, uint32_t 
     return flag | (uint64_t(c & LB_MASK) << 31) | uint64_t(s & LB_MASK);
 }
 
+// Iteration limits of the bounded device-side waits: each wait's own default, overridden
+// process-wide by bz_set_wait_limit (0 keeps the defaults); launches pass the value.
+constexpr uint32_t WAIT_LIMIT_DEFAULT = 1u << 22;  // look-back polls
+uint32_t host_wait_limit(uint32_t dflt = WAIT_LIMIT_DEFAULT);
+
 // Called by warp 0 of the block that owns ``tile``. Publishes (s, c) as the tile
-// aggregate, waits for predecessors (bounded), publishes the inclusive prefix and
-// returns the exclusive prefix in (*ps, *pc) on lane 0.
+// aggregate, waits for predecessors (at most ``wait_limit`` polls in all), publishes the
+// inclusive prefix and returns the exclusive prefix in (*ps, *pc) on lane 0. A wait that
+// runs out counts the missing tiles as empty and raises BZ_DEV_LOOKBACK.
 __device__ inline void lookback(uint64_t *status_arr, int tile, uint32_t s, uint32_t c, uint32_t *ps, uint32_t *pc,
-                                uint32_t *err) {
+                                uint32_t *err, uint32_t wait_limit) {
     const int lane = threadIdx.x & 31;
     if (tile == 0) {
         if (lane == 0) {
@@ -303,7 +309,7 @@ __device__ inline void lookback(uint64_t *status_arr, int tile, uint32_t s, uint
         unsigned needed = (stop == 31) ? 0xffffffffu : ((1u << (stop + 1)) - 1u);
         unsigned not_ready = __ballot_sync(0xffffffffu, flag == 0) & needed;
         if (not_ready && !timed_out) {
-            if (++spins > (1u << 22)) {
+            if (++spins > wait_limit) {
                 timed_out = true;  // give up waiting: count missing tiles as empty, flag it
                 if (lane == 0) atomicOr(err, BZ_DEV_LOOKBACK);
             } else {

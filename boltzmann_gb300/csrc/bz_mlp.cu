@@ -278,8 +278,8 @@ __device__ __forceinline__ void tc_commit(uint32_t mbar) {
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase) {
-    for (uint32_t it = 0; it < TC_WAIT_LIMIT; ++it) {
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase, uint32_t limit) {
+    for (uint32_t it = 0; it < limit; ++it) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
@@ -311,7 +311,7 @@ __device__ __forceinline__ int canon_off(int r, int c8, int K) { return (r >> 3)
 
 template <int L, bool SAVE>
 __device__ __forceinline__ bool tc_layer(unsigned char *wc, unsigned char *act, const float *bs, uint32_t tmem,
-                                         uint32_t mbar, uint32_t &phase, int row0, int n, float *z, float *y) {
+                                         uint32_t mbar, uint32_t &phase, uint32_t wl, int row0, int n, float *z, float *y) {
     constexpr int K = mlp_in(L), N = mlp_out(L);
     const int tid = threadIdx.x, warp = tid >> 5;
     // every thread's operand writes are complete and visible to the tensor core
@@ -329,7 +329,7 @@ __device__ __forceinline__ bool tc_layer(unsigned char *wc, unsigned char *act, 
         tc_commit(mbar);
     }
     // one decision for the whole block (every thread reaches this barrier)
-    const bool ok = __syncthreads_and(mbar_wait(mbar, phase)) != 0;
+    const bool ok = __syncthreads_and(mbar_wait(mbar, phase, wl)) != 0;
     phase ^= 1u;
     if (!ok) return false;
     tc_fence_after();
@@ -384,7 +384,8 @@ __device__ __forceinline__ bool tc_layer(unsigned char *wc, unsigned char *act, 
 
 template <bool SAVE>
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    k_mlp_fwd_tc(const uint16_t *wb, const float *prm, const float *x, const int32_t *idx, int n, float *y, float *z) {
+    k_mlp_fwd_tc(const uint16_t *wb, const float *prm, const float *x, const int32_t *idx, int n, float *y, float *z,
+                 uint32_t wl) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     // 1024-byte aligned operand region
     unsigned char *base = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023u)) & 1023u);
@@ -441,11 +442,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             u.w = pack_bf16(q1.z, q1.w);
             *reinterpret_cast<uint4 *>(act + canon_off(rl, c8, MLP_IN)) = u;
         }
-        ok = tc_layer<0, SAVE>(wc, act, bs, tmem, mbar, phase, row0, n, z, y) &&
-             tc_layer<1, SAVE>(wc, act, bs, tmem, mbar, phase, row0, n, z, y) &&
-             tc_layer<2, SAVE>(wc, act, bs, tmem, mbar, phase, row0, n, z, y) &&
-             tc_layer<3, SAVE>(wc, act, bs, tmem, mbar, phase, row0, n, z, y) &&
-             tc_layer<4, SAVE>(wc, act, bs, tmem, mbar, phase, row0, n, z, y);
+        ok = tc_layer<0, SAVE>(wc, act, bs, tmem, mbar, phase, wl, row0, n, z, y) &&
+             tc_layer<1, SAVE>(wc, act, bs, tmem, mbar, phase, wl, row0, n, z, y) &&
+             tc_layer<2, SAVE>(wc, act, bs, tmem, mbar, phase, wl, row0, n, z, y) &&
+             tc_layer<3, SAVE>(wc, act, bs, tmem, mbar, phase, wl, row0, n, z, y) &&
+             tc_layer<4, SAVE>(wc, act, bs, tmem, mbar, phase, wl, row0, n, z, y);
         // every TMEM read and shared write of this tile is done before the next one
         tc_fence_before();
         __syncthreads();
@@ -742,7 +743,7 @@ __device__ __forceinline__ void tcb_put_at(unsigned char *at, int rl, int half, 
 
 template <int L>
 __device__ __forceinline__ bool tcb_layer(unsigned char *wtc, unsigned char *dz, unsigned char *dzt,
-                                          unsigned char *at, uint32_t tmem, uint32_t mbar, uint32_t &phase,
+                                          unsigned char *at, uint32_t tmem, uint32_t mbar, uint32_t &phase, uint32_t wl,
                                           int row0, int n, const float *x, const int32_t *idx, const float *z,
                                           float *part, bool first, float (&d)[64]) {
     constexpr int NO = mlp_out(L), NI = mlp_in(L);
@@ -786,7 +787,7 @@ __device__ __forceinline__ bool tcb_layer(unsigned char *wtc, unsigned char *dz,
         }
         tc_commit(mbar);
     }
-    const bool ok = __syncthreads_and(mbar_wait(mbar, phase)) != 0;
+    const bool ok = __syncthreads_and(mbar_wait(mbar, phase, wl)) != 0;
     phase ^= 1u;
     if (!ok) return false;
     tc_fence_after();
@@ -836,7 +837,7 @@ __device__ __forceinline__ bool tcb_layer(unsigned char *wtc, unsigned char *dz,
 
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_mlp_bwd_tc(const uint16_t *wt, const float *x, const float *tg, const float *wcol, const int32_t *idx, int n,
-                 const float *y, const float *z, float *partials, float *loss) {
+                 const float *y, const float *z, float *partials, float *loss, uint32_t wl) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *base = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023u)) & 1023u);
     unsigned char *wtc = base;
@@ -899,11 +900,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 d[j] = e * inv_n;
             }
         }
-        ok = tcb_layer<4>(wtc, dz, dzt, at, tmem, mbar, phase, row0, n, x, idx, z, part, first, d) &&
-             tcb_layer<3>(wtc, dz, dzt, at, tmem, mbar, phase, row0, n, x, idx, z, part, first, d) &&
-             tcb_layer<2>(wtc, dz, dzt, at, tmem, mbar, phase, row0, n, x, idx, z, part, first, d) &&
-             tcb_layer<1>(wtc, dz, dzt, at, tmem, mbar, phase, row0, n, x, idx, z, part, first, d) &&
-             tcb_layer<0>(wtc, dz, dzt, at, tmem, mbar, phase, row0, n, x, idx, z, part, first, d);
+        ok = tcb_layer<4>(wtc, dz, dzt, at, tmem, mbar, phase, wl, row0, n, x, idx, z, part, first, d) &&
+             tcb_layer<3>(wtc, dz, dzt, at, tmem, mbar, phase, wl, row0, n, x, idx, z, part, first, d) &&
+             tcb_layer<2>(wtc, dz, dzt, at, tmem, mbar, phase, wl, row0, n, x, idx, z, part, first, d) &&
+             tcb_layer<1>(wtc, dz, dzt, at, tmem, mbar, phase, wl, row0, n, x, idx, z, part, first, d) &&
+             tcb_layer<0>(wtc, dz, dzt, at, tmem, mbar, phase, wl, row0, n, x, idx, z, part, first, d);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
@@ -996,7 +997,8 @@ static int mlp_forward(const uint16_t *wb, const float *prm, const float *x, con
             if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TC_SMEM)) != cudaSuccess)
                 return BZ_ERR_UNSUPPORTED;
             const int tiles = int(ceil_div(n, TC_ROWS));
-            kern<<<std::min(tiles, num_sms_mlp()), TC_THREADS, TC_SMEM, st>>>(wb, prm, x, idx, n, y, z);
+            kern<<<std::min(tiles, num_sms_mlp()), TC_THREADS, TC_SMEM, st>>>(wb, prm, x, idx, n, y, z,
+                                                                       host_wait_limit(TC_WAIT_LIMIT));
             return cudaGetLastError() == cudaSuccess ? int(BZ_OK) : int(BZ_ERR_CUDA);
         };
         return z ? run_tc(k_mlp_fwd_tc<true>) : run_tc(k_mlp_fwd_tc<false>);
@@ -1030,7 +1032,8 @@ static int mlp_backward(const uint16_t *wt, const float *x, const float *t, cons
             return BZ_ERR_UNSUPPORTED;
         const int slices = mlp_bwd_slices(n);
         float *part = static_cast<float *>(ws);
-        k_mlp_bwd_tc<<<slices, TC_THREADS, TCB_SMEM, st>>>(wt, x, t, wcol, idx, n, y, z, part, loss);
+        k_mlp_bwd_tc<<<slices, TC_THREADS, TCB_SMEM, st>>>(wt, x, t, wcol, idx, n, y, z, part, loss,
+                                                            host_wait_limit(TC_WAIT_LIMIT));
         if (cudaGetLastError() != cudaSuccess) return BZ_ERR_CUDA;
         k_mlp_reduce<<<int(ceil_div(MLP_NPARAM, 256)), 256, 0, st>>>(part, slices, grad);
         return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
@@ -1070,11 +1073,52 @@ static size_t mlp_train_ws(int n) {
            align256(size_t(MLP_NL - 1) * n * MLP_H * 4) + align256(mlp_bwd_ws(n));
 }
 
+// The tensor-core completion wait on its own, in the network kernels' sequence: TMEM
+// allocated, the mbarrier initialised for one arrival, the bounded wait of every thread
+// decided together, BZ_DEV_LOOKBACK on a wait that ran out, TMEM freed. When ``arrive`` is
+// 0 nothing arrives on the mbarrier (no MMA is issued), so the wait runs out after
+// wait_limit polls; when it is 1, thread 0 arrives first and the wait completes.
+__global__ void __launch_bounds__(128, 1) k_mlp_wait_selftest(int arrive, uint32_t wl, uint32_t *done) {
+    __shared__ __align__(8) uint64_t mbar_s;
+    __shared__ uint32_t tmem_slot;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t mbar = smem_u32(&mbar_s);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;" ::"r"(smem_u32(&tmem_slot))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+    if (arrive && tid == 0) {
+        asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(mbar) : "memory");
+    }
+    const bool ok = __syncthreads_and(mbar_wait(mbar, 0u, wl)) != 0;
+    if (!ok && tid == 0) atomicOr(&g_mlp_status, BZ_DEV_LOOKBACK);
+    if (tid == 0) *done = ok ? 1u : 2u;
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;" ::"r"(tmem) : "memory");
+}
+
 }  // namespace bz
 
 using namespace bz;
 
 extern "C" {
+
+int bz_mlp_wait_selftest(int32_t arrive, uint32_t *done, void *stream) {
+    if ((arrive != 0 && arrive != 1) || !done) return BZ_ERR_ARG;
+    k_mlp_wait_selftest<<<1, 128, 0, as_stream(stream)>>>(arrive, host_wait_limit(TC_WAIT_LIMIT), done);
+    return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+}
 
 int32_t bz_mlp_param_count(void) { return MLP_NPARAM; }
 

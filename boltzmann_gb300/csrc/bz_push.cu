@@ -12,7 +12,10 @@
 // (post_processing_1D.py:26-38) leaves. The deposit of post_processing
 // (post_processing_1D.py:44-57, kernels-new.cu:56-132) is accumulated in a per-CTA
 // shared-memory grid and merged into the float64 moments once per CTA.
+#include <cuda.h>
+
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <mutex>
 
@@ -29,7 +32,7 @@ __global__ void __launch_bounds__(PT, BZ_PUSH_MINB) k_push(bz_params p, PushCons
                                              int64_t in_cap, SoA<T> out, int64_t cap, int32_t *counts, const T *E,
                                              const double *R, const double *gas, double *moments,
                                              unsigned int *ticket, uint64_t *tile_status, int max_tiles,
-                                             uint32_t *status) {
+                                             uint32_t *status, uint32_t wait_limit) {
     using A = typename AccT<T>::t;
     extern __shared__ __align__(16) unsigned char smem[];
     const int nf = p.advect ? p.n_faces : 1;
@@ -150,7 +153,7 @@ __global__ void __launch_bounds__(PT, BZ_PUSH_MINB) k_push(bz_params p, PushCons
             }
             uint32_t tot = __shfl_sync(0xffffffffu, wi, PWARPS - 1);
             if (lane < PWARPS) s_warp[lane] = wi - wv;  // exclusive warp offsets
-            lookback(tile_status, tile, tot & 0xffffu, tot >> 16, &s_ps, &s_pc, status);
+            lookback(tile_status, tile, tot & 0xffffu, tot >> 16, &s_ps, &s_pc, status, wait_limit);
             if (lane == 0 && tile == ntiles - 1) {
                 counts[0] = int32_t(s_ps + (tot & 0xffffu));
                 counts[1] = int32_t(s_pc + (tot >> 16));
@@ -258,7 +261,7 @@ static int launch_push_t(const bz_params &p, SoA<T> in, const int32_t *n_in, int
     if (grid > tiles_cap) grid = int(tiles_cap);
     PushConst<T> kc = make_push_const<T>(p);
     kern<<<grid, PT, smem, st>>>(p, kc, in, n_in, in_cap, out, cap, counts, E, R, gas, moments, ticket, tile_status,
-                                 int(std::min<int64_t>(max_tiles, INT32_MAX)), status);
+                                 int(std::min<int64_t>(max_tiles, INT32_MAX)), status, host_wait_limit());
     if (cudaGetLastError() != cudaSuccess) return BZ_ERR_CUDA;
     k_append_children<T><<<num_sms() * 2, 256, 0, st>>>(out, cap, counts, status);
     if (cudaGetLastError() != cudaSuccess) return BZ_ERR_CUDA;
@@ -292,6 +295,9 @@ static int push_entry(const bz_params *pp, P in_, const int32_t *n_in, int64_t i
     cudaStream_t st = as_stream(stream);
     const bool replay = R != nullptr;
     const bool dep = moments != nullptr;
+    if (dep && (p.flags & BZ_CLEAR_MOMENTS) &&
+        cudaMemsetAsync(moments, 0, sizeof(double) * 4 * size_t(p.n_nodes), st) != cudaSuccess)
+        return BZ_ERR_CUDA;
 #define BZ_PUSH_CASE(RP, XSM, DP)                                                                                   \
     if (replay == RP && p.xs_mode == XSM && dep == DP)                                                             \
         return launch_push_t<T, RP, XSM, DP>(p, in, n_in, in_cap, out, cap, counts, E, R, gas, moments, ws, ws_bytes,      \
@@ -332,9 +338,58 @@ __global__ void k_philox(const uint32_t *ctr, const uint32_t *key, int n, int va
     o[0] = r.x; o[1] = r.y; o[2] = r.z; o[3] = r.w;
 }
 
+static std::atomic<uint32_t> g_wait_limit{0};
+uint32_t host_wait_limit(uint32_t dflt) {
+    const uint32_t v = g_wait_limit.load(std::memory_order_relaxed);
+    return v ? v : dflt;
+}
+
+// The look-back wait on its own: CTAs take tiles first_tile, first_tile+1, ... from a
+// ticket and each publishes one survivor; prefix[tile] receives the exclusive prefix the
+// look-back gives. With first_tile = 1 no CTA owns tile 0, so every wait that reaches
+// tile 0 runs out after wait_limit polls, counts it as empty and raises BZ_DEV_LOOKBACK.
+__global__ void k_lookback_selftest(unsigned int *ticket, uint64_t *tile_status, int first_tile, int ntiles,
+                                    uint32_t *prefix, uint32_t *status, uint32_t wait_limit) {
+    if (threadIdx.x >= 32) return;
+    int tile = 0;
+    if (threadIdx.x == 0) tile = int(atomicAdd(ticket, 1u)) + first_tile;
+    tile = __shfl_sync(0xffffffffu, tile, 0);
+    if (tile >= ntiles) return;
+    uint32_t ps = 0, pc = 0;
+    lookback(tile_status, tile, 1u, 0u, &ps, &pc, status, wait_limit);
+    if (threadIdx.x == 0) prefix[tile] = ps;
+}
+
 }  // namespace bz
 
 extern "C" {
+
+int bz_set_wait_limit(uint32_t spins) {
+    bz::g_wait_limit.store(spins, std::memory_order_relaxed);
+    return BZ_OK;
+}
+uint32_t bz_wait_limit(void) { return bz::g_wait_limit.load(std::memory_order_relaxed); }
+
+size_t bz_lookback_selftest_workspace(int32_t ntiles) {
+    return bz::PushWsLayout::ticket_bytes + 8 * size_t(ntiles > 0 ? ntiles : 1);
+}
+
+int bz_lookback_selftest(int32_t ntiles, int32_t first_tile, uint32_t *prefix, void *workspace, size_t workspace_bytes,
+                         uint32_t *status, void *stream) {
+    if (ntiles < 1 || ntiles > (1 << 20) || first_tile < 0 || first_tile > 1 || !prefix || !workspace || !status)
+        return BZ_ERR_ARG;
+    if (workspace_bytes < bz_lookback_selftest_workspace(ntiles)) return BZ_ERR_WORKSPACE;
+    cudaStream_t st = bz::as_stream(stream);
+    if (cudaMemsetAsync(workspace, 0, bz_lookback_selftest_workspace(ntiles), st) != cudaSuccess) return BZ_ERR_CUDA;
+    if (cudaMemsetAsync(prefix, 0xff, sizeof(uint32_t) * size_t(ntiles), st) != cudaSuccess) return BZ_ERR_CUDA;
+    unsigned char *w = static_cast<unsigned char *>(workspace);
+    const int ctas = ntiles - first_tile;
+    if (ctas > 0)
+        bz::k_lookback_selftest<<<ctas, 32, 0, st>>>(reinterpret_cast<unsigned int *>(w),
+                                                     reinterpret_cast<uint64_t *>(w + bz::PushWsLayout::ticket_bytes),
+                                                     first_tile, ntiles, prefix, status, bz::host_wait_limit());
+    return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+}
 
 size_t bz_push_workspace(int64_t capacity) { return bz::PushWsLayout::bytes(capacity); }
 
@@ -379,24 +434,62 @@ static_assert(PushWsLayout::ticket_bytes == 256, "scratch header matches the wor
 // One copy per GPU that loads the library, alive until the process exits.
 static __device__ __align__(256) unsigned char g_push_noalloc_scratch[BZ_PUSH_NOALLOC_SCRATCH_BYTES];
 
-// Device address of the scratch array on the current device. The array's name in host
-// code only stands in for the symbol, so the address is asked of the runtime once per
-// device (with that device current) and remembered.
-constexpr int kMaxDevices = 64;
+// Device address of the scratch array in the current CUDA context. The array's name in
+// host code only stands in for the symbol, so the address is asked of the runtime once per
+// context (with that context current) and remembered under the context's unique id: a
+// host that creates its own contexts, switches between them or resets the device gets
+// the address that belongs to the context it launches in (an id is never reused).
+using PfnCtxGetCurrent = CUresult (*)(CUcontext *);
+using PfnCtxGetId = CUresult (*)(CUcontext, unsigned long long *);
+constexpr int kCtxCache = 64;
 static std::mutex g_noalloc_mu;
-static void *g_noalloc_ptr[kMaxDevices] = {};
+static unsigned long long g_noalloc_ctx[kCtxCache] = {};
+static void *g_noalloc_ptr[kCtxCache] = {};
+static int g_noalloc_next = 0;
+
+static int current_context_id(unsigned long long *id) {
+    static PfnCtxGetCurrent get_cur = nullptr;
+    static PfnCtxGetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_cur = reinterpret_cast<PfnCtxGetCurrent>(f);
+        f = nullptr;
+        q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<PfnCtxGetId>(f);
+    });
+    if (!get_cur || !get_id) return BZ_ERR_CUDA;
+    CUcontext ctx = nullptr;
+    if (get_cur(&ctx) != CUDA_SUCCESS) return BZ_ERR_CUDA;
+    if (!ctx) {  // nothing current yet: make the current device's primary context current
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaSetDevice(dev) != cudaSuccess) return BZ_ERR_CUDA;
+        if (get_cur(&ctx) != CUDA_SUCCESS || !ctx) return BZ_ERR_CUDA;
+    }
+    return get_id(ctx, id) == CUDA_SUCCESS ? BZ_OK : BZ_ERR_CUDA;
+}
 
 static int noalloc_scratch(void **out) {
-    int dev = -1;
-    if (cudaGetDevice(&dev) != cudaSuccess) return BZ_ERR_CUDA;
-    if (dev < 0 || dev >= kMaxDevices) return BZ_ERR_UNSUPPORTED;
+    unsigned long long id = 0;
+    int rc = current_context_id(&id);
+    if (rc != BZ_OK) return rc;
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
-        void *ptr = nullptr;
-        if (cudaGetSymbolAddress(&ptr, g_push_noalloc_scratch) != cudaSuccess || !ptr) return BZ_ERR_CUDA;
-        g_noalloc_ptr[dev] = ptr;
-    }
-    *out = g_noalloc_ptr[dev];
+    for (int i = 0; i < kCtxCache; ++i)
+        if (g_noalloc_ptr[i] && g_noalloc_ctx[i] == id) {
+            *out = g_noalloc_ptr[i];
+            return BZ_OK;
+        }
+    void *ptr = nullptr;
+    if (cudaGetSymbolAddress(&ptr, g_push_noalloc_scratch) != cudaSuccess || !ptr) return BZ_ERR_CUDA;
+    g_noalloc_ctx[g_noalloc_next] = id;  // the oldest entry makes room
+    g_noalloc_ptr[g_noalloc_next] = ptr;
+    g_noalloc_next = (g_noalloc_next + 1) % kCtxCache;
+    *out = ptr;
     return BZ_OK;
 }
 
@@ -412,9 +505,16 @@ int bz_push_collide_f32_noalloc(const bz_params *p, bz_particles_f32 in, const i
     void *scratch = nullptr;
     int rc = bz::noalloc_scratch(&scratch);
     if (rc != BZ_OK) return rc;
-    // the scratch is cleared by the launch (cudaMemsetAsync on the caller's stream)
+    // only the prefix this input needs is used, and cleared by the launch (cudaMemsetAsync
+    // on the caller's stream)
+    const size_t used = bz::PushWsLayout::bytes(in_capacity);
     return bz::push_entry<float>(p, in, n_in, in_capacity, out, out_capacity, counts, E, replay_R, replay_gas,
-                                 moments, scratch, BZ_PUSH_NOALLOC_SCRATCH_BYTES, status, stream);
+                                 moments, scratch, used, status, stream);
+}
+
+int bz_push_noalloc_scratch_address(void **address) {
+    if (!address) return BZ_ERR_ARG;
+    return bz::noalloc_scratch(address);
 }
 
 }  // extern "C"

@@ -437,14 +437,18 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
         // scale the thermal part only: sum w e about the kept mean equals the original
         // thermal energy, so total energy is conserved (the reference's factor includes
         // the drift energy, boltzmann.py:861-869)
+        // (survivors that are all one particle have no kept thermal part to scale: what
+        // the subtraction leaves is rounding, below 1e-12 of their energy, and the factor
+        // stays 1; an original thermal part below zero by rounding counts as zero)
         double th_o = ew - efac * W * (ux * ux + uy * uy + uz * uz);
         double th_k = he - efac * W * (hx * hx + hy * hy + hz * hz);
-        Tfac = sqrt(th_o / th_k);
+        Tfac = th_k > 1e-12 * he ? sqrt(fmax(th_o, 0.0) / th_k) : 1.0;
     } else {
         Tfac = sqrt(T_cell / Te_hat);
     }
     __syncthreads();  // every read of the originals is done before they are zeroed / overwritten
-    double aW = 0, ax = 0, ay = 0, az = 0, ae = 0;
+    double aW = 0, ax = 0, ay = 0, az = 0, ae = 0;  // the survivors as stored
+    double fx = 0, fy = 0, fz = 0, fe = 0;          // the survivors as formed in float64
     #pragma unroll 4
     for (int k = threadIdx.x; k < K; k += RS_T) {
         int id = cnt[k];
@@ -452,6 +456,12 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
         double vx = ux + (double(s.vx[id]) - hx) * Tfac;
         double vy = uy + (double(s.vy[id]) - hy) * Tfac;
         double vz = uz + (double(s.vz[id]) - hz) * Tfac;
+        if (cons_diag) {
+            fx += wbar * vx;
+            fy += wbar * vy;
+            fz += wbar * vz;
+            fe += wbar * (efac * (vx * vx + vy * vy + vz * vz));
+        }
         T tx = T(vx), ty = T(vy), tz = T(vz);
         int64_t q = base + k;
         if (q < dcap) {
@@ -473,10 +483,13 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
         double m[5] = {aW, ax, ay, az, ae};
         block_sum_n<5>(m, shv);
         aW = m[0]; ax = m[1]; ay = m[2]; az = m[3]; ae = m[4];
+        double f[4] = {fx, fy, fz, fe};
+        block_sum_n<4>(f, shv);
         if (threadIdx.x == 0) {
-            double *d = cons_diag + size_t(key) * 10;
+            double *d = cons_diag + size_t(key) * BZ_CONS_DIAG_STRIDE;
             d[0] = W; d[1] = px; d[2] = py; d[3] = pz; d[4] = ew;
             d[5] = aW; d[6] = ax; d[7] = ay; d[8] = az; d[9] = ae;
+            d[10] = wbar * double(K); d[11] = f[0]; d[12] = f[1]; d[13] = f[2]; d[14] = f[3];
         }
     }
 }
@@ -490,7 +503,7 @@ template <typename T>
 __global__ void __launch_bounds__(CT) k_compact(SoAR<T> in, const int32_t *n_ptr, const int32_t *extra,
                                                 int64_t in_cap, SoAR<T> out, int64_t out_cap, int32_t *n_out,
                                                 unsigned int *ticket, uint64_t *tile_status, int max_tiles,
-                                                uint32_t *status) {
+                                                uint32_t *status, uint32_t wait_limit) {
     __shared__ int s_tile;
     __shared__ uint32_t s_ps, s_pc, s_warp[CT / 32];
     int64_t n = int64_t(max(*n_ptr, 0)) + (extra ? int64_t(max(*extra, 0)) : 0);
@@ -533,7 +546,7 @@ __global__ void __launch_bounds__(CT) k_compact(SoAR<T> in, const int32_t *n_ptr
             }
             uint32_t tot = __shfl_sync(0xffffffffu, wi, CT / 32 - 1);
             if (lane < CT / 32) s_warp[lane] = wi - wv;
-            lookback(tile_status, tile, tot, 0u, &s_ps, &s_pc, status);
+            lookback(tile_status, tile, tot, 0u, &s_ps, &s_pc, status, wait_limit);
             if (lane == 0 && tile == ntiles - 1) *n_out = int32_t(min(int64_t(s_ps + tot), out_cap));
         }
         __syncthreads();
@@ -575,7 +588,8 @@ static int launch_compact(SoAR<T> in, const int32_t *n, const int32_t *extra, in
     k_compact<T><<<sms * std::max(per_sm, 1), CT, 0, st>>>(in, n, extra, in_cap, out, out_cap, n_out,
                                                            reinterpret_cast<unsigned int *>(b),
                                                            reinterpret_cast<uint64_t *>(b + 256),
-                                                           int(std::min<int64_t>(max_tiles, INT32_MAX)), status);
+                                                           int(std::min<int64_t>(max_tiles, INT32_MAX)), status,
+                                                           host_wait_limit());
     return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
 }
 
@@ -607,7 +621,7 @@ static int resample_entry(const bz_params *pp, P s_, const int32_t *n, int64_t c
     cudaStream_t st = as_stream(stream);
     k_rs_decide<<<1, 1024, 0, st>>>(counts, hw_counts, p.n_nodes, nb, targets, split_below, merge_at, merge_keep,
                                     p.flags, act, app_off, draw_off, misc, need_out);
-    if (cons_diag && cudaMemsetAsync(cons_diag, 0, sizeof(double) * 10 * nkeys, st) != cudaSuccess) return BZ_ERR_CUDA;
+    if (cons_diag && cudaMemsetAsync(cons_diag, 0, sizeof(double) * BZ_CONS_DIAG_STRIDE * nkeys, st) != cudaSuccess) return BZ_ERR_CUDA;
     SoAR<T> s{s_.x, s_.vx, s_.vy, s_.vz, s_.w};
     SoAR<T> o{out_.x, out_.vx, out_.vy, out_.vz, out_.w};
     k_rs_apply<T><<<nkeys, RS_T, RS_CDF * sizeof(double), st>>>(p, s, n, cap, nb, targets, max_ppc, min_wt,
@@ -682,7 +696,7 @@ static int seg_resample_entry(const bz_params *pp, S s_, P app_, int64_t app_cap
     cudaStream_t st = as_stream(stream);
     k_rs_decide<<<1, 1024, 0, st>>>(counts, hw_counts, p.n_nodes, nb, targets, split_below, merge_at, merge_keep,
                                     p.flags, act, app_off, draw_off, misc, need_out);
-    if (cons_diag && cudaMemsetAsync(cons_diag, 0, sizeof(double) * 10 * nkeys, st) != cudaSuccess) return BZ_ERR_CUDA;
+    if (cons_diag && cudaMemsetAsync(cons_diag, 0, sizeof(double) * BZ_CONS_DIAG_STRIDE * nkeys, st) != cudaSuccess) return BZ_ERR_CUDA;
     SoAR<T> s{s_.x, s_.vx, s_.vy, s_.vz, s_.w};
     SoAR<T> app{app_.x, app_.vx, app_.vy, app_.vz, app_.w};
     k_rs_apply<T><<<nkeys, RS_T, RS_CDF * sizeof(double), st>>>(p, s, nullptr, cap, nb, targets, max_ppc, min_wt,

@@ -556,6 +556,9 @@ static int seg_push_entry(const bz_params *pp, S in_, S out_, const T *E, const 
     Seg<T> in = to_seg<T>(in_), out = to_seg<T>(out_);
     cudaStream_t st = as_stream(stream);
     const bool replay = R != nullptr, dep = moments != nullptr;
+    if (dep && (p.flags & BZ_CLEAR_MOMENTS) &&
+        cudaMemsetAsync(moments, 0, sizeof(double) * 4 * size_t(p.n_nodes), st) != cudaSuccess)
+        return BZ_ERR_CUDA;
     if constexpr (sizeof(T) == 4) {
         if (!replay && p.xs_mode == BZ_XS_TABLE && dep) {  // the hot loop: tunable CTA shape
 #define BZ_SEG_SHAPE(K)                                                                                            \

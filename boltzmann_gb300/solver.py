@@ -160,9 +160,11 @@ class BoltzmannGB300:
     # --------------------------------------------------------------------------------- reference entry points
     def electron_kernel(self):
         """Push + collide the current particles; deposit and compaction are fused in
-        (electron_kernel_numba.py:291-303 with post_processing_1D.py:40-68)."""
-        self.moments.zero_()
-        K.seg_electron_kernel(self.params(), self.A, self.B, self.E_push, self.status, self.seg_flags, self.ws,
+        (electron_kernel_numba.py:291-303 with post_processing_1D.py:40-68). The push
+        clears the moments itself before it deposits."""
+        p = self.params()
+        p.flags |= _lib.CLEAR_MOMENTS
+        K.seg_electron_kernel(p, self.A, self.B, self.E_push, self.status, self.seg_flags, self.ws,
                               moments=self.moments, n_pushed=self.particle_steps)
         self.A, self.B = self.B, self.A
 

@@ -72,9 +72,11 @@ class SwarmConfig:
 def swarm_100td(**kw):
     """One argon swarm: E/N = 100 Td, n = 3.22e22 m^-3, 1e5 equal-weight particles from an
     isotropic 1 eV Maxwellian, dt = 1e-12 s, float64, one energy bin merged back to the
-    1e5 target whenever the count exceeds twice it."""
+    1e5 target whenever the count exceeds twice it (checked every 10 steps: at 100 Td the
+    count grows by well under 1% in 1e4 steps, so no 10 steps can double it). Segments of
+    2 x 256 slots spread the 1e5 particles over ~1000 warps."""
     base = dict(E_over_N_Td=(100.0,), counts=(100_000,), precision="float64", merge_at=2.0, merge_keep=1.0,
-                capacity_factor=5.0)
+                capacity_factor=5.0, resample_every=10, seg_half=256)
     base.update(kw)
     return SwarmConfig(**base)
 
@@ -170,8 +172,9 @@ class SwarmEnsemble:
 
     def electron_kernel(self):
         """One push + collide of every swarm, deposit per swarm fused in."""
-        self.moments.zero_()
-        K.seg_electron_kernel(self.params(), self.A, self.B, self.E, self.status, self.seg_flags, self.ws,
+        p = self.params()
+        p.flags |= _lib.CLEAR_MOMENTS  # the push clears the moments before it deposits
+        K.seg_electron_kernel(p, self.A, self.B, self.E, self.status, self.seg_flags, self.ws,
                               moments=self.moments, n_pushed=self.particle_steps)
         self.A, self.B = self.B, self.A
         # pre-push population = after-push weight minus the children (every ionization

@@ -52,6 +52,8 @@ enum bz_status {
                                         (key = cell*nbins + bin) instead of per bin */
 #define BZ_MOMENT_EXCITATION 0x20u   /* the push's deposit adds sum(w) of the particles that excited
                                         this step to moments row 2 (ns_src, always 0 in the reference) */
+#define BZ_CLEAR_MOMENTS 0x40u       /* the push clears moments (4 x n_nodes float64) before it
+                                        accumulates into them (a memset on the caller's stream) */
 
 /* particle motion (bz_params.advect) */
 #define BZ_ADVECT_NONE 0      /* one 0-D swarm: no drift, E[0] everywhere, every particle in node/cell 0 */
@@ -164,8 +166,11 @@ int bz_bin_f64(const bz_params *p, bz_particles_f64 s, const int32_t *n, int64_t
  * Random numbers: Philox (replay_u == NULL) or replay_u[] consumed in processing order
  * (per key: split draws or merge draws). need_out[0] = 1 when resampling ran.
  * capacity bounds both s and out.
- * cons_diag (optional, [nkeys][10] float64): W, px, py, pz, sum w*energy before the
- * merge, then the same of the stored survivors. */
+ * cons_diag (optional, [nkeys][BZ_CONS_DIAG_STRIDE] float64, zeroed for keys that do not
+ * merge): W, px, py, pz, sum w*energy of the merged originals; the same of the survivors
+ * as stored (weights and velocities in the state's precision); the same of the survivors
+ * as formed in float64 before they are stored (K * W/K and the rescaled velocities). */
+#define BZ_CONS_DIAG_STRIDE 15
 size_t bz_resample_workspace(int64_t capacity, int32_t nkeys);
 int bz_resample_f32(const bz_params *p, bz_particles_f32 s, const int32_t *n, int64_t capacity,
                     bz_particles_f32 out, int32_t *n_out, int32_t nbins, const int32_t *targets,
@@ -331,6 +336,32 @@ int bz_seg_resample_f64(const bz_params *p, bz_segments_f64 s, bz_particles_f64 
                         uint32_t *status, void *stream);
 
 /* ---------------------------------------------------------------------------------- */
+/* bounded device-side waits                                                            */
+/* ---------------------------------------------------------------------------------- */
+/* No counterpart in the reference (its only device-side check is the ion fluid's break
+ * flag, heavies_kernel_1D.py:44-46). Every wait on the device is bounded: the look-back of
+ * bz_push_collide_* and bz_compact_* (default 2^22 polls) and the tensor-core completion
+ * waits of the network kernels (default 2^24 polls). A wait that runs out raises
+ * BZ_DEV_LOOKBACK (the network kernels: in bz_mlp_status), stops waiting and returns.
+ * bz_set_wait_limit sets one limit for all of them (0 restores the defaults);
+ * process-wide, read by later launches. */
+int bz_set_wait_limit(uint32_t spins);
+uint32_t bz_wait_limit(void);
+/* The look-back on its own, for checks of its timeout: ntiles - first_tile single-warp
+ * CTAs take tiles first_tile, first_tile+1, ... and each publishes one survivor;
+ * prefix[tile] receives the exclusive prefix it sees (0xffffffff for tiles nobody took).
+ * first_tile = 1 leaves tile 0 unpublished, so the waits that reach it run out and count
+ * it as empty. workspace: bz_lookback_selftest_workspace(ntiles) bytes. */
+size_t bz_lookback_selftest_workspace(int32_t ntiles);
+int bz_lookback_selftest(int32_t ntiles, int32_t first_tile, uint32_t *prefix, void *workspace,
+                         size_t workspace_bytes, uint32_t *status, void *stream);
+/* The network kernels' tensor-core completion wait on its own (one CTA: TMEM allocated,
+ * mbarrier for one arrival, the bounded wait, TMEM freed). arrive = 1: the arrival comes
+ * and *done = 1; arrive = 0: nothing arrives, the wait runs out, *done = 2 and
+ * BZ_DEV_LOOKBACK is raised in bz_mlp_status. done is a device pointer. */
+int bz_mlp_wait_selftest(int32_t arrive, uint32_t *done, void *stream);
+
+/* ---------------------------------------------------------------------------------- */
 /* allocation-free push                                                                 */
 /* ---------------------------------------------------------------------------------- */
 /* No counterpart in the reference. The same fused push + collide + deposit + compaction
@@ -343,8 +374,10 @@ int bz_seg_resample_f64(const bz_params *p, bz_segments_f64 s, bz_particles_f64 
  * and keeps until the process exits. Limits and behaviour:
  *   - in_capacity may not exceed BZ_PUSH_NOALLOC_MAX_PARTICLES (64 Mi particles);
  *     larger inputs return BZ_ERR_TOO_LARGE and nothing is launched;
- *   - the first call on a device looks up the array's device address (with that device
- *     current); make that first call before capturing any stream;
+ *   - the first call in a CUDA context looks up the array's device address in that
+ *     context (with it current) and remembers it under the context's unique id, so hosts
+ *     that make their own contexts or reset the device get the right address; make that
+ *     first call before capturing any stream;
  *   - every call on a device shares the one array and clears it first, so calls that
  *     overlap on the GPU (two streams, or two threads) race: serialise them;
  *   - nothing is allocated: no cudaMalloc, no cudaFree, no allocating library call. */
@@ -355,6 +388,9 @@ int bz_push_collide_f32_noalloc(const bz_params *p, bz_particles_f32 in, const i
                                 int32_t *counts, const float *E, const double *replay_R,
                                 const double *replay_gas, double *moments, uint32_t *status,
                                 void *stream);
+/* The scratch array's device address in the current context (the set-up of the first
+ * call, run now if it has not run yet); for checks that a context switch is seen. */
+int bz_push_noalloc_scratch_address(void **address);
 
 /* ---------------------------------------------------------------------------------------
  * Surrogate network of the learned CCP start-up (no counterpart in the reference: its

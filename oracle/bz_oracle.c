@@ -550,9 +550,12 @@ int64_t orc_resample(const orc_params *p, int64_t n, double *data, double *tosum
                 if (flags & 2) {
                     /* energy-conserving: scale only the thermal part (kept about its own mean) */
                     double half_m = 0.5 * m_e * j_ev;
+                    /* survivors that are all one particle have no kept thermal part (the
+                       subtraction leaves rounding, below 1e-12 of their energy): factor 1; an
+                       original thermal part below zero by rounding counts as zero */
                     double th_o = 1.5 * T_cell - half_m * (ux * ux + uy * uy + uz * uz);
                     double th_k = 1.5 * Te_hat - half_m * (hx * hx + hy * hy + hz * hz);
-                    Tfac = sqrt(th_o / th_k);
+                    Tfac = th_k > 1e-12 * 1.5 * Te_hat ? sqrt((th_o > 0.0 ? th_o : 0.0) / th_k) : 1.0;
                 } else {
                     Tfac = sqrt(T_cell / Te_hat);
                 }

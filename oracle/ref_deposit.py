@@ -30,7 +30,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
 CUBIN = os.path.join(REF_DIR, "kernels_new.sm_103a.cubin")
-REF_SRC = "/root/reference/1bin/kernels/reduction/cuda_reduction/kernels-new.cu"
+REF_ROOT = os.environ.get("BZ_REFERENCE_ROOT", "/root/reference")
+REF_SRC = os.path.join(REF_ROOT, "1bin", "kernels", "reduction", "cuda_reduction", "kernels-new.cu")
 # the kernels' C++ names (Itanium ABI): reda(double*, double*, double*, int, int, int),
 # redcheck(double*, int, int, int)
 REDA = b"_Z4redaPdS_S_iii"

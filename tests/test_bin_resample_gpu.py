@@ -118,7 +118,7 @@ def run_resample_gpu(x, v, w, N, edges, targets, max_ppc, min_wt, dtype, flags, 
     tg = torch.as_tensor(np.asarray(targets, dtype=np.int32), device="cuda")
     mp = torch.as_tensor(np.asarray(max_ppc, dtype=np.int32), device="cuda")
     ru = None if replay_u is None else torch.as_tensor(np.asarray(replay_u, dtype=np.float64), device="cuda")
-    cd = torch.zeros(nkeys, 10, dtype=torch.float64, device="cuda") if diag else None
+    cd = torch.zeros(nkeys, _lib.CONS_DIAG_STRIDE, dtype=torch.float64, device="cuda") if diag else None
     K.resample(p, s, out, nb, tg, mp, min_wt, split_below, merge_at, merge_keep, perm, offsets, counts, hw, st, ws,
                need=need, replay_u=ru, cons_diag=cd)
     torch.cuda.synchronize()
@@ -168,6 +168,112 @@ def test_resample_conserves_weight_momentum_energy():
     pm = np.abs(b[:, 1:4]).max() + np.sqrt(b[:, 0] * b[:, 4]).max()
     np.testing.assert_allclose(a[:, 1:4], b[:, 1:4], rtol=1e-12, atol=1e-12 * pm * 1e3)
     np.testing.assert_allclose(a[:, 4], b[:, 4], rtol=1e-12)
+
+
+EFAC = 0.5 * 9.10938e-31 * 6.241509e18  # |v|^2 (m/s)^2 -> eV
+U24 = 2.0 ** -24  # unit roundoff of float32
+
+
+def check_merge_conservation(cd, f32):
+    """Per merged key: the survivors as formed in float64 conserve weight, momentum and
+    energy of the originals to 1e-12; as stored they keep weight to 2^-24 relative,
+    momentum to 2.1 * 2^-24 of sum(w|v|) and energy to 3.1 * 2^-24 relative (float32
+    storage: the weight W/K and every velocity component rounded once each, relative error
+    u = 2^-24; a momentum term w v picks up at most (1+u)^2 - 1, an energy term w v^2 at
+    most (1+u)^3 - 1); with float64 storage the stored sums are the formed ones."""
+    merged = cd[:, 0] > 0
+    b, a, f = cd[merged, 0:5], cd[merged, 5:10], cd[merged, 10:15]
+    W, E = b[:, 0], b[:, 4]
+    S = np.sqrt(W * E / EFAC)  # bounds sum(w |v_x|) by Cauchy-Schwarz
+    # formed in float64
+    np.testing.assert_allclose(f[:, 0], W, rtol=1e-12, atol=0)
+    for j in (1, 2, 3):
+        assert np.all(np.abs(f[:, j] - b[:, j]) <= 1e-12 * S), j
+    np.testing.assert_allclose(f[:, 4], E, rtol=1e-12, atol=0)
+    # stored
+    if f32:
+        assert np.all(np.abs(a[:, 0] - W) <= 1.01 * U24 * W)
+        for j in (1, 2, 3):
+            assert np.all(np.abs(a[:, j] - b[:, j]) <= 2.1 * U24 * S + 1e-12 * S), j
+        assert np.all(np.abs(a[:, 4] - E) <= 3.1 * U24 * E + 1e-12 * E)
+    else:
+        np.testing.assert_allclose(a[:, 0], W, rtol=1e-12, atol=0)
+        for j in (1, 2, 3):
+            assert np.all(np.abs(a[:, j] - b[:, j]) <= 1e-12 * S), j
+        np.testing.assert_allclose(a[:, 4], E, rtol=1e-12, atol=0)
+    return int(merged.sum())
+
+
+def test_merge_conserves_on_the_benchmark_path():
+    """The headline configuration's resampling path: float32 segmented state of a 1024-cell
+    1 Torr CCP with a drift, 5 bins (edges 2, 6, 11.5, 15.76 eV), the reference's split
+    indexing and trigger with the energy-conserving merge (the benchmark's setting), split
+    and merge both firing. cons_diag is read for every merged (cell, bin)."""
+    rng = np.random.default_rng(17)
+    N, n, L = 1024, 4_000_000, 2.54
+    x = rng.uniform(0, L, n)
+    e = rng.gamma(1.5, 1.2, n)  # ~1.8 eV mean, tail beyond 15.76 eV thin
+    v = np.sqrt(2 * e / (9.10938e-31 * 6.241509e18))[:, None] * rng.normal(size=(n, 3)) / np.sqrt(3)
+    v += np.array([2.0e5, -5.0e4, 0.0])  # a drift, where the reference's rescale loses energy
+    w = rng.uniform(0.5, 2.0, n)
+    f32 = lambda a: np.asarray(a, dtype=np.float32).astype(np.float64)
+    x, v, w = f32(x), f32(v), f32(w)
+    nb, nkeys = 5, (N + 1) * 5
+    edges = (2.0, 6.0, 11.5, 15.76)
+    T = [600, 400, 200, 70, 30]  # merges in the lower bins, splits in the sparse upper ones
+    seg = K.SegmentSet(-(-2 * n // 2048), 2048)
+    seg.load(x, v[:, 0], v[:, 1], v[:, 2], w)
+    p = grid_params(N, L, _lib.QUIRK_SPLIT_WRAP | _lib.QUIRK_TRIGGER_LAST | _lib.FIX_MERGE_ENERGY)
+    ed = torch.as_tensor(np.asarray(edges), device="cuda")
+    perm = torch.zeros(seg.capacity, dtype=torch.int32, device="cuda")
+    offs = torch.zeros(nkeys + 1, dtype=torch.int32, device="cuda")
+    cnts = torch.zeros(nkeys, dtype=torch.int32, device="cuda")
+    hw = torch.zeros(nkeys, dtype=torch.int32, device="cuda")
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    fl = torch.zeros(1, dtype=torch.int32, device="cuda")
+    need = torch.zeros(1, dtype=torch.int32, device="cuda")
+    ws = K.Workspace()
+    K.seg_bin_particles(p, seg, ed, 0.1, perm, offs, cnts, hw, st, ws)
+    app = K.ParticleSet(2 * n)
+    out = K.SegmentSet(seg.nseg, seg.half)
+    tg = torch.as_tensor(np.asarray(T, dtype=np.int32), device="cuda")
+    mp = torch.as_tensor(np.asarray([10 * t for t in T], dtype=np.int32), device="cuda")
+    cd = torch.zeros(nkeys, _lib.CONS_DIAG_STRIDE, dtype=torch.float64, device="cuda")
+    K.seg_resample(p, seg, app, out, nb, tg, mp, 0.1, 0.5, 3.0, 0.6, perm, offs, cnts, hw, st, fl, ws, need=need,
+                   cons_diag=cd)
+    torch.cuda.synchronize()
+    assert int(st.item()) == 0 and int(need.item()) == 1
+    c = cnts.cpu().numpy().reshape(N + 1, nb)
+    split = (c > 0) & (c < 0.5 * np.asarray(T))
+    assert split.sum() > 100  # both kinds fire
+    assert check_merge_conservation(cd.cpu().numpy(), f32=True) > 1000
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_merge_to_one_survivor_stays_finite(prec):
+    """Keys merged to a single survivor (K = int(0.6 * 2) = 1) have no kept thermal part:
+    the energy-conserving rescale keeps the factor 1 there, so the survivor carries the
+    originals' mean velocity (weight and momentum conserved) and nothing turns non-finite."""
+    rng = np.random.default_rng(4)
+    N, per = 8, 40
+    n = (N + 1) * per
+    dx = 2.54 / N
+    x = np.repeat(np.arange(N + 1) * dx, per) + rng.uniform(-0.3, 0.3, n) * dx
+    x = np.clip(x, 0.0, 2.54 - 1e-6)
+    v = rng.normal(0, 5e5, (n, 3)) + np.array([1e5, 0, 0])
+    w = rng.uniform(0.5, 2.0, n)
+    out, need, st, cd, counts = run_resample_gpu(x, v, w, N, (), [2], [20], 0.1, DT[prec], _lib.FIX_MERGE_ENERGY,
+                                                 diag=True)
+    assert st == 0 and need == 1
+    assert all(np.all(np.isfinite(out[f])) for f in K.ParticleSet.FIELDS)
+    merged = cd[:, 0] > 0
+    assert merged.sum() == N + 1
+    b, a = cd[merged, 0:5], cd[merged, 5:10]
+    rt = 1e-12 if prec == "f64" else 3e-7
+    np.testing.assert_allclose(a[:, 0], b[:, 0], rtol=rt)
+    S = np.sqrt(b[:, 0] * b[:, 4] / EFAC)
+    for j in (1, 2, 3):
+        assert np.all(np.abs(a[:, j] - b[:, j]) <= rt * S)
 
 
 def test_resample_counts_match_oracle_philox():

@@ -337,3 +337,66 @@ def test_steady_state_matches_16_seed_oracle_ensemble():
     assert abs(kiz_g.mean() - kiz_o.mean()) <= 0.01 * kiz_o.mean(), (kiz_g.mean(), kiz_o.mean(),
                                                                        kiz_g.std(ddof=1), kiz_o.std(ddof=1))
     assert 0.5 * np.abs(f_g - f_o).sum() < 0.01, 0.5 * np.abs(f_g - f_o).sum()
+
+
+def test_config1_fp64_swarm_matches_oracle_ensemble():
+    """The benchmark's FP64 swarm (100 Td, 1e5 particles from a 1 eV Maxwellian, dt = 1 ps,
+    1e4 steps, one energy bin merged back to 1e5 past 2e5) run 16 times on the GPU (16
+    independent copies in one ensemble) against 16 float64 oracle swarms of 2e4 particles
+    each (the swarms are 0-D and nothing is merged at these rates, so the particle count
+    only sets the noise). The swarm is still heating at 1e4 steps (about 4.8 eV), so the
+    comparison is of the same moment of the run: the mean energy over the last 1000 steps
+    and the energy distribution at the end within 1% / 0.01 total variation, the
+    ionization count per particle within four counting standard errors."""
+    S, steps, tail = 16, 10_000, 1000
+    cfg = swarm.swarm_100td(E_over_N_Td=(100.0,) * S, counts=(100_000,) * S, seed=7)
+    e = swarm.SwarmEnsemble(cfg)
+    e.run(steps - tail)
+    ion_g = e.acc[1].cpu().numpy().copy()
+    e.reset_averages()
+    e.run(tail)
+    torch.cuda.synchronize()
+    assert e.device_status() == 0
+    me_g = e.mean_energy()
+    ion_g = ion_g + e.acc[1].cpu().numpy()
+    f_g = e.eedf(nbins=32, emin=0.1, emax=100.0).mean(axis=0)
+    n_g = e.counts()
+    assert np.all(n_g < 2 * 100_000)  # never merged
+    tab = xsec.analytic_argon(2000)
+    E = td_to_vcm([100.0])
+    gas = math.sqrt(1.380649e-23 * 300.0 / 6.6e-26)
+    lib = O.lib()
+    import ctypes
+    per = 20_000
+    me_o, ion_o, f_o = [], [], []
+    for s in range(S):
+        rng = np.random.default_rng(500 + s)
+        v = rng.normal(0, math.sqrt(1.0 * 1.5 * 1.17255e11), (per, 3))
+        cap = 2 * per
+        d, t = O.soa_to_aos(np.zeros(per), v[:, 0], v[:, 1], v[:, 2], np.ones(per), cap=cap)
+        dtmp, ttmp = np.zeros((2 * cap, 6)), np.zeros((2 * cap, 4))
+        p = O.make_params(1, L=1.0, bnf=1, dt=1e-12, nn=NN, advect=0, rng_mode=1, precision=64, seed=5000 + s,
+                          gas_sigma=gas, xs_table=tab.nsigma(NN), xs_emin=tab.emin, xs_emax=tab.emax, e_exc=tab.e_exc)
+        p.n_nodes = 1
+        mom = np.zeros((4, 1))
+        n, acc, ion = per, np.zeros(4), 0.0
+        for k in range(steps):
+            p.step = k
+            n_new = lib.orc_step_omp(ctypes.byref(p), n, cap, d, t, dtmp, ttmp, E, mom, os.cpu_count() or 1)
+            assert n_new > 0
+            ion += mom[1, 0]
+            if k >= steps - tail:
+                acc += mom[:, 0]
+            n = int(n_new)
+        me_o.append(acc[3] / acc[0])
+        ion_o.append(ion / per)
+        f_o.append(O.eedf(p, np.zeros(n), d[:n, 3], d[:n, 4], d[:n, 5], t[:n, 0], 32, 0.1, 100.0)[0] / t[:n, 0].sum())
+    me_o, f_o = np.array(me_o), np.mean(f_o, axis=0)
+    ig, io = ion_g.sum() / (S * 100_000), float(np.sum(ion_o)) / S
+    print(f"FP64 swarm, 100 Td, after 1e4 steps: mean energy {me_g.mean():.5g} / {me_o.mean():.5g} eV, "
+          f"ionizations per particle {ig:.4g} / {io:.4g}, EEDF total variation {0.5 * np.abs(f_g - f_o).sum():.4f}")
+    assert abs(me_g.mean() - me_o.mean()) <= 0.01 * me_o.mean(), (me_g.mean(), me_o.mean())
+    # counting noise of the two ionization totals (Poisson)
+    sig = math.sqrt(ig / (S * 100_000) + io / (S * per))
+    assert io > 0 and abs(ig - io) <= 4 * sig, (ig, io, sig)
+    assert 0.5 * np.abs(f_g - f_o).sum() < 0.01, 0.5 * np.abs(f_g - f_o).sum()
