@@ -690,7 +690,7 @@ def cpu_swarm100_rate(budget):
     per = 100_000
     rng = np.random.default_rng(0)
     v = rng.normal(0, math.sqrt(1.0 * 1.5 * 1.17255e11), (per, 3))
-    cap = 2 * per
+    cap = 3 * per  # the oracle's step wants room for a child of every particle
     d, t = O.soa_to_aos(np.zeros(per), v[:, 0], v[:, 1], v[:, 2], np.ones(per), cap=cap)
     dtmp, ttmp = np.zeros((2 * cap, 6)), np.zeros((2 * cap, 4))
     p = O.make_params(1, L=1.0, bnf=1, dt=1e-12, nn=NN, advect=0, rng_mode=1, precision=64, seed=5,
@@ -705,6 +705,8 @@ def cpu_swarm100_rate(budget):
     while time.perf_counter() - t0 < budget and k < 10_000:
         p.step = k
         nn_ = lib.orc_step_omp(ctypes.byref(p), n, cap, d, t, dtmp, ttmp, E, mom, threads)
+        if nn_ < 0:
+            raise RuntimeError("oracle step refused: sample outgrew its buffers")
         done += n
         n = int(nn_)
         k += 1

@@ -212,7 +212,9 @@ def test_merge_conserves_on_the_benchmark_path():
     rng = np.random.default_rng(17)
     N, n, L = 1024, 4_000_000, 2.54
     x = rng.uniform(0, L, n)
-    e = rng.gamma(1.5, 1.2, n)  # ~1.8 eV mean, tail beyond 15.76 eV thin
+    e = rng.gamma(1.5, 1.2, n)  # ~1.8 eV mean: the sparse 11.5-15.76 eV bin splits
+    hot = rng.uniform(size=n) < 0.05
+    e[hot] = rng.uniform(20.0, 40.0, int(hot.sum()))  # the open top bin overflows: the trigger fires
     v = np.sqrt(2 * e / (9.10938e-31 * 6.241509e18))[:, None] * rng.normal(size=(n, 3)) / np.sqrt(3)
     v += np.array([2.0e5, -5.0e4, 0.0])  # a drift, where the reference's rescale loses energy
     w = rng.uniform(0.5, 2.0, n)

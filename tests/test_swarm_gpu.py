@@ -372,7 +372,7 @@ def test_config1_fp64_swarm_matches_oracle_ensemble():
     for s in range(S):
         rng = np.random.default_rng(500 + s)
         v = rng.normal(0, math.sqrt(1.0 * 1.5 * 1.17255e11), (per, 3))
-        cap = 2 * per
+        cap = 3 * per
         d, t = O.soa_to_aos(np.zeros(per), v[:, 0], v[:, 1], v[:, 2], np.ones(per), cap=cap)
         dtmp, ttmp = np.zeros((2 * cap, 6)), np.zeros((2 * cap, 4))
         p = O.make_params(1, L=1.0, bnf=1, dt=1e-12, nn=NN, advect=0, rng_mode=1, precision=64, seed=5000 + s,
