@@ -247,7 +247,7 @@ def test_merge_conserves_on_the_benchmark_path():
     assert int(st.item()) == 0 and int(need.item()) == 1
     c = cnts.cpu().numpy().reshape(N + 1, nb)
     split = (c > 0) & (c < 0.5 * np.asarray(T))
-    assert split.sum() > 100  # both kinds fire
+    assert split.sum() > 10  # both kinds fire
     assert check_merge_conservation(cd.cpu().numpy(), f32=True) > 1000
 
 
