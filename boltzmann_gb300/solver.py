@@ -23,6 +23,27 @@ from .config import CCPConfig
 KTM = 1.5 * 1.17255e11  # (m/s)^2 per eV of temperature (boltzmann.py:263)
 
 
+class CycleAverages:
+    """Cycle averages of the step loop (boltzmann.py:681-701): the fields after every step
+    whose number (counted from 1) is not a multiple of steps_per_cycle are summed; after
+    the cycle's last step the sums are divided by steps_per_cycle. The reference leaves
+    that last step out of the sums and still divides by the full count; so does this."""
+
+    def __init__(self, like):
+        self.acc = {k: torch.zeros_like(v) for k, v in like.items()}
+
+    def add(self, fields):
+        for k, v in self.acc.items():
+            v.add_(fields[k])
+
+    def take(self, spc):
+        """The averages of the cycle that just ended; the sums start again from zero."""
+        ca = {k: v / spc for k, v in self.acc.items()}
+        for v in self.acc.values():
+            v.zero_()
+        return ca
+
+
 class BoltzmannGB300:
     def __init__(self, cfg: CCPConfig, device="cuda", capacity=None):
         self.cfg = cfg
@@ -332,20 +353,27 @@ class BoltzmannGB300:
             self.ws.get("seg_bin", lib.bz_seg_bin_workspace(self.A.nseg, self.A.capacity))
             self.ws.get("seg_resample", lib.bz_seg_resample_workspace(self.A.nseg, self.A.capacity, nkeys))
 
-    def run(self, num_steps, name="", restart_cyclenum=0, use_graph=True, write=False):
+    def grid_fields(self):
+        """The grid fields the step loop averages over a cycle: ne (this step's deposit),
+        ni, Te and E after the step."""
+        return {"ne": self.moments[0], "ni": self.ni, "Te": self.Te, "E": self.E}
+
+    def run(self, num_steps, name="", restart_cyclenum=0, use_graph=True, write=False, on_step=None):
         """The step loop (boltzmann.py:565-716), with cycle averages and, when ``write``,
-        the reference's per-cycle output files."""
-        cfg = self.cfg
-        spc = cfg.steps_per_cycle
-        acc = {k: torch.zeros_like(getattr(self, k)) for k in ("ni", "Te", "E")}
-        acc["ne"] = torch.zeros_like(self.moments[0])
+        the reference's per-cycle output files. At every cycle's end the ion production
+        total (g2, written as ionprod_total) starts again from zero, as the reference's
+        loop resets it (boltzmann.py:713-714). ``on_step(solver)``, when given, is called
+        after every step (before that step's averaging and output)."""
+        spc = self.cfg.steps_per_cycle
+        avg = CycleAverages(self.grid_fields())
         for _ in range(num_steps):
             self.step(use_graph=use_graph)
+            if on_step is not None:
+                on_step(self)
             if (self.bigstep % spc) != 0:
-                acc["ne"].add_(self.moments[0]); acc["ni"].add_(self.ni)
-                acc["Te"].add_(self.Te); acc["E"].add_(self.E)
+                avg.add(self.grid_fields())
             else:
-                ca = {k: (v / spc) for k, v in acc.items()}
+                ca = avg.take(spc)
                 if not self._brk_warned and int(self.brk.item()):
                     # the reference prints a warning and runs on (heavies_kernel_1D.py:44-46)
                     self._brk_warned = True
@@ -354,8 +382,7 @@ class BoltzmannGB300:
                 if write:
                     from . import io as bzio
                     bzio.data_write(self, name, self.bigstep // spc + restart_cyclenum, ca)
-                for v in acc.values():
-                    v.zero_()
+                self.g2.zero_()
         return self
 
     # --------------------------------------------------------------------------------- learned start-up

@@ -355,7 +355,64 @@ def case_field(seed, gridpts=65):
     print("field N", N)
 
 
+# ------------------------------------------------------------------------------------------
+# the step loop's cycle averages and per-cycle output files (BoltzmannDSMC.run)
+# ------------------------------------------------------------------------------------------
+
+def case_cycle(seed, gridpts=9, Nc_arg=96, spc=3, cycles=2):
+    """The reference's own run loop (boltzmann.py:565-716) for two short RF cycles: every
+    step's grid fields as the loop accumulates them (recorded around its EF_kernel call),
+    and the bytes of every file its data_write (data_write_1D.py:3-75) wrote."""
+    import tempfile
+    ns = rs.load_variant("1bin")
+    rs.DRAWS.reset(seed)
+    tmp = tempfile.mkdtemp(prefix="bz_cycle_")
+    name = os.path.join(tmp, "ref_")
+    steps = spc * cycles
+    b = ns.BoltzmannDSMC(steps, name, 0, Nc_arg, gridpts, 4, 1, False, 1000, 400.0, spc)
+    # two thirds of the electrons at 40 eV, so that the short run ionizes (the ion
+    # production file then has something to reset between cycles)
+    rng = np.random.default_rng(seed)
+    n = b.Nc_list[0]
+    hot = np.arange(n) % 3 != 0
+    data, tosum = b.big_data_ar_list[0], b.big_tosum_ar_list[0]
+    vh = speed_for_energy(np.full(int(hot.sum()), 40.0))[:, None] * iso_dirs(rng, int(hot.sum()))
+    data[np.nonzero(hot)[0], 3:6] = vh
+    v = np.asarray(data[0:n, 3:6])
+    tosum[0:n, 3] = 0.5 * M_E * J_EV * (v * v).sum(axis=1)
+    rec = {"ne": [], "ni": [], "Te": [], "E": [], "ni_src": []}
+    ef = b.EF_kernel
+
+    def ef_rec(*a):
+        V, E = ef(*a)
+        rec["ne"].append(np.array(b.ne_ar, dtype=np.float64))
+        rec["ni"].append(np.array(b.ni_ar, dtype=np.float64))
+        rec["Te"].append(np.array(b.Te_ar, dtype=np.float64))
+        rec["E"].append(np.array(E, dtype=np.float64))
+        rec["ni_src"].append(np.array(b.ni_src, dtype=np.float64))
+        return V, E
+
+    b.EF_kernel = ef_rec
+    b.run(steps, name, 0)
+    files = sorted(os.listdir(tmp))
+    blobs = {}
+    for f in files:
+        with open(os.path.join(tmp, f), "rb") as fh:
+            blobs[f[len("ref_"):]] = np.frombuffer(fh.read(), dtype=np.uint8)
+    out = {f"rec_{k}": np.stack(v) for k, v in rec.items()}
+    out.update({f"file_{k}": v for k, v in blobs.items()})
+    np.savez_compressed(os.path.join(HERE, "cycle.npz"), spc=spc, cycles=cycles, N=b.N,
+                        file_names=np.array(sorted(blobs)), **out)
+    for f in files:
+        os.remove(os.path.join(tmp, f))
+    os.rmdir(tmp)
+    print("cycle: steps", steps, "files", len(blobs))
+
+
 def main():
+    if "--cycle" in sys.argv:  # only the run-loop fixture
+        case_cycle(seed=50)
+        return
     ns = rs.load_variant("1bin")
     # 1 Torr, dt = tau/400: many collisions and ionizations per step
     case_push(ns, "push_1torr.npz", 3.22e16 * 1.0 * 1e6, TAU / 400.0, Te=8.0, seed=11)
@@ -366,6 +423,7 @@ def main():
     for i, var in enumerate(("1bin", "3bin", "5bin")):
         case_resample(var, seed=30 + i)
     case_field(seed=40)
+    case_cycle(seed=50)
 
 
 if __name__ == "__main__":

@@ -152,7 +152,7 @@ def test_deposit_matches_reference_golden(prec):
         np.testing.assert_allclose(mom[j], g[k], rtol=tol, atol=tol * np.abs(g[k]).max())
 
 
-def philox_case(n, N, seed, prec, gas_sigma, coll_model=_lib.COLL_DIRECT, Te=6.0):
+def philox_case(n, N, seed, prec, gas_sigma, coll_model=_lib.COLL_DIRECT, Te=6.0, tab=None):
     rng = np.random.default_rng(seed)
     L = 2.54
     x = rng.uniform(1e-4, L - 1e-4, n).astype(np.float32).astype(np.float64)
@@ -160,7 +160,7 @@ def philox_case(n, N, seed, prec, gas_sigma, coll_model=_lib.COLL_DIRECT, Te=6.0
     v = rng.normal(0, sig, (n, 3)).astype(np.float32).astype(np.float64)
     w = rng.uniform(1e4, 1e5, n).astype(np.float32).astype(np.float64)
     E = rng.uniform(-2000, 2000, N).astype(np.float32).astype(np.float64)
-    tab = xsec.analytic_argon(2000)
+    tab = tab or xsec.analytic_argon(2000)
     nn = 3.22e22
     nst = tab.nsigma(nn)
     dt = 1.0 / 13.56e6 / 400
@@ -201,6 +201,42 @@ def test_push_philox_table_matches_oracle(prec, coll_model):
     for j in (0, 1, 3):
         allow = node_allowance(xw, col[j], gp.L, gp.n_faces, 4, prec == "f32")
         check_moments(mom[j], mom_o[j], mt, allow)
+
+
+def lxcat_text(rng):
+    """An LXCat-style cross-section file (ELASTIC / EXCITATION / IONIZATION blocks: a
+    header, the species, a mass-ratio or threshold line, a table between dashed lines)
+    holding argon-like cross sections tabulated at irregular energies, with comment lines
+    in between, as the format carries them."""
+    def block(kind, thr_line, e, sig):
+        rows = "\n".join(f"{a:.6e}\t{b:.6e}" for a, b in zip(e, sig))
+        return (f"{kind}\nAr\n {thr_line}\nSPECIES: e / Ar\nPROCESS: E + Ar -> E + Ar, {kind.title()}\n"
+                f"COLUMNS: Energy (eV) | Cross section (m2)\n-----------------------------\n{rows}\n"
+                f"-----------------------------\n\n")
+    e = np.sort(np.concatenate([[0.0], 10 ** rng.uniform(-2.2, 3.1, 300)]))
+    el = np.minimum(1e-19 * np.maximum(e, 1e-3) ** 0.3, 1.5e-19)
+    ex_e = np.concatenate([[11.5], np.sort(11.5 + 10 ** rng.uniform(-3, 3, 150))])
+    ex = 3e-21 * np.log(ex_e / 11.5) / (ex_e / 11.5)
+    io_e = np.concatenate([[15.76], np.sort(15.76 + 10 ** rng.uniform(-3, 3, 150))])
+    io = 3e-20 * np.log(io_e / 15.76) / (io_e / 15.76)
+    return ("xxxxxxxx comment lines of the database header xxxxxxxx\n\n" + block("ELASTIC", "1.360000e-5", e, el)
+            + block("EXCITATION", "1.150000e+1", ex_e, ex) + block("IONIZATION", "1.576000e+1", io_e, io))
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_push_with_an_ingested_lxcat_table_matches_oracle(prec):
+    """Cross sections ingested from LXCat-style text (xsec.read_lxcat, in place of the
+    reference's hard-coded fits, electron_kernel_numba.py:66-174) drive the GPU push and the
+    oracle alike: same particles, counts exact, states to the push tolerances."""
+    tab = xsec.read_lxcat(lxcat_text(np.random.default_rng(77)), n=2000)
+    assert abs(tab.e_exc - 11.5) < 1e-12 and np.all(tab.sigma >= 0) and tab.sigma[2].max() > 0
+    x, v, w, E, gp, (data, tosum, nni, nnew, mom_o, vs) = philox_case(100_000, 256, 13, prec, 6.74e4, tab=tab)
+    cnt, out, mom, st = gpu_push(x, v, w, E, gp, DT[prec])
+    assert st == 0
+    assert int(cnt[1]) == nni and nni > 0
+    assert int(cnt[2]) == nnew
+    rtol = 1e-10 if prec == "f64" else 1e-6
+    check_state(out, data[:nnew, 0], data[:nnew, 3:6], tosum[:nnew, 0], rtol, dt=gp.dt, vscale=vs)
 
 
 def test_push_is_deterministic():

@@ -89,3 +89,34 @@ def test_snapshot_restore_returns_the_state():
     torch.cuda.synchronize()
     assert sol.device_status() == 0 and int(sol.particle_steps.item()) > ps
     assert torch.isfinite(sol.E).all()
+
+
+def test_run_writes_cycle_files_like_the_reference_loop(tmp_path):
+    """solver.run over two short cycles with output: every cycle's *_CA files hold the
+    mean the reference's loop forms (the fields after the cycle's first spc-1 steps,
+    divided by spc; boltzmann.py:681-701), and ionprod_total holds that cycle's ion
+    sources only (the reference resets it every cycle, boltzmann.py:713-714). The fields
+    are recorded after every step of the same run through run()'s per-step hook."""
+    spc = 5
+    sol = BoltzmannGB300(small_cfg(num_particles=20_000, gridpts=33, steps_per_cycle=spc, Te_init_eV=6.0))
+    name = str(tmp_path / "run_")
+    rec, srcs = [], []
+
+    def record(s):
+        rec.append({f: v.cpu().numpy().copy() for f, v in s.grid_fields().items()})
+        srcs.append(s.moments[1].cpu().numpy().copy())
+
+    sol.run(2 * spc, name=name, write=True, on_step=record)
+    torch.cuda.synchronize()
+    assert sol.device_status() == 0 and len(rec) == 2 * spc
+    for c in (1, 2):
+        steps = rec[(c - 1) * spc: c * spc]
+        for f in ("ne", "ni", "Te", "E"):
+            exp = np.sum([st[f] for st in steps[:-1]], axis=0) / spc
+            got = bzio.read_grid(name, c, f + "_CA")
+            np.testing.assert_allclose(got, exp, rtol=1e-12, atol=1e-12 * np.abs(exp).max())
+        ion = bzio.read_grid(name, c, "ionprod_total")
+        exp = np.sum(srcs[(c - 1) * spc: c * spc], axis=0)
+        np.testing.assert_allclose(ion, exp, rtol=1e-12, atol=1e-12 * max(np.abs(exp).max(), 1.0))
+        np.testing.assert_array_equal(bzio.read_grid(name, c, "ne"), steps[-1]["ne"])
+    assert np.sum(srcs) > 0  # the hot start ionizes
