@@ -32,9 +32,13 @@ struct RsWs {
         misc = draw_off + al(4 * k);
         cdf = misc + 256;
         cnt = cdf + al(8 * c);
-        total = cnt + al(12 * c);  // three int32 regions: counts, candidate ids, copy targets
+        // six int32 regions of the key's list length: draw counts, candidate ids, copy
+        // targets, and for the split's divisions the target groups (starts, fill, members)
+        total = cnt + al(24 * c);
     }
 };
+
+constexpr size_t RS_APPLY_SMEM = RS_CDF * (sizeof(double) + sizeof(int32_t));
 
 // misc[0] = total appended, misc[1] = need flag
 __global__ void __launch_bounds__(1024) k_rs_decide(const int32_t *counts, const int32_t *hw_counts, int n_nodes,
@@ -132,6 +136,24 @@ __device__ __forceinline__ int upper_bound_d(const double *a, int n, double v) {
     int lo = 0, hi = n;
     while (lo < hi) { int m = (lo + hi) >> 1; if (__double_as_longlong(a[m]) <= vb) lo = m + 1; else hi = m; }
     return lo;
+}
+
+// The split's draws in the integer domain. A Philox draw is u = (2k+1) 2^-53 with k the
+// 52-bit integer of two output words (rs_uniform). With X = cdf 2^53 (exact: a power-of-two
+// scaling) and H = 2 floor(X) + [X not an integer], cdf > u holds exactly when H > 2(2k+1),
+// so the binary search for the first cumulative weight above u runs on 64-bit integers
+// and gives the index the float64 search gives.
+__device__ __forceinline__ uint64_t cdf_key(double c) {
+    const double X = c * 0x1p53;
+    const double G = floor(X);
+    return 2ull * uint64_t(G) + (X != G ? 1ull : 0ull);
+}
+__device__ __forceinline__ int draw_index(const uint64_t *H, int n, uint32_t a, uint32_t b) {
+    const uint64_t k = (uint64_t(a >> 6) << 26) | uint64_t(b >> 6);
+    const uint64_t v = 4ull * k + 2ull;  // 2 (2k + 1)
+    int lo = 0, hi = n;
+    while (lo < hi) { int m = (lo + hi) >> 1; if (H[m] <= v) lo = m + 1; else hi = m; }
+    return lo < n ? lo : n - 1;
 }
 
 // block helpers (RS_T threads)
@@ -264,7 +286,8 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
     const int tk = (p.flags & BZ_PER_KEY_TARGETS) ? key : b;  // target / max_ppc entry
     const int64_t T_ = targets[tk];
     const double efac = 0.5 * m_e() * j_ev();
-    extern __shared__ double cdf_sh[];
+    extern __shared__ double cdf_sh[];  // RS_CDF doubles, then RS_CDF int32 draw counts
+    int32_t *cnt_sh = reinterpret_cast<int32_t *>(cdf_sh + RS_CDF);
     // table length: the split's candidates (at most n_k) or the merge's first max_ppc
     const int tab_len = (a == ACT_SPLIT) ? n_k : min(n_k, int(max_ppc[tk]));
     double *cdf = tab_len <= RS_CDF ? cdf_sh : ws_cdf + off;
@@ -273,14 +296,26 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
         // ---- split (boltzmann.py:806-823): candidates w > min_wt, in index order
         int nhw = 0;
         double W = 0.0;
-        // compact candidates into cnt[] (their particle ids) with a block scan, chunk by chunk
-        for (int c0 = 0; c0 < n_k; c0 += RS_T) {
-            int j = c0 + threadIdx.x;
-            int id = j < n_k ? perm[off + j] : -1;
-            bool hw = id >= 0 && above_min(s.w[id], min_wt, wmin_f);
+        // compact candidates into cnt[] (their particle ids), RS_ITEMS consecutive entries per
+        // thread and one block scan per RS_T * RS_ITEMS entries
+        for (int c0 = 0; c0 < n_k; c0 += RS_T * RS_ITEMS) {
+            const int j0 = c0 + threadIdx.x * RS_ITEMS;
+            int ids[RS_ITEMS];
+            uint32_t hwm = 0;
+            int local = 0;
+#pragma unroll
+            for (int i = 0; i < RS_ITEMS; ++i) {
+                ids[i] = j0 + i < n_k ? perm[off + j0 + i] : -1;
+                if (ids[i] >= 0 && above_min(s.w[ids[i]], min_wt, wmin_f)) {
+                    hwm |= 1u << i;
+                    ++local;
+                }
+            }
             int64_t tot;
-            int64_t pos = block_excl_scan<int64_t>(hw ? 1 : 0, shi, &tot);
-            if (hw) cnt[nhw + pos] = id;
+            int64_t pos = block_excl_scan<int64_t>(local, shi, &tot);
+#pragma unroll
+            for (int i = 0; i < RS_ITEMS; ++i)
+                if ((hwm >> i) & 1u) cnt[nhw + pos++] = ids[i];
             nhw += int(tot);
         }
         __syncthreads();
@@ -298,81 +333,135 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
         const double inv_W = 1.0 / W;
         block_cumsum(nhw, [&](int j) { return cdf[j] * inv_W; }, cdf, shd);  // in place
         __syncthreads();
-        const double last = cdf[nhw - 1];
-        const double inv_last = 1.0 / last;
-        for (int j = threadIdx.x; j < nhw; j += RS_T) cdf[j] = cdf[j] * inv_last;
-        __syncthreads();
-        // scratch regions of this key: cnt = draw counts, hw_ids = candidate ids, tgt = copy targets
+        const double inv_last = 1.0 / cdf[nhw - 1];
+        // scratch regions of this key: hw_ids = candidate ids, tgt = copy targets, and the
+        // target groups of the divisions (gstart, gfill, gmem); the draw counts sit in shared
+        // memory when the table does, else in cnt
         int32_t *hw_ids = ws_cnt + cap + off;
         int32_t *tgt = ws_cnt + 2 * cap + off;
-        for (int j = threadIdx.x; j < nhw; j += RS_T) hw_ids[j] = cnt[j];
+        int32_t *gstart = ws_cnt + 3 * cap + off;
+        int32_t *gfill = ws_cnt + 4 * cap + off;
+        int32_t *gmem = ws_cnt + 5 * cap + off;
+        int32_t *dcnt = nhw <= RS_CDF ? cnt_sh : cnt;
+        const bool ints = replay_u == nullptr;  // Philox draws: the table as integer keys
+        uint64_t *H = reinterpret_cast<uint64_t *>(cdf);
+        for (int j = threadIdx.x; j < nhw; j += RS_T) {
+            const double c = cdf[j] * inv_last;
+            if (ints) H[j] = cdf_key(c);
+            else cdf[j] = c;
+            hw_ids[j] = cnt[j];
+        }
         __syncthreads();
-        for (int j = threadIdx.x; j < nhw; j += RS_T) cnt[j] = 0;
+        for (int j = threadIdx.x; j < nhw; j += RS_T) {
+            dcnt[j] = 0;
+            gstart[j] = 0;
+        }
         __syncthreads();
         const int m = int(2 * T_ - n_k);
-        for (int k = threadIdx.x; k < m; k += RS_T) {
-            double u = rs_uniform(rng, replay_u, draw_off[key], key, k);
-            int ix = upper_bound_d(cdf, nhw, u);
-            if (ix > nhw - 1) ix = nhw - 1;
-            atomicAdd(&cnt[ix], 1);
-        }
-        __syncthreads();
-        if (p.flags & BZ_QUIRK_SPLIT_WRAP) {
-            // HW_ids[unique_ids[v]]: the drawn particle id indexes the candidate list and
-            // CuPy wraps it modulo the list length (boltzmann.py:818-823). Two entries may
-            // land on the same particle and divide its weight twice, in entry order. Warp 0
-            // takes 32 entries at a time; lanes that share a target go one after another in
-            // lane (= entry) order, the others at once.
-            if (threadIdx.x < 32) {
-                const int lane = threadIdx.x;
-                for (int j0 = 0; j0 < nhw; j0 += 32) {
-                    const int j = j0 + lane;
-                    const int c = j < nhw ? cnt[j] : 0;
-                    const int t = c ? hw_ids[hw_ids[j] % nhw] : -1;
-                    const unsigned grp = __match_any_sync(0xffffffffu, t);
-                    unsigned pending = __ballot_sync(0xffffffffu, c != 0);
-                    while (pending) {  // at most 32 rounds: each round serves every group's first lane
-                        const bool now = ((pending >> lane) & 1u) && !(grp & pending & ((1u << lane) - 1u));
-                        if (now) {
-                            const double wt = double(s.w[t]) / double(c + 1);
-                            s.w[t] = T(wt);
-                            cdf[j] = double(T(wt));  // weight of this entry's copies
-                            tgt[j] = t;
-                        }
-                        __syncwarp();  // this round's weights are visible to the next
-                        pending &= ~__ballot_sync(0xffffffffu, now);
-                    }
-                }
+        if (ints) {
+            // draws 2i and 2i+1 come from one Philox call (rs_uniform's stream)
+            for (int i = threadIdx.x; 2 * i < m; i += RS_T) {
+                const u32x4 r = philox(uint32_t(key), uint32_t(i), rng.s0, 3u | (rng.s1 << 8), rng.k0, rng.k1);
+                atomicAdd(&dcnt[draw_index(H, nhw, r.x, r.y)], 1);
+                if (2 * i + 1 < m) atomicAdd(&dcnt[draw_index(H, nhw, r.z, r.w)], 1);
             }
         } else {
-            for (int j = threadIdx.x; j < nhw; j += RS_T) {
-                int c = cnt[j];
-                if (!c) continue;
-                int t = hw_ids[j];
-                double wt = double(s.w[t]) / double(c + 1);
-                s.w[t] = T(wt);
-                cdf[j] = double(T(wt));
-                tgt[j] = t;
+            for (int k = threadIdx.x; k < m; k += RS_T) {
+                const double u = replay_u[draw_off[key] + k];
+                int ix = upper_bound_d(cdf, nhw, u);
+                if (ix > nhw - 1) ix = nhw - 1;
+                atomicAdd(&dcnt[ix], 1);
             }
         }
         __syncthreads();
-        // copies, in entry order: exclusive scan of counts
-        int64_t carry2 = 0;
-        for (int c0 = 0; c0 < nhw; c0 += RS_T) {
-            int j = c0 + threadIdx.x;
-            int c = j < nhw ? cnt[j] : 0;
-            int64_t tot;
-            int64_t ex = block_excl_scan<int64_t>(c, shi, &tot);
-            if (c) {
-                int t = tgt[j];
-                T xx = s.x[t], a1 = s.vx[t], a2 = s.vy[t], a3 = s.vz[t], ww = T(cdf[j]);
-                for (int r = 0; r < c; ++r) {
-                    int64_t q = base + carry2 + ex + r;
-                    if (q < dcap) {
-                        dst.x[q] = xx; dst.vx[q] = a1; dst.vy[q] = a2; dst.vz[q] = a3; dst.w[q] = ww;
-                    } else {
-                        atomicOr(status, BZ_DEV_CAPACITY);
+        // the divisions. Entry j (a candidate drawn c > 0 times) divides its target's weight
+        // by c+1 and its copies carry the result. The target is candidate j itself, or with
+        // the reference's indexing candidate (id of j) mod nhw (HW_ids[unique_ids[v]], CuPy
+        // wrapping the index, boltzmann.py:818-823), so several entries may share a target and
+        // divide its weight in turn, in entry order. Entries are grouped by target (counting
+        // sort), and each target's group is worked through by one thread in entry order,
+        // all targets at once.
+        const bool wrap = (p.flags & BZ_QUIRK_SPLIT_WRAP) != 0;
+        for (int j = threadIdx.x; j < nhw; j += RS_T)
+            if (dcnt[j]) atomicAdd(&gstart[wrap ? hw_ids[j] % nhw : j], 1);
+        __syncthreads();
+        {
+            int64_t carry = 0;  // group sizes -> group starts (exclusive scan)
+            for (int c0 = 0; c0 < nhw; c0 += RS_T * RS_ITEMS) {
+                const int j0 = c0 + threadIdx.x * RS_ITEMS;
+                int v[RS_ITEMS];
+                int local = 0;
+#pragma unroll
+                for (int i = 0; i < RS_ITEMS; ++i) {
+                    v[i] = j0 + i < nhw ? gstart[j0 + i] : 0;
+                    local += v[i];
+                }
+                int64_t tot;
+                int64_t acc = carry + block_excl_scan<int64_t>(local, shi, &tot);
+#pragma unroll
+                for (int i = 0; i < RS_ITEMS; ++i)
+                    if (j0 + i < nhw) {
+                        gstart[j0 + i] = int32_t(acc);
+                        gfill[j0 + i] = int32_t(acc);
+                        acc += v[i];
                     }
+                carry += tot;
+            }
+        }
+        __syncthreads();
+        for (int j = threadIdx.x; j < nhw; j += RS_T)
+            if (dcnt[j]) gmem[atomicAdd(&gfill[wrap ? hw_ids[j] % nhw : j], 1)] = j;
+        __syncthreads();
+        for (int g = threadIdx.x; g < nhw; g += RS_T) {
+            const int g0 = gstart[g], g1 = gfill[g];  // after the fill, gfill[g] is the group's end
+            if (g1 == g0) continue;
+            for (int a1 = g0 + 1; a1 < g1; ++a1) {  // entry order (groups are a few entries)
+                const int e = gmem[a1];
+                int a2 = a1 - 1;
+                while (a2 >= g0 && gmem[a2] > e) { gmem[a2 + 1] = gmem[a2]; --a2; }
+                gmem[a2 + 1] = e;
+            }
+            const int t = hw_ids[g];
+            T wcur = s.w[t];
+            for (int a1 = g0; a1 < g1; ++a1) {
+                const int j = gmem[a1];
+                const double wt = double(wcur) / double(dcnt[j] + 1);
+                wcur = T(wt);
+                cdf[j] = double(wcur);  // weight of this entry's copies (the table is no longer read)
+                tgt[j] = t;
+            }
+            s.w[t] = wcur;
+        }
+        __syncthreads();
+        // copies, in entry order: exclusive scan of counts, RS_ITEMS entries per thread
+        int64_t carry2 = 0;
+        for (int c0 = 0; c0 < nhw; c0 += RS_T * RS_ITEMS) {
+            const int j0 = c0 + threadIdx.x * RS_ITEMS;
+            int cs[RS_ITEMS];
+            int local = 0;
+#pragma unroll
+            for (int i = 0; i < RS_ITEMS; ++i) {
+                cs[i] = j0 + i < nhw ? dcnt[j0 + i] : 0;
+                local += cs[i];
+            }
+            int64_t tot;
+            int64_t ex = carry2 + block_excl_scan<int64_t>(local, shi, &tot);
+#pragma unroll
+            for (int i = 0; i < RS_ITEMS; ++i) {
+                const int c = cs[i];
+                if (c) {
+                    const int j = j0 + i;
+                    const int t = tgt[j];
+                    const T xx = s.x[t], a1 = s.vx[t], a2 = s.vy[t], a3 = s.vz[t], ww = T(cdf[j]);
+                    for (int r = 0; r < c; ++r) {
+                        const int64_t q = base + ex + r;
+                        if (q < dcap) {
+                            dst.x[q] = xx; dst.vx[q] = a1; dst.vy[q] = a2; dst.vz[q] = a3; dst.w[q] = ww;
+                        } else {
+                            atomicOr(status, BZ_DEV_CAPACITY);
+                        }
+                    }
+                    ex += c;
                 }
             }
             carry2 += tot;
@@ -492,6 +581,14 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
             d[10] = wbar * double(K); d[11] = f[0]; d[12] = f[1]; d[13] = f[2]; d[14] = f[3];
         }
     }
+}
+
+// the apply kernel's dynamic shared memory (the table and the draw counts) is above the
+// default 48 KB: allowed once per precision
+template <typename T> static bool rs_apply_smem_ok() {
+    static const bool ok = cudaFuncSetAttribute(k_rs_apply<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                int(RS_APPLY_SMEM)) == cudaSuccess;
+    return ok;
 }
 
 // ------------------------------------------------------------------------------------
@@ -622,9 +719,10 @@ static int resample_entry(const bz_params *pp, P s_, const int32_t *n, int64_t c
     k_rs_decide<<<1, 1024, 0, st>>>(counts, hw_counts, p.n_nodes, nb, targets, split_below, merge_at, merge_keep,
                                     p.flags, act, app_off, draw_off, misc, need_out);
     if (cons_diag && cudaMemsetAsync(cons_diag, 0, sizeof(double) * BZ_CONS_DIAG_STRIDE * nkeys, st) != cudaSuccess) return BZ_ERR_CUDA;
+    if (!rs_apply_smem_ok<T>()) return BZ_ERR_UNSUPPORTED;
     SoAR<T> s{s_.x, s_.vx, s_.vy, s_.vz, s_.w};
     SoAR<T> o{out_.x, out_.vx, out_.vy, out_.vz, out_.w};
-    k_rs_apply<T><<<nkeys, RS_T, RS_CDF * sizeof(double), st>>>(p, s, n, cap, nb, targets, max_ppc, min_wt,
+    k_rs_apply<T><<<nkeys, RS_T, RS_APPLY_SMEM, st>>>(p, s, n, cap, nb, targets, max_ppc, min_wt,
                                                                 float_above(min_wt), merge_keep, perm, offsets,
                                           counts, act, app_off, draw_off, replay_u, cdf, cnt, cons_diag,
                                           SoAR<T>{nullptr, nullptr, nullptr, nullptr, nullptr}, 0, status);
@@ -697,9 +795,10 @@ static int seg_resample_entry(const bz_params *pp, S s_, P app_, int64_t app_cap
     k_rs_decide<<<1, 1024, 0, st>>>(counts, hw_counts, p.n_nodes, nb, targets, split_below, merge_at, merge_keep,
                                     p.flags, act, app_off, draw_off, misc, need_out);
     if (cons_diag && cudaMemsetAsync(cons_diag, 0, sizeof(double) * BZ_CONS_DIAG_STRIDE * nkeys, st) != cudaSuccess) return BZ_ERR_CUDA;
+    if (!rs_apply_smem_ok<T>()) return BZ_ERR_UNSUPPORTED;
     SoAR<T> s{s_.x, s_.vx, s_.vy, s_.vz, s_.w};
     SoAR<T> app{app_.x, app_.vx, app_.vy, app_.vz, app_.w};
-    k_rs_apply<T><<<nkeys, RS_T, RS_CDF * sizeof(double), st>>>(p, s, nullptr, cap, nb, targets, max_ppc, min_wt,
+    k_rs_apply<T><<<nkeys, RS_T, RS_APPLY_SMEM, st>>>(p, s, nullptr, cap, nb, targets, max_ppc, min_wt,
                                                                 float_above(min_wt), merge_keep, perm, offsets,
                                           counts, act, app_off, draw_off, replay_u, cdf, cnt, cons_diag, app, app_cap,
                                           status);
