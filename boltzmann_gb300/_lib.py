@@ -93,6 +93,7 @@ _PROTOS = {
     "bz_compact_f32": (ctypes.c_int, [Particles, _vp, _i64, Particles, _i64, _vp, _vp, _sz, _vp, _vp]),
     "bz_compact_f64": (ctypes.c_int, [Particles, _vp, _i64, Particles, _i64, _vp, _vp, _sz, _vp, _vp]),
     "bz_grid_update": (ctypes.c_int, [_i32, _vp, _vp, _vp, _vp, _vp]),
+    "bz_ion_source_closure": (ctypes.c_int, [_i32, _vp, _vp, _vp]),
     "bz_ion_fluid": (ctypes.c_int, [_i32, _f64, _f64, _f64, _f64, _vp, _vp, _vp, _vp, _vp]),
     "bz_poisson_factor": (ctypes.c_int, [_i32, _f64, _vp, _vp, _vp]),
     "bz_field_step": (ctypes.c_int, [_i32, _f64, _f64, _f64, _f64, _f64, _f64, _f64, _vp, _vp, _vp, _vp, _vp, _vp, _vp,

@@ -42,12 +42,21 @@ __device__ __forceinline__ u32x4 philox(uint32_t c0, uint32_t c1, uint32_t c2, u
     return {c0, c1, c2, c3};
 }
 
-// The same generator with the ten round keys precomputed (k + r*W, r = 0..9): when they sit
+// Rounds of the push's draws (gas velocity, collision, ionization). Salmon et al. report
+// Philox4x32 with 7 rounds as the smallest round count that passes all of TestU01's
+// BigCrush ("Crush-resistant", SC'11 Table 2) and recommend 10 as a margin; the push, whose
+// runtime these rounds dominate after the memory traffic, uses 7. Every other stream here
+// (resampling, energy redraws, minibatches, the known-answer checks) keeps 10.
+constexpr int PUSH_ROUNDS = 7;
+
+// The same generator with the round keys precomputed (k + r*W, r = 0..9): when they sit
 // in the kernel's parameter space the XORs read them directly and no key schedule runs.
+template <int ROUNDS = 10>
 __device__ __forceinline__ u32x4 philox_rk(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, const uint32_t *rk0,
                                            const uint32_t *rk1) {
+    static_assert(ROUNDS >= 1 && ROUNDS <= 10, "ten round keys");
 #pragma unroll
-    for (int r = 0; r < 10; ++r) {
+    for (int r = 0; r < ROUNDS; ++r) {
         const uint64_t p0 = uint64_t(0xD2511F53u) * c0;
         const uint64_t p1 = uint64_t(0xCD9E8D57u) * c2;
         const uint32_t hi0 = uint32_t(p0 >> 32), lo0 = uint32_t(p0);
@@ -62,12 +71,14 @@ __device__ __forceinline__ u32x4 philox_rk(uint32_t c0, uint32_t c1, uint32_t c2
 // Two independent counters (differing only in the last word) through the same rounds, one
 // round of each after the other: the two dependency chains interleave, so a warp has a
 // second multiply to issue while the first one's result is pending.
+template <int ROUNDS = 10>
 __device__ __forceinline__ void philox_rk_x2(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3a, uint32_t c3b,
                                              const uint32_t *rk0, const uint32_t *rk1, u32x4 &ra, u32x4 &rb) {
+    static_assert(ROUNDS >= 1 && ROUNDS <= 10, "ten round keys");
     uint32_t a0 = c0, a1 = c1, a2 = c2, a3 = c3a;
     uint32_t b0 = c0, b1 = c1, b2 = c2, b3 = c3b;
 #pragma unroll
-    for (int r = 0; r < 10; ++r) {
+    for (int r = 0; r < ROUNDS; ++r) {
         const uint64_t pa0 = uint64_t(0xD2511F53u) * a0, pa1 = uint64_t(0xCD9E8D57u) * a2;
         const uint64_t pb0 = uint64_t(0xD2511F53u) * b0, pb1 = uint64_t(0xCD9E8D57u) * b2;
         const uint32_t na0 = uint32_t(pa1 >> 32) ^ a1 ^ rk0[r], na2 = uint32_t(pa0 >> 32) ^ a3 ^ rk1[r];
@@ -129,19 +140,19 @@ __device__ __forceinline__ void draw4(const Rng &g, uint32_t slot, uint32_t tag,
 __device__ __forceinline__ void draw4x2(const Rng &g, const uint32_t *rk0, const uint32_t *rk1, uint32_t slot,
                                         uint32_t tag_a, uint32_t tag_b, Draw4<float> &da, Draw4<float> &db) {
     u32x4 a, b;
-    philox_rk_x2(slot, g.s0, g.s1, tag_a, tag_b, rk0, rk1, a, b);
+    philox_rk_x2<PUSH_ROUNDS>(slot, g.s0, g.s1, tag_a, tag_b, rk0, rk1, a, b);
     da.v[0] = uni_f(a.x); da.v[1] = uni_f(a.y); da.v[2] = uni_f(a.z); da.v[3] = uni_f(a.w);
     db.v[0] = uni_f(b.x); db.v[1] = uni_f(b.y); db.v[2] = uni_f(b.z); db.v[3] = uni_f(b.w);
 }
 __device__ __forceinline__ void draw4(const Rng &g, const uint32_t *rk0, const uint32_t *rk1, uint32_t slot,
                                       uint32_t tag, Draw4<float> &d) {
-    u32x4 r = philox_rk(slot, g.s0, g.s1, tag, rk0, rk1);
+    u32x4 r = philox_rk<PUSH_ROUNDS>(slot, g.s0, g.s1, tag, rk0, rk1);
     d.v[0] = uni_f(r.x); d.v[1] = uni_f(r.y); d.v[2] = uni_f(r.z); d.v[3] = uni_f(r.w);
 }
 __device__ __forceinline__ void draw4(const Rng &g, const uint32_t *rk0, const uint32_t *rk1, uint32_t slot,
                                       uint32_t tag, Draw4<double> &d) {
-    u32x4 a = philox_rk(slot, g.s0, g.s1, tag, rk0, rk1);
-    u32x4 b = philox_rk(slot, g.s0, g.s1, tag | (1u << 8), rk0, rk1);
+    u32x4 a = philox_rk<PUSH_ROUNDS>(slot, g.s0, g.s1, tag, rk0, rk1);
+    u32x4 b = philox_rk<PUSH_ROUNDS>(slot, g.s0, g.s1, tag | (1u << 8), rk0, rk1);
     d.v[0] = uni_d(a.x, a.y); d.v[1] = uni_d(a.z, a.w); d.v[2] = uni_d(b.x, b.y); d.v[3] = uni_d(b.z, b.w);
 }
 
@@ -175,6 +186,59 @@ static inline float float_above(double m) {
 // correctly rounded in double
 __device__ __forceinline__ float sqrt_pos(float x) { return x * rsqrtf(x); }
 __device__ __forceinline__ double sqrt_pos(double x) { return sqrt(x); }
+
+// Standard normal deviates from float uniforms by their quantile, Phi^-1(u) = x f(w) with
+// x = 2u - 1 = u - (1-u) (exact) and w = -log2(4 u (1-u)); f is a polynomial in w on the
+// central range w < 5/ln 2 (u in (0.00169, 0.99831)) and one in sqrt(w) in the tails. The
+// form is Giles' (M. Giles, "Approximating the erfinv function", GPU Computing Gems Jade
+// Edition, 2011); the coefficients are this library's own weighted least-squares fit of
+// degree 8 to the exact quantile over all 2^23 uniforms uni_f emits. Maximum relative
+// error 3.5e-7 in float32 arithmetic, including an absolute error of 2^-22 in the hardware
+// log2. One uniform per deviate (Box-Muller takes two per pair and a log, a square root, a
+// sine and a cosine) and no rejection.
+constexpr float NQ_W_TAIL = 7.213475f;  // 5 / ln 2
+__device__ __forceinline__ float nq_w(Uni<float> a) { return -2.0f - __log2f(a.u * a.c); }
+__device__ __forceinline__ float nq_central(float w) {
+    const float t = w - 3.6067376f;
+    float r = 2.177562797e-09f;
+    r = fmaf(r, t, 3.740066035e-08f);
+    r = fmaf(r, t, -5.542177632e-07f);
+    r = fmaf(r, t, -9.956440863e-07f);
+    r = fmaf(r, t, 7.136897329e-05f);
+    r = fmaf(r, t, -5.904508871e-04f);
+    r = fmaf(r, t, -2.838615328e-03f);
+    r = fmaf(r, t, 2.417715639e-01f);
+    return fmaf(r, t, 2.123313665e+00f);
+}
+__device__ __forceinline__ float nq_tail(float w) {
+    const float t = sqrt_pos(w) - 3.688112f;
+    float r = -9.029921785e-05f;
+    r = fmaf(r, t, -1.695100582e-05f);
+    r = fmaf(r, t, 6.919289590e-04f);
+    r = fmaf(r, t, -1.730788732e-03f);
+    r = fmaf(r, t, 3.062781878e-03f);
+    r = fmaf(r, t, -5.049590953e-03f);
+    r = fmaf(r, t, 7.831202820e-03f);
+    r = fmaf(r, t, 1.180825233e+00f);
+    return fmaf(r, t, 4.106443405e+00f);
+}
+// Three deviates times sigma. The tail polynomial runs only when a lane among those
+// executing this needs it (1% of lanes, in about a quarter of the warps); otherwise the
+// warp evaluates the central polynomial alone.
+__device__ __forceinline__ void normal_quantile3(Uni<float> a0, Uni<float> a1, Uni<float> a2, float sigma,
+                                                 float &g0, float &g1, float &g2) {
+    const float w0 = nq_w(a0), w1 = nq_w(a1), w2 = nq_w(a2);
+    float r0 = nq_central(w0), r1 = nq_central(w1), r2 = nq_central(w2);
+    const bool t0 = !(w0 < NQ_W_TAIL), t1 = !(w1 < NQ_W_TAIL), t2 = !(w2 < NQ_W_TAIL);
+    if (__any_sync(__activemask(), t0 || t1 || t2)) {
+        if (t0) r0 = nq_tail(w0);
+        if (t1) r1 = nq_tail(w1);
+        if (t2) r2 = nq_tail(w2);
+    }
+    g0 = (a0.u - a0.c) * sigma * r0;
+    g1 = (a1.u - a1.c) * sigma * r1;
+    g2 = (a2.u - a2.c) * sigma * r2;
+}
 
 // Box-Muller pair from uniforms (a, b): r = sqrt(-2 ln a), angle 2 pi b.
 template <typename T> __device__ __forceinline__ void box_muller(T a, T b, T &g0, T &g1) {

@@ -382,6 +382,12 @@ static bool field_cluster_ok(int G) {
     return cached;
 }
 
+// rate closure of the ion source: ni_src = nu_i ne per node (moments row 1 from row 0)
+__global__ void k_ion_source_closure(int nn, const double *rate, double *mom) {
+    for (int i = threadIdx.x + blockIdx.x * blockDim.x; i < nn; i += blockDim.x * gridDim.x)
+        mom[nn + i] = rate[i] * mom[i];
+}
+
 __global__ void k_advance_clock(double *t, uint64_t *step, double dt) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         if (t) *t = *t + dt;
@@ -395,6 +401,11 @@ extern "C" {
 int bz_grid_update(int32_t n_nodes, const double *moments, double *ni, double *Te, double *g2, void *stream) {
     if (n_nodes < 1 || !moments) return BZ_ERR_ARG;
     bz::k_grid_update<<<(n_nodes + 255) / 256, 256, 0, bz::as_stream(stream)>>>(n_nodes, moments, ni, Te, g2);
+    return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
+}
+int bz_ion_source_closure(int32_t n_nodes, const double *rate, double *moments, void *stream) {
+    if (n_nodes < 1 || !rate || !moments) return BZ_ERR_ARG;
+    bz::k_ion_source_closure<<<(n_nodes + 255) / 256, 256, 0, bz::as_stream(stream)>>>(n_nodes, rate, moments);
     return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
 }
 int bz_ion_fluid(int32_t N, double dx, double dt, double mu_i, double D_i, const double *E, double *ni, double *Ji,

@@ -316,7 +316,8 @@ static int push_entry(const bz_params *pp, P in_, const int32_t *n_in, int64_t i
 
 // Philox4x32-10 of n (counter, key) pairs through the device code the kernels use:
 // variant 0 the plain rounds, 1 and 2 the two halves of the interleaved pair with round
-// keys (philox_rk_x2, whose second counter differs in word 3: here the same counter).
+// keys (philox_rk_x2, whose second counter differs in word 3: here the same counter), 3 the
+// interleaved pair with the push's round count.
 __global__ void k_philox(const uint32_t *ctr, const uint32_t *key, int n, int variant, uint32_t *out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -331,8 +332,9 @@ __global__ void k_philox(const uint32_t *ctr, const uint32_t *key, int n, int va
             rk1[j] = k[1] + uint32_t(j) * 0xBB67AE85u;
         }
         u32x4 a, b;
-        philox_rk_x2(c[0], c[1], c[2], c[3], c[3], rk0, rk1, a, b);
-        r = variant == 1 ? a : b;
+        if (variant == 3) philox_rk_x2<PUSH_ROUNDS>(c[0], c[1], c[2], c[3], c[3], rk0, rk1, a, b);
+        else philox_rk_x2(c[0], c[1], c[2], c[3], c[3], rk0, rk1, a, b);
+        r = variant == 2 ? b : a;
     }
     uint32_t *o = out + 4 * size_t(i);
     o[0] = r.x; o[1] = r.y; o[2] = r.z; o[3] = r.w;
@@ -411,7 +413,7 @@ int bz_push_collide_f64(const bz_params *p, bz_particles_f64 in, const int32_t *
 
 int bz_philox4x32_10(const uint32_t *ctr, const uint32_t *key, int32_t n, int32_t variant, uint32_t *out,
                      void *stream) {
-    if (n < 0 || variant < 0 || variant > 2 || (n > 0 && (!ctr || !key || !out))) return BZ_ERR_ARG;
+    if (n < 0 || variant < 0 || variant > 3 || (n > 0 && (!ctr || !key || !out))) return BZ_ERR_ARG;
     if (n == 0) return BZ_OK;
     bz::k_philox<<<int(bz::ceil_div(n, 256)), 256, 0, bz::as_stream(stream)>>>(ctr, key, n, variant, out);
     return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;

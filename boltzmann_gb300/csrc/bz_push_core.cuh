@@ -145,6 +145,7 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
     // gas velocity (boltzmann.py:589, electron_kernel_numba.py:51-53) and uniforms
     T g0 = 0, g1 = 0, g2 = 0;
     Uni<T> u0, u1, u2, u3;
+    Uni<T> u5{T(0.5), T(0.5)};  // the child's azimuth (float32: the gas draw's fourth word)
     double r0_replay = 0.0;
     if (REPLAY) {
         g0 = T(gas[size_t(slot) * 3 + 0]);
@@ -164,7 +165,12 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
             draw4(rng, k.rk0, k.rk1, slot, 0u, dg);
             draw4(rng, k.rk0, k.rk1, slot, 1u, d);
         }
-        if (k.gas_sigma > T(0)) {
+        if constexpr (sizeof(T) == 4) {
+            // three normals by their quantiles from three words of the gas draw; its
+            // fourth word is the ionization child's azimuth (no third Philox call)
+            if (k.gas_sigma > T(0)) normal_quantile3(dg.v[0], dg.v[1], dg.v[2], k.gas_sigma, g0, g1, g2);
+            u5 = dg.v[3];
+        } else if (k.gas_sigma > T(0)) {
             T h;
             box_muller(dg.v[0].u, dg.v[1].u, g0, g1);
             box_muller(dg.v[2].u, dg.v[3].u, g2, h);
@@ -277,10 +283,9 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
         iso_dir(u1, u2, vn, nvx, nvy, nvz);
         if (proc == P_IONIZE) {
             // the new electron: same position and weight, its own isotropic direction
-            Uni<T> u5;
             if (REPLAY) {
                 u5 = uni_from_replay<T>(R[size_t(slot) * 7 + 5]);
-            } else {
+            } else if constexpr (sizeof(T) == 8) {
                 Draw4<T> d;
                 draw4(rng, k.rk0, k.rk1, slot, 2u, d);
                 u5 = d.v[0];

@@ -156,6 +156,26 @@ __device__ __forceinline__ int draw_index(const uint64_t *H, int n, uint32_t a, 
     return lo < n ? lo : n - 1;
 }
 
+// Sums of float32 terms as unevaluated pairs of floats (hi + lo): products made exact by
+// the fma error term, additions by the two-sum error term (Dekker 1971; Knuth, TAOCP
+// 4.2.2), renormalised after every addition, so each addition errs by about 2^-48 of the
+// running sum. They keep this part's narrow float64 pipe out of the per-particle sums; the
+// rounded operations are spelled out so that none is contracted into an fma.
+struct FF { float hi, lo; };
+__device__ __forceinline__ void ff_add(FF &a, float x, float xl) {
+    const float s = __fadd_rn(a.hi, x), bb = __fsub_rn(s, a.hi);
+    const float err = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+    const float lo = __fadd_rn(a.lo, __fadd_rn(err, xl));
+    const float h = __fadd_rn(s, lo);
+    a.lo = __fsub_rn(lo, __fsub_rn(h, s));
+    a.hi = h;
+}
+__device__ __forceinline__ void ff_add_prod(FF &a, float x, float y) {  // a += x y
+    const float p = __fmul_rn(x, y);
+    ff_add(a, p, fmaf(x, y, -p));
+}
+__device__ __forceinline__ double ff_value(const FF &a) { return double(a.hi) + double(a.lo); }
+
 // block helpers (RS_T threads)
 template <typename V> __device__ V block_sum(V v, V *sh) {
 #pragma unroll
@@ -433,35 +453,44 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
             s.w[t] = wcur;
         }
         __syncthreads();
-        // copies, in entry order: exclusive scan of counts, RS_ITEMS entries per thread
+        // copies, in entry order. One entry per thread: a block scan of the counts gives each
+        // warp one contiguous output range for its 32 entries, which the warp fills 32 slots
+        // at a time with coalesced stores; each lane finds the entry of its slot by a binary
+        // search over the lanes' offsets and takes the entry's values by shuffles. The slots
+        // and their values are the ones a loop over each entry's copies writes.
+        const int lane = threadIdx.x & 31;
         int64_t carry2 = 0;
-        for (int c0 = 0; c0 < nhw; c0 += RS_T * RS_ITEMS) {
-            const int j0 = c0 + threadIdx.x * RS_ITEMS;
-            int cs[RS_ITEMS];
-            int local = 0;
-#pragma unroll
-            for (int i = 0; i < RS_ITEMS; ++i) {
-                cs[i] = j0 + i < nhw ? dcnt[j0 + i] : 0;
-                local += cs[i];
-            }
+        for (int c0 = 0; c0 < nhw; c0 += RS_T) {
+            const int j = c0 + threadIdx.x;
+            const int c = j < nhw ? dcnt[j] : 0;
             int64_t tot;
-            int64_t ex = carry2 + block_excl_scan<int64_t>(local, shi, &tot);
+            const int64_t ex = carry2 + block_excl_scan<int64_t>(c, shi, &tot);
+            T xx = T(0), a1 = T(0), a2 = T(0), a3 = T(0), ww = T(0);
+            if (c) {
+                const int t = tgt[j];
+                xx = s.x[t]; a1 = s.vx[t]; a2 = s.vy[t]; a3 = s.vz[t]; ww = T(cdf[j]);
+            }
+            const int64_t wlo = __shfl_sync(0xffffffffu, ex, 0);
+            const int rel = int(ex - wlo);                               // this entry's first slot
+            const int wn = __shfl_sync(0xffffffffu, rel + c, 31);     // the warp's slots
+            for (int q0 = 0; q0 < wn; q0 += 32) {
+                const int q = q0 + lane;
+                int src = 0;  // the last lane whose first slot is at or below q (it has copies)
 #pragma unroll
-            for (int i = 0; i < RS_ITEMS; ++i) {
-                const int c = cs[i];
-                if (c) {
-                    const int j = j0 + i;
-                    const int t = tgt[j];
-                    const T xx = s.x[t], a1 = s.vx[t], a2 = s.vy[t], a3 = s.vz[t], ww = T(cdf[j]);
-                    for (int r = 0; r < c; ++r) {
-                        const int64_t q = base + ex + r;
-                        if (q < dcap) {
-                            dst.x[q] = xx; dst.vx[q] = a1; dst.vy[q] = a2; dst.vz[q] = a3; dst.w[q] = ww;
-                        } else {
-                            atomicOr(status, BZ_DEV_CAPACITY);
-                        }
+                for (int step = 16; step > 0; step >>= 1) {
+                    const int e = __shfl_sync(0xffffffffu, rel, src + step);
+                    if (e <= q) src += step;
+                }
+                const T vx0 = __shfl_sync(0xffffffffu, xx, src), vx1 = __shfl_sync(0xffffffffu, a1, src);
+                const T vx2 = __shfl_sync(0xffffffffu, a2, src), vx3 = __shfl_sync(0xffffffffu, a3, src);
+                const T vw = __shfl_sync(0xffffffffu, ww, src);
+                if (q < wn) {
+                    const int64_t d = base + wlo + q;
+                    if (d < dcap) {
+                        dst.x[d] = vx0; dst.vx[d] = vx1; dst.vy[d] = vx2; dst.vz[d] = vx3; dst.w[d] = vw;
+                    } else {
+                        atomicOr(status, BZ_DEV_CAPACITY);
                     }
-                    ex += c;
                 }
             }
             carry2 += tot;
@@ -476,16 +505,38 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
         return;
     }
     double W = 0, px = 0, py = 0, pz = 0, ew = 0;
-    #pragma unroll 4
-    for (int j = threadIdx.x; j < np_; j += RS_T) {
-        int id = perm[off + j];
-        double w = s.w[id], vx = s.vx[id], vy = s.vy[id], vz = s.vz[id];
-        cdf[j] = w;  // kept for the cumsum
-        W += w;
-        px += vx * w;
-        py += vy * w;
-        pz += vz * w;
-        ew += w * (efac * (vx * vx + vy * vy + vz * vz));
+    if constexpr (sizeof(T) == 4) {
+        // float32 state: each thread's five sums as pairs of floats (sum w |v|^2 here, times
+        // efac in float64 once per thread), then float64 across the block
+        FF fW{0.f, 0.f}, fx{0.f, 0.f}, fy{0.f, 0.f}, fz{0.f, 0.f}, fe{0.f, 0.f};
+        #pragma unroll 2
+        for (int j = threadIdx.x; j < np_; j += RS_T) {
+            const int id = perm[off + j];
+            const float w = s.w[id], vx = s.vx[id], vy = s.vy[id], vz = s.vz[id];
+            cdf[j] = double(w);  // kept for the cumsum
+            ff_add(fW, w, 0.f);
+            ff_add_prod(fx, vx, w);
+            ff_add_prod(fy, vy, w);
+            ff_add_prod(fz, vz, w);
+            FF v2{__fmul_rn(vx, vx), fmaf(vx, vx, -__fmul_rn(vx, vx))};
+            ff_add_prod(v2, vy, vy);
+            ff_add_prod(v2, vz, vz);
+            const float ph = __fmul_rn(w, v2.hi);
+            ff_add(fe, ph, __fadd_rn(fmaf(w, v2.hi, -ph), __fmul_rn(w, v2.lo)));
+        }
+        W = ff_value(fW); px = ff_value(fx); py = ff_value(fy); pz = ff_value(fz); ew = efac * ff_value(fe);
+    } else {
+        #pragma unroll 4
+        for (int j = threadIdx.x; j < np_; j += RS_T) {
+            int id = perm[off + j];
+            double w = s.w[id], vx = s.vx[id], vy = s.vy[id], vz = s.vz[id];
+            cdf[j] = w;  // kept for the cumsum
+            W += w;
+            px += vx * w;
+            py += vy * w;
+            pz += vz * w;
+            ew += w * (efac * (vx * vx + vy * vy + vz * vz));
+        }
     }
     {
         double m[5] = {W, px, py, pz, ew};
@@ -545,12 +596,6 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
         double vx = ux + (double(s.vx[id]) - hx) * Tfac;
         double vy = uy + (double(s.vy[id]) - hy) * Tfac;
         double vz = uz + (double(s.vz[id]) - hz) * Tfac;
-        if (cons_diag) {
-            fx += wbar * vx;
-            fy += wbar * vy;
-            fz += wbar * vz;
-            fe += wbar * (efac * (vx * vx + vy * vy + vz * vz));
-        }
         T tx = T(vx), ty = T(vy), tz = T(vz);
         int64_t q = base + k;
         if (q < dcap) {
@@ -558,12 +603,18 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
         } else {
             atomicOr(status, BZ_DEV_CAPACITY);
         }
-        double wd = double(wbar_t), dx = tx, dy = ty, dz = tz;
-        aW += wd;
-        ax += wd * dx;
-        ay += wd * dy;
-        az += wd * dz;
-        ae += wd * (efac * (dx * dx + dy * dy + dz * dz));
+        if (cons_diag) {
+            fx += wbar * vx;
+            fy += wbar * vy;
+            fz += wbar * vz;
+            fe += wbar * (efac * (vx * vx + vy * vy + vz * vz));
+            double wd = double(wbar_t), dx = tx, dy = ty, dz = tz;
+            aW += wd;
+            ax += wd * dx;
+            ay += wd * dy;
+            az += wd * dz;
+            ae += wd * (efac * (dx * dx + dy * dy + dz * dz));
+        }
     }
     __syncthreads();
     #pragma unroll 4

@@ -352,6 +352,11 @@ def grid_update(n_nodes, moments, ni, Te, g2):
     call("bz_grid_update", int(n_nodes), _ptr(moments), _ptr(ni), _ptr(Te), _ptr(g2), _stream())
 
 
+def ion_source_closure(n_nodes, rate, moments):
+    """moments[1] = rate * moments[0] per node (the ion source from a rate closure)."""
+    call("bz_ion_source_closure", int(n_nodes), _ptr(rate), _ptr(moments), _stream())
+
+
 def heavies_kernel_fluid(N, dx, dt, mu_i, D_i, E, ni, Ji, brk=None):
     call("bz_ion_fluid", int(N), float(dx), float(dt), float(mu_i), float(D_i), _ptr(E), _ptr(ni), _ptr(Ji),
          _ptr(brk), _stream())

@@ -120,6 +120,7 @@ class BoltzmannGB300:
         self._replayed = set()  # graph keys replayed at least once since their capture
         self._kinds = set()
         self._host_io = None
+        self._ion_rate = None  # ion-source rate closure per node (set_ion_closure), else None
         self._brk_warned = False
         if N >= 3:
             K.poisson_factor(N, cfg.dx, self.chol_d, self.chol_l, self.poisson_plan)
@@ -253,6 +254,8 @@ class BoltzmannGB300:
         else:
             self._repack_if_needed()
         self.electron_kernel()
+        if self._ion_rate is not None:
+            K.ion_source_closure(self.nnodes, self._ion_rate, self.moments)
         self._grid_solves(advance=True)
         if self._host_io is not None:  # back_to_cpu (post_processing_1D.py:6-24)
             self._host_io.copy_(self.io, non_blocking=True)
@@ -406,11 +409,14 @@ class BoltzmannGB300:
         phase = 2.0 * math.pi * ((cfg.freq * float(self.t.item())) % 1.0)
         return td, mean, f, phase
 
-    def learned_start(self, mlp, seed=None):
+    def learned_start(self, mlp, seed=None, closure=False):
         """Redraw every electron's velocity from the surrogate network's steady-state energy
-        distribution for its node (features from ``node_state``), then refresh the
-        moments. Positions, weights and the field are unchanged; the plain step loop
-        continues from here. Returns the network's per-node (eedf, k_exc, k_ion)."""
+        distribution for its node (features from ``node_state``), each node's energies
+        scaled to the network's predicted mean energy, then refresh the moments. Positions,
+        weights and the field are unchanged; the plain step loop continues from here. With
+        ``closure`` the ion source of the following steps is the network's ionization rate
+        times the electron density (``set_ion_closure``) instead of the counted
+        ionizations. Returns the network's per-node (eedf, k_exc, k_ion, mean energy)."""
         from . import surrogate as S
         td, mean, f, phase = self.node_state()
         out = S.learned_start(mlp, self.params(step_on_device=False), self.A, td, np.maximum(mean, 1e-3),
@@ -418,7 +424,22 @@ class BoltzmannGB300:
                               device=self.device)
         self.moments.zero_()
         K.seg_deposit(self.params(step_on_device=False), self.A, self.moments)
+        if closure:
+            self.set_ion_closure(out[2])
         return out
+
+    def set_ion_closure(self, k_ion=None):
+        """Ion source from a rate closure: ni_src = k_ion n_gas dt ne per node (k_ion in m^3/s
+        per deposit node, e.g. the learned start-up network's), replacing the counted
+        ionizations of the push (post_processing_1D.py:50-55); None restores the counted
+        source. The step graphs are captured again."""
+        if k_ion is None:
+            self._ion_rate = None
+        else:
+            k = np.broadcast_to(np.asarray(k_ion, dtype=np.float64), (self.nnodes,))
+            self._ion_rate = torch.as_tensor(k * self.cfg.nn_m3 * self.cfg.dt, dtype=torch.float64,
+                                             device=self.device).contiguous()
+        self._graphs = {}
 
     # --------------------------------------------------------------------------------- diagnostics
     def kernel_launches(self, resample):
@@ -429,7 +450,7 @@ class BoltzmannGB300:
         then per 8-bit radix pass a histogram, scan and scatter), decide + apply (2) and the
         repack of the survivors with the appended particles (1)."""
         passes = 2 if self.nnodes * self.nb >= 256 else 1
-        return 2 + (4 + 3 * passes + 2 + 1 if resample else 1)
+        return 2 + (4 + 3 * passes + 2 + 1 if resample else 1) + (self._ion_rate is not None)
 
     def snapshot(self):
         """A device copy of the simulation state: the particles (the buffer that holds

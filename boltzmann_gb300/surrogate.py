@@ -20,11 +20,15 @@ Features (9 of BZ_MLP_IN = 16, the rest zero):
   0: log10(E/N in Td) / 3          1: log10(mean energy in eV) / 2
   2, 3: sin and cos of the RF phase (both 0 for a DC field: swarms)
   4..8: weight fractions in the energy bins [0,2), [2,6), [6,11.5), [11.5,15.76), >= 15.76 eV
-Outputs (66 of BZ_MLP_OUT = 80):
+Outputs (67 of BZ_MLP_OUT = 80):
   0..63: (log10(f_k + 1e-6) + 3) / 3, f_k the weight fraction in log bin k of 64 over
          0.01-100 eV
   64, 65: (log10(k + 1e-20) + 16.5) / 3.5, k the excitation and ionization rate
          coefficients in m^3/s
+  66: log10(mean energy in eV) / 2 of the same steady state. The fit of the log fractions
+      weighs every bin alike, so the mean of the distribution it gives errs by about a
+      percent (the tail above the bulk carries much of the energy); the start-up scales the
+      drawn energies so that each key's mean is this output's.
 """
 from __future__ import annotations
 
@@ -41,7 +45,8 @@ LAYERS = ((16, 128), (128, 128), (128, 128), (128, 128), (128, 80))  # (in, out)
 EEDF_BINS, EEDF_EMIN, EEDF_EMAX = 64, 0.01, 100.0
 BIN_EDGES5 = (2.0, 6.0, 11.5, 15.76)
 F_FLOOR, K_FLOOR = 1e-6, 1e-20
-N_FEAT, N_TGT = 9, EEDF_BINS + 2
+N_FEAT, N_TGT = 9, EEDF_BINS + 3
+I_MEAN = EEDF_BINS + 2
 
 
 def eedf_centres():
@@ -74,12 +79,15 @@ def features(td, mean_e, phase, fr5):
     return x
 
 
-def targets(eedf, k_exc, k_ion):
+def targets(eedf, k_exc, k_ion, mean_e=None):
+    """Network targets; mean_e (eV) defaults to the distribution's own mean (eedf_mean)."""
     n = len(eedf)
     t = np.zeros((n, NOUT), dtype=np.float32)
     t[:, :EEDF_BINS] = (np.log10(np.asarray(eedf) + F_FLOOR) + 3.0) / 3.0
     t[:, EEDF_BINS] = (np.log10(np.maximum(k_exc, 0) + K_FLOOR) + 16.5) / 3.5
     t[:, EEDF_BINS + 1] = (np.log10(np.maximum(k_ion, 0) + K_FLOOR) + 16.5) / 3.5
+    m = eedf_mean(eedf) if mean_e is None else np.broadcast_to(np.asarray(mean_e, dtype=np.float64), (n,))
+    t[:, I_MEAN] = np.log10(np.maximum(m, 1e-3)) / 2.0
     return t
 
 
@@ -94,6 +102,11 @@ def decode(y):
     return f, kx, ki
 
 
+def decode_mean(y):
+    """Network outputs -> the predicted mean energy (eV) [n]."""
+    return 10.0 ** (2.0 * np.asarray(y, dtype=np.float64)[:, I_MEAN])
+
+
 def eedf_mean(eedf):
     """Mean energy (eV) of weight fractions in the 64 log bins, each bin log-uniform (the
     start-up's draw): sum_k f_k (e_k+1 - e_k) / ln(e_k+1 / e_k)."""
@@ -103,10 +116,11 @@ def eedf_mean(eedf):
     return np.asarray(eedf, dtype=np.float64) @ mk
 
 
-def output_weights(eedf_weight=1.0, rate_weight=1.0):
+def output_weights(eedf_weight=1.0, rate_weight=1.0, mean_weight=4.0):
     w = np.zeros(NOUT, dtype=np.float32)
     w[:EEDF_BINS] = eedf_weight
-    w[EEDF_BINS:N_TGT] = rate_weight
+    w[EEDF_BINS:I_MEAN] = rate_weight
+    w[I_MEAN] = mean_weight
     return w
 
 
@@ -181,6 +195,11 @@ class SurrogateMLP:
         """(eedf [n,64], k_exc [n], k_ion [n]) for feature rows x [n,16]."""
         return decode(self.forward(torch.as_tensor(np.asarray(x, dtype=np.float32))).cpu().numpy())
 
+    def predict_all(self, x):
+        """(eedf [n,64], k_exc [n], k_ion [n], mean energy [n]) for feature rows x [n,16]."""
+        y = self.forward(torch.as_tensor(np.asarray(x, dtype=np.float32))).cpu().numpy()
+        return decode(y) + (decode_mean(y),)
+
 
 # ------------------------------------------------------------------------------------ data from swarms
 def swarm_state(ens):
@@ -215,7 +234,7 @@ def swarm_dataset(td, counts, steps, snapshot_every, settle_fraction=0.5, seed=1
         eedfs.append(f)
     f_ss = np.mean(eedfs[settle:], axis=0)
     kion, kexc = ens.rate_coefficients()
-    tg = targets(f_ss, kexc, kion)
+    tg = targets(f_ss, kexc, kion, np.mean(means[settle:], axis=0))
     X = np.concatenate(feats)
     T = np.concatenate([tg] * n_snap)
     # the initial state is a sample too (what the start-up sees)
@@ -247,13 +266,16 @@ def eedf_cdf(eedf):
 
 def learned_start(mlp: SurrogateMLP, params, segs, td, mean_e, fr5, phase=None, seed=11, device="cuda"):
     """Redraw the velocities of every particle from the network's steady-state EEDF for
-    its key (swarm / deposit node): features per key from (td, mean_e, fr5, phase; phase
-    None for a DC field)."""
+    its key (swarm / deposit node), the energies scaled so that each key's mean is the
+    network's predicted mean energy: features per key from (td, mean_e, fr5, phase; phase
+    None for a DC field). Returns (eedf, k_exc, k_ion, mean energy) per key."""
     x = features(td, mean_e, phase, fr5)
-    f, kx, ki = mlp.predict(x)
+    f, kx, ki, em = mlp.predict_all(x)
     cdf = torch.as_tensor(eedf_cdf(f), dtype=torch.float64, device=device)
-    K.seg_sample_energy(params, segs, cdf, EEDF_EMIN, EEDF_EMAX, seed)
-    return f, kx, ki
+    scale = np.clip(em / np.maximum(eedf_mean(f), 1e-6), 0.5, 2.0)
+    K.seg_sample_energy(params, segs, cdf, EEDF_EMIN, EEDF_EMAX, seed,
+                        scale=torch.as_tensor(scale, dtype=torch.float64, device=device))
+    return f, kx, ki, em
 
 
 def steps_to_steady(series, final, tol=0.02, window=5):
@@ -314,6 +336,7 @@ def ccp_dataset(cfg, cycles, snaps_per_cycle=8, settle_cycles=None, min_density=
     settle = cycles - settle_n
     snaps = []
     f_acc = np.zeros((snaps_per_cycle, nn_, EEDF_BINS))
+    m_acc = np.zeros((snaps_per_cycle, nn_))
     ev = torch.zeros(3, nn_, dtype=torch.float64, device=device)
     for c in range(cycles):
         for k in range(snaps_per_cycle):
@@ -321,6 +344,7 @@ def ccp_dataset(cfg, cycles, snaps_per_cycle=8, settle_cycles=None, min_density=
             snaps.append((k, features(td, np.maximum(mean, 1e-3), phase, bin_fractions(f))))
             if c >= settle:
                 f_acc[k] += f
+                m_acc[k] += mean
             for _ in range(every):
                 sv.step()
                 if c >= settle:
@@ -328,6 +352,7 @@ def ccp_dataset(cfg, cycles, snaps_per_cycle=8, settle_cycles=None, min_density=
                     ev[1].add_(sv.moments[2])
                     ev[2].add_(sv.moments[0])
     f_ss = f_acc / settle_n
+    m_ss = m_acc / settle_n
     e = ev.cpu().numpy()
     den = np.maximum(e[2], 1e-300) * cfg.nn_m3 * cfg.dt
     k_ion, k_exc = e[0] / den, e[1] / den
@@ -336,8 +361,9 @@ def ccp_dataset(cfg, cycles, snaps_per_cycle=8, settle_cycles=None, min_density=
     # the fit then weighs nodes as the gap's energy balance does
     rep = np.maximum(1, np.round(density_repeat * e[2] / e[2].max())).astype(int)[keep]
     X = np.concatenate([np.repeat(x[keep], rep, axis=0) for _, x in snaps])
-    T = np.concatenate([np.repeat(targets(f_ss[k][keep], k_exc[keep], k_ion[keep]), rep, axis=0) for k, _ in snaps])
-    info = {"nodes": np.nonzero(keep)[0], "eedf_ss": f_ss, "k_ion": k_ion, "k_exc": k_exc,
+    T = np.concatenate([np.repeat(targets(f_ss[k][keep], k_exc[keep], k_ion[keep], np.maximum(m_ss[k][keep], 1e-3)),
+                                  rep, axis=0) for k, _ in snaps])
+    info = {"nodes": np.nonzero(keep)[0], "eedf_ss": f_ss, "mean_ss": m_ss, "k_ion": k_ion, "k_exc": k_exc,
             "status": sv.device_status(), "n_end": sv.n()}
     return X, T, info
 

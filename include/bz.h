@@ -200,6 +200,12 @@ int bz_compact_f64(bz_particles_f64 in, const int32_t *n, int64_t in_capacity, b
 /* Host-side grid update of the step loop (boltzmann.py:643-647): ni += ni_src,
  * Te = (2/3) nrg/ne (NaN -> 0), g2 += ni_src, from moments[4][n_nodes]. */
 int bz_grid_update(int32_t n_nodes, const double *moments, double *ni, double *Te, double *g2, void *stream);
+/* Ion-source rate closure (no counterpart in the reference, whose ion source is always the
+ * push's counted ionizations, post_processing_1D.py:50-55 -> boltzmann.py:643): replaces
+ * moments row 1 (ni_src) by rate[i] * moments row 0 (ne) for every node, rate[n_nodes] the
+ * ionizations per electron per step (k_ion n_gas dt, e.g. from the learned start-up's
+ * network). Launched between the push and the grid step. */
+int bz_ion_source_closure(int32_t n_nodes, const double *rate, double *moments, void *stream);
 /* heavies_kernel_fluid (heavies_kernel_1D.py:4-64), ion part; break flag -> *brk. */
 int bz_ion_fluid(int32_t N, double dx, double dt, double mu_i, double D_i, const double *E, double *ni,
                  double *Ji, int32_t *brk, void *stream);
@@ -469,7 +475,8 @@ int bz_seg_sample_energy_f64(const bz_params *p, bz_segments_f64 s, int32_t n_ke
 /* Philox4x32-10 (Salmon et al. 2011) of n counters ctr[n][4] under keys key[n][2] into
  * out[n][4], all device pointers, through the device code the kernels draw from: variant 0
  * the plain rounds, 1 and 2 the two outputs of the interleaved pair with precomputed round
- * keys (both given the same counter). For known-answer checks of the generator. */
+ * keys (both given the same counter); variant 3 the interleaved pair with the push's round
+ * count (7, Philox4x32-7). For known-answer checks of the generator. */
 int bz_philox4x32_10(const uint32_t *ctr, const uint32_t *key, int32_t n, int32_t variant, uint32_t *out,
                      void *stream);
 

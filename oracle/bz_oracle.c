@@ -28,10 +28,11 @@ static double c_jev(void) { return 6.241509 * 1e18; }
 /* ------------------------------------------------------------------------------------ */
 /* Philox4x32-10                                                                         */
 /* ------------------------------------------------------------------------------------ */
-void orc_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+/* Philox4x32 with a given number of rounds (10: Philox4x32-10) */
+void orc_philox_rounds(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4], int rounds) {
     uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
     uint32_t k0 = key[0], k1 = key[1];
-    for (int r = 0; r < 10; ++r) {
+    for (int r = 0; r < rounds; ++r) {
         uint64_t p0 = (uint64_t)0xD2511F53u * c0;
         uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
         uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
@@ -45,12 +46,18 @@ void orc_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
     }
     out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
+void orc_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) { orc_philox_rounds(ctr, key, out, 10); }
+
+/* Rounds of the push's draws (tags 0-2: gas velocity, collision, ionization), as in the
+ * kernels: Philox4x32-7. Resampling draws (tag 3) keep 10. */
+#define PUSH_ROUNDS 7
 
 /* Uniform conventions shared with the CUDA kernels (exact in the target type, and so is
  * the complement 1-u):
  *   float path : u = ((r >> 9) + 0.5) * 2^-23
  *   double path: u = (((r_a >> 6) << 26 | (r_b >> 6)) + 0.5) * 2^-52           */
 static void draw_u(const orc_params *p, uint64_t slot, uint32_t tag, double *u, int nu) {
+    const int rounds = tag <= 2u ? PUSH_ROUNDS : 10;
     uint32_t key[2] = {(uint32_t)p->seed, (uint32_t)(p->seed >> 32)};
     uint32_t ctr[4] = {(uint32_t)slot, (uint32_t)p->step, (uint32_t)(p->step >> 32), tag};
     uint32_t r[4];
@@ -58,16 +65,36 @@ static void draw_u(const orc_params *p, uint64_t slot, uint32_t tag, double *u, 
         int k = 0;
         for (uint32_t c = 0; k < nu; ++c) {
             ctr[3] = tag | (c << 8);
-            orc_philox(ctr, key, r);
+            orc_philox_rounds(ctr, key, r, rounds);
             for (int j = 0; j < 2 && k < nu; ++j, ++k) {
                 uint64_t m = ((uint64_t)(r[2 * j] >> 6) << 26) | (uint64_t)(r[2 * j + 1] >> 6);
                 u[k] = ((double)m + 0.5) * 0x1p-52;
             }
         }
     } else {
-        orc_philox(ctr, key, r);
+        orc_philox_rounds(ctr, key, r, rounds);
         for (int k = 0; k < nu && k < 4; ++k) u[k] = ((double)(r[k] >> 9) + 0.5) * 0x1p-23;
     }
+}
+
+/* Standard normal quantile Phi^-1(u) in float64, for the float32 kernels' gas velocity
+ * (they evaluate the same quantile in float32 from a polynomial fit, relative error
+ * 3.5e-7). A rational start (Abramowitz & Stegun 26.2.23, |error| < 4.5e-4), then Halley
+ * steps on 0.5 erfc(-g/sqrt 2) - q, with q the smaller of u and 1-u so that the tails keep
+ * their relative accuracy. */
+static double orc_ndtri(double u) {
+    const int upper = u > 0.5;
+    const double q = upper ? 1.0 - u : u; /* exact for the uniforms used here */
+    if (q == 0.5) return 0.0;
+    double t = sqrt(-2.0 * log(q));
+    double g = -(t - (2.515517 + 0.802853 * t + 0.010328 * t * t) / (1.0 + 1.432788 * t + 0.189269 * t * t + 0.001308 * t * t * t));
+    for (int it = 0; it < 4; ++it) {
+        double F = 0.5 * erfc(-g / M_SQRT2) - q;
+        double phi = exp(-0.5 * g * g) / sqrt(2.0 * M_PI);
+        double e = F / phi;
+        g -= e / (1.0 + 0.5 * g * e);
+    }
+    return upper ? -g : g;
 }
 
 /* Box-Muller: (r cos 2πb, r sin 2πb) with r = sqrt(-2 ln a). */
@@ -155,17 +182,26 @@ static void push_one(const orc_params *p, int64_t i, const double *in_d, const d
         for (int k = 0; k < 3; ++k) g[k] = gas[i * 3 + k];
     } else {
         double ug[4], uc[4], ui[1];
-        if (p->gas_sigma > 0) {
-            draw_u(p, (uint64_t)i, 0u, ug, 4);
-            double g3;
-            box_muller(ug[0], ug[1], &g[0], &g[1]);
-            box_muller(ug[2], ug[3], &g[2], &g3);
-            for (int k = 0; k < 3; ++k) g[k] *= p->gas_sigma;
+        g[0] = g[1] = g[2] = 0.0;
+        if (p->precision == 64) {
+            /* float64: Box-Muller from the gas draw, the child's azimuth from tag 2 */
+            if (p->gas_sigma > 0) {
+                draw_u(p, (uint64_t)i, 0u, ug, 4);
+                double g3;
+                box_muller(ug[0], ug[1], &g[0], &g[1]);
+                box_muller(ug[2], ug[3], &g[2], &g3);
+                for (int k = 0; k < 3; ++k) g[k] *= p->gas_sigma;
+            }
+            draw_u(p, (uint64_t)i, 2u, ui, 1);
         } else {
-            g[0] = g[1] = g[2] = 0.0;
+            /* float32: three normals by their quantiles from the gas draw's first three
+             * words, the child's azimuth from its fourth */
+            draw_u(p, (uint64_t)i, 0u, ug, 4);
+            if (p->gas_sigma > 0)
+                for (int k = 0; k < 3; ++k) g[k] = orc_ndtri(ug[k]) * p->gas_sigma;
+            ui[0] = ug[3];
         }
         draw_u(p, (uint64_t)i, 1u, uc, 4);
-        draw_u(p, (uint64_t)i, 2u, ui, 1);
         Ru[0] = uc[0]; Ru[1] = uc[1]; Ru[2] = uc[2]; Ru[3] = uc[3]; Ru[4] = 0.0; Ru[5] = ui[0];
     }
     double ax = vx - g[0], ay = vy - g[1], az = vz - g[2];

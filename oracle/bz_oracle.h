@@ -41,6 +41,7 @@ typedef struct orc_params {
 
 /* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11). */
 void orc_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+void orc_philox_rounds(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4], int rounds);
 
 /* electron_kernel_numba.py:38-287 for particles 0..n-1; children appended at n+k in
  * parent order. Returns the number of children (the reference's curr_count). */

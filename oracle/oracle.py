@@ -55,6 +55,8 @@ def lib():
         P = ctypes.POINTER(OrcParams)
         L.orc_philox.argtypes = [np.ctypeslib.ndpointer(np.uint32), np.ctypeslib.ndpointer(np.uint32),
                                  np.ctypeslib.ndpointer(np.uint32)]
+        L.orc_philox_rounds.argtypes = [np.ctypeslib.ndpointer(np.uint32), np.ctypeslib.ndpointer(np.uint32),
+                                        np.ctypeslib.ndpointer(np.uint32), ctypes.c_int]
         L.orc_push.argtypes = [P, ctypes.c_int64, _f64p, _f64p, _f64p, ctypes.c_void_p, ctypes.c_void_p]
         L.orc_push.restype = ctypes.c_int64
         L.orc_push_margin.argtypes = [P, ctypes.c_int64, _f64p, _f64p, _f64p, ctypes.c_void_p, ctypes.c_void_p,
@@ -212,7 +214,7 @@ def fluid(N, dx, dt, mu_i, D_i, E, ni):
     return ni, Ji, brk
 
 
-def philox(ctr, key):
+def philox(ctr, key, rounds=10):
     out = np.zeros(4, dtype=np.uint32)
-    lib().orc_philox(np.asarray(ctr, dtype=np.uint32), np.asarray(key, dtype=np.uint32), out)
+    lib().orc_philox_rounds(np.asarray(ctr, dtype=np.uint32), np.asarray(key, dtype=np.uint32), out, int(rounds))
     return out

@@ -77,9 +77,12 @@ def test_encodings_round_trip():
     np.testing.assert_allclose(f2, f, rtol=2e-3, atol=1e-6)
     np.testing.assert_allclose(kx2, kx, rtol=1e-5)
     np.testing.assert_allclose(ki2, ki, rtol=1e-5)
-    assert np.all(t[:, 66:] == 0)
+    np.testing.assert_allclose(S.decode_mean(t), S.eedf_mean(f), rtol=1e-5)  # default: the distribution's mean
+    m = rng.uniform(0.5, 20.0, 5)
+    np.testing.assert_allclose(S.decode_mean(S.targets(f, kx, ki, m)), m, rtol=1e-5)
+    assert np.all(t[:, 67:] == 0)
     w = S.output_weights()
-    assert w[:66].min() > 0 and np.all(w[66:] == 0)
+    assert w[:67].min() > 0 and np.all(w[67:] == 0)
 
 
 def test_features_and_bin_fractions():

@@ -94,3 +94,21 @@ def test_philox_known_answer():
     assert list(O.philox([0xffffffff] * 4, [0xffffffff] * 2)) == [0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd]
     assert list(O.philox([0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344], [0xa4093822, 0x299f31d0])) == \
         [0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1]
+
+
+def test_philox_seven_rounds_sanity():
+    """The push draws from Philox4x32-7 (the round count Salmon et al. report as passing
+    BigCrush). The round-parametrised generator gives Philox4x32-10 at 10 rounds, and its
+    7-round words are uniform and uncorrelated at the level a quick check sees: chi-square
+    of the top byte over 2^18 words, lag-1 correlation of consecutive counters."""
+    from scipy.stats import chi2
+    ctr0 = [0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344]
+    key = [0xa4093822, 0x299f31d0]
+    assert list(O.philox(ctr0, key, rounds=10)) == list(O.philox(ctr0, key))
+    words = np.array([O.philox([i, 17, 0, 1], key, rounds=7) for i in range(1 << 16)], dtype=np.uint64).ravel()
+    hist = np.bincount((words >> 24).astype(np.int64), minlength=256)
+    stat = float(((hist - words.size / 256) ** 2 / (words.size / 256)).sum())
+    assert chi2.sf(stat, 255) > 1e-4, stat
+    u = (words.astype(np.float64) + 0.5) / 2.0 ** 32
+    r = np.corrcoef(u[:-4:4], u[4::4])[0, 1]  # word 0 of counter i against word 0 of counter i+1
+    assert abs(r) < 5.0 / np.sqrt(u.size / 4), r

@@ -271,9 +271,9 @@ def test_push_capacity_flag():
 
 
 def test_device_philox_known_answer():
-    """The device Philox4x32-10 (plain rounds and the interleaved pair with round keys the
-    push draws from) gives the Random123 known-answer vectors and agrees with the oracle's
-    Philox on random counters and keys."""
+    """The device Philox4x32-10 (plain rounds and the interleaved pair with round keys)
+    gives the Random123 known-answer vectors and agrees with the oracle's Philox on random
+    counters and keys; so does the 7-round form the push draws from."""
     ctr = [[0, 0, 0, 0], [0xffffffff] * 4, [0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344]]
     key = [[0, 0], [0xffffffff] * 2, [0xa4093822, 0x299f31d0]]
     kat = [[0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8], [0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd],
@@ -286,3 +286,8 @@ def test_device_philox_known_answer():
     got = K.philox(c, k, 1)
     for i in range(0, 1000, 37):
         assert list(got[i]) == list(O.philox([int(v) for v in c[i]], [int(v) for v in k[i]])), i
+    # the push's draws: the same generator with 7 rounds (Philox4x32-7), device and oracle
+    got = K.philox(c, k, 3)
+    for i in range(0, 1000, 37):
+        assert list(got[i]) == list(O.philox([int(v) for v in c[i]], [int(v) for v in k[i]], rounds=7)), i
+    assert got[0].tolist() != K.philox(c[:1], k[:1], 1)[0].tolist()
