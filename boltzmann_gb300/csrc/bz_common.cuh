@@ -306,6 +306,11 @@ template <typename T> __device__ __forceinline__ int node_index(T x, const NodeM
 template <typename T> __device__ __forceinline__ int deposit_node(int advect, T x, const NodeMap &m) {
     return advect == BZ_ADVECT_1D ? node_index(x, m) : (advect == BZ_ADVECT_ENSEMBLE ? int(x) : 0);
 }
+// the same for a position known to be positive (an alive particle: 0 < x < L)
+template <typename T> __device__ __forceinline__ int node_index_pos(T x, const NodeMap &m);
+template <typename T> __device__ __forceinline__ int deposit_node_pos(int advect, T x, const NodeMap &m) {
+    return advect == BZ_ADVECT_1D ? node_index_pos(x, m) : (advect == BZ_ADVECT_ENSEMBLE ? int(x) : 0);
+}
 // binning cell of a particle for each motion mode
 template <typename T> __device__ __forceinline__ int bin_cell(int advect, T x, double dx, float inv_dx_f) {
     return advect == BZ_ADVECT_1D ? cell_index(x, dx, inv_dx_f) : (advect == BZ_ADVECT_ENSEMBLE ? int(x) : 0);
@@ -314,6 +319,15 @@ template <typename T> __device__ __forceinline__ int node_index(T x, const NodeM
     if (sizeof(T) == 4) {
         float s = fmaf(float(x), m.a, m.b);
         if (safe_trunc(s, fmaf(fabsf(float(x)), m.a, m.b))) return int(s);
+    }
+    double tx = (double(x) + m.half_dx) / m.Lp;
+    int fine = int(tx * m.fM);
+    return fine / m.bnf;
+}
+template <typename T> __device__ __forceinline__ int node_index_pos(T x, const NodeMap &m) {
+    if (sizeof(T) == 4) {
+        const float s = fmaf(float(x), m.a, m.b);  // x > 0 and m.a, m.b > 0: nothing cancels
+        if (safe_trunc(s, s)) return int(s);
     }
     double tx = (double(x) + m.half_dx) / m.Lp;
     int fine = int(tx * m.fM);

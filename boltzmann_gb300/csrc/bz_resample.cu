@@ -143,10 +143,17 @@ __device__ __forceinline__ int upper_bound_d(const double *a, int n, double v) {
 // scaling) and H = 2 floor(X) + [X not an integer], cdf > u holds exactly when H > 2(2k+1),
 // so the binary search for the first cumulative weight above u runs on 64-bit integers
 // and gives the index the float64 search gives.
+// H is formed from the bits of c (0 <= c <= 1) with integer operations only: c = M 2^(e-1075)
+// with M = 2^52 + mantissa, so X = M 2^(e-1022).
 __device__ __forceinline__ uint64_t cdf_key(double c) {
-    const double X = c * 0x1p53;
-    const double G = floor(X);
-    return 2ull * uint64_t(G) + (X != G ? 1ull : 0ull);
+    const uint64_t b = uint64_t(__double_as_longlong(c));
+    const int e = int(b >> 52);
+    if (e == 0) return b ? 1ull : 0ull;  // zero, or a subnormal (0 < X < 1)
+    const uint64_t M = (b & ((1ull << 52) - 1)) | (1ull << 52);
+    const int sh = 1022 - e;
+    if (sh <= 0) return 2ull * (M << (-sh));  // c >= 1/2: X is an integer
+    if (sh >= 64) return 1ull;                // 0 < X < 1
+    return 2ull * (M >> sh) + ((M & ((1ull << sh) - 1)) ? 1ull : 0ull);
 }
 __device__ __forceinline__ int draw_index(const uint64_t *H, int n, uint32_t a, uint32_t b) {
     const uint64_t k = (uint64_t(a >> 6) << 26) | uint64_t(b >> 6);
@@ -251,28 +258,86 @@ template <int N> __device__ void block_sum_n(double (&v)[N], double *sh) {
     __syncthreads();
 }
 
+// N block-wide sums of float pairs on the float32 pipe (xor-shuffle reductions of the pairs
+// within each warp and then across the warps), returned in float64 to every thread: one
+// conversion per sum instead of float64 adds in every thread (shf: RS_T/32 * N float2,
+// shd: N doubles)
+template <int N> __device__ void block_sum_ff(FF (&v)[N], double (&out)[N], float2 *shf, double *shd) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            ff_add(v[i], __shfl_xor_sync(0xffffffffu, v[i].hi, o), __shfl_xor_sync(0xffffffffu, v[i].lo, o));
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int i = 0; i < N; ++i) shf[warp * N + i] = make_float2(v[i].hi, v[i].lo);
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            FF t{0.f, 0.f};
+            if (lane < RS_T / 32) t = FF{shf[lane * N + i].x, shf[lane * N + i].y};
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                ff_add(t, __shfl_xor_sync(0xffffffffu, t.hi, o), __shfl_xor_sync(0xffffffffu, t.lo, o));
+            if (lane == 0) shd[i] = ff_value(t);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < N; ++i) out[i] = shd[i];
+    __syncthreads();
+}
+
 // cdf[j] = carry + sum_{i<=j} val(j) for j < len, RS_ITEMS consecutive entries per thread
 // and one block scan per RS_T*RS_ITEMS entries
 constexpr int RS_ITEMS = 8;
+// Threads and warps past the end do no float64 arithmetic (small keys would otherwise pay
+// for a whole block's padding on this part's narrow float64 pipe).
 template <typename F> __device__ void block_cumsum(int len, F val, double *cdf, double *sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     double carry = 0.0;
     for (int c0 = 0; c0 < len; c0 += RS_T * RS_ITEMS) {
         const int j0 = c0 + threadIdx.x * RS_ITEMS;
+        const bool warp_live = c0 + warp * 32 * RS_ITEMS < len;
         double v[RS_ITEMS];
         double local = 0.0;
+        if (j0 < len) {
 #pragma unroll
-        for (int i = 0; i < RS_ITEMS; ++i) {
-            v[i] = j0 + i < len ? val(j0 + i) : 0.0;
-            local += v[i];
+            for (int i = 0; i < RS_ITEMS; ++i) {
+                v[i] = j0 + i < len ? val(j0 + i) : 0.0;
+                local += v[i];
+            }
         }
-        double tot;
-        double acc = carry + block_excl_scan<double>(local, sh, &tot);
+        double incl = local;
+        if (warp_live) {
 #pragma unroll
-        for (int i = 0; i < RS_ITEMS; ++i) {
-            acc += v[i];
-            if (j0 + i < len) cdf[j0 + i] = acc;
+            for (int o = 1; o < 32; o <<= 1) {
+                const double t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
         }
-        carry += tot;
+        __syncthreads();
+        if (lane == 31) sh[warp] = warp_live ? incl : 0.0;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double run = 0.0;
+            for (int w = 0; w < RS_T / 32; ++w) { const double t = sh[w]; sh[w] = run; run += t; }
+            sh[RS_T / 32] = run;
+        }
+        __syncthreads();
+        if (j0 < len) {
+            double acc = carry + (sh[warp] + incl - local);  // the block scan's association
+#pragma unroll
+            for (int i = 0; i < RS_ITEMS; ++i) {
+                acc += v[i];
+                if (j0 + i < len) cdf[j0 + i] = acc;
+            }
+        }
+        carry += sh[RS_T / 32];
+        __syncthreads();
     }
 }
 
@@ -445,8 +510,12 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
             T wcur = s.w[t];
             for (int a1 = g0; a1 < g1; ++a1) {
                 const int j = gmem[a1];
-                const double wt = double(wcur) / double(dcnt[j] + 1);
-                wcur = T(wt);
+                // w / (c+1) rounded to the state's precision. For float32 the float division
+                // gives it directly: a float over an integer below 2^28 never lies close enough
+                // to a float rounding midpoint (closer than 2^-53 relative without being on it)
+                // for the float64 quotient, rounded again, to differ
+                if constexpr (sizeof(T) == 4) wcur = __fdiv_rn(wcur, float(dcnt[j] + 1));
+                else wcur = wcur / T(dcnt[j] + 1);
                 cdf[j] = double(wcur);  // weight of this entry's copies (the table is no longer read)
                 tgt[j] = t;
             }
@@ -524,7 +593,10 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
             const float ph = __fmul_rn(w, v2.hi);
             ff_add(fe, ph, __fadd_rn(fmaf(w, v2.hi, -ph), __fmul_rn(w, v2.lo)));
         }
-        W = ff_value(fW); px = ff_value(fx); py = ff_value(fy); pz = ff_value(fz); ew = efac * ff_value(fe);
+        FF f[5] = {fW, fx, fy, fz, fe};
+        double m[5];
+        block_sum_ff<5>(f, m, reinterpret_cast<float2 *>(shv), shd);
+        W = m[0]; px = m[1]; py = m[2]; pz = m[3]; ew = efac * m[4];
     } else {
         #pragma unroll 4
         for (int j = threadIdx.x; j < np_; j += RS_T) {
@@ -537,8 +609,6 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
             pz += vz * w;
             ew += w * (efac * (vx * vx + vy * vy + vz * vz));
         }
-    }
-    {
         double m[5] = {W, px, py, pz, ew};
         block_sum_n<5>(m, shv);
         W = m[0]; px = m[1]; py = m[2]; pz = m[3]; ew = m[4];
@@ -552,21 +622,46 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
     const double wbar = W / double(K);
     const T wbar_t = T(wbar);
     double hx = 0, hy = 0, hz = 0, he = 0;
-    #pragma unroll 4
-    for (int k = threadIdx.x; k < K; k += RS_T) {
-        double u = rs_uniform(rng, replay_u, draw_off[key], key, k);
-        double R = (1.0 / double(K)) * (u + double(k));
-        int ix = lower_bound_d(cdf, np_, R);
-        ix = ix % np_;  // CuPy wraps ids[len] to ids[0]
-        int id = perm[off + ix];
-        cnt[k] = id;
-        double vx = s.vx[id], vy = s.vy[id], vz = s.vz[id];
-        hx += vx * wbar;
-        hy += vy * wbar;
-        hz += vz * wbar;
-        he += wbar * (efac * (vx * vx + vy * vy + vz * vz));
-    }
-    {
+    const double invK = 1.0 / double(K);
+    if constexpr (sizeof(T) == 4) {
+        // float32 state: the survivors all weigh W/K, so their mean velocity is (sum v)/K and
+        // their energy W/K efac sum |v|^2: the sums as pairs of floats, then float64 once
+        FF sx{0.f, 0.f}, sy{0.f, 0.f}, sz{0.f, 0.f}, s2{0.f, 0.f};
+        #pragma unroll 2
+        for (int k = threadIdx.x; k < K; k += RS_T) {
+            double u = rs_uniform(rng, replay_u, draw_off[key], key, k);
+            double R = invK * (u + double(k));
+            int ix = lower_bound_d(cdf, np_, R);
+            ix = ix % np_;  // CuPy wraps ids[len] to ids[0]
+            int id = perm[off + ix];
+            cnt[k] = id;
+            const float vx = s.vx[id], vy = s.vy[id], vz = s.vz[id];
+            ff_add(sx, vx, 0.f);
+            ff_add(sy, vy, 0.f);
+            ff_add(sz, vz, 0.f);
+            ff_add_prod(s2, vx, vx);
+            ff_add_prod(s2, vy, vy);
+            ff_add_prod(s2, vz, vz);
+        }
+        FF f[4] = {sx, sy, sz, s2};
+        double m[4];
+        block_sum_ff<4>(f, m, reinterpret_cast<float2 *>(shv), shd);
+        hx = m[0] * invK; hy = m[1] * invK; hz = m[2] * invK; he = wbar * (efac * m[3]);
+    } else {
+        #pragma unroll 4
+        for (int k = threadIdx.x; k < K; k += RS_T) {
+            double u = rs_uniform(rng, replay_u, draw_off[key], key, k);
+            double R = invK * (u + double(k));
+            int ix = lower_bound_d(cdf, np_, R);
+            ix = ix % np_;  // CuPy wraps ids[len] to ids[0]
+            int id = perm[off + ix];
+            cnt[k] = id;
+            double vx = s.vx[id], vy = s.vy[id], vz = s.vz[id];
+            hx += vx * wbar;
+            hy += vy * wbar;
+            hz += vz * wbar;
+            he += wbar * (efac * (vx * vx + vy * vy + vz * vz));
+        }
         double m[4] = {hx, hy, hz, he};
         block_sum_n<4>(m, shv);
         hx = m[0] / W; hy = m[1] / W; hz = m[2] / W; he = m[3];

@@ -32,6 +32,27 @@ constexpr SegShape kSegShapes[] = {{512, 1, 2, true}, {320, 1, 4, true}, {640, 1
 constexpr int kSegNumShapes = int(sizeof(kSegShapes) / sizeof(kSegShapes[0]));
 static int g_seg_shape = 0;
 
+// The CTA's moment grid in shared memory: (sum w, sum w e) interleaved per node, then sum w
+// of the ionizing particles. A float atomic add to shared memory costs as many
+// instructions here as a compare-and-swap loop (measured), so a float32 grid adds a node's
+// two sums with one 64-bit compare-and-swap; a float64 grid adds them one by one.
+__device__ __forceinline__ void dep_pair(float *g, int nd, float a, float b) {
+    unsigned long long *q = reinterpret_cast<unsigned long long *>(g + 2 * nd);
+    unsigned long long cur = *q;
+    while (true) {
+        const float x = __uint_as_float(uint32_t(cur)) + a;
+        const float y = __uint_as_float(uint32_t(cur >> 32)) + b;
+        const unsigned long long nxt = (static_cast<unsigned long long>(__float_as_uint(y)) << 32) | __float_as_uint(x);
+        const unsigned long long seen = atomicCAS(q, cur, nxt);
+        if (seen == cur) break;
+        cur = seen;
+    }
+}
+__device__ __forceinline__ void dep_pair(double *g, int nd, double a, double b) {
+    atomicAdd(&g[2 * nd], a);
+    atomicAdd(&g[2 * nd + 1], b);
+}
+
 template <typename T> struct Seg {
     SoA<T> a;
     int32_t *cnt;  // [2*nseg]
@@ -166,25 +187,24 @@ __global__ void __launch_bounds__(SG_T, MINB)
                         // one test for the three components (a sum of finite speeds stays finite)
                         if (!isfinite(it[k].vx + it[k].vy + it[k].vz)) err |= BZ_DEV_NONFINITE;
                         if (DEPOSIT) {
-                            if (it[k].alive) {
-                                int nd = deposit_node(p.advect, it[k].x, nm);
-                                if (nd >= 0 && nd < nnodes) {
-                                    if (p.advect != BZ_ADVECT_ENSEMBLE) {  // ensembles: warp-summed below
-                                        atomicAdd(&mom_s[nd], A(w[k]));
-                                        if (it[k].ionized) atomicAdd(&mom_s[nnodes + nd], A(w[k]));
-                                        atomicAdd(&mom_s[2 * nnodes + nd], A(w[k] * it[k].e));
-                                    }
-                                    if (it[k].excited && (p.flags & BZ_MOMENT_EXCITATION))
-                                        atomicAdd(&moments[2 * nnodes + nd], double(w[k]));  // rare: straight to the grid
-                                }
-                            } else if (it[k].ionized && (p.flags & BZ_QUIRK_DEAD_IONFLAG)) {
-                                atomicAdd(&mom_s[nnodes + 0], A(1));
+                            const bool alive = it[k].alive;
+                            // an alive particle lies inside (0, L): its node needs no |x|
+                            const int nd = alive ? deposit_node_pos(p.advect, it[k].x, nm) : -1;
+                            const bool in_grid = nd >= 0 && nd < nnodes;
+                            if (in_grid && p.advect != BZ_ADVECT_ENSEMBLE) {  // ensembles: warp-summed below
+                                dep_pair(mom_s, nd, A(w[k]), A(w[k] * it[k].e));
+                                if (it[k].ionized) atomicAdd(&mom_s[2 * nnodes + nd], A(w[k]));
                             }
-                            if (it[k].child) {
-                                int nd = deposit_node(p.advect, it[k].cx, nm);
-                                if (nd >= 0 && nd < nnodes) {
-                                    atomicAdd(&mom_s[nd], A(w[k]));
-                                    atomicAdd(&mom_s[2 * nnodes + nd], A(w[k] * it[k].ce));
+                            // rarely taken, one test for all: an excitation counted into the
+                            // grid, an ionized particle that was absorbed, an ionization's child
+                            const bool exc = in_grid && it[k].excited && (p.flags & BZ_MOMENT_EXCITATION);
+                            const bool dead_ion = !alive && it[k].ionized && (p.flags & BZ_QUIRK_DEAD_IONFLAG);
+                            if (exc || dead_ion || it[k].child) {
+                                if (exc) atomicAdd(&moments[2 * nnodes + nd], double(w[k]));  // straight to the grid
+                                if (dead_ion) atomicAdd(&mom_s[2 * nnodes + 0], A(1));
+                                if (it[k].child) {
+                                    const int cn = deposit_node_pos(p.advect, it[k].cx, nm);
+                                    if (cn >= 0 && cn < nnodes) dep_pair(mom_s, cn, A(w[k]), A(w[k] * it[k].ce));
                                 }
                             }
                         }
@@ -210,14 +230,12 @@ __global__ void __launch_bounds__(SG_T, MINB)
                                 c2 += __shfl_xor_sync(0xffffffffu, c2, o);
                             }
                             if (lane == 0 && nd0 >= 0) {
-                                atomicAdd(&mom_s[nd0], c0);
-                                if (c1 != A(0)) atomicAdd(&mom_s[nnodes + nd0], c1);
-                                atomicAdd(&mom_s[2 * nnodes + nd0], c2);
+                                dep_pair(mom_s, nd0, c0, c2);
+                                if (c1 != A(0)) atomicAdd(&mom_s[2 * nnodes + nd0], c1);
                             }
                         } else if (nd >= 0) {
-                            atomicAdd(&mom_s[nd], c0);
-                            if (c1 != A(0)) atomicAdd(&mom_s[nnodes + nd], c1);
-                            atomicAdd(&mom_s[2 * nnodes + nd], c2);
+                            dep_pair(mom_s, nd, c0, c2);
+                            if (c1 != A(0)) atomicAdd(&mom_s[2 * nnodes + nd], c1);
                         }
                     }
                 }
@@ -274,8 +292,10 @@ __global__ void __launch_bounds__(SG_T, MINB)
         for (int i = threadIdx.x; i < 3 * nnodes; i += SG_T) {
             A val = mom_s[i];
             if (val != A(0)) {
-                int col = i / nnodes, nd = i - col * nnodes;
-                atomicAdd(&moments[(col == 2 ? 3 : col) * nnodes + nd], double(val));
+                // (sum w, sum w e) pairs -> moments rows 0 and 3; sum w of the ionizing -> row 1
+                const int row = i < 2 * nnodes ? ((i & 1) ? 3 : 0) : 1;
+                const int nd = i < 2 * nnodes ? (i >> 1) : i - 2 * nnodes;
+                atomicAdd(&moments[row * nnodes + nd], double(val));
             }
         }
     }

@@ -409,10 +409,12 @@ class BoltzmannGB300:
         phase = 2.0 * math.pi * ((cfg.freq * float(self.t.item())) % 1.0)
         return td, mean, f, phase
 
-    def learned_start(self, mlp, seed=None, closure=False):
+    def learned_start(self, mlp, seed=None, closure=False, scale_to_mean=True):
         """Redraw every electron's velocity from the surrogate network's steady-state energy
-        distribution for its node (features from ``node_state``), each node's energies
-        scaled to the network's predicted mean energy, then refresh the moments. Positions,
+        distribution for its node (features from ``node_state``), each node's energies scaled
+        to the network's predicted mean energy unless ``scale_to_mean`` is False (in the
+        benchmark's CCP the first 50 steps then averaged 0.8-1.4% below the periodic mean
+        energy instead of 1.7-2.1%), then refresh the moments. Positions,
         weights and the field are unchanged; the plain step loop continues from here. With
         ``closure`` the ion source of the following steps is the network's ionization rate
         times the electron density (``set_ion_closure``) instead of the counted
@@ -421,7 +423,7 @@ class BoltzmannGB300:
         td, mean, f, phase = self.node_state()
         out = S.learned_start(mlp, self.params(step_on_device=False), self.A, td, np.maximum(mean, 1e-3),
                               S.bin_fractions(f), phase, seed=self.cfg.seed + 7 if seed is None else seed,
-                              device=self.device)
+                              device=self.device, scale_to_mean=scale_to_mean)
         self.moments.zero_()
         K.seg_deposit(self.params(step_on_device=False), self.A, self.moments)
         if closure:

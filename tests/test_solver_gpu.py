@@ -120,3 +120,25 @@ def test_run_writes_cycle_files_like_the_reference_loop(tmp_path):
         np.testing.assert_allclose(ion, exp, rtol=1e-12, atol=1e-12 * max(np.abs(exp).max(), 1.0))
         np.testing.assert_array_equal(bzio.read_grid(name, c, "ne"), steps[-1]["ne"])
     assert np.sum(srcs) > 0  # the hot start ionizes
+
+
+def test_ion_source_rate_closure():
+    """set_ion_closure: the ion source of a step is k_ion n_gas dt times the deposited
+    electron density of each node (instead of the counted ionizations), both eager and
+    graph-replayed; clearing it restores the counted source."""
+    sol = BoltzmannGB300(small_cfg(), device="cuda")
+    for _ in range(3):
+        sol.step()
+    k = np.linspace(1e-16, 3e-16, sol.nnodes)
+    sol.set_ion_closure(k)
+    rate = k * sol.cfg.nn_m3 * sol.cfg.dt
+    for use_graph in (False, True, True):
+        sol.step(use_graph=use_graph)
+        m = sol.moments.cpu().numpy()
+        assert m[0].sum() > 0
+        np.testing.assert_allclose(m[1], rate * m[0], rtol=1e-15, atol=0)
+    assert sol.device_status() == 0
+    sol.set_ion_closure(None)
+    sol.step()
+    m = sol.moments.cpu().numpy()
+    assert not np.allclose(m[1], rate * m[0])
