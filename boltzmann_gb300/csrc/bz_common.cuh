@@ -23,10 +23,11 @@ constexpr double X_DEAD = 0.00000001;  // where the reference parks absorbed par
 // --------------------------------------------------------------------------------------
 struct u32x4 { uint32_t x, y, z, w; };
 
-__device__ __forceinline__ u32x4 philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0,
-                                        uint32_t k1) {
+template <int ROUNDS = 10>
+__device__ __forceinline__ u32x4 philox_r(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0,
+                                          uint32_t k1) {
 #pragma unroll
-    for (int r = 0; r < 10; ++r) {
+    for (int r = 0; r < ROUNDS; ++r) {
         // one 32x32 -> 64-bit product per multiplier gives both halves
         const uint64_t p0 = uint64_t(0xD2511F53u) * c0;
         const uint64_t p1 = uint64_t(0xCD9E8D57u) * c2;
@@ -41,13 +42,18 @@ __device__ __forceinline__ u32x4 philox(uint32_t c0, uint32_t c1, uint32_t c2, u
     }
     return {c0, c1, c2, c3};
 }
+__device__ __forceinline__ u32x4 philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0,
+                                        uint32_t k1) {
+    return philox_r<10>(c0, c1, c2, c3, k0, k1);
+}
 
 // Rounds of the push's draws (gas velocity, collision, ionization). Salmon et al. report
 // Philox4x32 with 7 rounds as the smallest round count that passes all of TestU01's
 // BigCrush ("Crush-resistant", SC'11 Table 2) and recommend 10 as a margin; the push, whose
-// runtime these rounds dominate after the memory traffic, uses 7. Every other stream here
-// (resampling, energy redraws, minibatches, the known-answer checks) keeps 10.
+// runtime these rounds dominate after the memory traffic, uses 7, and so do the resampling
+// draws (RS_ROUNDS). The energy redraws, the minibatches and the known-answer checks keep 10.
 constexpr int PUSH_ROUNDS = 7;
+constexpr int RS_ROUNDS = 7;
 
 // The same generator with the round keys precomputed (k + r*W, r = 0..9): when they sit
 // in the kernel's parameter space the XORs read them directly and no key schedule runs.

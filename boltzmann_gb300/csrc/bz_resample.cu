@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(1024) k_rs_decide(const int32_t *counts, const
 __device__ __forceinline__ double rs_uniform(const Rng &g, const double *replay_u, int64_t draw_base, int key,
                                              int j) {
     if (replay_u) return replay_u[draw_base + j];
-    u32x4 r = philox(uint32_t(key), uint32_t(j >> 1), g.s0, 3u | (g.s1 << 8), g.k0, g.k1);
+    u32x4 r = philox_r<RS_ROUNDS>(uint32_t(key), uint32_t(j >> 1), g.s0, 3u | (g.s1 << 8), g.k0, g.k1);
     return (j & 1) ? uni_d(r.z, r.w).u : uni_d(r.x, r.y).u;
 }
 
@@ -341,6 +341,34 @@ template <typename F> __device__ void block_cumsum(int len, F val, double *cdf, 
     }
 }
 
+// in-place exclusive scan of a[0, n) (int32), RS_ITEMS consecutive entries per thread and
+// one block scan per RS_T * RS_ITEMS entries; the result also into b when given; returns
+// the total to every thread. Ends without a barrier: callers synchronise before reading.
+__device__ int64_t block_scan_inplace(int32_t *a, int32_t *b, int n, int64_t *shi) {
+    int64_t carry = 0;
+    for (int c0 = 0; c0 < n; c0 += RS_T * RS_ITEMS) {
+        const int j0 = c0 + threadIdx.x * RS_ITEMS;
+        int v[RS_ITEMS];
+        int local = 0;
+#pragma unroll
+        for (int i = 0; i < RS_ITEMS; ++i) {
+            v[i] = j0 + i < n ? a[j0 + i] : 0;
+            local += v[i];
+        }
+        int64_t tot;
+        int64_t acc = carry + block_excl_scan<int64_t>(local, shi, &tot);
+#pragma unroll
+        for (int i = 0; i < RS_ITEMS; ++i)
+            if (j0 + i < n) {
+                a[j0 + i] = int32_t(acc);
+                if (b) b[j0 + i] = int32_t(acc);
+                acc += v[i];
+            }
+        carry += tot;
+    }
+    return carry;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const int32_t *n_ptr, int64_t cap, int nb,
                                                    const int32_t *targets, const int32_t *max_ppc, double min_wt,
@@ -381,17 +409,20 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
         // ---- split (boltzmann.py:806-823): candidates w > min_wt, in index order
         int nhw = 0;
         double W = 0.0;
-        // compact candidates into cnt[] (their particle ids), RS_ITEMS consecutive entries per
-        // thread and one block scan per RS_T * RS_ITEMS entries
+        // compact candidates into cnt[] (their particle ids) and their weights, in float64,
+        // into the table (kept for the cumsum): RS_ITEMS consecutive entries per thread and one
+        // block scan per RS_T * RS_ITEMS entries
         for (int c0 = 0; c0 < n_k; c0 += RS_T * RS_ITEMS) {
             const int j0 = c0 + threadIdx.x * RS_ITEMS;
             int ids[RS_ITEMS];
+            T wv[RS_ITEMS];
             uint32_t hwm = 0;
             int local = 0;
 #pragma unroll
             for (int i = 0; i < RS_ITEMS; ++i) {
                 ids[i] = j0 + i < n_k ? perm[off + j0 + i] : -1;
-                if (ids[i] >= 0 && above_min(s.w[ids[i]], min_wt, wmin_f)) {
+                wv[i] = ids[i] >= 0 ? s.w[ids[i]] : T(0);
+                if (ids[i] >= 0 && above_min(wv[i], min_wt, wmin_f)) {
                     hwm |= 1u << i;
                     ++local;
                 }
@@ -400,17 +431,17 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
             int64_t pos = block_excl_scan<int64_t>(local, shi, &tot);
 #pragma unroll
             for (int i = 0; i < RS_ITEMS; ++i)
-                if ((hwm >> i) & 1u) cnt[nhw + pos++] = ids[i];
+                if ((hwm >> i) & 1u) {
+                    const double wd = double(wv[i]);
+                    cnt[nhw + pos] = ids[i];
+                    cdf[nhw + pos] = wd;
+                    W += wd;
+                    ++pos;
+                }
             nhw += int(tot);
         }
         __syncthreads();
         if (nhw == 0) return;
-        #pragma unroll 4
-        for (int j = threadIdx.x; j < nhw; j += RS_T) {  // the weights in float64, kept for the cumsum
-            const double wd = double(s.w[cnt[j]]);
-            cdf[j] = wd;
-            W += wd;
-        }
         W = block_sum<double>(W, shd);
         // cdf = cumsum(w/W), then / cdf[-1] (CuPy RandomState.choice with p); the
         // divisions are multiplications by the reciprocal (within 2 ulp; float64 division
@@ -419,34 +450,36 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
         block_cumsum(nhw, [&](int j) { return cdf[j] * inv_W; }, cdf, shd);  // in place
         __syncthreads();
         const double inv_last = 1.0 / cdf[nhw - 1];
-        // scratch regions of this key: hw_ids = candidate ids, tgt = copy targets, and the
-        // target groups of the divisions (gstart, gfill, gmem); the draw counts sit in shared
-        // memory when the table does, else in cnt
-        int32_t *hw_ids = ws_cnt + cap + off;
+        // Scratch of this key. A table that fits shared memory (small) keeps the draw counts
+        // there too, so cnt keeps the candidate ids and, once the draws are made, the table's
+        // space holds the target groups' starts and fill pointers; otherwise the draw counts,
+        // a copy of the ids and the groups live in the scratch. gmem (the groups' members),
+        // tgt (each entry's target) and wgt (the weight of each entry's copies) are scratch.
+        const bool small = nhw <= RS_CDF;
+        int32_t *dcnt = small ? cnt_sh : cnt;
+        int32_t *hw_ids = small ? cnt : ws_cnt + cap + off;
         int32_t *tgt = ws_cnt + 2 * cap + off;
-        int32_t *gstart = ws_cnt + 3 * cap + off;
-        int32_t *gfill = ws_cnt + 4 * cap + off;
+        int32_t *gstart = small ? reinterpret_cast<int32_t *>(cdf_sh) : ws_cnt + 3 * cap + off;
+        int32_t *gfill = small ? reinterpret_cast<int32_t *>(cdf_sh) + nhw : ws_cnt + 4 * cap + off;
         int32_t *gmem = ws_cnt + 5 * cap + off;
-        int32_t *dcnt = nhw <= RS_CDF ? cnt_sh : cnt;
+        T *wgt = reinterpret_cast<T *>(ws_cdf + off);
         const bool ints = replay_u == nullptr;  // Philox draws: the table as integer keys
         uint64_t *H = reinterpret_cast<uint64_t *>(cdf);
         for (int j = threadIdx.x; j < nhw; j += RS_T) {
             const double c = cdf[j] * inv_last;
             if (ints) H[j] = cdf_key(c);
             else cdf[j] = c;
-            hw_ids[j] = cnt[j];
+            if (!small) hw_ids[j] = cnt[j];
         }
         __syncthreads();
-        for (int j = threadIdx.x; j < nhw; j += RS_T) {
-            dcnt[j] = 0;
-            gstart[j] = 0;
-        }
+        for (int j = threadIdx.x; j < nhw; j += RS_T) dcnt[j] = 0;
         __syncthreads();
         const int m = int(2 * T_ - n_k);
         if (ints) {
             // draws 2i and 2i+1 come from one Philox call (rs_uniform's stream)
             for (int i = threadIdx.x; 2 * i < m; i += RS_T) {
-                const u32x4 r = philox(uint32_t(key), uint32_t(i), rng.s0, 3u | (rng.s1 << 8), rng.k0, rng.k1);
+                const u32x4 r = philox_r<RS_ROUNDS>(uint32_t(key), uint32_t(i), rng.s0, 3u | (rng.s1 << 8), rng.k0,
+                                                    rng.k1);
                 atomicAdd(&dcnt[draw_index(H, nhw, r.x, r.y)], 1);
                 if (2 * i + 1 < m) atomicAdd(&dcnt[draw_index(H, nhw, r.z, r.w)], 1);
             }
@@ -467,36 +500,17 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
         // sort), and each target's group is worked through by one thread in entry order,
         // all targets at once.
         const bool wrap = (p.flags & BZ_QUIRK_SPLIT_WRAP) != 0;
+        for (int j = threadIdx.x; j < nhw; j += RS_T) gstart[j] = 0;  // the table is no longer read
+        __syncthreads();
         for (int j = threadIdx.x; j < nhw; j += RS_T)
             if (dcnt[j]) atomicAdd(&gstart[wrap ? hw_ids[j] % nhw : j], 1);
         __syncthreads();
-        {
-            int64_t carry = 0;  // group sizes -> group starts (exclusive scan)
-            for (int c0 = 0; c0 < nhw; c0 += RS_T * RS_ITEMS) {
-                const int j0 = c0 + threadIdx.x * RS_ITEMS;
-                int v[RS_ITEMS];
-                int local = 0;
-#pragma unroll
-                for (int i = 0; i < RS_ITEMS; ++i) {
-                    v[i] = j0 + i < nhw ? gstart[j0 + i] : 0;
-                    local += v[i];
-                }
-                int64_t tot;
-                int64_t acc = carry + block_excl_scan<int64_t>(local, shi, &tot);
-#pragma unroll
-                for (int i = 0; i < RS_ITEMS; ++i)
-                    if (j0 + i < nhw) {
-                        gstart[j0 + i] = int32_t(acc);
-                        gfill[j0 + i] = int32_t(acc);
-                        acc += v[i];
-                    }
-                carry += tot;
-            }
-        }
+        block_scan_inplace(gstart, gfill, nhw, shi);  // group sizes -> group starts (and fill pointers)
         __syncthreads();
         for (int j = threadIdx.x; j < nhw; j += RS_T)
             if (dcnt[j]) gmem[atomicAdd(&gfill[wrap ? hw_ids[j] % nhw : j], 1)] = j;
         __syncthreads();
+        #pragma unroll 4
         for (int g = threadIdx.x; g < nhw; g += RS_T) {
             const int g0 = gstart[g], g1 = gfill[g];  // after the fill, gfill[g] is the group's end
             if (g1 == g0) continue;
@@ -516,32 +530,48 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
                 // for the float64 quotient, rounded again, to differ
                 if constexpr (sizeof(T) == 4) wcur = __fdiv_rn(wcur, float(dcnt[j] + 1));
                 else wcur = wcur / T(dcnt[j] + 1);
-                cdf[j] = double(wcur);  // weight of this entry's copies (the table is no longer read)
+                wgt[j] = wcur;
                 tgt[j] = t;
             }
             s.w[t] = wcur;
         }
         __syncthreads();
-        // copies, in entry order. One entry per thread: a block scan of the counts gives each
-        // warp one contiguous output range for its 32 entries, which the warp fills 32 slots
-        // at a time with coalesced stores; each lane finds the entry of its slot by a binary
-        // search over the lanes' offsets and takes the entry's values by shuffles. The slots
-        // and their values are the ones a loop over each entry's copies writes.
-        const int lane = threadIdx.x & 31;
-        int64_t carry2 = 0;
-        for (int c0 = 0; c0 < nhw; c0 += RS_T) {
-            const int j = c0 + threadIdx.x;
-            const int c = j < nhw ? dcnt[j] : 0;
-            int64_t tot;
-            const int64_t ex = carry2 + block_excl_scan<int64_t>(c, shi, &tot);
-            T xx = T(0), a1 = T(0), a2 = T(0), a3 = T(0), ww = T(0);
-            if (c) {
-                const int t = tgt[j];
-                xx = s.x[t]; a1 = s.vx[t]; a2 = s.vy[t]; a3 = s.vz[t]; ww = T(cdf[j]);
+        // copies, in entry order: the counts become each entry's first output slot (one block
+        // scan in place), then every warp works through chunks of 32 entries on its own, with
+        // no block barrier: the chunk's slots are one contiguous range, which the warp fills 32
+        // slots at a time with coalesced stores, each lane finding the entry of its slot by a
+        // binary search over the lanes' first slots and taking the entry's values by shuffles.
+        // The slots and their values are the ones a loop over each entry's copies writes.
+        const int total = int(block_scan_inplace(dcnt, nullptr, nhw, shi));
+        __syncthreads();
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        // one chunk's entry per lane: its first slot, its count and its copy's values
+        struct Chunk { int st, en; T x, vx, vy, vz, w; };
+        auto load_chunk = [&](int c0) {
+            Chunk k{0, 0, T(0), T(0), T(0), T(0), T(0)};
+            const int j = c0 + lane;
+            if (c0 < nhw && j < nhw) {
+                k.st = dcnt[j];
+                k.en = j + 1 < nhw ? dcnt[j + 1] : total;
+                if (k.en > k.st) {
+                    const int t = tgt[j];
+                    k.x = s.x[t]; k.vx = s.vx[t]; k.vy = s.vy[t]; k.vz = s.vz[t]; k.w = wgt[j];
+                }
             }
-            const int64_t wlo = __shfl_sync(0xffffffffu, ex, 0);
-            const int rel = int(ex - wlo);                               // this entry's first slot
-            const int wn = __shfl_sync(0xffffffffu, rel + c, 31);     // the warp's slots
+            return k;
+        };
+        Chunk nxt = load_chunk(warp * 32);
+        for (int c0 = warp * 32; c0 < nhw; c0 += RS_T) {
+            const Chunk cur = nxt;
+            nxt = load_chunk(c0 + RS_T);  // the next chunk's gathers are in flight while this one is written
+            const int j = c0 + lane;
+            const bool valid = j < nhw;
+            const int st = cur.st, en = cur.en;
+            const T xx = cur.x, a1 = cur.vx, a2 = cur.vy, a3 = cur.vz, ww = cur.w;
+            const int last = min(31, nhw - 1 - c0);                      // the chunk's last entry
+            const int wlo = __shfl_sync(0xffffffffu, st, 0);
+            const int wn = __shfl_sync(0xffffffffu, en, last) - wlo;      // the chunk's slots
+            const int rel = valid ? st - wlo : 0x7fffffff;                 // this entry's first slot
             for (int q0 = 0; q0 < wn; q0 += 32) {
                 const int q = q0 + lane;
                 int src = 0;  // the last lane whose first slot is at or below q (it has copies)
@@ -562,7 +592,6 @@ __global__ void __launch_bounds__(RS_T) k_rs_apply(bz_params p, SoAR<T> s, const
                     }
                 }
             }
-            carry2 += tot;
         }
         return;
     }

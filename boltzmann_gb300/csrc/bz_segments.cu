@@ -27,28 +27,20 @@ namespace bz {
 // prefetch: the next round's particle is loaded into registers while this round computes
 // (one particle per lane only; costs five registers, so it pairs with 64-register shapes).
 struct SegShape { int threads, per_lane, min_blocks; bool prefetch; };
-constexpr SegShape kSegShapes[] = {{512, 1, 2, true}, {320, 1, 4, true}, {640, 1, 2, true}, {384, 1, 3, true},
-                                   {448, 1, 2, true}, {320, 1, 4, false}, {256, 2, 4, false}, {256, 1, 4, true}};
+// The last two take four consecutive particles per lane with 128-bit loads of each column.
+constexpr SegShape kSegShapes[] = {{512, 1, 2, true},  {320, 1, 4, true},  {640, 1, 2, true},
+                                   {384, 1, 3, true},  {448, 1, 2, true},  {320, 1, 4, false},
+                                   {256, 2, 4, false}, {256, 1, 4, true},  {256, 4, 2, false},
+                                   {128, 4, 4, false}};
 constexpr int kSegNumShapes = int(sizeof(kSegShapes) / sizeof(kSegShapes[0]));
 static int g_seg_shape = 0;
 
 // The CTA's moment grid in shared memory: (sum w, sum w e) interleaved per node, then sum w
-// of the ionizing particles. A float atomic add to shared memory costs as many
-// instructions here as a compare-and-swap loop (measured), so a float32 grid adds a node's
-// two sums with one 64-bit compare-and-swap; a float64 grid adds them one by one.
-__device__ __forceinline__ void dep_pair(float *g, int nd, float a, float b) {
-    unsigned long long *q = reinterpret_cast<unsigned long long *>(g + 2 * nd);
-    unsigned long long cur = *q;
-    while (true) {
-        const float x = __uint_as_float(uint32_t(cur)) + a;
-        const float y = __uint_as_float(uint32_t(cur >> 32)) + b;
-        const unsigned long long nxt = (static_cast<unsigned long long>(__float_as_uint(y)) << 32) | __float_as_uint(x);
-        const unsigned long long seen = atomicCAS(q, cur, nxt);
-        if (seen == cur) break;
-        cur = seen;
-    }
-}
-__device__ __forceinline__ void dep_pair(double *g, int nd, double a, double b) {
+// of the ionizing particles; a node's two sums are added one after the other. (One 64-bit
+// compare-and-swap for both float32 sums took fewer instructions but was slower where many
+// lanes of a warp hit one node, as right after a resampling step appends cell-ordered
+// copies: 628 -> 820 us for that push.)
+template <typename A> __device__ __forceinline__ void dep_pair(A *g, int nd, A a, A b) {
     atomicAdd(&g[2 * nd], a);
     atomicAdd(&g[2 * nd + 1], b);
 }
@@ -594,12 +586,14 @@ static int seg_push_entry(const bz_params *pp, S in_, S out_, const T *E, const 
                 BZ_SEG_SHAPE(5)
                 BZ_SEG_SHAPE(6)
                 BZ_SEG_SHAPE(7)
+                BZ_SEG_SHAPE(8)
+                BZ_SEG_SHAPE(9)
                 default: break;
             }
 #undef BZ_SEG_SHAPE
         }
     }
-    static_assert(kSegNumShapes == 8, "one case per CTA shape");
+    static_assert(kSegNumShapes == 10, "one case per CTA shape");
 #define BZ_SEG_CASE(RP, XSM, DP)                                                                                    \
     if (replay == RP && p.xs_mode == XSM && dep == DP)                                                             \
         return launch_seg_push<T, RP, XSM, DP>(p, in, out, E, R, gas, moments, n_pushed, ws, seg_flags, status, st);
