@@ -796,12 +796,14 @@ def run_learned(args, world, rank, local, pg):
         torch.cuda.synchronize()
         t_cl = time.perf_counter() - t4
         cc, fc, sc = S.ccp_relaxation(ccfg, 2 * spc, cch, mlp=mlp, device=dev, closure=True, ion_flux=True)
+        cr, fr, sr = S.ccp_relaxation(ccfg, 2 * spc, cch, mlp=mlp, device=dev, ion_flux=True, redraw_after=1)
         cyc = lambda f: [float(f[:per].mean()), float(f[per:].mean())]
         ccp_runs.append({"steps_plain": S.steps_to_periodic(cp, per) * cch,
                          "steps_learned": S.steps_to_periodic(cl, per) * cch,
                          "steps_learned_closure": S.steps_to_periodic(cc, per) * cch,
+                         "steps_learned_redraw_after_50": S.steps_to_periodic(cr, per) * cch,
                          "ms_per_step_plain": t_cp * 1e3 / (2 * spc), "ms_per_step_learned": t_cl * 1e3 / (2 * spc),
-                         "mean_eV_first_chunk": [float(cp[0]), float(cl[0]), float(cc[0])],
+                         "mean_eV_first_chunks": [[float(v) for v in c[:4]] for c in (cp, cl, cc, cr)],
                          "mean_eV_cycle2": [float(cp[per:].mean()), float(cl[per:].mean()), float(cc[per:].mean())],
                          "ion_flux_per_cycle": {"plain": cyc(fp), "learned": cyc(fl), "learned_closure": cyc(fc)},
                          "status": [sp.device_status(), sl.device_status(), sc.device_status()]})

@@ -138,10 +138,13 @@ template <typename U> __device__ __forceinline__ int choose(U u, U r0, U r1, U r
     return P_NONE;
 }
 
-template <typename T, bool REPLAY, int XS>
+// HOT: 1D drift and the direct collision probability fixed at compile time
+template <typename T, bool REPLAY, int XS, bool HOT = false>
 __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T> &k, const Rng &rng, uint32_t slot, T x, T vx, T vy,
                                           T vz, const T *E_s, const float4 *xs_s, const double *R,
                                           const double *gas, Item<T> &o) {
+    const int advect = HOT ? int(BZ_ADVECT_1D) : p.advect;
+    const int coll_model = HOT ? int(BZ_COLL_DIRECT) : p.coll_model;
     // gas velocity (boltzmann.py:589, electron_kernel_numba.py:51-53) and uniforms
     T g0 = 0, g1 = 0, g2 = 0;
     Uni<T> u0, u1, u2, u3;
@@ -182,9 +185,9 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
     // the field at the pre-push face (electron_kernel_numba.py:257-263), read first: it
     // depends on x only, and its shared-memory load overlaps the collision arithmetic
     int face = 0;
-    if (p.advect == BZ_ADVECT_ENSEMBLE) {
+    if (advect == BZ_ADVECT_ENSEMBLE) {
         face = min(max(int(x), 0), k.face_max);
-    } else if (p.advect) {
+    } else if (advect) {
         face = face_index(x, p.dx, k.inv_dx_f);
         face = min(max(face, 0), k.face_max);
     }
@@ -206,7 +209,7 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
         s0 *= p.nn;
         s2 *= p.nn;
         double q0, q2;
-        if (p.coll_model == BZ_COLL_DIRECT) {
+        if (coll_model == BZ_COLL_DIRECT) {
             double st = s0 + s2;
             double P = 1.0 - exp(-p.dt * vm * st);
             double pc = P * (1.0 / st);
@@ -232,7 +235,7 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
         if (e < k.e_exc) s1 = T(0);
         if (e < T(E_ION)) s2 = T(0);
         T r0, r1, r2;
-        if (p.coll_model == BZ_COLL_DIRECT) {
+        if (coll_model == BZ_COLL_DIRECT) {
             T st = s0 + s1 + s2;
             T P = coll_prob(k.dt * vmag * st);
             T pc = fdiv_fast(P, st);
@@ -301,7 +304,7 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
     // absorbing walls (electron_kernel_numba.py:257-276)
     T xn = x;
     bool valid = true;
-    if (p.advect == BZ_ADVECT_1D) {
+    if (advect == BZ_ADVECT_1D) {
         xn = x + k.c100dt * nvx;
         if (xn < k.wall_lo || xn > k.wall_hi) {
             // near a wall: decide in float64 like the reference

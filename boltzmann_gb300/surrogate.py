@@ -383,10 +383,12 @@ def steps_to_periodic(series, period, tol=0.02, window=5):
 
 
 def ccp_relaxation(cfg, steps, chunk, mlp: Optional[SurrogateMLP] = None, device="cuda", closure=False,
-                   ion_flux=False):
+                   ion_flux=False, redraw_after=0):
     """Mean electron energy of a CCP (weight-averaged over the whole gap) per chunk of
     ``chunk`` steps, from the plain start or, with ``mlp``, the learned start (with
-    ``closure``, its ion source from the network's rate closure); also returns the solver.
+    ``closure``, its ion source from the network's rate closure; with ``redraw_after`` > 0
+    the learned start is applied once more after that many chunks, from the state the
+    fields have reached by then); also returns the solver.
     With ``ion_flux`` it returns (energies, ion fluxes, solver), the ion flux per chunk being
     the mean of |Ji| at the two electrodes (heavies_kernel_1D.py:37-38)."""
     from .solver import BoltzmannGB300
@@ -395,7 +397,9 @@ def ccp_relaxation(cfg, steps, chunk, mlp: Optional[SurrogateMLP] = None, device
         sv.learned_start(mlp, closure=closure)
     acc = torch.zeros(3, dtype=torch.float64, device=device)
     out, flux = [], []
-    for _ in range(steps // chunk):
+    for c in range(steps // chunk):
+        if mlp is not None and redraw_after and c == redraw_after:
+            sv.learned_start(mlp, closure=closure)
         acc.zero_()
         for _ in range(chunk):
             sv.step()

@@ -68,6 +68,8 @@ def test_learned_start_of_the_ccp():
     np.testing.assert_allclose(learned[per:].mean(), plain[per:].mean(), rtol=0.03)
     kp = S.steps_to_periodic(plain, per)
     kl = S.steps_to_periodic(learned, per)
+    print("CCP chunks to the periodic state: plain", kp, "learned", kl, "first chunk", plain[0], learned[0],
+          "periodic", plain[per:].mean())
     assert kl <= 0.6 * kp, (kp, kl)
     assert abs(learned[0] / plain[per] - 1) < 0.15  # within 15% of the periodic value at once
     assert abs(plain[0] / plain[per] - 1) > 0.5     # the plain start is far from it
