@@ -138,13 +138,13 @@ template <typename U> __device__ __forceinline__ int choose(U u, U r0, U r1, U r
     return P_NONE;
 }
 
-// HOT: 1D drift and the direct collision probability fixed at compile time
-template <typename T, bool REPLAY, int XS, bool HOT = false>
+// ADV >= 0: the motion mode (ADV) and the direct collision probability fixed at compile time
+template <typename T, bool REPLAY, int XS, int ADV = -1>
 __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T> &k, const Rng &rng, uint32_t slot, T x, T vx, T vy,
                                           T vz, const T *E_s, const float4 *xs_s, const double *R,
                                           const double *gas, Item<T> &o) {
-    const int advect = HOT ? int(BZ_ADVECT_1D) : p.advect;
-    const int coll_model = HOT ? int(BZ_COLL_DIRECT) : p.coll_model;
+    const int advect = ADV >= 0 ? ADV : p.advect;
+    const int coll_model = ADV >= 0 ? int(BZ_COLL_DIRECT) : p.coll_model;
     // gas velocity (boltzmann.py:589, electron_kernel_numba.py:51-53) and uniforms
     T g0 = 0, g1 = 0, g2 = 0;
     Uni<T> u0, u1, u2, u3;

@@ -60,15 +60,16 @@ __device__ __forceinline__ uint32_t seg_slot32(int seg, int run, int half, int j
     return uint32_t(seg) * (2u * uint32_t(half)) + uint32_t(run) * uint32_t(half) + uint32_t(j);
 }
 
-// HOT: the motion mode and collision model are known at compile time (1D drift, direct
-// collision probability: the CCP's hot loop), so their tests leave the loop (4% of its time)
-template <typename T, bool REPLAY, int XS, bool DEPOSIT, int SG_T, int SG_I, int MINB, bool PF, bool HOT>
+// ADV >= 0: the motion mode (ADV) and the direct collision probability are known at compile
+// time (the CCP's hot loop: 1D drift; the swarm ensemble), so their tests leave the loop (4%
+// of the CCP push's time); ADV < 0 reads both from the parameters
+template <typename T, bool REPLAY, int XS, bool DEPOSIT, int SG_T, int SG_I, int MINB, bool PF, int ADV>
 __global__ void __launch_bounds__(SG_T, MINB)
     k_seg_push(bz_params p, PushConst<T> kc, Seg<T> in, Seg<T> out, const T *E, const double *R, const double *gas,
                double *moments, unsigned long long *n_pushed, unsigned int *ticket, uint32_t *seg_flags,
                uint32_t *status) {
     using A = typename AccT<T>::t;
-    const int advect = HOT ? int(BZ_ADVECT_1D) : p.advect;
+    const int advect = ADV >= 0 ? ADV : p.advect;
     constexpr int SG_R = 32 * SG_I;  // particles per warp round
     extern __shared__ __align__(16) unsigned char smem[];
     const int nf = advect ? p.n_faces : 1;
@@ -177,7 +178,7 @@ __global__ void __launch_bounds__(SG_T, MINB)
                     it[k].ionized = false;
                     it[k].excited = false;
                     if (w[k] > T(0)) {
-                        push_item<T, REPLAY, XS, HOT>(p, kc, rng, rbase + uint32_t(j0 + k), x[k], vx[k], vy[k], vz[k], E_s,
+                        push_item<T, REPLAY, XS, ADV>(p, kc, rng, rbase + uint32_t(j0 + k), x[k], vx[k], vy[k], vz[k], E_s,
                                                  xs_s, R, gas, it[k]);
                         // one test for the three components (a sum of finite speeds stays finite)
                         if (!isfinite(it[k].vx + it[k].vy + it[k].vz)) err |= BZ_DEV_NONFINITE;
@@ -522,7 +523,7 @@ template <typename T, typename S> static Seg<T> to_seg(const S &s) {
 
 template <typename T, bool REPLAY, int XS, bool DEPOSIT, int SG_T = kSegShapes[0].threads,
           int SG_I = kSegShapes[0].per_lane, int MINB = kSegShapes[0].min_blocks, bool PF = kSegShapes[0].prefetch,
-          bool HOT = false>
+          int ADV = -1>
 static int launch_seg_push(const bz_params &p, Seg<T> in, Seg<T> out, const T *E, const double *R, const double *gas,
                            double *moments, uint64_t *n_pushed, void *ws, uint32_t *seg_flags, uint32_t *status,
                            cudaStream_t st) {
@@ -531,7 +532,7 @@ static int launch_seg_push(const bz_params &p, Seg<T> in, Seg<T> out, const T *E
     const int xsn = (XS == BZ_XS_TABLE) ? p.xs_n : 0;
     const size_t smem = size_t(xsn) * sizeof(float4) + (DEPOSIT ? size_t(3) * p.n_nodes * sizeof(A) : 0) +
                         size_t(nf) * sizeof(T);
-    auto kern = k_seg_push<T, REPLAY, XS, DEPOSIT, SG_T, SG_I, MINB, PF, HOT>;
+    auto kern = k_seg_push<T, REPLAY, XS, DEPOSIT, SG_T, SG_I, MINB, PF, ADV>;
     if (smem > 48 * 1024 &&
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess)
         return BZ_ERR_UNSUPPORTED;
@@ -577,19 +578,21 @@ static int seg_push_entry(const bz_params *pp, S in_, S out_, const T *E, const 
         return BZ_ERR_CUDA;
     if constexpr (sizeof(T) == 4) {
         if (!replay && p.xs_mode == BZ_XS_TABLE && dep) {  // the hot loop: tunable CTA shape
-            // the CCP's hot loop (1D drift, direct collision probability) takes the kernels
-            // with both modes fixed at compile time
-            const bool hot = p.advect == BZ_ADVECT_1D && p.coll_model == BZ_COLL_DIRECT;
+            // the CCP's hot loop (1D drift) and the swarm ensemble, with the direct collision
+            // probability, take kernels with both modes fixed at compile time in the selected
+            // shape; other modes (one 0-D swarm, null collision) the default shape's general kernel
+            const int adv = p.coll_model != BZ_COLL_DIRECT ? -1 : p.advect;
 #define BZ_SEG_SHAPE(K)                                                                                            \
     case K:                                                                                                        \
-        if (hot)                                                                                                   \
+        if (adv == BZ_ADVECT_1D)                                                                                   \
             return launch_seg_push<T, false, BZ_XS_TABLE, true, kSegShapes[K].threads, kSegShapes[K].per_lane,       \
-                                   kSegShapes[K].min_blocks, kSegShapes[K].prefetch, true>(                          \
+                                   kSegShapes[K].min_blocks, kSegShapes[K].prefetch, BZ_ADVECT_1D>(                  \
                 p, in, out, E, R, gas, moments, n_pushed, ws, seg_flags, status, st);                              \
-        return launch_seg_push<T, false, BZ_XS_TABLE, true, kSegShapes[K].threads, kSegShapes[K].per_lane,           \
-                               kSegShapes[K].min_blocks, kSegShapes[K].prefetch, false>(p, in, out, E, R, gas,     \
-                                                                                        moments, n_pushed, ws,     \
-                                                                                        seg_flags, status, st);
+        if (adv == BZ_ADVECT_ENSEMBLE)                                                                             \
+            return launch_seg_push<T, false, BZ_XS_TABLE, true, kSegShapes[K].threads, kSegShapes[K].per_lane,       \
+                                   kSegShapes[K].min_blocks, kSegShapes[K].prefetch, BZ_ADVECT_ENSEMBLE>(            \
+                p, in, out, E, R, gas, moments, n_pushed, ws, seg_flags, status, st);                              \
+        break;
             switch (g_seg_shape) {
                 BZ_SEG_SHAPE(0)
                 BZ_SEG_SHAPE(1)

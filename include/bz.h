@@ -278,8 +278,10 @@ int bz_seg_push_collide_f64(const bz_params *p, bz_segments_f64 in, bz_segments_
 /* CTA shapes of the float32 table + deposit segmented push (threads per CTA, particles
  * per lane per round, CTAs per SM the registers are budgeted for, whether the next
  * round is prefetched into registers). Shape 0 is the default; bz_seg_push_select sets
- * the shape later launches use (process-wide; select before capturing a graph). Results
- * do not depend on the shape except for the summation order of the float moments. */
+ * the shape later launches use (process-wide; select before capturing a graph) in the
+ * 1D-drift and ensemble modes with the direct collision probability, whose kernels have
+ * both modes fixed at compile time; other modes run shape 0. Results do not depend on the
+ * shape except for the summation order of the float moments. */
 int32_t bz_seg_push_shapes(void);
 int bz_seg_push_shape_info(int32_t shape, int32_t *threads, int32_t *per_lane, int32_t *min_blocks,
                            int32_t *prefetch);
