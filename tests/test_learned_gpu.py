@@ -47,8 +47,10 @@ def test_learned_start_reaches_steady_state_sooner():
 
 def test_learned_start_of_the_ccp():
     """A network trained on a plain CCP run (and the swarm sweep) starts a new CCP run
-    (another seed) at its periodic electron energy: the plain 1 eV start needs a quarter
-    of an RF cycle to heat up."""
+    (another seed) near its periodic electron energy: the plain 1 eV start needs a quarter
+    of an RF cycle to heat up. Measured with this small training set (3000 Adam steps):
+    plain 19 chunks, learned 9 (0.47x); the benchmark's network (2e4 steps, 2e5 rows)
+    reaches 0.22x."""
     from boltzmann_gb300 import config as C
     kw = dict(ne_uniform=1e9, in_dt=4000.0, steps_per_cycle=4000, num_particles=1_000_000)
     Xc, Tc, info = S.ccp_dataset(C.ccp_256(**kw), cycles=2, snaps_per_cycle=16, settle_cycles=1)
@@ -63,14 +65,19 @@ def test_learned_start_of_the_ccp():
     per, chunk = 4000 // 50, 50
     plain, sp = S.ccp_relaxation(cfg, 8000, chunk)
     learned, sl = S.ccp_relaxation(cfg, 8000, chunk, mlp=mlp)
-    assert sp.device_status() == 0 and sl.device_status() == 0
+    closure, sc = S.ccp_relaxation(cfg, 8000, chunk, mlp=mlp, closure=True)
+    assert sp.device_status() == 0 and sl.device_status() == 0 and sc.device_status() == 0
     # the same periodic state in the second cycle
     np.testing.assert_allclose(learned[per:].mean(), plain[per:].mean(), rtol=0.03)
     kp = S.steps_to_periodic(plain, per)
     kl = S.steps_to_periodic(learned, per)
-    print("CCP chunks to the periodic state: plain", kp, "learned", kl, "first chunk", plain[0], learned[0],
-          "periodic", plain[per:].mean())
+    kc = S.steps_to_periodic(closure, per)
+    print("CCP chunks to the periodic state: plain", kp, "learned", kl, "with the rate closure", kc, "first chunk",
+          plain[0], learned[0], "periodic", plain[per:].mean(), closure[per:].mean())
     assert kl <= 0.6 * kp, (kp, kl)
+    # the network's ion-source rate closure: no slower, and the same periodic energy within 2%
+    assert kc <= 0.6 * kp, (kp, kc)
+    assert abs(closure[per:].mean() / plain[per:].mean() - 1) < 0.02
     assert abs(learned[0] / plain[per] - 1) < 0.15  # within 15% of the periodic value at once
     assert abs(plain[0] / plain[per] - 1) > 0.5     # the plain start is far from it
 
