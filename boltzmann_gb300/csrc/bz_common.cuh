@@ -110,15 +110,17 @@ template <typename T> struct Uni { T u, c; };
 
 __device__ __forceinline__ Uni<float> uni_f(uint32_t r) {
     // k = r >> 9 spliced into the mantissa of 1.0 gives 1 + k 2^-23 exactly; subtracting
-    // 1 - 2^-24 (exact, Sterbenz) leaves (k + 1/2) 2^-23. The complement uses 2^23-1-k.
+    // 1 - 2^-24 (exact, Sterbenz) leaves u = (2k + 1) 2^-24. Its complement
+    // (2^24 - 2k - 1) 2^-24 has 24 significant bits at most, so 1 - u is exact too.
     const float one_minus = 0x1.fffffep-1f;  // 1 - 2^-24
     const float u = __int_as_float(0x3F800000u | (r >> 9)) - one_minus;
-    const float c = __int_as_float(0x3F800000u | (~r >> 9)) - one_minus;
-    return {u, c};
+    return {u, 1.0f - u};
 }
 __device__ __forceinline__ Uni<double> uni_d(uint32_t a, uint32_t b) {
+    // u = (2k + 1) 2^-53 with k < 2^52; 1 - u has 53 significant bits at most: exact
     uint64_t k = (uint64_t(a >> 6) << 26) | uint64_t(b >> 6);
-    return {(double(k) + 0.5) * 0x1p-52, (double((uint64_t(1) << 52) - k) - 0.5) * 0x1p-52};
+    const double u = (double(k) + 0.5) * 0x1p-52;
+    return {u, 1.0 - u};
 }
 
 // Key and step words of the stream: key = seed, counter = (slot, step lo, step hi, tag).
