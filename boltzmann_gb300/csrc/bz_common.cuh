@@ -164,6 +164,42 @@ __device__ __forceinline__ void draw4(const Rng &g, const uint32_t *rk0, const u
     d.v[0] = uni_d(a.x, a.y); d.v[1] = uni_d(a.z, a.w); d.v[2] = uni_d(b.x, b.y); d.v[3] = uni_d(b.z, b.w);
 }
 
+// The hardware approximations (one MUFU instruction each) in their flush-to-zero forms:
+// without .ftz a subnormal input is first scaled into the normal range, which costs several
+// instructions per call. Every caller here passes a normal number, or one whose flush to
+// zero gives the same result downstream (stated at the call), and for normal inputs the two
+// forms return the same value.
+__device__ __forceinline__ float lg2_ftz(float x) {
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float ex2_ftz(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcp_ftz(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float sin_ftz(float x) {
+    float y;
+    asm("sin.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float cos_ftz(float x) {
+    float y;
+    asm("cos.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 __device__ __forceinline__ void sincospi_t(float a, float *s, float *c) { sincospif(a, s, c); }
 __device__ __forceinline__ void sincospi_t(double a, double *s, double *c) { sincospi(a, s, c); }
 
@@ -171,11 +207,9 @@ __device__ __forceinline__ void sincospi_t(double a, double *s, double *c) { sin
 // reduced to (-pi, pi), where its absolute error is below 2^-21.4 (sin(2 pi u) =
 // -sin(2 pi (u - 1/2))); double: sincospi.
 __device__ __forceinline__ void sincos2pi(float u, float *s, float *c) {
-    float a = 6.28318530717958647692f * (u - 0.5f);
-    float ss, cc;
-    __sincosf(a, &ss, &cc);
-    *s = -ss;
-    *c = -cc;
+    const float a = 6.28318530717958647692f * (u - 0.5f);  // |a| < pi: normal or zero
+    *s = -sin_ftz(a);
+    *c = -cos_ftz(a);
 }
 __device__ __forceinline__ void sincos2pi(double u, double *s, double *c) { sincospi(2.0 * u, s, c); }
 
@@ -192,7 +226,9 @@ static inline float float_above(double m) {
 
 // square root of a positive argument: x * rsqrt(x) in float (relative error ~1e-7),
 // correctly rounded in double
-__device__ __forceinline__ float sqrt_pos(float x) { return x * rsqrtf(x); }
+// (float callers pass squared speeds floored at 1e-30, energies above a threshold and
+// products of two uniforms: normal numbers)
+__device__ __forceinline__ float sqrt_pos(float x) { return x * rsqrt_ftz(x); }
 __device__ __forceinline__ double sqrt_pos(double x) { return sqrt(x); }
 
 // Standard normal deviates from float uniforms by their quantile, Phi^-1(u) = x f(w) with
@@ -205,7 +241,7 @@ __device__ __forceinline__ double sqrt_pos(double x) { return sqrt(x); }
 // log2. One uniform per deviate (Box-Muller takes two per pair and a log, a square root, a
 // sine and a cosine) and no rejection.
 constexpr float NQ_W_TAIL = 7.213475f;  // 5 / ln 2
-__device__ __forceinline__ float nq_w(Uni<float> a) { return -2.0f - __log2f(a.u * a.c); }
+__device__ __forceinline__ float nq_w(Uni<float> a) { return -2.0f - lg2_ftz(a.u * a.c); }  // u c > 2^-25
 __device__ __forceinline__ float nq_central(float w) {
     const float t = w - 3.6067376f;
     float r = 2.177562797e-09f;

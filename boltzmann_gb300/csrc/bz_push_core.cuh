@@ -117,10 +117,11 @@ __device__ __forceinline__ float excess_energy_f(float ax, float ay, float az, f
 // 1 - exp(-x), x >= 0. float: the hardware exponential, absolute error ~2e-7 (the
 // collision test compares this probability with a uniform, so an absolute error is what
 // matters); double: expm1.
-__device__ __forceinline__ float coll_prob(float x) { return 1.0f - __expf(-x); }
+// (exp(-x) = 2^(-x log2 e); a result flushed to zero leaves P = 1, as its float32 value is)
+__device__ __forceinline__ float coll_prob(float x) { return 1.0f - ex2_ftz(x * -1.4426950408889634f); }
 __device__ __forceinline__ double coll_prob(double x) { return -expm1(-x); }
 
-__device__ __forceinline__ float fdiv_fast(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ float fdiv_fast(float a, float b) { return a * rcp_ftz(b); }  // b: a normal sum of n sigma
 __device__ __forceinline__ double fdiv_fast(double a, double b) { return a / b; }
 
 template <typename T> __device__ __forceinline__ Uni<T> uni_from_replay(double r) {
@@ -195,7 +196,8 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
     // energy of the gas-relative velocity (electron_kernel_numba.py:55-63)
     T ax = vx - g0, ay = vy - g1, az = vz - g2;
     T v2 = ax * ax + ay * ay + az * az;
-    T vmag = sqrt_pos(v2 > T(0) ? v2 : T(1e-30));
+    // (float: floored at 1e-30, a normal number, for the flush-to-zero reciprocal root)
+    T vmag = sqrt_pos(sizeof(T) == 4 ? (v2 > T(1e-30) ? v2 : T(1e-30)) : (v2 > T(0) ? v2 : T(1e-30)));
     T e = k.efac * v2;
     int proc;
     if (XS == BZ_XS_REF_FITS) {
@@ -224,7 +226,9 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
         vmag = T(vm);
     } else {
         // n*sigma table, linear in log2(e) on the log grid
-        float lt = fmaf(__log2f(float(e)), k.xs_inv_d, -k.xs_off);
+        // (a subnormal energy flushes to log2 = -inf, which the clamp below turns into the
+        // table's first point, where any energy below its start lands)
+        float lt = fmaf(lg2_ftz(float(e)), k.xs_inv_d, -k.xs_off);
         lt = fminf(fmaxf(lt, 0.0f), k.xs_last);
         int i = min(int(lt), k.xs_imax);
         float f = lt - float(i);
