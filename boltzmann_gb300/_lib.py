@@ -14,7 +14,7 @@ LIB_PATH = os.path.join(PKG, "libbz.so")
 BZ_OK, BZ_ERR_ARG, BZ_ERR_CUDA, BZ_ERR_WORKSPACE, BZ_ERR_UNSUPPORTED, BZ_ERR_TOO_LARGE = 0, 1, 2, 3, 4, 5
 DEV_CAPACITY, DEV_LOOKBACK, DEV_NONFINITE, DEV_BINRANGE = 0x1, 0x2, 0x4, 0x8
 QUIRK_SPLIT_WRAP, QUIRK_DEAD_IONFLAG, QUIRK_TRIGGER_LAST, FIX_MERGE_ENERGY = 0x1, 0x2, 0x4, 0x8
-PER_KEY_TARGETS, MOMENT_EXCITATION, CLEAR_MOMENTS = 0x10, 0x20, 0x40
+PER_KEY_TARGETS, MOMENT_EXCITATION, CLEAR_MOMENTS, RESAMPLE_IN_PLACE = 0x10, 0x20, 0x40, 0x80
 ADVECT_NONE, ADVECT_1D, ADVECT_ENSEMBLE = 0, 1, 2
 XS_TABLE, XS_REF_FITS = 0, 1
 COLL_DIRECT, COLL_NULL = 0, 1
@@ -124,6 +124,9 @@ _PROTOS = {
     "bz_seg_deposit_f64": (ctypes.c_int, [_P, Segments, _vp, _vp]),
     "bz_seg_rebalance_f32": (ctypes.c_int, [Segments, Segments, _vp, _sz, _vp, _vp, _vp, _vp]),
     "bz_seg_rebalance_f64": (ctypes.c_int, [Segments, Segments, _vp, _sz, _vp, _vp, _vp, _vp]),
+    "bz_seg_place_workspace": (_sz, [_i32]),
+    "bz_seg_place_f32": (ctypes.c_int, [Segments, Particles, _vp, _i64, Segments, _vp, _sz, _vp, _vp, _vp]),
+    "bz_seg_place_f64": (ctypes.c_int, [Segments, Particles, _vp, _i64, Segments, _vp, _sz, _vp, _vp, _vp]),
     "bz_seg_eedf_f32": (ctypes.c_int, [_P, Segments, ctypes.c_int32, ctypes.c_double, ctypes.c_double, _vp, _vp]),
     "bz_seg_eedf_f64": (ctypes.c_int, [_P, Segments, ctypes.c_int32, ctypes.c_double, ctypes.c_double, _vp, _vp]),
     "bz_seg_bin_workspace": (_sz, [_i32, _i64]),

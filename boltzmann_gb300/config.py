@@ -73,6 +73,9 @@ class CCPConfig:
     min_wt: float = 0.1
     split_below: float = 0.5
     merge_at: float = 3.0
+    # the resampling step's appended particles go into the free slots of the segments (merged
+    # ones are dropped by the next push) instead of a full repack of every particle
+    resample_in_place: bool = True
     merge_keep: float = 0.6
     max_ppc_factor: float = 10.0
     # collisions

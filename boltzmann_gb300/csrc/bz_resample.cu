@@ -917,7 +917,7 @@ static int seg_resample_entry(const bz_params *pp, S s_, P app_, int64_t app_cap
 
 extern "C" {
 size_t bz_seg_resample_workspace(int32_t nseg, int64_t capacity, int32_t nkeys) {
-    return bz::RsWs(capacity, nkeys).total + bz_seg_repack_workspace(nseg);
+    return bz::RsWs(capacity, nkeys).total + std::max(bz_seg_repack_workspace(nseg), bz_seg_place_workspace(nseg));
 }
 int bz_seg_resample_f32(const bz_params *p, bz_segments_f32 s, bz_particles_f32 app, int64_t app_capacity,
                         bz_segments_f32 out, int32_t nbins, const int32_t *targets, const int32_t *max_ppc,
@@ -957,7 +957,9 @@ static int seg_resample_entry(const bz_params *pp, S s_, P app_, int64_t app_cap
     const int nkeys = p.n_nodes * nb;
     const int64_t cap = int64_t(s_.nseg) * 2 * s_.half;
     RsWs L(cap, nkeys);
-    const size_t rws = bz_seg_repack_workspace(s_.nseg);
+    const bool in_place = (p.flags & BZ_RESAMPLE_IN_PLACE) != 0;
+    if (in_place && (out_.nseg != s_.nseg || out_.half != s_.half)) return BZ_ERR_ARG;
+    const size_t rws = in_place ? bz_seg_place_workspace(s_.nseg) : bz_seg_repack_workspace(s_.nseg);
     if (ws_bytes < L.total + rws) return BZ_ERR_WORKSPACE;
     unsigned char *b = static_cast<unsigned char *>(ws);
     int32_t *act = reinterpret_cast<int32_t *>(b + L.act);
@@ -978,8 +980,23 @@ static int seg_resample_entry(const bz_params *pp, S s_, P app_, int64_t app_cap
                                           counts, act, app_off, draw_off, replay_u, cdf, cnt, cons_diag, app, app_cap,
                                           status);
     if (cudaGetLastError() != cudaSuccess) return BZ_ERR_CUDA;
-    // everything left in s (w != 0) followed by the appended particles, spread over out
     int rc;
+    if (in_place) {
+        // the appended particles into the free slots of s (out: the scratch of a repack when
+        // they do not fit)
+        if (sizeof(T) == 4)
+            rc = bz_seg_place_f32(*reinterpret_cast<const bz_segments_f32 *>(&s_),
+                                  *reinterpret_cast<const bz_particles_f32 *>(&app_), misc, app_cap,
+                                  *reinterpret_cast<const bz_segments_f32 *>(&out_), b + L.total, rws, seg_flags,
+                                  status, stream);
+        else
+            rc = bz_seg_place_f64(*reinterpret_cast<const bz_segments_f64 *>(&s_),
+                                  *reinterpret_cast<const bz_particles_f64 *>(&app_), misc, app_cap,
+                                  *reinterpret_cast<const bz_segments_f64 *>(&out_), b + L.total, rws, seg_flags,
+                                  status, stream);
+        return rc;
+    }
+    // everything left in s (w != 0) followed by the appended particles, spread over out
     if (sizeof(T) == 4)
         rc = bz_seg_repack_f32(reinterpret_cast<const bz_segments_f32 *>(&s_),
                                *reinterpret_cast<const bz_particles_f32 *>(&app_), misc, app_cap,

@@ -13,6 +13,7 @@
 // leaves at most one survivor and one child. After a push, a segment above half raises
 // BZ_SEG_NEEDS_REPACK; k_seg_repack* then spreads all particles evenly again.
 #include <algorithm>
+#include <type_traits>
 
 #include <cooperative_groups.h>
 
@@ -91,6 +92,7 @@ __global__ void __launch_bounds__(SG_T, MINB)
     const int lane = threadIdx.x & 31;
     const int H = in.half;
     uint32_t err = 0;
+    uint32_t pushed = 0;  // particles with w > 0 this lane pushed (slots emptied by merges are not counted)
     bool overfull = false;
     while (true) {
         int seg = 0;
@@ -104,7 +106,6 @@ __global__ void __launch_bounds__(SG_T, MINB)
                 err |= BZ_DEV_CAPACITY;
                 cnt = cnt < 0 ? 0 : H;
             }
-            if (n_pushed && lane == 0 && cnt > 0) atomicAdd(n_pushed, (unsigned long long)cnt);
             const uint32_t rbase = seg_slot32(seg, run, H, 0);
             // one particle of the run (zeros past its end)
             auto fetch = [&](int j, T &a, T &b, T &c, T &d, T &e) {
@@ -178,6 +179,7 @@ __global__ void __launch_bounds__(SG_T, MINB)
                     it[k].ionized = false;
                     it[k].excited = false;
                     if (w[k] > T(0)) {
+                        ++pushed;
                         push_item<T, REPLAY, XS, ADV>(p, kc, rng, rbase + uint32_t(j0 + k), x[k], vx[k], vy[k], vz[k], E_s,
                                                  xs_s, R, gas, it[k]);
                         // one test for the three components (a sum of finite speeds stays finite)
@@ -283,6 +285,11 @@ __global__ void __launch_bounds__(SG_T, MINB)
     }
     if (err) atomicOr(status, err);
     if (overfull && lane == 0) atomicOr(seg_flags, BZ_SEG_NEEDS_REPACK);
+    if (n_pushed) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) pushed += __shfl_xor_sync(0xffffffffu, pushed, o);
+        if (lane == 0 && pushed) atomicAdd(n_pushed, (unsigned long long)pushed);
+    }
     if (DEPOSIT) {
         __syncthreads();
         for (int i = threadIdx.x; i < 3 * nnodes; i += SG_T) {
@@ -473,6 +480,212 @@ __global__ void __launch_bounds__(RP_T) k_seg_repack(Seg<T> in, SoA<T> app, cons
             back.cnt[s2] = out.cnt[s2];
     }
     if (blockIdx.x == 0 && threadIdx.x == 0 && seg_flags) *seg_flags = 0u;  // the request is served
+}
+
+// ------------------------------------------------------------------------------------
+// place: the particles a resampling step appended (app[0 .. n_app)) go into the free slots
+// of run 1 of the segments, in place, instead of a full repack of everything. Segment k
+// (live_k slots with w != 0, n1_k slots in run 1) takes at most
+// cap_k = min(half - n1_k, half - live_k) of them: its run 1 has the room, and its live
+// particles plus the placed ones fill at most one output run of the next push, so that push
+// cannot overflow. A first pass gives each segment up to fill = ceil(total / nseg) live
+// particles in all, a second hands out what is left in segment order; app order is kept
+// within each pass (app[0 .. A1) in the first, app[A1 ..) in the second). Slots emptied by
+// merges (w = 0) stay: the next push or repack drops them. When the particles do not fit
+// that way, or a segment already holds more than half live particles, nothing is placed
+// and the fallback word gets BZ_SEG_NEEDS_REPACK for a conditional repack of the segments
+// and app together. Each CTA owns a contiguous range of segments through all phases:
+// live counts | totals and CTA-local scans of the shares | CTA offsets and copies, with
+// grid-wide barriers between them (cooperative launch) and the per-CTA partial sums as the
+// only exchange; deterministic.
+// ------------------------------------------------------------------------------------
+struct PlaceWs {
+    size_t live, loc1, loce, part, misc, total;
+    static int max_ctas(int nseg) { return int(ceil_div(std::max(nseg, 1), RP_T / 32)); }
+    explicit PlaceWs(int nseg) {
+        auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+        const size_t m = size_t(std::max(nseg, 1));
+        live = 0;
+        loc1 = al(4 * m);
+        loce = loc1 + al(4 * m);
+        part = loce + al(4 * m);
+        misc = part + al(8 * 4 * size_t(max_ctas(nseg)));  // four int64 partials per CTA
+        total = misc + 256;
+    }
+};
+// misc[0]: the fallback word
+
+// segment k's first-pass share and its room beyond it
+__device__ __forceinline__ void place_share(int live, int n1, int half, int fill, int &a1, int &room) {
+    const int cap = max(0, min(half - n1, half - live));
+    a1 = min(max(fill - live, 0), cap);
+    room = cap - a1;
+}
+
+// exclusive block scan (RP_T threads) of two int64 values; ta, tb get the block totals
+__device__ __forceinline__ void rp_scan2(int64_t &a, int64_t &b, int64_t &ta, int64_t &tb, int64_t *sa, int64_t *sb) {
+    const int t = threadIdx.x;
+    sa[t] = a;
+    sb[t] = b;
+    __syncthreads();
+    for (int o = 1; o < RP_T; o <<= 1) {
+        const int64_t xa = t >= o ? sa[t - o] : 0, xb = t >= o ? sb[t - o] : 0;
+        __syncthreads();
+        sa[t] += xa;
+        sb[t] += xb;
+        __syncthreads();
+    }
+    ta = sa[RP_T - 1];
+    tb = sb[RP_T - 1];
+    a = sa[t] - a;
+    b = sb[t] - b;
+    __syncthreads();
+}
+
+__device__ __forceinline__ int nz4(float4 v) { return (v.x != 0.f) + (v.y != 0.f) + (v.z != 0.f) + (v.w != 0.f); }
+__device__ __forceinline__ int nz4(double2 v) { return (v.x != 0.0) + (v.y != 0.0); }
+
+// slots with w != 0 among w[b .. b + cnt), this lane's share (16-byte loads when w is aligned)
+template <typename T> __device__ __forceinline__ int count_live(const T *w, uint32_t b, int cnt, int lane) {
+    using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+    constexpr int PER = 16 / int(sizeof(T));
+    int c = 0, j0 = 0;
+    if ((reinterpret_cast<uintptr_t>(w) & 15u) == 0) {  // b is a multiple of 4 (half is)
+        const V *p = reinterpret_cast<const V *>(w + b);
+        const int nv = cnt / PER;
+#pragma unroll 4
+        for (int i = lane; i < nv; i += 32) c += nz4(p[i]);
+        j0 = nv * PER;
+    }
+    for (int j = j0 + lane; j < cnt; j += 32) c += (w[b + uint32_t(j)] != T(0));
+    return c;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(RP_T) k_seg_place(Seg<T> s, SoA<T> app, const int32_t *app_n, int64_t app_cap,
+                                                    int32_t *live, int32_t *loc1, int32_t *loce, int64_t *part,
+                                                    int32_t *misc, uint32_t *seg_flags) {
+    cooperative_groups::grid_group grid = cooperative_groups::this_grid();
+    __shared__ int64_t sa[RP_T], sb[RP_T];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    constexpr int NW = RP_T / 32;
+    const int G = gridDim.x, b = blockIdx.x;
+    const int m = s.nseg, H = s.half;
+    const int S = (m + G - 1) / G;  // this CTA's segments: [lo, hi)
+    const int lo = min(m, b * S), hi = min(m, lo + S);
+    int64_t *p_live = part, *p_bad = part + G, *p_a1 = part + 2 * G, *p_room = part + 3 * G;
+    auto n1_of = [&](int k) { return min(max(s.cnt[2 * k + 1], 0), H); };
+    // 1. live particles per segment (warp per segment) and the CTA's sum
+    int64_t my_live = 0, my_bad = 0;
+    for (int seg = lo + warp; seg < hi; seg += NW) {
+        int c = 0;
+        for (int run = 0; run < 2; ++run)
+            c += count_live(s.a.w, seg_slot32(seg, run, H, 0), min(max(s.cnt[2 * seg + run], 0), H), lane);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+        if (lane == 0) {
+            live[seg] = c;
+            my_live += c;
+            my_bad |= c > H;
+        }
+    }
+    {
+        int64_t tl, tb;
+        rp_scan2(my_live, my_bad, tl, tb, sa, sb);
+        if (t == 0) {
+            p_live[b] = tl;
+            p_bad[b] = tb;
+        }
+    }
+    grid.sync();
+    // 2. totals (every CTA from the same partials), then this CTA's shares, scanned locally
+    int64_t TL = 0, BAD = 0;
+    for (int i = t; i < G; i += RP_T) {
+        TL += p_live[i];
+        BAD += p_bad[i];
+    }
+    {
+        int64_t x = TL, y = BAD;
+        rp_scan2(x, y, TL, BAD, sa, sb);
+    }
+    const int64_t na = min(int64_t(max(*app_n, 0)), app_cap);
+    const int fill = int(max(int64_t(1), (TL + na + m - 1) / m));
+    int64_t c1 = 0, ce = 0;
+    for (int base = lo; base < hi; base += RP_T) {
+        const int k = base + t;
+        int a1 = 0, room = 0;
+        if (k < hi) place_share(live[k], n1_of(k), H, fill, a1, room);
+        int64_t x1 = a1, xe = room, t1, te;
+        rp_scan2(x1, xe, t1, te, sa, sb);
+        if (k < hi) {
+            loc1[k] = int32_t(c1 + x1);
+            loce[k] = int32_t(ce + xe);
+        }
+        c1 += t1;
+        ce += te;
+    }
+    if (t == 0) {
+        p_a1[b] = c1;
+        p_room[b] = ce;
+    }
+    grid.sync();
+    // 3. the CTA's offsets in both passes and the totals, the decision, the copies
+    int64_t A1 = 0, R = 0, pre1 = 0, pree = 0;
+    for (int i = t; i < G; i += RP_T) {
+        const int64_t v1 = p_a1[i], ve = p_room[i];
+        A1 += v1;
+        R += ve;
+        if (i < b) {
+            pre1 += v1;
+            pree += ve;
+        }
+    }
+    {
+        int64_t x = A1, y = R;
+        rp_scan2(x, y, A1, R, sa, sb);
+        x = pre1;
+        y = pree;
+        rp_scan2(x, y, pre1, pree, sa, sb);
+    }
+    const bool fallback = BAD != 0 || A1 + R < na;  // the same in every CTA
+    if (b == 0 && t == 0) {
+        misc[0] = fallback ? int32_t(BZ_SEG_NEEDS_REPACK) : 0;
+        // every segment will hold at most half live particles: a pending request is served
+        if (!fallback && seg_flags) *seg_flags = 0u;
+    }
+    if (fallback) return;  // the conditional repack takes s and app together
+    for (int seg = lo + warp; seg < hi; seg += NW) {
+        const int n1 = n1_of(seg);
+        int a1, room;
+        place_share(live[seg], n1, H, fill, a1, room);
+        const int64_t s1 = pre1 + loc1[seg], s2 = A1 + pree + loce[seg];
+        const int len1 = int(max(int64_t(0), min(int64_t(a1), na - s1)));
+        const int len2 = A1 < na ? int(max(int64_t(0), min(int64_t(room), na - s2))) : 0;
+        const int len = len1 + len2;
+        const uint32_t base = seg_slot32(seg, 1, H, n1);
+        // four rounds of 32 at a time: all their loads in flight before the stores
+        for (int j0 = 0; j0 < len; j0 += 4 * 32) {
+            T xx[4], a1v[4], a2v[4], a3v[4], wv[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int j = j0 + u * 32 + lane;
+                if (j < len) {
+                    const int64_t i = j < len1 ? s1 + j : s2 + (j - len1);
+                    xx[u] = app.x[i]; a1v[u] = app.vx[i]; a2v[u] = app.vy[i]; a3v[u] = app.vz[i]; wv[u] = app.w[i];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int j = j0 + u * 32 + lane;
+                if (j < len) {
+                    const uint32_t q = base + uint32_t(j);
+                    s.a.x[q] = xx[u]; s.a.vx[q] = a1v[u]; s.a.vy[q] = a2v[u]; s.a.vz[q] = a3v[u]; s.a.w[q] = wv[u];
+                }
+            }
+        }
+        __syncwarp();  // every lane has read n1
+        if (lane == 0) s.cnt[2 * seg + 1] = n1 + len;
+    }
 }
 
 // moments of a segmented state (post_processing_1D.py:44-57), one warp per segment
@@ -669,6 +882,38 @@ static int seg_repack_entry(const S *in_, P app_, const int32_t *app_n, int64_t 
     return BZ_OK;
 }
 
+template <typename T, typename S, typename P>
+static int seg_place_entry(S s_, P app_, const int32_t *app_n, int64_t app_cap, S scratch_, void *ws,
+                           size_t ws_bytes, uint32_t *seg_flags, uint32_t *status, void *stream) {
+    if (!ws || !status || !app_n || !seg_ok<T>(s_) || !seg_ok<T>(scratch_)) return BZ_ERR_ARG;
+    if (scratch_.nseg != s_.nseg || scratch_.half != s_.half) return BZ_ERR_ARG;
+    if (!app_.x || !app_.vx || !app_.vy || !app_.vz || !app_.w || app_cap < 0) return BZ_ERR_ARG;
+    if (int64_t(s_.nseg) * 2 * s_.half > int64_t(INT32_MAX)) return BZ_ERR_TOO_LARGE;  // int32 shares and offsets
+    PlaceWs L(s_.nseg);
+    const size_t rws = RepackWs(s_.nseg).total;
+    if (ws_bytes < L.total + rws) return BZ_ERR_WORKSPACE;
+    unsigned char *b = static_cast<unsigned char *>(ws);
+    int32_t *live = reinterpret_cast<int32_t *>(b + L.live);
+    int32_t *loc1 = reinterpret_cast<int32_t *>(b + L.loc1);
+    int32_t *loce = reinterpret_cast<int32_t *>(b + L.loce);
+    int64_t *part = reinterpret_cast<int64_t *>(b + L.part);
+    int32_t *misc = reinterpret_cast<int32_t *>(b + L.misc);
+    Seg<T> s = to_seg<T>(s_);
+    SoA<T> app{app_.x, app_.vx, app_.vy, app_.vz, app_.w};
+    auto kern = k_seg_place<T>;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, RP_T, 0) != cudaSuccess || per_sm < 1)
+        return BZ_ERR_UNSUPPORTED;
+    const int grid = std::max(1, std::min(num_sms() * per_sm, PlaceWs::max_ctas(s.nseg)));
+    void *args[] = {&s, &app, (void *)&app_n, &app_cap, &live, &loc1, &loce, &part, &misc, &seg_flags};
+    if (cudaLaunchCooperativeKernel(reinterpret_cast<void *>(kern), dim3(grid), dim3(RP_T), args, 0,
+                                    as_stream(stream)) != cudaSuccess)
+        return BZ_ERR_CUDA;
+    // when they did not fit: the segments and app together through scratch and back
+    return seg_repack_entry<T>(&s_, app_, app_n, app_cap, scratch_, b + L.total, rws,
+                               reinterpret_cast<const uint32_t *>(misc), seg_flags, status, stream, &s_);
+}
+
 // energy distribution per node (swarm): one warp per segment. The bin is taken from a
 // float log2 unless it lies within 1e-4 of a bin edge, where it is recomputed in float64
 // (the float estimate is off by far less than that).
@@ -854,6 +1099,19 @@ int bz_seg_rebalance_f64(bz_segments_f64 s, bz_segments_f64 scratch, void *works
                          const uint32_t *only_if, uint32_t *seg_flags, uint32_t *status, void *stream) {
     return bz::seg_repack_entry<double>(&s, bz_particles_f64{}, nullptr, 0, scratch, workspace, workspace_bytes,
                                         only_if, seg_flags, status, stream, &s);
+}
+size_t bz_seg_place_workspace(int32_t nseg) { return bz::PlaceWs(nseg).total + bz::RepackWs(nseg).total; }
+int bz_seg_place_f32(bz_segments_f32 s, bz_particles_f32 app, const int32_t *app_n, int64_t app_capacity,
+                     bz_segments_f32 scratch, void *workspace, size_t workspace_bytes, uint32_t *seg_flags,
+                     uint32_t *status, void *stream) {
+    return bz::seg_place_entry<float>(s, app, app_n, app_capacity, scratch, workspace, workspace_bytes, seg_flags,
+                                      status, stream);
+}
+int bz_seg_place_f64(bz_segments_f64 s, bz_particles_f64 app, const int32_t *app_n, int64_t app_capacity,
+                     bz_segments_f64 scratch, void *workspace, size_t workspace_bytes, uint32_t *seg_flags,
+                     uint32_t *status, void *stream) {
+    return bz::seg_place_entry<double>(s, app, app_n, app_capacity, scratch, workspace, workspace_bytes, seg_flags,
+                                       status, stream);
 }
 int bz_seg_deposit_f32(const bz_params *p, bz_segments_f32 s, double *moments, void *stream) {
     return bz::seg_deposit_entry<float>(p, s, moments, stream);

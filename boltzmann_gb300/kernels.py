@@ -319,6 +319,16 @@ def seg_rebalance(s: SegmentSet, scratch: SegmentSet, status, ws: Workspace, onl
          _ptr(status), _stream())
 
 
+def seg_place(s: SegmentSet, app: ParticleSet, scratch: SegmentSet, status, ws: Workspace, app_n=None, clear=None,
+              name="seg_place"):
+    """app[0:n) into the free slots of s's segments, in place (through scratch and back
+    into s when they do not fit that way)."""
+    w = ws.get(name, _lib.load().bz_seg_place_workspace(s.nseg))
+    an = _ptr(app_n) if app_n is not None else app.n_ptr()
+    call(f"bz_seg_place_{s.suffix}", s.struct(), app.struct(), an, app.capacity, scratch.struct(), _ptr(w),
+         w.numel(), _ptr(clear), _ptr(status), _stream())
+
+
 def seg_deposit(params, s: SegmentSet, moments):
     call(f"bz_seg_deposit_{s.suffix}", ctypes.byref(params), s.struct(), _ptr(moments), _stream())
 
@@ -339,7 +349,12 @@ def seg_bin_particles(params, s: SegmentSet, edges, min_wt, perm, offsets, count
 
 def seg_resample(params, s: SegmentSet, app: ParticleSet, out: SegmentSet, nb, targets, max_ppc, min_wt, split_below,
                  merge_at, merge_keep, perm, offsets, counts, hw_counts, status, seg_flags, ws: Workspace, need=None,
-                 replay_u=None, cons_diag=None):
+                 replay_u=None, cons_diag=None, in_place=False):
+    """ES-WPNC resampling of s: the result in out, or with ``in_place`` in s itself (out is
+    then the scratch of a repack, needed only when the appended particles do not fit)."""
+    if in_place:
+        params = type(params).from_buffer_copy(params)
+        params.flags |= _lib.RESAMPLE_IN_PLACE
     nkeys = params.n_nodes * nb
     w = ws.get("seg_resample", _lib.load().bz_seg_resample_workspace(s.nseg, s.capacity, nkeys))
     call(f"bz_seg_resample_{s.suffix}", ctypes.byref(params), s.struct(), app.struct(), app.capacity, out.struct(), nb,

@@ -209,8 +209,10 @@ class BoltzmannGB300:
         cfg = self.cfg
         K.seg_resample(self.params(), self.A, self.app, self.B, self.nb, self.targets, self.max_ppc, cfg.min_wt,
                        cfg.split_below, cfg.merge_at, cfg.merge_keep, self.perm, self.offsets, self.bin_counts,
-                       self.hw_counts, self.status, self.seg_flags, self.ws, need=self.need)
-        self.A, self.B = self.B, self.A
+                       self.hw_counts, self.status, self.seg_flags, self.ws, need=self.need,
+                       in_place=cfg.resample_in_place)
+        if not cfg.resample_in_place:
+            self.A, self.B = self.B, self.A
 
     def _repack_if_needed(self):
         """Spread the particles evenly again when the last push left a segment above
@@ -272,7 +274,7 @@ class BoltzmannGB300:
             gr.replay()
             self._replayed.add(key)
             # the graph swaps A and B internally; mirror the swaps on the host side
-            for _ in range(2 if resample else 1):
+            for _ in range(2 if resample and not self.cfg.resample_in_place else 1):
                 self.A, self.B = self.B, self.A
         else:
             self._kinds.add(resample)
@@ -449,10 +451,12 @@ class BoltzmannGB300:
         Every step: the push and the fused grid step (grid update, clock, ion fluid,
         Poisson) (2); a plain step adds the conditional rebalance (one cooperative
         kernel); a resampling step adds binning (segment totals, key offsets twice, keys,
-        then per 8-bit radix pass a histogram, scan and scatter), decide + apply (2) and the
-        repack of the survivors with the appended particles (1)."""
+        then per 8-bit radix pass a histogram, column sums, column scan and scatter),
+        decide + apply (2) and either the placement of the appended particles with its
+        conditional repack (2) or the repack of the survivors with them (1)."""
         passes = 2 if self.nnodes * self.nb >= 256 else 1
-        return 2 + (4 + 3 * passes + 2 + 1 if resample else 1) + (self._ion_rate is not None)
+        tail = 2 if self.cfg.resample_in_place else 1
+        return 2 + (4 + 4 * passes + 2 + tail if resample else 1) + (self._ion_rate is not None)
 
     def snapshot(self):
         """A device copy of the simulation state: the particles (the buffer that holds

@@ -52,6 +52,7 @@ class SwarmConfig:
     merge_keep: float = 1.0
     max_ppc_factor: float = 10.0
     min_wt: float = 0.1
+    resample_in_place: bool = True   # appended particles into free slots instead of a full repack
     capacity_factor: float = 7.0      # slots per initial particle: bins may grow to 3x target, run 0 holds half
     seg_half: int = 2048
     seed: int = 1
@@ -193,8 +194,9 @@ class SwarmEnsemble:
                             self.status, self.ws)
         K.seg_resample(p, self.A, self.app, self.B, self.nb, self.targets, self.max_ppc, cfg.min_wt, cfg.split_below,
                        cfg.merge_at, cfg.merge_keep, self.perm, self.offsets, self.bin_counts, self.hw_counts,
-                       self.status, self.seg_flags, self.ws, need=self.need)
-        self.A, self.B = self.B, self.A
+                       self.status, self.seg_flags, self.ws, need=self.need, in_place=cfg.resample_in_place)
+        if not cfg.resample_in_place:
+            self.A, self.B = self.B, self.A
 
     def _step_body(self, resample):
         self.electron_kernel()
@@ -213,7 +215,7 @@ class SwarmEnsemble:
         if use_graph and resample in self._kinds:
             gr = self._graphs.get(key) or self._capture_key(key)
             gr.replay()
-            for _ in range(2 if resample else 1):
+            for _ in range(2 if resample and not self.cfg.resample_in_place else 1):
                 self.A, self.B = self.B, self.A
         else:
             self._kinds.add(resample)

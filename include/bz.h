@@ -54,6 +54,9 @@ enum bz_status {
                                         this step to moments row 2 (ns_src, always 0 in the reference) */
 #define BZ_CLEAR_MOMENTS 0x40u       /* the push clears moments (4 x n_nodes float64) before it
                                         accumulates into them (a memset on the caller's stream) */
+#define BZ_RESAMPLE_IN_PLACE 0x80u   /* bz_seg_resample_*: the result stays in s (bz_seg_place_*: the
+                                        appended particles into free slots, merged ones left as w = 0);
+                                        out is only the scratch of a repack when they do not fit */
 
 /* particle motion (bz_params.advect) */
 #define BZ_ADVECT_NONE 0      /* one 0-D swarm: no drift, E[0] everywhere, every particle in node/cell 0 */
@@ -264,7 +267,8 @@ typedef struct bz_segments_f64 { double *x, *vx, *vy, *vz, *w; int32_t *counts; 
 
 /* Push + collide (+ deposit) of a segmented state into another (same nseg, half); the
  * per-particle arithmetic of bz_push_collide_*. Philox counters use the input slot.
- * n_pushed (optional, device) accumulates the number of input particles pushed. Slots are
+ * Slots with w <= 0 (left by merges) are dropped, not pushed. n_pushed (optional, device)
+ * accumulates the number of input particles pushed (w > 0). Slots are
  * indexed with 32 bits: nseg * 2 * half above 2^32 - 1 returns BZ_ERR_TOO_LARGE. */
 size_t bz_seg_push_workspace(void);
 int bz_seg_push_collide_f32(const bz_params *p, bz_segments_f32 in, bz_segments_f32 out, const float *E,
@@ -305,6 +309,24 @@ int bz_seg_rebalance_f32(bz_segments_f32 s, bz_segments_f32 scratch, void *works
                          const uint32_t *only_if, uint32_t *seg_flags, uint32_t *status, void *stream);
 int bz_seg_rebalance_f64(bz_segments_f64 s, bz_segments_f64 scratch, void *workspace, size_t workspace_bytes,
                          const uint32_t *only_if, uint32_t *seg_flags, uint32_t *status, void *stream);
+/* Places app[0 .. *app_n) (capped at app_capacity) into s in place, the step after a
+ * resampling's merges and splits: into the free slots of run 1 of each segment, after its n1
+ * particles. Segment k, with live_k slots of w != 0, takes at most
+ * min(half - n1_k, half - live_k), so that the next push cannot overflow it: first up to
+ * ceil(total / nseg) live particles in all, then what is left in segment order; app order
+ * is kept within each of the two passes. Slots with w = 0 stay (a push or repack drops
+ * them). When the particles do not fit that way, or a segment holds more than half live
+ * particles, s and app are repacked through scratch (s's geometry) and back into s instead,
+ * evenly as bz_seg_repack_* spreads them. Either way *seg_flags (if given) is cleared.
+ * Workspace: bz_seg_place_workspace(s.nseg) bytes. BZ_ERR_TOO_LARGE when
+ * 2 * nseg * half exceeds INT32_MAX. */
+size_t bz_seg_place_workspace(int32_t nseg);
+int bz_seg_place_f32(bz_segments_f32 s, bz_particles_f32 app, const int32_t *app_n, int64_t app_capacity,
+                     bz_segments_f32 scratch, void *workspace, size_t workspace_bytes, uint32_t *seg_flags,
+                     uint32_t *status, void *stream);
+int bz_seg_place_f64(bz_segments_f64 s, bz_particles_f64 app, const int32_t *app_n, int64_t app_capacity,
+                     bz_segments_f64 scratch, void *workspace, size_t workspace_bytes, uint32_t *seg_flags,
+                     uint32_t *status, void *stream);
 /* Moments (sum w, 0, 0, sum w*energy) of a segmented state (no ion flags are stored). */
 int bz_seg_deposit_f32(const bz_params *p, bz_segments_f32 s, double *moments, void *stream);
 int bz_seg_deposit_f64(const bz_params *p, bz_segments_f64 s, double *moments, void *stream);
@@ -326,7 +348,9 @@ int bz_seg_bin_f64(const bz_params *p, bz_segments_f64 s, int32_t nbins, const d
                    int32_t *perm, int32_t *offsets, int32_t *counts, int32_t *hw_counts, void *workspace,
                    size_t workspace_bytes, uint32_t *status, void *stream);
 /* ES-WPNC resampling of a segmented state: as bz_resample_*, with the appended particles
- * collected in app (capacity app_capacity) and everything repacked into out. */
+ * collected in app (capacity app_capacity) and everything repacked into out; with
+ * BZ_RESAMPLE_IN_PLACE in p->flags the result stays in s instead (bz_seg_place_* with out
+ * as its scratch: out then needs s's geometry). */
 size_t bz_seg_resample_workspace(int32_t nseg, int64_t capacity, int32_t nkeys);
 int bz_seg_resample_f32(const bz_params *p, bz_segments_f32 s, bz_particles_f32 app, int64_t app_capacity,
                         bz_segments_f32 out, int32_t nbins, const int32_t *targets, const int32_t *max_ppc,
