@@ -123,6 +123,12 @@ __device__ __forceinline__ Uni<double> uni_d(uint32_t a, uint32_t b) {
     return {u, 1.0 - u};
 }
 
+// the 23 bits of three Philox words that uni_f leaves unused (their low 9, 9 and 5 bits),
+// placed where uni_f reads: an independent uniform without another Philox call
+__device__ __forceinline__ uint32_t low_bits_word(uint32_t a, uint32_t b, uint32_t c) {
+    return (a << 23) | ((b & 511u) << 14) | ((c & 511u) << 5);
+}
+
 // Key and step words of the stream: key = seed, counter = (slot, step lo, step hi, tag).
 struct Rng {
     uint32_t k0, k1, s0, s1;
@@ -145,12 +151,15 @@ __device__ __forceinline__ void draw4(const Rng &g, uint32_t slot, uint32_t tag,
     d.v[0] = uni_d(a.x, a.y); d.v[1] = uni_d(a.z, a.w); d.v[2] = uni_d(b.x, b.y); d.v[3] = uni_d(b.z, b.w);
 }
 // the same draws with precomputed round keys
+// (and a ninth uniform from the second draw's unused low bits)
 __device__ __forceinline__ void draw4x2(const Rng &g, const uint32_t *rk0, const uint32_t *rk1, uint32_t slot,
-                                        uint32_t tag_a, uint32_t tag_b, Draw4<float> &da, Draw4<float> &db) {
+                                        uint32_t tag_a, uint32_t tag_b, Draw4<float> &da, Draw4<float> &db,
+                                        Uni<float> &low_b) {
     u32x4 a, b;
     philox_rk_x2<PUSH_ROUNDS>(slot, g.s0, g.s1, tag_a, tag_b, rk0, rk1, a, b);
     da.v[0] = uni_f(a.x); da.v[1] = uni_f(a.y); da.v[2] = uni_f(a.z); da.v[3] = uni_f(a.w);
     db.v[0] = uni_f(b.x); db.v[1] = uni_f(b.y); db.v[2] = uni_f(b.z); db.v[3] = uni_f(b.w);
+    low_b = uni_f(low_bits_word(b.x, b.y, b.z));
 }
 __device__ __forceinline__ void draw4(const Rng &g, const uint32_t *rk0, const uint32_t *rk1, uint32_t slot,
                                       uint32_t tag, Draw4<float> &d) {
@@ -231,57 +240,23 @@ static inline float float_above(double m) {
 __device__ __forceinline__ float sqrt_pos(float x) { return x * rsqrt_ftz(x); }
 __device__ __forceinline__ double sqrt_pos(double x) { return sqrt(x); }
 
-// Standard normal deviates from float uniforms by their quantile, Phi^-1(u) = x f(w) with
-// x = 2u - 1 = u - (1-u) (exact) and w = -log2(4 u (1-u)); f is a polynomial in w on the
-// central range w < 5/ln 2 (u in (0.00169, 0.99831)) and one in sqrt(w) in the tails. The
-// form is Giles' (M. Giles, "Approximating the erfinv function", GPU Computing Gems Jade
-// Edition, 2011); the coefficients are this library's own weighted least-squares fit of
-// degree 8 to the exact quantile over all 2^23 uniforms uni_f emits. Maximum relative
-// error 3.5e-7 in float32 arithmetic, including an absolute error of 2^-22 in the hardware
-// log2. One uniform per deviate (Box-Muller takes two per pair and a log, a square root, a
-// sine and a cosine) and no rejection.
-constexpr float NQ_W_TAIL = 7.213475f;  // 5 / ln 2
-__device__ __forceinline__ float nq_w(Uni<float> a) { return -2.0f - lg2_ftz(a.u * a.c); }  // u c > 2^-25
-__device__ __forceinline__ float nq_central(float w) {
-    const float t = w - 3.6067376f;
-    float r = 2.177562797e-09f;
-    r = fmaf(r, t, 3.740066035e-08f);
-    r = fmaf(r, t, -5.542177632e-07f);
-    r = fmaf(r, t, -9.956440863e-07f);
-    r = fmaf(r, t, 7.136897329e-05f);
-    r = fmaf(r, t, -5.904508871e-04f);
-    r = fmaf(r, t, -2.838615328e-03f);
-    r = fmaf(r, t, 2.417715639e-01f);
-    return fmaf(r, t, 2.123313665e+00f);
-}
-__device__ __forceinline__ float nq_tail(float w) {
-    const float t = sqrt_pos(w) - 3.688112f;
-    float r = -9.029921785e-05f;
-    r = fmaf(r, t, -1.695100582e-05f);
-    r = fmaf(r, t, 6.919289590e-04f);
-    r = fmaf(r, t, -1.730788732e-03f);
-    r = fmaf(r, t, 3.062781878e-03f);
-    r = fmaf(r, t, -5.049590953e-03f);
-    r = fmaf(r, t, 7.831202820e-03f);
-    r = fmaf(r, t, 1.180825233e+00f);
-    return fmaf(r, t, 4.106443405e+00f);
-}
-// Three deviates times sigma. The tail polynomial runs only when a lane among those
-// executing this needs it (1% of lanes, in about a quarter of the warps); otherwise the
-// warp evaluates the central polynomial alone.
-__device__ __forceinline__ void normal_quantile3(Uni<float> a0, Uni<float> a1, Uni<float> a2, float sigma,
-                                                 float &g0, float &g1, float &g2) {
-    const float w0 = nq_w(a0), w1 = nq_w(a1), w2 = nq_w(a2);
-    float r0 = nq_central(w0), r1 = nq_central(w1), r2 = nq_central(w2);
-    const bool t0 = !(w0 < NQ_W_TAIL), t1 = !(w1 < NQ_W_TAIL), t2 = !(w2 < NQ_W_TAIL);
-    if (__any_sync(__activemask(), t0 || t1 || t2)) {
-        if (t0) r0 = nq_tail(w0);
-        if (t1) r1 = nq_tail(w1);
-        if (t2) r2 = nq_tail(w2);
-    }
-    g0 = (a0.u - a0.c) * sigma * r0;
-    g1 = (a1.u - a1.c) * sigma * r1;
-    g2 = (a2.u - a2.c) * sigma * r2;
+// Two standard normals times sigma from two float uniforms by Box-Muller (radius
+// sqrt(-2 ln a), angle 2 pi b), with the hardware log2, reciprocal root, sine and cosine.
+// -ln a comes from the log2 where a <= 1 - 2^-6 (|ln a| > 0.0157: the log2's absolute error
+// of 2^-22.6 is then below 1e-5 of it) and from the series of -ln(1 - c) in the exact
+// complement c = 1 - a above (relative truncation error c^4 / 5 < 1.2e-8), so the radius
+// keeps its relative accuracy down to the smallest one; both are normal numbers (a <= 1 -
+// 2^-24), as x rsqrt(x) needs.
+__device__ __forceinline__ void box_muller_f(Uni<float> a, Uni<float> b, float sigma, float &g0, float &g1) {
+    const float c = a.c;
+    // 2 (c + c^2/2 + c^3/3 + c^4/4) = -2 ln(1 - c) for small c
+    const float ser = c * fmaf(c, fmaf(c, fmaf(c, 0.5f, 0.6666667f), 1.0f), 2.0f);
+    const float r2 = c < 0.015625f ? ser : -1.3862944f * lg2_ftz(a.u);  // -2 ln 2 log2(a)
+    const float r = sigma * sqrt_pos(r2);
+    float s, co;
+    sincos2pi(b.u, &s, &co);
+    g0 = r * co;
+    g1 = r * s;
 }
 
 // Box-Muller pair from uniforms (a, b): r = sqrt(-2 ln a), angle 2 pi b.

@@ -149,7 +149,7 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
     // gas velocity (boltzmann.py:589, electron_kernel_numba.py:51-53) and uniforms
     T g0 = 0, g1 = 0, g2 = 0;
     Uni<T> u0, u1, u2, u3;
-    Uni<T> u5{T(0.5), T(0.5)};  // the child's azimuth (float32: the gas draw's fourth word)
+    Uni<T> u5{T(0.5), T(0.5)};  // the child's azimuth (float32: the collision draw's unused low bits)
     double r0_replay = 0.0;
     if (REPLAY) {
         g0 = T(gas[size_t(slot) * 3 + 0]);
@@ -163,17 +163,21 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
     } else {
         Draw4<T> dg, d;
         if constexpr (sizeof(T) == 4) {
-            // gas-velocity and collision uniforms from one interleaved pair of Philox calls
-            draw4x2(rng, k.rk0, k.rk1, slot, 0u, 1u, dg, d);
+            // gas-velocity and collision uniforms from one interleaved pair of Philox calls;
+            // the ionization child's azimuth from the collision words' unused low bits (no
+            // third Philox call)
+            draw4x2(rng, k.rk0, k.rk1, slot, 0u, 1u, dg, d, u5);
         } else {
             draw4(rng, k.rk0, k.rk1, slot, 0u, dg);
             draw4(rng, k.rk0, k.rk1, slot, 1u, d);
         }
         if constexpr (sizeof(T) == 4) {
-            // three normals by their quantiles from three words of the gas draw; its
-            // fourth word is the ionization child's azimuth (no third Philox call)
-            if (k.gas_sigma > T(0)) normal_quantile3(dg.v[0], dg.v[1], dg.v[2], k.gas_sigma, g0, g1, g2);
-            u5 = dg.v[3];
+            // Box-Muller pairs from the gas draw's words (0, 1) and (2, 3), as in float64
+            if (k.gas_sigma > T(0)) {
+                float h;
+                box_muller_f(dg.v[0], dg.v[1], k.gas_sigma, g0, g1);
+                box_muller_f(dg.v[2], dg.v[3], k.gas_sigma, g2, h);
+            }
         } else if (k.gas_sigma > T(0)) {
             T h;
             box_muller(dg.v[0].u, dg.v[1].u, g0, g1);

@@ -77,24 +77,11 @@ static void draw_u(const orc_params *p, uint64_t slot, uint32_t tag, double *u, 
     }
 }
 
-/* Standard normal quantile Phi^-1(u) in float64, for the float32 kernels' gas velocity
- * (they evaluate the same quantile in float32 from a polynomial fit, relative error
- * 3.5e-7). A rational start (Abramowitz & Stegun 26.2.23, |error| < 4.5e-4), then Halley
- * steps on 0.5 erfc(-g/sqrt 2) - q, with q the smaller of u and 1-u so that the tails keep
- * their relative accuracy. */
-static double orc_ndtri(double u) {
-    const int upper = u > 0.5;
-    const double q = upper ? 1.0 - u : u; /* exact for the uniforms used here */
-    if (q == 0.5) return 0.0;
-    double t = sqrt(-2.0 * log(q));
-    double g = -(t - (2.515517 + 0.802853 * t + 0.010328 * t * t) / (1.0 + 1.432788 * t + 0.189269 * t * t + 0.001308 * t * t * t));
-    for (int it = 0; it < 4; ++it) {
-        double F = 0.5 * erfc(-g / M_SQRT2) - q;
-        double phi = exp(-0.5 * g * g) / sqrt(2.0 * M_PI);
-        double e = F / phi;
-        g -= e / (1.0 + 0.5 * g * e);
-    }
-    return upper ? -g : g;
+/* The raw words of a float-path draw (tag <= 2: the push's rounds). */
+static void draw_raw(const orc_params *p, uint64_t slot, uint32_t tag, uint32_t r[4]) {
+    uint32_t key[2] = {(uint32_t)p->seed, (uint32_t)(p->seed >> 32)};
+    uint32_t ctr[4] = {(uint32_t)slot, (uint32_t)p->step, (uint32_t)(p->step >> 32), tag};
+    orc_philox_rounds(ctr, key, r, tag <= 2u ? PUSH_ROUNDS : 10);
 }
 
 /* Box-Muller: (r cos 2πb, r sin 2πb) with r = sqrt(-2 ln a). */
@@ -194,12 +181,21 @@ static void push_one(const orc_params *p, int64_t i, const double *in_d, const d
             }
             draw_u(p, (uint64_t)i, 2u, ui, 1);
         } else {
-            /* float32: three normals by their quantiles from the gas draw's first three
-             * words, the child's azimuth from its fourth */
+            /* float32: Box-Muller pairs from the gas draw's words (0, 1) and (2, 3), as in
+             * float64; the child's azimuth from the bits of the collision draw's first three
+             * words that its uniforms leave unused (the low 9, 9 and 5), placed where a
+             * float-path uniform takes its 23 bits */
             draw_u(p, (uint64_t)i, 0u, ug, 4);
-            if (p->gas_sigma > 0)
-                for (int k = 0; k < 3; ++k) g[k] = orc_ndtri(ug[k]) * p->gas_sigma;
-            ui[0] = ug[3];
+            if (p->gas_sigma > 0) {
+                double g3;
+                box_muller(ug[0], ug[1], &g[0], &g[1]);
+                box_muller(ug[2], ug[3], &g[2], &g3);
+                for (int k = 0; k < 3; ++k) g[k] *= p->gas_sigma;
+            }
+            uint32_t rc[4];
+            draw_raw(p, (uint64_t)i, 1u, rc);
+            const uint32_t r5 = (rc[0] << 23) | ((rc[1] & 511u) << 14) | ((rc[2] & 511u) << 5);
+            ui[0] = ((double)(r5 >> 9) + 0.5) * 0x1p-23;
         }
         draw_u(p, (uint64_t)i, 1u, uc, 4);
         Ru[0] = uc[0]; Ru[1] = uc[1]; Ru[2] = uc[2]; Ru[3] = uc[3]; Ru[4] = 0.0; Ru[5] = ui[0];
