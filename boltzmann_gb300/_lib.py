@@ -107,6 +107,7 @@ _PROTOS = {
     "bz_philox4x32_10": (ctypes.c_int, [_vp, _vp, _i32, _i32, _vp, _vp]),
     "bz_field_step_selected": (ctypes.c_int, []),
     "bz_seg_push_workspace": (_sz, []),
+    "bz_seg_push_workspace_nodes": (_sz, [_i32]),
     "bz_seg_push_shapes": (ctypes.c_int32, []),
     "bz_seg_push_shape_info": (ctypes.c_int, [ctypes.c_int32, _vp, _vp, _vp, _vp]),
     "bz_seg_push_select": (ctypes.c_int, [ctypes.c_int32]),

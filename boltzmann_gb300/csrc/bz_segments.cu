@@ -45,6 +45,18 @@ template <typename A> __device__ __forceinline__ void dep_pair(A *g, int nd, A a
     atomicAdd(&g[2 * nd], a);
     atomicAdd(&g[2 * nd + 1], b);
 }
+// The float32 alternative when the caller's workspace holds a grid per CTA in global memory:
+// a node's two sums as one vector reduction, performed in L2 without a return value, so the
+// lane does not wait for it (a float add to shared memory is a compare-and-swap loop on this
+// part, with retries where lanes of a warp meet on a node).
+// (written as a global-space reduction: a vector atomic on a generic pointer is not)
+__device__ __forceinline__ void dep_red(float2 *g, int nd, float a, float b) {
+    asm volatile("red.relaxed.gpu.global.add.v2.f32 [%0], {%1, %2};" ::"l"(__cvta_generic_to_global(g + nd)), "f"(a),
+                 "f"(b)
+                 : "memory");
+}
+
+constexpr size_t SEG_PUSH_TICKET_BYTES = 256;  // the push's segment ticket (cleared per launch)
 
 template <typename T> struct Seg {
     SoA<T> a;
@@ -63,12 +75,13 @@ __device__ __forceinline__ uint32_t seg_slot32(int seg, int run, int half, int j
 
 // ADV >= 0: the motion mode (ADV) and the direct collision probability are known at compile
 // time (the CCP's hot loop: 1D drift; the swarm ensemble), so their tests leave the loop (4%
-// of the CCP push's time); ADV < 0 reads both from the parameters
-template <typename T, bool REPLAY, int XS, bool DEPOSIT, int SG_T, int SG_I, int MINB, bool PF, int ADV>
+// of the CCP push's time); ADV < 0 reads both from the parameters. GRED: the float32 deposit
+// goes to this CTA's grid in global memory (gdep, from the workspace) by vector reductions
+template <typename T, bool REPLAY, int XS, bool DEPOSIT, int SG_T, int SG_I, int MINB, bool PF, int ADV, bool GRED>
 __global__ void __launch_bounds__(SG_T, MINB)
     k_seg_push(bz_params p, PushConst<T> kc, Seg<T> in, Seg<T> out, const T *E, const double *R, const double *gas,
                double *moments, unsigned long long *n_pushed, unsigned int *ticket, uint32_t *seg_flags,
-               uint32_t *status) {
+               uint32_t *status, float2 *gdep) {
     using A = typename AccT<T>::t;
     const int advect = ADV >= 0 ? ADV : p.advect;
     constexpr int SG_R = 32 * SG_I;  // particles per warp round
@@ -86,6 +99,14 @@ __global__ void __launch_bounds__(SG_T, MINB)
             xs_s[i] = make_float4(p.xs_table[i], p.xs_table[xsn + i], p.xs_table[2 * xsn + i], 0.0f);
     if (DEPOSIT)
         for (int i = threadIdx.x; i < 3 * nnodes; i += SG_T) mom_s[i] = A(0);
+    // GRED: (sum w, sum w e) in this CTA's grid in global memory (the ionized particles' sums
+    // and the rare paths stay in shared memory)
+    static_assert(!GRED || (DEPOSIT && sizeof(T) == 4 && ADV == BZ_ADVECT_1D), "global grid: float32 1D deposit");
+    float2 *gd = nullptr;
+    if constexpr (GRED) {
+        gd = gdep + size_t(blockIdx.x) * size_t(nnodes);
+        for (int i = threadIdx.x; i < nnodes; i += SG_T) gd[i] = make_float2(0.f, 0.f);
+    }
     __syncthreads();
     const NodeMap &nm = kc.nm;
     const Rng rng = make_rng(p);
@@ -190,7 +211,10 @@ __global__ void __launch_bounds__(SG_T, MINB)
                             const int nd = alive ? deposit_node_pos(advect, it[k].x, nm) : -1;
                             const bool in_grid = nd >= 0 && nd < nnodes;
                             if (in_grid && advect != BZ_ADVECT_ENSEMBLE) {  // ensembles: warp-summed below
-                                dep_pair(mom_s, nd, A(w[k]), A(w[k] * it[k].e));
+                                if constexpr (GRED)
+                                    dep_red(gd, nd, float(w[k]), float(w[k] * it[k].e));
+                                else
+                                    dep_pair(mom_s, nd, A(w[k]), A(w[k] * it[k].e));
                                 if (it[k].ionized) atomicAdd(&mom_s[2 * nnodes + nd], A(w[k]));
                             }
                             // rarely taken, one test for all: an excitation counted into the
@@ -291,7 +315,15 @@ __global__ void __launch_bounds__(SG_T, MINB)
         if (lane == 0 && pushed) atomicAdd(n_pushed, (unsigned long long)pushed);
     }
     if (DEPOSIT) {
+        if constexpr (GRED) __threadfence();  // this CTA's reductions are performed before the reads below
         __syncthreads();
+        if constexpr (GRED) {
+            for (int i = threadIdx.x; i < nnodes; i += SG_T) {
+                const float2 v = __ldcg(gd + i);  // from L2
+                if (v.x != 0.f) atomicAdd(&moments[i], double(v.x));
+                if (v.y != 0.f) atomicAdd(&moments[3 * nnodes + i], double(v.y));
+            }
+        }
         for (int i = threadIdx.x; i < 3 * nnodes; i += SG_T) {
             A val = mom_s[i];
             if (val != A(0)) {
@@ -736,16 +768,16 @@ template <typename T, typename S> static Seg<T> to_seg(const S &s) {
 
 template <typename T, bool REPLAY, int XS, bool DEPOSIT, int SG_T = kSegShapes[0].threads,
           int SG_I = kSegShapes[0].per_lane, int MINB = kSegShapes[0].min_blocks, bool PF = kSegShapes[0].prefetch,
-          int ADV = -1>
+          int ADV = -1, bool GRED = false>
 static int launch_seg_push(const bz_params &p, Seg<T> in, Seg<T> out, const T *E, const double *R, const double *gas,
-                           double *moments, uint64_t *n_pushed, void *ws, uint32_t *seg_flags, uint32_t *status,
-                           cudaStream_t st) {
+                           double *moments, uint64_t *n_pushed, void *ws, size_t ws_bytes, uint32_t *seg_flags,
+                           uint32_t *status, cudaStream_t st) {
     using A = typename AccT<T>::t;
     const int nf = p.advect ? p.n_faces : 1;
     const int xsn = (XS == BZ_XS_TABLE) ? p.xs_n : 0;
     const size_t smem = size_t(xsn) * sizeof(float4) + (DEPOSIT ? size_t(3) * p.n_nodes * sizeof(A) : 0) +
                         size_t(nf) * sizeof(T);
-    auto kern = k_seg_push<T, REPLAY, XS, DEPOSIT, SG_T, SG_I, MINB, PF, ADV>;
+    auto kern = k_seg_push<T, REPLAY, XS, DEPOSIT, SG_T, SG_I, MINB, PF, ADV, GRED>;
     if (smem > 48 * 1024 &&
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess)
         return BZ_ERR_UNSUPPORTED;
@@ -753,12 +785,19 @@ static int launch_seg_push(const bz_params &p, Seg<T> in, Seg<T> out, const T *E
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, SG_T, smem) != cudaSuccess || per_sm < 1)
         return BZ_ERR_UNSUPPORTED;
-    if (cudaMemsetAsync(ws, 0, 256, st) != cudaSuccess) return BZ_ERR_CUDA;
     int grid = num_sms() * per_sm;
     grid = std::max(1, std::min(grid, int(ceil_div(in.nseg, SG_T / 32))));
+    // GRED: the per-CTA grids follow the ticket in the workspace; without the room for them the
+    // caller takes a kernel with the deposit in shared memory instead
+    float2 *gdep = nullptr;
+    if (GRED) {
+        if (ws_bytes < SEG_PUSH_TICKET_BYTES + size_t(grid) * size_t(p.n_nodes) * sizeof(float2)) return BZ_ERR_WORKSPACE;
+        gdep = reinterpret_cast<float2 *>(static_cast<unsigned char *>(ws) + SEG_PUSH_TICKET_BYTES);
+    }
+    if (cudaMemsetAsync(ws, 0, SEG_PUSH_TICKET_BYTES, st) != cudaSuccess) return BZ_ERR_CUDA;
     kern<<<grid, SG_T, smem, st>>>(p, make_push_const<T>(p), in, out, E, R, gas, moments,
                                    reinterpret_cast<unsigned long long *>(n_pushed), static_cast<unsigned int *>(ws),
-                                   seg_flags, status);
+                                   seg_flags, status, gdep);
     return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
 }
 
@@ -770,7 +809,7 @@ static int seg_push_entry(const bz_params *pp, S in_, S out_, const T *E, const 
     if (!pp || !E || !ws || !status || !seg_flags || !seg_ok<T>(in_) || !seg_ok<T>(out_)) return BZ_ERR_ARG;
     if (in_.nseg != out_.nseg || in_.half != out_.half) return BZ_ERR_ARG;
     if (int64_t(in_.nseg) * 2 * in_.half > int64_t(UINT32_MAX)) return BZ_ERR_TOO_LARGE;  // 32-bit slot indices
-    if (ws_bytes < 256) return BZ_ERR_WORKSPACE;
+    if (ws_bytes < SEG_PUSH_TICKET_BYTES) return BZ_ERR_WORKSPACE;
     if ((R == nullptr) != (gas == nullptr)) return BZ_ERR_ARG;
     const bz_params &p = *pp;
     if (p.advect < BZ_ADVECT_NONE || p.advect > BZ_ADVECT_ENSEMBLE) return BZ_ERR_ARG;
@@ -797,14 +836,18 @@ static int seg_push_entry(const bz_params *pp, S in_, S out_, const T *E, const 
             const int adv = p.coll_model != BZ_COLL_DIRECT ? -1 : p.advect;
 #define BZ_SEG_SHAPE(K)                                                                                            \
     case K:                                                                                                        \
-        if (adv == BZ_ADVECT_1D)                                                                                   \
-            return launch_seg_push<T, false, BZ_XS_TABLE, true, kSegShapes[K].threads, kSegShapes[K].per_lane,       \
-                                   kSegShapes[K].min_blocks, kSegShapes[K].prefetch, BZ_ADVECT_1D>(                  \
-                p, in, out, E, R, gas, moments, n_pushed, ws, seg_flags, status, st);                              \
+        if (adv == BZ_ADVECT_1D) {                                                                                 \
+            const int rc = launch_seg_push<T, false, BZ_XS_TABLE, true, kSegShapes[K].threads,                     \
+                                           kSegShapes[K].per_lane, kSegShapes[K].min_blocks, kSegShapes[K].prefetch, \
+                                           BZ_ADVECT_1D, true>(p, in, out, E, R, gas, moments, n_pushed, ws,          \
+                                                               ws_bytes, seg_flags, status, st);                    \
+            if (rc != BZ_ERR_WORKSPACE) return rc;                                                                 \
+            break; /* no room for the per-CTA grids: the general kernel below */                                    \
+        }                                                                                                          \
         if (adv == BZ_ADVECT_ENSEMBLE)                                                                             \
             return launch_seg_push<T, false, BZ_XS_TABLE, true, kSegShapes[K].threads, kSegShapes[K].per_lane,       \
                                    kSegShapes[K].min_blocks, kSegShapes[K].prefetch, BZ_ADVECT_ENSEMBLE>(            \
-                p, in, out, E, R, gas, moments, n_pushed, ws, seg_flags, status, st);                              \
+                p, in, out, E, R, gas, moments, n_pushed, ws, ws_bytes, seg_flags, status, st);                    \
         break;
             switch (g_seg_shape) {
                 BZ_SEG_SHAPE(0)
@@ -825,7 +868,8 @@ static int seg_push_entry(const bz_params *pp, S in_, S out_, const T *E, const 
     static_assert(kSegNumShapes == 10, "one case per CTA shape");
 #define BZ_SEG_CASE(RP, XSM, DP)                                                                                    \
     if (replay == RP && p.xs_mode == XSM && dep == DP)                                                             \
-        return launch_seg_push<T, RP, XSM, DP>(p, in, out, E, R, gas, moments, n_pushed, ws, seg_flags, status, st);
+        return launch_seg_push<T, RP, XSM, DP>(p, in, out, E, R, gas, moments, n_pushed, ws, ws_bytes, seg_flags,     \
+                                               status, st);
     BZ_SEG_CASE(false, BZ_XS_TABLE, true)
     BZ_SEG_CASE(false, BZ_XS_TABLE, false)
     BZ_SEG_CASE(false, BZ_XS_REF_FITS, true)
@@ -1045,7 +1089,11 @@ static int seg_deposit_entry(const bz_params *pp, S s_, double *moments, void *s
 
 extern "C" {
 
-size_t bz_seg_push_workspace(void) { return 256; }
+size_t bz_seg_push_workspace(void) { return bz::SEG_PUSH_TICKET_BYTES; }
+size_t bz_seg_push_workspace_nodes(int32_t n_nodes) {
+    // the ticket, then one float2 per node for every CTA the push can launch (at most 8 per SM)
+    return bz::SEG_PUSH_TICKET_BYTES + size_t(bz::num_sms()) * 8 * size_t(std::max(n_nodes, 0)) * sizeof(float2);
+}
 int32_t bz_seg_push_shapes(void) { return bz::kSegNumShapes; }
 int bz_seg_push_shape_info(int32_t shape, int32_t *threads, int32_t *per_lane, int32_t *min_blocks,
                            int32_t *prefetch) {

@@ -239,7 +239,7 @@ def seg_electron_kernel(params, src: SegmentSet, dst: SegmentSet, E, status, seg
         raise TypeError("precision mismatch")
     if n_pushed is not None and n_pushed.dtype != torch.int64:
         raise TypeError("n_pushed must be int64")
-    w = ws.get("seg_push", _lib.load().bz_seg_push_workspace())
+    w = ws.get("seg_push", _lib.load().bz_seg_push_workspace_nodes(params.n_nodes))
     call(f"bz_seg_push_collide_{src.suffix}", ctypes.byref(params), src.struct(), dst.struct(), _ptr(E),
          _ptr(replay_R), _ptr(replay_gas), _ptr(moments), _ptr(n_pushed), _ptr(w), w.numel(), _ptr(seg_flags),
          _ptr(status), _stream())

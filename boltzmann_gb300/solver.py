@@ -351,7 +351,7 @@ class BoltzmannGB300:
         """Allocate every workspace the step uses without running the step."""
         lib = _lib.load()
         nkeys = self.nnodes * self.nb
-        self.ws.get("seg_push", lib.bz_seg_push_workspace())
+        self.ws.get("seg_push", lib.bz_seg_push_workspace_nodes(self.nnodes))
         self.ws.get("seg_rebalance", lib.bz_seg_repack_workspace(self.A.nseg))
         self.ws.get("field_coop", lib.bz_field_step_coop_workspace(self.N))
         if resample:

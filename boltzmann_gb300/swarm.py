@@ -253,7 +253,7 @@ class SwarmEnsemble:
 
     def _capture(self, resample):
         lib = _lib.load()
-        self.ws.get("seg_push", lib.bz_seg_push_workspace())
+        self.ws.get("seg_push", lib.bz_seg_push_workspace_nodes(self.S))
         self.ws.get("seg_rebalance", lib.bz_seg_repack_workspace(self.A.nseg))
         self.ws.get("seg_bin", lib.bz_seg_bin_workspace(self.A.nseg, self.A.capacity))
         self.ws.get("seg_resample", lib.bz_seg_resample_workspace(self.A.nseg, self.A.capacity, self.S * self.nb))

@@ -271,6 +271,13 @@ typedef struct bz_segments_f64 { double *x, *vx, *vy, *vz, *w; int32_t *counts; 
  * accumulates the number of input particles pushed (w > 0). Slots are
  * indexed with 32 bits: nseg * 2 * half above 2^32 - 1 returns BZ_ERR_TOO_LARGE. */
 size_t bz_seg_push_workspace(void);
+/* A workspace of this many bytes (or more) also holds, for the float32 push with an n*sigma
+ * table, the direct collision model, 1D drift and a deposit (the tuned kernels), one float2
+ * (sum w, sum w*energy) per node for every CTA: the deposit then accumulates there by vector
+ * reductions in L2 instead of by shared-memory atomics (float32 per-CTA sums as before,
+ * merged into the float64 moments at the CTA's end). Any workspace of at least
+ * bz_seg_push_workspace() bytes works; the larger one is faster. */
+size_t bz_seg_push_workspace_nodes(int32_t n_nodes);
 int bz_seg_push_collide_f32(const bz_params *p, bz_segments_f32 in, bz_segments_f32 out, const float *E,
                             const double *replay_R, const double *replay_gas, double *moments,
                             uint64_t *n_pushed, void *workspace, size_t workspace_bytes, uint32_t *seg_flags,

@@ -5,6 +5,7 @@ is checked against the golden vectors like the dense push; many segments are che
 against the oracle run on the slot-indexed array (Philox counters are slot indices);
 repack, binning, resampling and deposit are checked against their dense counterparts.
 """
+import ctypes
 import os
 
 import numpy as np
@@ -248,6 +249,48 @@ def test_seg_deposit_matches_dense():
     K.deposit(p, dense, m2)
     torch.cuda.synchronize()
     np.testing.assert_allclose(m1.cpu().numpy(), m2.cpu().numpy(), rtol=1e-5, atol=1e-9)
+
+
+def test_deposit_grid_in_the_workspace_matches_shared_memory():
+    """With a workspace of bz_seg_push_workspace_nodes bytes the float32 1D deposit sums into
+    per-CTA grids in global memory; with the minimal workspace, into shared memory. The
+    particles are identical, the moments equal up to the float32 summation order."""
+    rng = np.random.default_rng(23)
+    n, N, L, nseg, half = 150_000, 256, 2.54, 96, 2048
+    x = rng.uniform(1e-4, L - 1e-4, n)
+    v = rng.normal(0, 1.4e6, (n, 3))
+    w = rng.uniform(1e4, 1e5, n)
+    E = torch.as_tensor(rng.uniform(-1200, 1200, N), dtype=torch.float32, device="cuda")
+    seg = K.SegmentSet(nseg, half, torch.float32)
+    seg.load(x, v[:, 0], v[:, 1], v[:, 2], w)
+    tab = xsec.analytic_argon(2000)
+    nn = 3.22e22
+    xt = torch.as_tensor(tab.nsigma(nn), device="cuda")
+    p = K.make_params(n_faces=N, n_nodes=N + 1, bnf=4, advect=1, L=L, dx=L / N, dt=1.0 / 13.56e6 / 400, nn=nn,
+                      gas_sigma=6.74e4, e_exc=tab.e_exc, xs_mode=_lib.XS_TABLE, xs_table=xt, xs_emin=tab.emin,
+                      xs_emax=tab.emax, flags=_lib.QUIRK_DEAD_IONFLAG, seed=4, step=3)
+    lib = _lib.load()
+    small, big = lib.bz_seg_push_workspace(), lib.bz_seg_push_workspace_nodes(N + 1)
+    assert small == 256 and big > small + 152 * (N + 1) * 8
+    res = []
+    for nbytes in (small, big):
+        out = K.SegmentSet(nseg, half, torch.float32)
+        mom = torch.zeros(4, N + 1, dtype=torch.float64, device="cuda")
+        st = torch.zeros(1, dtype=torch.int32, device="cuda")
+        fl = torch.zeros(1, dtype=torch.int32, device="cuda")
+        ws = torch.zeros(nbytes, dtype=torch.uint8, device="cuda")
+        K.call("bz_seg_push_collide_f32", ctypes.byref(p), seg.struct(), out.struct(), K._ptr(E), None, None,
+               K._ptr(mom), None, K._ptr(ws), nbytes, K._ptr(fl), K._ptr(st), K._stream())
+        torch.cuda.synchronize()
+        assert int(st.item()) == 0
+        res.append((out.to_numpy("segments"), out.counts.cpu().numpy(), mom.cpu().numpy()))
+    (o1, c1, m1), (o2, c2, m2) = res
+    np.testing.assert_array_equal(c1, c2)
+    for f in K.SegmentSet.FIELDS:
+        np.testing.assert_array_equal(o1[f], o2[f])
+    assert m1[0].sum() > 0
+    for j in (0, 1, 3):
+        np.testing.assert_allclose(m2[j], m1[j], rtol=1e-5, atol=1e-6 * np.abs(m1[j]).max())
 
 
 def test_every_cta_shape_gives_the_same_particles():
