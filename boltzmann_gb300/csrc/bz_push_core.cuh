@@ -261,52 +261,56 @@ __device__ __forceinline__ void push_item(const bz_params &p, const PushConst<T>
     o.child = false;
     o.ionized = false;
     o.excited = (proc == P_EXCITE);
-    T nvx = vx, nvy = vy, nvz = vz;
-    if (proc != P_NONE) {
-        // speed after the collision; one isotropic redirection for every process (warps
-        // whose lanes collide differently run it once)
-        T vn;
-        if (proc == P_ELASTIC) {
-            // |v| (1 - 2 m_e/m_n)^1/2 (electron_kernel_numba.py:197-209)
-            vn = vmag * k.f_el;
-        } else {
-            // energy left after the threshold: in the working precision when e - threshold
-            // keeps at least a quarter of e, else without the subtraction's cancellation
-            // (float32: two-float arithmetic; float64: the float64 expression);
-            // excitation loses e_exc (the reference has no excitation: sigma_g1 = 0),
-            // ionization shares e - 15.76 equally (electron_kernel_numba.py:211-255)
-            // (the float thresholds are the float64 ones rounded on the host, so no float64
-            // conversion runs here)
-            const bool ex = proc == P_EXCITE;
-            T thr;
-            if constexpr (sizeof(T) == 4) thr = ex ? k.exc_h : k.ion_h;
-            else thr = ex ? p.e_exc : E_ION;
-            if (sizeof(T) == 8 || e - thr >= T(0.25) * e) {
-                T en = ex ? (e - thr) : T(0.5) * (e - thr);
-                vn = sqrt_pos(en * k.e2v);
-            } else if constexpr (sizeof(T) == 4) {
-                float d = fabsf(excess_energy_f(ax, ay, az, k.efac_h, k.efac_l, ex ? k.exc_h : k.ion_h,
-                                                ex ? k.exc_l : k.ion_l));
-                if (!ex) d = 0.5f * d;
-                vn = sqrt_pos(d * k.e2v);
-            }
+    // speed after a collision: elastic |v| (1 - 2 m_e/m_n)^1/2 (electron_kernel_numba.py:197-209)
+    T vn = vmag * k.f_el;
+    if (proc >= P_EXCITE) {
+        // energy left after the threshold: in the working precision when e - threshold
+        // keeps at least a quarter of e, else without the subtraction's cancellation
+        // (float32: two-float arithmetic; float64: the float64 expression);
+        // excitation loses e_exc (the reference has no excitation: sigma_g1 = 0),
+        // ionization shares e - 15.76 equally (electron_kernel_numba.py:211-255)
+        // (the float thresholds are the float64 ones rounded on the host, so no float64
+        // conversion runs here)
+        const bool ex = proc == P_EXCITE;
+        T thr;
+        if constexpr (sizeof(T) == 4) thr = ex ? k.exc_h : k.ion_h;
+        else thr = ex ? p.e_exc : E_ION;
+        if (sizeof(T) == 8 || e - thr >= T(0.25) * e) {
+            T en = ex ? (e - thr) : T(0.5) * (e - thr);
+            vn = sqrt_pos(en * k.e2v);
+        } else if constexpr (sizeof(T) == 4) {
+            float d = fabsf(excess_energy_f(ax, ay, az, k.efac_h, k.efac_l, ex ? k.exc_h : k.ion_h,
+                                            ex ? k.exc_l : k.ion_l));
+            if (!ex) d = 0.5f * d;
+            vn = sqrt_pos(d * k.e2v);
         }
-        iso_dir(u1, u2, vn, nvx, nvy, nvz);
-        if (proc == P_IONIZE) {
-            // the new electron: same position and weight, its own isotropic direction
-            if (REPLAY) {
-                u5 = uni_from_replay<T>(R[size_t(slot) * 7 + 5]);
-            } else if constexpr (sizeof(T) == 8) {
-                Draw4<T> d;
-                draw4(rng, k.rk0, k.rk1, slot, 2u, d);
-                u5 = d.v[0];
-            }
-            iso_dir(u3, u5, vn, o.cvx, o.cvy, o.cvz);
-            o.cx = x;
-            o.child = true;
-            o.ionized = true;
-            o.ce = k.efac * (o.cvx * o.cvx + o.cvy * o.cvy + o.cvz * o.cvz);
+    }
+    // one isotropic redirection for every process, computed in every lane and kept where the
+    // particle collided: with a collision probability of 0.2-0.3 per step nearly every warp
+    // has a colliding lane, so a branch around it would save nothing
+    T nvx, nvy, nvz;
+    {
+        T ix, iy, iz;
+        iso_dir(u1, u2, vn, ix, iy, iz);
+        const bool coll = proc != P_NONE;
+        nvx = coll ? ix : vx;
+        nvy = coll ? iy : vy;
+        nvz = coll ? iz : vz;
+    }
+    if (proc == P_IONIZE) {
+        // the new electron: same position and weight, its own isotropic direction
+        if (REPLAY) {
+            u5 = uni_from_replay<T>(R[size_t(slot) * 7 + 5]);
+        } else if constexpr (sizeof(T) == 8) {
+            Draw4<T> d;
+            draw4(rng, k.rk0, k.rk1, slot, 2u, d);
+            u5 = d.v[0];
         }
+        iso_dir(u3, u5, vn, o.cvx, o.cvy, o.cvz);
+        o.cx = x;
+        o.child = true;
+        o.ionized = true;
+        o.ce = k.efac * (o.cvx * o.cvx + o.cvy * o.cvy + o.cvz * o.cvz);
     }
     // drift with the post-collision velocity, kick with E at the pre-push face,
     // absorbing walls (electron_kernel_numba.py:257-276)
