@@ -242,14 +242,20 @@ __global__ void __launch_bounds__(32 * MF_WARPS, 1)
 // a timeout the kernel raises a status bit and stops.
 // ------------------------------------------------------------------------------------
 constexpr int TC_ROWS = 128;
-constexpr int TC_THREADS = 256;  // warps w and w+4 share TMEM lanes 32*(w%4).. and split the columns
+constexpr int TC_THREADS = 256;  // backward: warps w and w+4 share TMEM lanes 32*(w%4).. and split the columns
+// forward: 16 warps, four per TMEM lane quarter (warps w, w+4, w+8, w+12 read lanes 32*(w%4)..
+// and take a quarter of the 16-column chunks each): the epilogue, not the tensor core, sets
+// the forward's time, so it gets four warps per row block
+constexpr int TCF_THREADS = 512;
+constexpr int TCF_GROUPS = TCF_THREADS / TC_ROWS;
 constexpr uint32_t TC_WAIT_LIMIT = 1u << 24;
 __host__ __device__ constexpr int wc_off(int l) { return l == 0 ? 0 : wc_off(l - 1) + mlp_out(l - 1) * mlp_in(l - 1) * 2; }
 constexpr int WC_BYTES = wc_off(MLP_NL);
 constexpr int TC_ACT_BYTES = TC_ROWS * MLP_H * 2;
 constexpr size_t TC_SMEM = 1024 + size_t(WC_BYTES) + TC_ACT_BYTES + BS_TOTAL * 4 + 64;
 static_assert(TC_SMEM <= 227 * 1024, "shared memory");
-static_assert(TC_THREADS == 2 * TC_ROWS && MLP_IN == 16, "two threads per row: the 16 inputs as two 16-byte chunks");
+static_assert(TC_THREADS == 2 * TC_ROWS && TCF_THREADS >= 2 * TC_ROWS && MLP_IN == 16,
+              "two threads per row: the 16 inputs as two 16-byte chunks");
 
 __device__ uint32_t g_mlp_status = 0;
 
@@ -333,43 +339,40 @@ __device__ __forceinline__ bool tc_layer(unsigned char *wc, unsigned char *act, 
     phase ^= 1u;
     if (!ok) return false;
     tc_fence_after();
-    // epilogue: this thread owns row 32*(warp%4) + lane (its TMEM lane) and half of the
-    // 16-column chunks (warps 0-3 the first, 4-7 the second)
-    constexpr int NCH = N / 16, HALF = (NCH + 1) / 2;
-    const int lo = (warp >> 2) ? HALF : 0, hi = (warp >> 2) ? NCH : HALF;
+    // epilogue: this thread owns row 32*(warp%4) + lane (its TMEM lane) and a quarter of the
+    // 16-column chunks (warps 0-3 the first, 4-7 the second, ...)
+    constexpr int NCH = N / 16, HALF = (NCH + TCF_GROUPS - 1) / TCF_GROUPS;  // chunks per warp group
+    const int lo = min(NCH, (warp >> 2) * HALF), hi = min(NCH, lo + HALF);
     const int rl = 32 * (warp & 3) + (tid & 31);
     const uint32_t tl = tmem + (uint32_t(32 * (warp & 3)) << 16);
-    float v[HALF * 16];
-#pragma unroll
-    for (int j = 0; j < HALF; ++j)
-        if (lo + j < hi) tmem_ld16(tl + uint32_t((lo + j) * 16), v + 16 * j);
-    tmem_wait_ld();
     const int r = row0 + rl;
     const float *b = bs + bs_off(L);
+    // one 16-column chunk at a time: 16 accumulators live
 #pragma unroll
     for (int j = 0; j < HALF; ++j) {
         if (lo + j >= hi) break;
         const int c0 = (lo + j) * 16;
+        float v[16];
+        tmem_ld16(tl + uint32_t(c0), v);
+        tmem_wait_ld();
 #pragma unroll
-        for (int c = 0; c < 16; ++c) v[16 * j + c] += b[c0 + c];
+        for (int c = 0; c < 16; ++c) v[c] += b[c0 + c];
         if (L == MLP_NL - 1) {
             if (r < n) {
                 float4 *yr = reinterpret_cast<float4 *>(y + size_t(r) * MLP_OUT + c0);
 #pragma unroll
-                for (int c = 0; c < 16; c += 4)
-                    yr[c / 4] = make_float4(v[16 * j + c], v[16 * j + c + 1], v[16 * j + c + 2], v[16 * j + c + 3]);
+                for (int c = 0; c < 16; c += 4) yr[c / 4] = make_float4(v[c], v[c + 1], v[c + 2], v[c + 3]);
             }
         } else {
             if (SAVE && r < n) {
                 float4 *zr = reinterpret_cast<float4 *>(z + (size_t(L) * n + r) * MLP_H + c0);
 #pragma unroll
-                for (int c = 0; c < 16; c += 4)
-                    zr[c / 4] = make_float4(v[16 * j + c], v[16 * j + c + 1], v[16 * j + c + 2], v[16 * j + c + 3]);
+                for (int c = 0; c < 16; c += 4) zr[c / 4] = make_float4(v[c], v[c + 1], v[c + 2], v[c + 3]);
             }
             // the next layer's A operand (K = 128): two 16-byte chunks of 8 activations
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                const float *a = v + 16 * j + 8 * h;
+                const float *a = v + 8 * h;
                 uint4 q;
                 q.x = pack_bf16(gelu(a[0]), gelu(a[1]));
                 q.y = pack_bf16(gelu(a[2]), gelu(a[3]));
@@ -383,7 +386,7 @@ __device__ __forceinline__ bool tc_layer(unsigned char *wc, unsigned char *act, 
 }
 
 template <bool SAVE>
-__global__ void __launch_bounds__(TC_THREADS, 1)
+__global__ void __launch_bounds__(TCF_THREADS, 1)
     k_mlp_fwd_tc(const uint16_t *wb, const float *prm, const float *x, const int32_t *idx, int n, float *y, float *z,
                  uint32_t wl) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -399,11 +402,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
     for (int l = 0; l < MLP_NL; ++l) {
         const int K = mlp_in(l), N = mlp_out(l), chunks = K / 8;
-        for (int e = tid; e < N * chunks; e += TC_THREADS) {
+        for (int e = tid; e < N * chunks; e += TCF_THREADS) {
             const int r = e / chunks, c8 = e - r * chunks;
             cp_async16(wc + wc_off(l) + canon_off(r, c8, K), wb + mlp_woff(l) + size_t(r) * K + c8 * 8);
         }
-        for (int i = tid; i < N; i += TC_THREADS) bs[bs_off(l) + i] = prm[mlp_boff(l) + i];
+        for (int i = tid; i < N; i += TCF_THREADS) bs[bs_off(l) + i] = prm[mlp_boff(l) + i];
     }
     const uint32_t mbar = smem_u32(mbar_p);
     if (tid == 0) {
@@ -425,8 +428,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int tiles = int(ceil_div(n, TC_ROWS));
     for (int tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
         const int row0 = tile * TC_ROWS;
-        // the tile's inputs (K = 16): one 16-byte chunk (8 features) per thread
-        {
+        // the tile's inputs (K = 16): one 16-byte chunk (8 features) per thread of the first 256
+        if (tid < 2 * TC_ROWS) {
             const int rl = tid & (TC_ROWS - 1), c8 = tid / TC_ROWS;
             const int r = row0 + rl;
             float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0;
@@ -997,7 +1000,7 @@ static int mlp_forward(const uint16_t *wb, const float *prm, const float *x, con
             if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TC_SMEM)) != cudaSuccess)
                 return BZ_ERR_UNSUPPORTED;
             const int tiles = int(ceil_div(n, TC_ROWS));
-            kern<<<std::min(tiles, num_sms_mlp()), TC_THREADS, TC_SMEM, st>>>(wb, prm, x, idx, n, y, z,
+            kern<<<std::min(tiles, num_sms_mlp()), TCF_THREADS, TC_SMEM, st>>>(wb, prm, x, idx, n, y, z,
                                                                        host_wait_limit(TC_WAIT_LIMIT));
             return cudaGetLastError() == cudaSuccess ? int(BZ_OK) : int(BZ_ERR_CUDA);
         };
