@@ -272,9 +272,10 @@ def workload_config(args):
 # our arm
 # --------------------------------------------------------------------------------------
 def dense_push_leg(sol, prm, reps, peak):
-    """The drop-in dense push (bz_push_collide_f32: the reference's global order, decoupled
-    look-back between tiles) on the solver's current particles, gathered into one dense
-    list on the device: launch time and algorithmic bandwidth (40 B per particle)."""
+    """The drop-in dense push (bz_push_collide_f32: the reference's global order) on the
+    solver's current particles, gathered into one dense list on the device: launch time and
+    algorithmic bandwidth (40 B per particle), with the fast workspace and with the minimal
+    one."""
     import torch
     from boltzmann_gb300 import kernels as K
     A = sol.A
@@ -299,22 +300,32 @@ def dense_push_leg(sol, prm, reps, peak):
     ws = K.Workspace(dev)
     stream = torch.cuda.current_stream()
 
-    def once():
-        K.electron_kernel(prm, src, dst, sol.E_push, st, ws, moments=mom)
+    def timed(fast):
+        def once():
+            K.electron_kernel(prm, src, dst, sol.E_push, st, ws, moments=mom, fast=fast)
 
-    for _ in range(3):
-        once()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(reps):
-        once()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / reps
+        for _ in range(3):
+            once()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            once()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    # with the minimal workspace: the single-pass push with the decoupled look-back; with
+    # bz_push_workspace_fast_f32 bytes: the segmented kernel and a gather into the order
+    ms_lb = timed(False)
+    ms = timed(True)
     gbs = BYTES_PER_PARTICLE * n / (ms * 1e-3) / 1e9
-    return {"kernel": "k_push + k_append_children (bz_push_collide_f32: dense reference order, decoupled "
-                      "look-back)", "launch_ms": ms, "particles": n, "achieved_gbs": gbs, "frac": gbs / peak,
+    gbs_lb = BYTES_PER_PARTICLE * n / (ms_lb * 1e-3) / 1e9
+    return {"kernel": "k_seg_push over the array read as segments + k_dense_gather (bz_push_collide_f32 with "
+                      "the fast workspace: dense reference order)", "launch_ms": ms, "particles": n,
+            "achieved_gbs": gbs, "frac": gbs / peak,
+            "lookback": {"kernel": "k_push + k_append_children (minimal workspace: decoupled look-back)",
+                         "launch_ms": ms_lb, "achieved_gbs": gbs_lb, "frac": gbs_lb / peak},
             "device_status": int(st.item())}
 
 

@@ -75,6 +75,8 @@ _P = ctypes.POINTER(BzParams)
 _PROTOS = {
     "bz_version": (ctypes.c_char_p, []),
     "bz_push_workspace": (_sz, [_i64]),
+    "bz_push_workspace_fast_f32": (_sz, [_i64, _i32]),
+    "bz_push_workspace_fast_f64": (_sz, [_i64, _i32]),
     "bz_push_collide_f32": (ctypes.c_int, [_P, Particles, _vp, _i64, Particles, _i64, _vp, _vp, _vp, _vp, _vp, _vp,
                                            _sz, _vp, _vp]),
     "bz_push_collide_f64": (ctypes.c_int, [_P, Particles, _vp, _i64, Particles, _i64, _vp, _vp, _vp, _vp, _vp, _vp,

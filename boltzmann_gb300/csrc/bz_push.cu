@@ -298,6 +298,13 @@ static int push_entry(const bz_params *pp, P in_, const int32_t *n_in, int64_t i
     if (dep && (p.flags & BZ_CLEAR_MOMENTS) &&
         cudaMemsetAsync(moments, 0, sizeof(double) * 4 * size_t(p.n_nodes), st) != cudaSuccess)
         return BZ_ERR_CUDA;
+    // with a workspace of bz_push_workspace_fast_* bytes: the segmented kernel and a gather
+    // into the reference order (no tile waits for its predecessors)
+    {
+        const int rc = dense_push_segmented<T>(p, in, n_in, in_cap, out, cap, counts, E, R, gas, moments, ws, ws_bytes,
+                                               status, st);
+        if (rc != BZ_ERR_WORKSPACE) return rc;
+    }
 #define BZ_PUSH_CASE(RP, XSM, DP)                                                                                   \
     if (replay == RP && p.xs_mode == XSM && dep == DP)                                                             \
         return launch_push_t<T, RP, XSM, DP>(p, in, n_in, in_cap, out, cap, counts, E, R, gas, moments, ws, ws_bytes,      \

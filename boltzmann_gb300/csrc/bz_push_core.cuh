@@ -384,5 +384,11 @@ template <typename T> inline PushConst<T> make_push_const(const bz_params &p) {
     return k;
 }
 
+// The dense push through the segmented kernel (bz_segments.cu): BZ_ERR_WORKSPACE when the
+// workspace is smaller than bz_push_workspace_fast_*, and the caller pushes with k_push.
+template <typename T>
+int dense_push_segmented(const bz_params &p, SoA<T> in, const int32_t *n_in, int64_t in_cap, SoA<T> out, int64_t cap,
+                         int32_t *counts, const T *E, const double *R, const double *gas, double *moments, void *ws,
+                         size_t ws_bytes, uint32_t *status, cudaStream_t st);
 
 }  // namespace bz

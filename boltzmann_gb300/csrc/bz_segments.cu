@@ -81,7 +81,7 @@ template <typename T, bool REPLAY, int XS, bool DEPOSIT, int SG_T, int SG_I, int
 __global__ void __launch_bounds__(SG_T, MINB)
     k_seg_push(bz_params p, PushConst<T> kc, Seg<T> in, Seg<T> out, const T *E, const double *R, const double *gas,
                double *moments, unsigned long long *n_pushed, unsigned int *ticket, uint32_t *seg_flags,
-               uint32_t *status, float2 *gdep) {
+               uint32_t *status, float2 *gdep, uint32_t in_stride) {
     using A = typename AccT<T>::t;
     const int advect = ADV >= 0 ? ADV : p.advect;
     constexpr int SG_R = 32 * SG_I;  // particles per warp round
@@ -127,7 +127,9 @@ __global__ void __launch_bounds__(SG_T, MINB)
                 err |= BZ_DEV_CAPACITY;
                 cnt = cnt < 0 ? 0 : H;
             }
-            const uint32_t rbase = seg_slot32(seg, run, H, 0);
+            // input slot (and Philox counter) of the run's first particle: segments in_stride
+            // slots apart (2 half; half for a dense array read as segments with run 1 empty)
+            const uint32_t rbase = uint32_t(seg) * in_stride + uint32_t(run) * uint32_t(H);
             // one particle of the run (zeros past its end)
             auto fetch = [&](int j, T &a, T &b, T &c, T &d, T &e) {
                 const bool ok = j < cnt;
@@ -771,7 +773,7 @@ template <typename T, bool REPLAY, int XS, bool DEPOSIT, int SG_T = kSegShapes[0
           int ADV = -1, bool GRED = false>
 static int launch_seg_push(const bz_params &p, Seg<T> in, Seg<T> out, const T *E, const double *R, const double *gas,
                            double *moments, uint64_t *n_pushed, void *ws, size_t ws_bytes, uint32_t *seg_flags,
-                           uint32_t *status, cudaStream_t st) {
+                           uint32_t *status, cudaStream_t st, uint32_t in_stride) {
     using A = typename AccT<T>::t;
     const int nf = p.advect ? p.n_faces : 1;
     const int xsn = (XS == BZ_XS_TABLE) ? p.xs_n : 0;
@@ -797,9 +799,14 @@ static int launch_seg_push(const bz_params &p, Seg<T> in, Seg<T> out, const T *E
     if (cudaMemsetAsync(ws, 0, SEG_PUSH_TICKET_BYTES, st) != cudaSuccess) return BZ_ERR_CUDA;
     kern<<<grid, SG_T, smem, st>>>(p, make_push_const<T>(p), in, out, E, R, gas, moments,
                                    reinterpret_cast<unsigned long long *>(n_pushed), static_cast<unsigned int *>(ws),
-                                   seg_flags, status, gdep);
+                                   seg_flags, status, gdep, in_stride);
     return cudaGetLastError() == cudaSuccess ? BZ_OK : BZ_ERR_CUDA;
 }
+
+template <typename T>
+static int seg_push_run(const bz_params &p, Seg<T> in, uint32_t in_stride, Seg<T> out, const T *E, const double *R,
+                        const double *gas, double *moments, uint64_t *n_pushed, void *ws, size_t ws_bytes,
+                        uint32_t *seg_flags, uint32_t *status, cudaStream_t st);
 
 template <typename T, typename S>
 static int seg_push_entry(const bz_params *pp, S in_, S out_, const T *E, const double *R, const double *gas,
@@ -822,8 +829,15 @@ static int seg_push_entry(const bz_params *pp, S in_, S out_, const T *E, const 
     if (p.coll_model == BZ_COLL_NULL && !(p.nu_max > 0)) return BZ_ERR_ARG;
     auto al = [](const void *q) { return (reinterpret_cast<uintptr_t>(q) & 15u) == 0; };
     if (sizeof(T) == 4 && !(al(in_.x) && al(in_.vx) && al(in_.vy) && al(in_.vz) && al(in_.w))) return BZ_ERR_ARG;
-    Seg<T> in = to_seg<T>(in_), out = to_seg<T>(out_);
-    cudaStream_t st = as_stream(stream);
+    return seg_push_run<T>(p, to_seg<T>(in_), 2u * uint32_t(in_.half), to_seg<T>(out_), E, R, gas, moments, n_pushed,
+                           ws, ws_bytes, seg_flags, status, as_stream(stream));
+}
+
+// the push of validated segments (in_stride: slots between the input segments' starts)
+template <typename T>
+static int seg_push_run(const bz_params &p, Seg<T> in, uint32_t in_stride, Seg<T> out, const T *E, const double *R,
+                        const double *gas, double *moments, uint64_t *n_pushed, void *ws, size_t ws_bytes,
+                        uint32_t *seg_flags, uint32_t *status, cudaStream_t st) {
     const bool replay = R != nullptr, dep = moments != nullptr;
     if (dep && (p.flags & BZ_CLEAR_MOMENTS) &&
         cudaMemsetAsync(moments, 0, sizeof(double) * 4 * size_t(p.n_nodes), st) != cudaSuccess)
@@ -840,14 +854,14 @@ static int seg_push_entry(const bz_params *pp, S in_, S out_, const T *E, const 
             const int rc = launch_seg_push<T, false, BZ_XS_TABLE, true, kSegShapes[K].threads,                     \
                                            kSegShapes[K].per_lane, kSegShapes[K].min_blocks, kSegShapes[K].prefetch, \
                                            BZ_ADVECT_1D, true>(p, in, out, E, R, gas, moments, n_pushed, ws,          \
-                                                               ws_bytes, seg_flags, status, st);                    \
+                                                               ws_bytes, seg_flags, status, st, in_stride);         \
             if (rc != BZ_ERR_WORKSPACE) return rc;                                                                 \
             break; /* no room for the per-CTA grids: the general kernel below */                                    \
         }                                                                                                          \
         if (adv == BZ_ADVECT_ENSEMBLE)                                                                             \
             return launch_seg_push<T, false, BZ_XS_TABLE, true, kSegShapes[K].threads, kSegShapes[K].per_lane,       \
                                    kSegShapes[K].min_blocks, kSegShapes[K].prefetch, BZ_ADVECT_ENSEMBLE>(            \
-                p, in, out, E, R, gas, moments, n_pushed, ws, ws_bytes, seg_flags, status, st);                    \
+                p, in, out, E, R, gas, moments, n_pushed, ws, ws_bytes, seg_flags, status, st, in_stride);         \
         break;
             switch (g_seg_shape) {
                 BZ_SEG_SHAPE(0)
@@ -869,7 +883,7 @@ static int seg_push_entry(const bz_params *pp, S in_, S out_, const T *E, const 
 #define BZ_SEG_CASE(RP, XSM, DP)                                                                                    \
     if (replay == RP && p.xs_mode == XSM && dep == DP)                                                             \
         return launch_seg_push<T, RP, XSM, DP>(p, in, out, E, R, gas, moments, n_pushed, ws, ws_bytes, seg_flags,     \
-                                               status, st);
+                                               status, st, in_stride);
     BZ_SEG_CASE(false, BZ_XS_TABLE, true)
     BZ_SEG_CASE(false, BZ_XS_TABLE, false)
     BZ_SEG_CASE(false, BZ_XS_REF_FITS, true)
@@ -957,6 +971,191 @@ static int seg_place_entry(S s_, P app_, const int32_t *app_n, int64_t app_cap, 
     return seg_repack_entry<T>(&s_, app_, app_n, app_cap, scratch_, b + L.total, rws,
                                reinterpret_cast<const uint32_t *>(misc), seg_flags, status, stream, &s_);
 }
+
+// ------------------------------------------------------------------------------------
+// The dense push (bz_push_collide_*: survivors in input order, then children in parent
+// order, the order reshuffle_data_atomics leaves, post_processing_1D.py:26-38) through the
+// segmented kernel: the input array read as segments of DENSE_HALF particles (run 1 empty,
+// so a particle's Philox counter stays its index in the array), pushed into segments in
+// the workspace, then gathered into the reference's order. No tile waits for its
+// predecessors' counts (the look-back of k_push), at the price of one more pass over the
+// output (20 B read and 20 B written per particle).
+// ------------------------------------------------------------------------------------
+constexpr int DENSE_HALF = 2048;
+struct DenseWs {
+    int nseg;
+    size_t push, cin, cout, part, flags, cols, col_bytes, total;
+    DenseWs(int64_t in_cap, int n_nodes, size_t elem) {
+        auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+        nseg = int(std::max<int64_t>(1, ceil_div(std::max<int64_t>(in_cap, 1), DENSE_HALF)));
+        push = 0;
+        cin = push + al(bz_seg_push_workspace_nodes(n_nodes));
+        cout = cin + al(8 * size_t(nseg));
+        part = cout + al(8 * size_t(nseg));
+        flags = part + al(16 * size_t(PlaceWs::max_ctas(nseg)));  // two int64 partials per gather CTA
+        cols = flags + 256;
+        col_bytes = al(size_t(nseg) * 2 * DENSE_HALF * elem);
+        total = cols + 5 * col_bytes;
+    }
+};
+
+// input counts of the array read as segments: min(half, n - k half) in run 0, run 1 empty
+__global__ void k_dense_in_counts(const int32_t *n_in, int64_t in_cap, int nseg, int half, int32_t *cin,
+                                  uint32_t *status) {
+    int64_t n = *n_in;
+    if (n < 0 || n > in_cap) {  // as k_push: flag it and take what the array holds
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(status, BZ_DEV_CAPACITY);
+        n = n < 0 ? 0 : in_cap;
+    }
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nseg; k += gridDim.x * blockDim.x) {
+        cin[2 * k] = int32_t(min(int64_t(half), max(int64_t(0), n - int64_t(k) * half)));
+        cin[2 * k + 1] = 0;
+    }
+}
+
+// Segments -> the reference's order: survivors of segment 0, 1, ... then children of
+// segment 0, 1, ...; the counts [survivors, children, total] as k_push leaves them. Each CTA
+// owns a contiguous range of segments: its sums | every CTA's offsets from all partials,
+// then per chunk of RP_T segments a block scan and a warp per segment copying its runs
+// (cooperative launch).
+template <typename T>
+__global__ void __launch_bounds__(RP_T) k_dense_gather(Seg<T> s, SoA<T> out, int64_t cap, int32_t *counts,
+                                                       int64_t *part, uint32_t *status) {
+    cooperative_groups::grid_group grid = cooperative_groups::this_grid();
+    __shared__ int64_t sa[RP_T], sb[RP_T], o_s[RP_T], o_c[RP_T];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    constexpr int NW = RP_T / 32;
+    const int G = gridDim.x, b = blockIdx.x, m = s.nseg, H = s.half;
+    const int S = (m + G - 1) / G;
+    const int lo = min(m, b * S), hi = min(m, lo + S);
+    auto cnt_of = [&](int k, int run) { return min(max(s.cnt[2 * k + run], 0), H); };
+    {
+        int64_t ls = 0, lc = 0, ts, tc;
+        for (int k = lo + t; k < hi; k += RP_T) {
+            ls += cnt_of(k, 0);
+            lc += cnt_of(k, 1);
+        }
+        rp_scan2(ls, lc, ts, tc, sa, sb);
+        if (t == 0) {
+            part[2 * b] = ts;
+            part[2 * b + 1] = tc;
+        }
+    }
+    grid.sync();
+    int64_t TS = 0, TC = 0, ps = 0, pc = 0;
+    for (int i = t; i < G; i += RP_T) {
+        const int64_t a = part[2 * i], c = part[2 * i + 1];
+        TS += a;
+        TC += c;
+        if (i < b) {
+            ps += a;
+            pc += c;
+        }
+    }
+    {
+        int64_t x = TS, y = TC;
+        rp_scan2(x, y, TS, TC, sa, sb);
+        x = ps;
+        y = pc;
+        rp_scan2(x, y, ps, pc, sa, sb);
+    }
+    uint32_t err = 0;
+    for (int base = lo; base < hi; base += RP_T) {
+        const int k = base + t;
+        int64_t xs = k < hi ? cnt_of(k, 0) : 0, xc = k < hi ? cnt_of(k, 1) : 0, t1, t2;
+        rp_scan2(xs, xc, t1, t2, sa, sb);
+        o_s[t] = ps + xs;       // survivors from here
+        o_c[t] = TS + pc + xc;  // children after every survivor
+        __syncthreads();
+        const int nk = min(RP_T, hi - base);
+        for (int q = warp; q < nk; q += NW) {
+            const int kk = base + q;
+            for (int run = 0; run < 2; ++run) {
+                const int c = cnt_of(kk, run);
+                const int64_t d0 = run ? o_c[q] : o_s[q];
+                const uint32_t s0 = seg_slot32(kk, run, H, 0);
+                // four rounds of 32 at a time: their loads in flight before the stores
+                for (int j0 = 0; j0 < c; j0 += 4 * 32) {
+                    T xx[4], a1[4], a2[4], a3[4], wv[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int j = j0 + u * 32 + lane;
+                        if (j < c) {
+                            const uint32_t q0 = s0 + uint32_t(j);
+                            xx[u] = s.a.x[q0]; a1[u] = s.a.vx[q0]; a2[u] = s.a.vy[q0]; a3[u] = s.a.vz[q0];
+                            wv[u] = s.a.w[q0];
+                        }
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int j = j0 + u * 32 + lane;
+                        if (j < c) {
+                            const int64_t d = d0 + j;
+                            if (d < cap) {
+                                out.x[d] = xx[u]; out.vx[d] = a1[u]; out.vy[d] = a2[u]; out.vz[d] = a3[u];
+                                out.w[d] = wv[u];
+                            } else {
+                                err |= BZ_DEV_CAPACITY;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        ps += t1;
+        pc += t2;
+        __syncthreads();  // o_s and o_c are rewritten by the next chunk
+    }
+    if (err) atomicOr(status, err);
+    if (b == 0 && t == 0) {
+        const int64_t ns = min(TS, cap), nc = max(int64_t(0), min(TC, cap - ns));
+        counts[0] = int32_t(ns);
+        counts[1] = int32_t(nc);
+        counts[2] = int32_t(ns + nc);
+    }
+}
+
+template <typename T>
+int dense_push_segmented(const bz_params &p, SoA<T> in, const int32_t *n_in, int64_t in_cap, SoA<T> out, int64_t cap,
+                         int32_t *counts, const T *E, const double *R, const double *gas, double *moments, void *ws,
+                         size_t ws_bytes, uint32_t *status, cudaStream_t st) {
+    const DenseWs L(in_cap, p.n_nodes, sizeof(T));
+    if (ws_bytes < L.total) return BZ_ERR_WORKSPACE;  // the caller runs the look-back push instead
+    if (int64_t(L.nseg) * 2 * DENSE_HALF > int64_t(UINT32_MAX) || cap > int64_t(INT32_MAX)) return BZ_ERR_TOO_LARGE;
+    unsigned char *b = static_cast<unsigned char *>(ws);
+    int32_t *cin = reinterpret_cast<int32_t *>(b + L.cin);
+    int32_t *cout = reinterpret_cast<int32_t *>(b + L.cout);
+    int64_t *part = reinterpret_cast<int64_t *>(b + L.part);
+    uint32_t *flags = reinterpret_cast<uint32_t *>(b + L.flags);
+    T *col[5];
+    for (int k = 0; k < 5; ++k) col[k] = reinterpret_cast<T *>(b + L.cols + size_t(k) * L.col_bytes);
+    Seg<T> sin{in, cin, L.nseg, DENSE_HALF};
+    Seg<T> sout{SoA<T>{col[0], col[1], col[2], col[3], col[4]}, cout, L.nseg, DENSE_HALF};
+    k_dense_in_counts<<<int(std::min<int64_t>(ceil_div(L.nseg, 256), 1024)), 256, 0, st>>>(n_in, in_cap, L.nseg,
+                                                                                            DENSE_HALF, cin, status);
+    if (cudaGetLastError() != cudaSuccess) return BZ_ERR_CUDA;
+    if (cudaMemsetAsync(flags, 0, sizeof(uint32_t), st) != cudaSuccess) return BZ_ERR_CUDA;
+    bz_params pp = p;
+    pp.flags &= ~uint32_t(BZ_CLEAR_MOMENTS);  // the dense entry has cleared them
+    int rc = seg_push_run<T>(pp, sin, uint32_t(DENSE_HALF), sout, E, R, gas, moments, nullptr, b + L.push,
+                             L.cin - L.push, flags, status, st);
+    if (rc != BZ_OK) return rc;
+    auto kern = k_dense_gather<T>;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, RP_T, 0) != cudaSuccess || per_sm < 1)
+        return BZ_ERR_UNSUPPORTED;
+    const int grid = std::max(1, std::min(num_sms() * per_sm, PlaceWs::max_ctas(L.nseg)));
+    void *args[] = {&sout, &out, &cap, &counts, &part, &status};
+    if (cudaLaunchCooperativeKernel(reinterpret_cast<void *>(kern), dim3(grid), dim3(RP_T), args, 0, st) != cudaSuccess)
+        return BZ_ERR_CUDA;
+    return BZ_OK;
+}
+template int dense_push_segmented<float>(const bz_params &, SoA<float>, const int32_t *, int64_t, SoA<float>, int64_t,
+                                         int32_t *, const float *, const double *, const double *, double *, void *,
+                                         size_t, uint32_t *, cudaStream_t);
+template int dense_push_segmented<double>(const bz_params &, SoA<double>, const int32_t *, int64_t, SoA<double>,
+                                          int64_t, int32_t *, const double *, const double *, const double *, double *,
+                                          void *, size_t, uint32_t *, cudaStream_t);
 
 // energy distribution per node (swarm): one warp per segment. The bin is taken from a
 // float log2 unless it lies within 1e-4 of a bin edge, where it is recomputed in float64
@@ -1149,6 +1348,12 @@ int bz_seg_rebalance_f64(bz_segments_f64 s, bz_segments_f64 scratch, void *works
                                         only_if, seg_flags, status, stream, &s);
 }
 size_t bz_seg_place_workspace(int32_t nseg) { return bz::PlaceWs(nseg).total + bz::RepackWs(nseg).total; }
+size_t bz_push_workspace_fast_f32(int64_t in_capacity, int32_t n_nodes) {
+    return bz::DenseWs(in_capacity, n_nodes, sizeof(float)).total;
+}
+size_t bz_push_workspace_fast_f64(int64_t in_capacity, int32_t n_nodes) {
+    return bz::DenseWs(in_capacity, n_nodes, sizeof(double)).total;
+}
 int bz_seg_place_f32(bz_segments_f32 s, bz_particles_f32 app, const int32_t *app_n, int64_t app_capacity,
                      bz_segments_f32 scratch, void *workspace, size_t workspace_bytes, uint32_t *seg_flags,
                      uint32_t *status, void *stream) {

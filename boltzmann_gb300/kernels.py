@@ -175,16 +175,22 @@ def make_params(*, n_faces, n_nodes, bnf, advect, L, dx, dt, nn, gas_sigma=0.0, 
 # --------------------------------------------------------------------------------------
 
 def electron_kernel(params, src: ParticleSet, dst: ParticleSet, E, status, ws: Workspace, moments=None,
-                    replay_R=None, replay_gas=None):
+                    replay_R=None, replay_gas=None, fast=True):
     """Push + collide src into dst (compacted, children appended); optionally deposit
     moments [4, n_nodes] (float64, accumulated). electron_kernel_numba.py:291-303 plus
-    the deposit and compaction of post_processing_1D.py:40-68."""
+    the deposit and compaction of post_processing_1D.py:40-68. ``fast``: with the larger
+    workspace the push runs through the segmented kernel and a gather (same results);
+    otherwise the single-pass push with the decoupled look-back."""
     if src.dtype != dst.dtype:
         raise TypeError("src and dst precision differ")
     if E.dtype != src.dtype:
         raise TypeError("E must have the particle precision")
-    nbytes = _lib.load().bz_push_workspace(max(src.capacity, dst.capacity))
-    w = ws.get("push", nbytes)
+    lib = _lib.load()
+    if fast:
+        nbytes = getattr(lib, f"bz_push_workspace_fast_{src.suffix}")(src.capacity, params.n_nodes)
+        w = ws.get("push_fast", nbytes)
+    else:
+        w = ws.get("push", lib.bz_push_workspace(max(src.capacity, dst.capacity)))
     call(f"bz_push_collide_{src.suffix}", ctypes.byref(params), src.struct(), src.n_ptr(), src.capacity, dst.struct(),
          dst.capacity, dst.counts_ptr(), _ptr(E), _ptr(replay_R), _ptr(replay_gas), _ptr(moments), _ptr(w),
          w.numel(), _ptr(status), _stream())

@@ -120,6 +120,14 @@ typedef struct bz_particles_f64 { double *x, *vx, *vy, *vz, *w; } bz_particles_f
  * BZ_DEV_CAPACITY is raised; out_capacity must leave room for ns + 2*nc (children are
  * staged at the tail before they are moved behind the survivors). */
 size_t bz_push_workspace(int64_t capacity);
+/* With a workspace of this many bytes (or more) the same call pushes through the segmented
+ * kernel instead: the input read as segments of 2048 particles (each particle keeps its
+ * index as its Philox counter, so the results are the same), pushed into segments held in
+ * the workspace (about 40 * in_capacity bytes in float32), then gathered into the order
+ * above; no tile waits for its predecessors' counts. Particles beyond out_capacity are
+ * dropped with BZ_DEV_CAPACITY (children first); n_nodes is bz_params.n_nodes. */
+size_t bz_push_workspace_fast_f32(int64_t in_capacity, int32_t n_nodes);
+size_t bz_push_workspace_fast_f64(int64_t in_capacity, int32_t n_nodes);
 int bz_push_collide_f32(const bz_params *p, bz_particles_f32 in, const int32_t *n_in, int64_t in_capacity,
                         bz_particles_f32 out, int64_t out_capacity, int32_t *counts,
                         const float *E, const double *replay_R, const double *replay_gas,

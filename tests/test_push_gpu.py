@@ -256,6 +256,36 @@ def test_push_empty_and_tiny():
         assert int(cnt[2]) <= 2 * n
 
 
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_dense_push_through_segments_matches_lookback(prec):
+    """bz_push_collide_* with the fast workspace (the segmented kernel over the array read
+    as segments, then a gather into the reference order) against the single-pass look-back
+    push: the same particles in the same order, the same counts, the moments up to the
+    float summation order."""
+    x, v, w, E, gp, _ = philox_case(150_000, 256, 9, prec, 6.74e4)
+    res = []
+    for fast in (False, True):
+        n = len(x)
+        src = K.ParticleSet(n, DT[prec])
+        dst = K.ParticleSet(3 * n, DT[prec])
+        src.load(x, v[:, 0], v[:, 1], v[:, 2], w)
+        mom = torch.zeros(4, gp.n_nodes, dtype=torch.float64, device="cuda")
+        st = torch.zeros(1, dtype=torch.int32, device="cuda")
+        K.electron_kernel(gp, src, dst, torch.as_tensor(E, dtype=DT[prec], device="cuda"), st, K.Workspace(),
+                          moments=mom, fast=fast)
+        torch.cuda.synchronize()
+        assert int(st.item()) == 0
+        cnt = dst.cnt.cpu().numpy()
+        res.append((cnt, dst.to_numpy(int(cnt[2])), mom.cpu().numpy()))
+    (c1, o1, m1), (c2, o2, m2) = res
+    np.testing.assert_array_equal(c1[:3], c2[:3])
+    assert c1[1] > 0  # children were appended
+    for f in K.ParticleSet.FIELDS:
+        np.testing.assert_array_equal(o2[f], o1[f])
+    for j in (0, 1, 3):
+        np.testing.assert_allclose(m2[j], m1[j], rtol=1e-5, atol=1e-6 * np.abs(m1[j]).max())
+
+
 def test_push_capacity_flag():
     """Too small an output buffer: the kernel drops particles and raises BZ_DEV_CAPACITY,
     it does not write out of bounds."""
