@@ -271,6 +271,15 @@ def workload_config(args):
 # --------------------------------------------------------------------------------------
 # our arm
 # --------------------------------------------------------------------------------------
+def pushed_per_launch(launch, device):
+    """Particles one push takes (w > 0; slots that merges emptied are not pushed), from the
+    push's own counter in one more launch after the timed ones."""
+    import torch
+    c = torch.zeros(1, dtype=torch.int64, device=device)
+    launch(c)
+    return int(c.item())
+
+
 def dense_push_leg(sol, prm, reps, peak):
     """The drop-in dense push (bz_push_collide_f32: the reference's global order) on the
     solver's current particles, gathered into one dense list on the device: launch time and
@@ -435,7 +444,8 @@ def run_ours(args, world, rank, local, pg):
     ev[1].record(st)
     torch.cuda.synchronize()
     push_ms = ev[0].elapsed_time(ev[1]) / M
-    n_now = A.n()
+    n_now = pushed_per_launch(lambda c: K.seg_electron_kernel(prm, A, B, sol.E_push, sol.status, sol.seg_flags,
+                                                              sol.ws, moments=mom, n_pushed=c), sol.device)
     sol.status.copy_(saved[0]); sol.seg_flags.copy_(saved[1]); mom.copy_(saved[2])
     # algorithmic bytes: read the particles pushed (20 B), write them back (20 B)
     bytes_per_launch = BYTES_PER_PARTICLE * n_now
@@ -569,8 +579,9 @@ def run_swarms(args, world, rank, local, pg):
     ev1.record(st)
     torch.cuda.synchronize()
     push_ms = ev0.elapsed_time(ev1) / 20
+    n_now = pushed_per_launch(lambda c: K.seg_electron_kernel(prm, ens.A, ens.B, ens.E, ens.status, ens.seg_flags,
+                                                              ens.ws, moments=ens.moments, n_pushed=c), ens.device)
     ens.status.copy_(saved[0]); ens.seg_flags.copy_(saved[1]); ens.moments.copy_(saved[2])
-    n_now = ens.A.n()
     achieved = BYTES_PER_PARTICLE * n_now / (push_ms * 1e-3) / 1e9
     peak, kind = peaks()
     if rank != 0:
@@ -643,8 +654,9 @@ def run_swarm100(args, world, rank, local, pg):
     ev1.record(st)
     torch.cuda.synchronize()
     push_ms = ev0.elapsed_time(ev1) / 200
+    n_now = pushed_per_launch(lambda c: K.seg_electron_kernel(prm, ens.A, ens.B, ens.E, ens.status, ens.seg_flags,
+                                                              ens.ws, moments=ens.moments, n_pushed=c), ens.device)
     ens.status.copy_(saved[0]); ens.seg_flags.copy_(saved[1]); ens.moments.copy_(saved[2])
-    n_now = ens.A.n()
     achieved = 80 * n_now / (push_ms * 1e-3) / 1e9
     peak, kind = peaks()
     # e2e through the ensemble's step with a swarm caller's per-step host traffic: the field
