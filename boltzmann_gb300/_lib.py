@@ -135,6 +135,10 @@ _PROTOS = {
     "bz_seg_bin_workspace": (_sz, [_i32, _i64]),
     "bz_seg_bin_f32": (ctypes.c_int, [_P, Segments, _i32, _vp, _f64, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp]),
     "bz_seg_bin_f64": (ctypes.c_int, [_P, Segments, _i32, _vp, _f64, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp]),
+    "bz_seg_bin_check_f32": (ctypes.c_int, [_P, Segments, _i32, _vp, _f64, _vp, _vp, _vp, _vp, _vp, _f64, _f64, _vp,
+                                            _vp, _sz, _vp, _vp]),
+    "bz_seg_bin_check_f64": (ctypes.c_int, [_P, Segments, _i32, _vp, _f64, _vp, _vp, _vp, _vp, _vp, _f64, _f64, _vp,
+                                            _vp, _sz, _vp, _vp]),
     "bz_seg_resample_workspace": (_sz, [_i32, _i64, _i32]),
     "bz_seg_resample_f32": (ctypes.c_int, [_P, Segments, Particles, _i64, Segments, _i32, _vp, _vp, _f64, _f64, _f64,
                                            _f64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp, _vp]),

@@ -520,14 +520,42 @@ struct SegBinWs {
         hist = slots + al(4 * c);
         tot = hist + al((nt + 1) * RADIX * 4);  // the tiles' digit counts, then the digit totals
         pre = tot + al(4 * size_t(nseg));
-        total = pre + al(4 * (size_t(nseg) + 1));
+        total = pre + al(4 * (size_t(nseg) + 2));  // the offsets, the live total, the count to sort
     }
+};
+
+// The resampling trigger from the key counts (the rule k_rs_decide applies), before the
+// sort: n_sort gets the live total when resampling will run and 0 when it will not, so the
+// radix passes that read it have nothing to do in a step whose check finds nothing.
+__global__ void __launch_bounds__(1024) k_bin_need(const int32_t *counts, int nkeys, int nb, const int32_t *targets,
+                                                   double split_below, double merge_at, int flags,
+                                                   const int32_t *n_live, int32_t *n_sort, int32_t *need_out) {
+    const bool per_key = (flags & BZ_PER_KEY_TARGETS) != 0;
+    int need_any = 0, need_last = 0;
+    for (int k = threadIdx.x; k < nkeys; k += blockDim.x) {
+        const int b = k % nb;
+        rs_key_need(counts[k], targets[per_key ? k : b], b == nb - 1, split_below, merge_at, need_any, need_last);
+    }
+    need_any = __syncthreads_or(need_any);
+    need_last = __syncthreads_or(need_last);
+    if (threadIdx.x == 0) {
+        const int need = (flags & BZ_QUIRK_TRIGGER_LAST) ? need_last : need_any;
+        *n_sort = need ? *n_live : 0;
+        if (need_out) *need_out = need;
+    }
+}
+
+// the trigger's inputs for a binning that sorts only when resampling will run
+struct BinCheck {
+    const int32_t *targets;
+    double split_below, merge_at;
+    int32_t *need_out;
 };
 
 template <typename T, typename S>
 static int seg_bin_entry(const bz_params *pp, S s, int nb, const double *edges, double min_wt, int32_t *perm,
                          int32_t *offsets, int32_t *counts, int32_t *hw_counts, void *ws, size_t ws_bytes,
-                         uint32_t *status, void *stream) {
+                         uint32_t *status, void *stream, const BinCheck *chk = nullptr) {
     if (!pp || !perm || !offsets || !counts || !hw_counts || !ws || !status) return BZ_ERR_ARG;
     if (!s.x || !s.vx || !s.vy || !s.vz || !s.w || !s.counts || s.nseg <= 0 || s.half <= 0) return BZ_ERR_ARG;
     const bz_params &p = *pp;
@@ -553,6 +581,7 @@ static int seg_bin_entry(const bz_params *pp, S s, int nb, const double *edges, 
     k_seg_totals<<<int(std::min<int64_t>(ceil_div(s.nseg, 256), 4096)), 256, 0, st>>>(s.counts, s.nseg, s.half, tot);
     k_key_offsets<<<1, 1024, 0, st>>>(tot, s.nseg, pre);
     const int32_t *n = pre + s.nseg;  // live total on the device
+    if (chk && (!chk->targets || !(chk->merge_at > chk->split_below))) return BZ_ERR_ARG;
     size_t smem = sizeof(uint32_t) * 2 * size_t(nkeys);
     auto kk = k_seg_bin_keys<T>;
     if (smem > 48 * 1024 &&
@@ -565,7 +594,13 @@ static int seg_bin_entry(const bz_params *pp, S s, int nb, const double *edges, 
     kk<<<kb, 256, smem, st>>>(p, s.x, s.vx, s.vy, s.vz, s.w, s.counts, s.nseg, s.half, pre, nb, edges, min_wt,
                               float_above(min_wt), float(1.0 / p.dx), keys_a,
                               slots, counts, hw_counts, nkeys, status);
-    const int grid = int(ceil_div(cap, RB_TILE));
+    if (chk) {
+        // the trigger first: the passes below sort nothing when it finds nothing to resample
+        int32_t *n_sort = pre + s.nseg + 1;
+        k_bin_need<<<1, 1024, 0, st>>>(counts, nkeys, nb, chk->targets, chk->split_below, chk->merge_at, p.flags, n,
+                                       n_sort, chk->need_out);
+        n = n_sort;
+    }
     const bool two = nkeys >= RADIX;
     k_radix_hist<<<radix_grid(cap, false), RB_T, 0, st>>>(keys_a, n, cap, 0, hist);
     k_radix_colsum<<<RADIX, RS_COL_T, 0, st>>>(hist, n, cap, dig_tot);
@@ -603,6 +638,22 @@ int bz_seg_bin_f32(const bz_params *p, bz_segments_f32 s, int32_t nbins, const d
                    size_t workspace_bytes, uint32_t *status, void *stream) {
     return bz::seg_bin_entry<float>(p, s, nbins, edges, min_wt, perm, offsets, counts, hw_counts, workspace,
                                     workspace_bytes, status, stream);
+}
+int bz_seg_bin_check_f32(const bz_params *p, bz_segments_f32 s, int32_t nbins, const double *edges, double min_wt,
+                         int32_t *perm, int32_t *offsets, int32_t *counts, int32_t *hw_counts, const int32_t *targets,
+                         double split_below, double merge_at, int32_t *need_out, void *workspace,
+                         size_t workspace_bytes, uint32_t *status, void *stream) {
+    const bz::BinCheck chk{targets, split_below, merge_at, need_out};
+    return bz::seg_bin_entry<float>(p, s, nbins, edges, min_wt, perm, offsets, counts, hw_counts, workspace,
+                                    workspace_bytes, status, stream, &chk);
+}
+int bz_seg_bin_check_f64(const bz_params *p, bz_segments_f64 s, int32_t nbins, const double *edges, double min_wt,
+                         int32_t *perm, int32_t *offsets, int32_t *counts, int32_t *hw_counts, const int32_t *targets,
+                         double split_below, double merge_at, int32_t *need_out, void *workspace,
+                         size_t workspace_bytes, uint32_t *status, void *stream) {
+    const bz::BinCheck chk{targets, split_below, merge_at, need_out};
+    return bz::seg_bin_entry<double>(p, s, nbins, edges, min_wt, perm, offsets, counts, hw_counts, workspace,
+                                     workspace_bytes, status, stream, &chk);
 }
 int bz_seg_bin_f64(const bz_params *p, bz_segments_f64 s, int32_t nbins, const double *edges, double min_wt,
                    int32_t *perm, int32_t *offsets, int32_t *counts, int32_t *hw_counts, void *workspace,

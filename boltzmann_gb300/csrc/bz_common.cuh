@@ -435,6 +435,19 @@ __device__ inline void lookback(uint64_t *status_arr, int tile, uint32_t s, uint
 
 __host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
+// The resampling trigger of one (cell, bin) key with n particles and target T
+// (boltzmann.py:894-916; 3bin :1063-1113, 5bin :1256-1334): too few (0 < n < split_below T)
+// or too many (n >= merge_at T) sets need_any; too many in the last bin sets need_last,
+// the one test that decides under BZ_QUIRK_TRIGGER_LAST.
+__device__ __forceinline__ void rs_key_need(int64_t n, int64_t T, bool last_bin, double split_below, double merge_at,
+                                            int &need_any, int &need_last) {
+    if (n > 0 && double(n) < split_below * double(T)) need_any = 1;
+    if (double(n) >= merge_at * double(T)) {
+        need_any = 1;
+        if (last_bin) need_last = 1;
+    }
+}
+
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
 }  // namespace bz

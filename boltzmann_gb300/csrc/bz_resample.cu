@@ -69,11 +69,7 @@ __global__ void __launch_bounds__(1024) k_rs_decide(const int32_t *counts, const
             a = ACT_MERGE;
             app = int64_t(merge_keep * double(T));  // boltzmann.py:829
         }
-        if (n > 0 && double(n) < split_below * double(T)) need_any = 1;
-        if (double(n) >= merge_at * double(T)) {
-            need_any = 1;
-            if (b == nb - 1) need_last = 1;
-        }
+        rs_key_need(n, T, b == nb - 1, split_below, merge_at, need_any, need_last);
         act[k] = a;
         sa += app;
         sd += app;

@@ -609,6 +609,13 @@ __global__ void __launch_bounds__(RP_T) k_seg_place(Seg<T> s, SoA<T> app, const 
     const int lo = min(m, b * S), hi = min(m, lo + S);
     int64_t *p_live = part, *p_bad = part + G, *p_a1 = part + 2 * G, *p_room = part + 3 * G;
     auto n1_of = [&](int k) { return min(max(s.cnt[2 * k + 1], 0), H); };
+    // nothing appended and no repack requested (a resampling step whose check found nothing,
+    // or merges only): nothing to place or rebalance (the same for every CTA: both words
+    // change only after the last barrier below)
+    if (*app_n <= 0 && !(seg_flags && (*seg_flags & BZ_SEG_NEEDS_REPACK))) {
+        if (b == 0 && t == 0) misc[0] = 0;
+        return;
+    }
     // 1. live particles per segment (warp per segment) and the CTA's sum
     int64_t my_live = 0, my_bad = 0;
     for (int seg = lo + warp; seg < hi; seg += NW) {

@@ -345,12 +345,22 @@ def seg_eedf(params, s: SegmentSet, hist, emin, emax):
          _ptr(hist), _stream())
 
 
-def seg_bin_particles(params, s: SegmentSet, edges, min_wt, perm, offsets, counts, hw_counts, status, ws: Workspace):
+def seg_bin_particles(params, s: SegmentSet, edges, min_wt, perm, offsets, counts, hw_counts, status, ws: Workspace,
+                      check=None):
+    """Bin s by (cell, energy bin). ``check`` = (targets, split_below, merge_at, need): the
+    resampling trigger is evaluated from the counts first (need gets 1 or 0) and the sort
+    runs only when it is 1 (perm and offsets are then valid only in that case)."""
     nb = int(edges.numel()) + 1
     w = ws.get("seg_bin", _lib.load().bz_seg_bin_workspace(s.nseg, s.capacity))
-    call(f"bz_seg_bin_{s.suffix}", ctypes.byref(params), s.struct(), nb, _ptr(edges) if nb > 1 else None,
-         float(min_wt), _ptr(perm), _ptr(offsets), _ptr(counts), _ptr(hw_counts), _ptr(w), w.numel(), _ptr(status),
-         _stream())
+    if check is None:
+        call(f"bz_seg_bin_{s.suffix}", ctypes.byref(params), s.struct(), nb, _ptr(edges) if nb > 1 else None,
+             float(min_wt), _ptr(perm), _ptr(offsets), _ptr(counts), _ptr(hw_counts), _ptr(w), w.numel(),
+             _ptr(status), _stream())
+        return
+    targets, split_below, merge_at, need = check
+    call(f"bz_seg_bin_check_{s.suffix}", ctypes.byref(params), s.struct(), nb, _ptr(edges) if nb > 1 else None,
+         float(min_wt), _ptr(perm), _ptr(offsets), _ptr(counts), _ptr(hw_counts), _ptr(targets), float(split_below),
+         float(merge_at), _ptr(need), _ptr(w), w.numel(), _ptr(status), _stream())
 
 
 def seg_resample(params, s: SegmentSet, app: ParticleSet, out: SegmentSet, nb, targets, max_ppc, min_wt, split_below,

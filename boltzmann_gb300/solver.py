@@ -201,9 +201,13 @@ class BoltzmannGB300:
                             self.ws)
 
     def _check_for_resampling(self):
-        """Bin the particles (the trigger itself is evaluated on the device inside
-        _do_resampling, boltzmann.py:894-916)."""
-        self.bin_particles()
+        """Bin the particles and evaluate the trigger on the device (boltzmann.py:894-916);
+        the sort by key runs only when resampling will (_do_resampling evaluates the same
+        trigger again and does nothing when it is off)."""
+        cfg = self.cfg
+        K.seg_bin_particles(self.params(), self.A, self.edges[: self.nb - 1] if self.nb > 1 else self.edges[:0],
+                            cfg.min_wt, self.perm, self.offsets, self.bin_counts, self.hw_counts, self.status,
+                            self.ws, check=(self.targets, cfg.split_below, cfg.merge_at, self.need))
 
     def _do_resampling(self):
         cfg = self.cfg
@@ -450,13 +454,14 @@ class BoltzmannGB300:
         """libbz kernels one step launches (torch's memset of the moments not counted).
         Every step: the push and the fused grid step (grid update, clock, ion fluid,
         Poisson) (2); a plain step adds the conditional rebalance (one cooperative
-        kernel); a resampling step adds binning (segment totals, key offsets twice, keys,
-        then per 8-bit radix pass a histogram, column sums, column scan and scatter),
-        decide + apply (2) and either the placement of the appended particles with its
-        conditional repack (2) or the repack of the survivors with them (1)."""
+        kernel); a resampling step adds binning (segment totals, key offsets twice, keys, the
+        resampling trigger, then per 8-bit radix pass a histogram, column sums, column scan
+        and scatter, which sort nothing when the trigger is off), decide + apply (2) and
+        either the placement of the appended particles with its conditional repack (2) or the
+        repack of the survivors with them (1)."""
         passes = 2 if self.nnodes * self.nb >= 256 else 1
         tail = 2 if self.cfg.resample_in_place else 1
-        return 2 + (4 + 4 * passes + 2 + tail if resample else 1) + (self._ion_rate is not None)
+        return 2 + (5 + 4 * passes + 2 + tail if resample else 1) + (self._ion_rate is not None)
 
     def snapshot(self):
         """A device copy of the simulation state: the particles (the buffer that holds

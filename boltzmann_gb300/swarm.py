@@ -190,8 +190,9 @@ class SwarmEnsemble:
         cfg = self.cfg
         p = self.params()
         ed = self.edges[: self.nb - 1] if self.nb > 1 else self.edges[:0]
+        # the trigger from the counts first: the sort by key runs only when resampling will
         K.seg_bin_particles(p, self.A, ed, cfg.min_wt, self.perm, self.offsets, self.bin_counts, self.hw_counts,
-                            self.status, self.ws)
+                            self.status, self.ws, check=(self.targets, cfg.split_below, cfg.merge_at, self.need))
         K.seg_resample(p, self.A, self.app, self.B, self.nb, self.targets, self.max_ppc, cfg.min_wt, cfg.split_below,
                        cfg.merge_at, cfg.merge_keep, self.perm, self.offsets, self.bin_counts, self.hw_counts,
                        self.status, self.seg_flags, self.ws, need=self.need, in_place=cfg.resample_in_place)

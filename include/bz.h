@@ -362,6 +362,19 @@ int bz_seg_bin_f32(const bz_params *p, bz_segments_f32 s, int32_t nbins, const d
 int bz_seg_bin_f64(const bz_params *p, bz_segments_f64 s, int32_t nbins, const double *edges, double min_wt,
                    int32_t *perm, int32_t *offsets, int32_t *counts, int32_t *hw_counts, void *workspace,
                    size_t workspace_bytes, uint32_t *status, void *stream);
+/* Binning of a segmented state that also evaluates the resampling trigger (the rule of
+ * bz_seg_resample_*: targets per bin, or per key with BZ_PER_KEY_TARGETS; BZ_QUIRK_TRIGGER_LAST
+ * in p->flags) from the counts before it sorts: *need_out (device, may be NULL) gets 1 or 0,
+ * and when it is 0 the sort is skipped, so perm and offsets are valid only when resampling
+ * will run. counts and hw_counts are always complete. Workspace: bz_seg_bin_workspace. */
+int bz_seg_bin_check_f32(const bz_params *p, bz_segments_f32 s, int32_t nbins, const double *edges, double min_wt,
+                         int32_t *perm, int32_t *offsets, int32_t *counts, int32_t *hw_counts, const int32_t *targets,
+                         double split_below, double merge_at, int32_t *need_out, void *workspace,
+                         size_t workspace_bytes, uint32_t *status, void *stream);
+int bz_seg_bin_check_f64(const bz_params *p, bz_segments_f64 s, int32_t nbins, const double *edges, double min_wt,
+                         int32_t *perm, int32_t *offsets, int32_t *counts, int32_t *hw_counts, const int32_t *targets,
+                         double split_below, double merge_at, int32_t *need_out, void *workspace,
+                         size_t workspace_bytes, uint32_t *status, void *stream);
 /* ES-WPNC resampling of a segmented state: as bz_resample_*, with the appended particles
  * collected in app (capacity app_capacity) and everything repacked into out; with
  * BZ_RESAMPLE_IN_PLACE in p->flags the result stays in s instead (bz_seg_place_* with out

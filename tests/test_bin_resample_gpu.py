@@ -301,3 +301,69 @@ def test_resample_counts_match_oracle_philox():
             elif m >= 3 * t:
                 expect += int(0.6 * t) - min(m, 10 * t)
     assert len(out["x"]) == expect
+
+
+@pytest.mark.parametrize("case", ["merge", "split", "none", "trigger_last", "per_key"])
+def test_binning_with_the_trigger_sorts_only_when_resampling_runs(case):
+    """bz_seg_bin_check_*: the trigger it evaluates from the counts equals the one
+    bz_seg_resample_* evaluates; counts are complete either way; when the trigger is on the
+    permutation and offsets equal the plain binning's, when it is off nothing is sorted."""
+    rng = np.random.default_rng(31)
+    N, L, n, nb = 48, 2.54, 60_000, 3
+    x = rng.uniform(0.01, L - 0.01, n)
+    v = rng.normal(0, 1.3e6, (n, 3))
+    w = rng.uniform(0.5, 2.0, n)
+    flags = _lib.QUIRK_TRIGGER_LAST if case == "trigger_last" else 0
+    nkeys = (N + 1) * nb
+    per_key = case == "per_key"
+    if per_key:
+        flags |= _lib.PER_KEY_TARGETS
+    # about n / nkeys = 400 per key on average (fewer in the hot bin)
+    T = {"merge": 60, "split": 4000, "none": 300, "trigger_last": 60, "per_key": None}[case]
+    if per_key:
+        targ = np.full(nkeys, 300, dtype=np.int32)
+        targ[7 * nb + 1] = 20  # one key far above its target: merge
+    else:
+        targ = np.full(nb, T, dtype=np.int32)
+    split_below, merge_at = (0.5, 3.0) if case != "none" else (1e-9, 1e9)
+    p = grid_params(N, L, flags)
+    seg = K.SegmentSet(80, 1024)
+    seg.load(x, v[:, 0], v[:, 1], v[:, 2], w)
+    ed = torch.as_tensor(np.array([4.0, 11.5]), device="cuda")
+    tg = torch.as_tensor(targ, device="cuda")
+
+    def bins(check):
+        perm = torch.full((seg.capacity,), -7, dtype=torch.int32, device="cuda")
+        offs = torch.full((nkeys + 1,), -7, dtype=torch.int32, device="cuda")
+        cnts = torch.zeros(nkeys, dtype=torch.int32, device="cuda")
+        hw = torch.zeros(nkeys, dtype=torch.int32, device="cuda")
+        st = torch.zeros(1, dtype=torch.int32, device="cuda")
+        need = torch.full((1,), -1, dtype=torch.int32, device="cuda")
+        K.seg_bin_particles(p, seg, ed, 0.1, perm, offs, cnts, hw, st, K.Workspace(),
+                            check=(tg, split_below, merge_at, need) if check else None)
+        torch.cuda.synchronize()
+        assert int(st.item()) == 0
+        return perm, offs, cnts, hw, int(need.item())
+
+    perm0, offs0, cnt0, hw0, _ = bins(False)
+    perm1, offs1, cnt1, hw1, need = bins(True)
+    assert torch.equal(cnt0, cnt1) and torch.equal(hw0, hw1)
+    # the trigger of the resampling itself on the same counts
+    app = K.ParticleSet(2_000_000)  # room for every split's copies (up to 147 keys x 2T)
+    out = K.SegmentSet(2048, 1024)
+    mp = torch.as_tensor(10 * targ, dtype=torch.int32, device="cuda")
+    need_rs = torch.full((1,), -1, dtype=torch.int32, device="cuda")
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    fl = torch.zeros(1, dtype=torch.int32, device="cuda")
+    K.seg_resample(p, seg, app, out, nb, tg, mp, 0.1, split_below, merge_at, 0.6, perm0, offs0, cnt0, hw0, st, fl,
+                   K.Workspace(), need=need_rs)
+    torch.cuda.synchronize()
+    assert int(st.item()) == 0
+    assert need == int(need_rs.item())
+    assert need == (0 if case == "none" else 1)
+    if need:
+        assert torch.equal(offs0, offs1)
+        live = int(cnt0.sum().item())
+        assert torch.equal(perm0[:live], perm1[:live])
+    else:
+        assert int((perm1 != -7).sum().item()) == 0  # nothing sorted
