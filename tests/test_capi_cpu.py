@@ -72,3 +72,39 @@ def test_missing_library_fails_loudly(monkeypatch, tmp_path):
     monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "libbz.so"))
     with pytest.raises(_lib.BzLibraryError):
         _lib.load()
+
+
+def test_new_entry_points_validate_without_gpu(lib):
+    """The placement, the checked binning and the in-place resampling reject bad calls
+    before anything is launched; the workspace queries need no GPU."""
+    p = _lib.BzParams()
+    seg0 = _lib.Segments()
+    empty = _lib.Particles()
+    # null pointers
+    assert lib.bz_seg_place_f32(seg0, empty, None, 0, seg0, None, 0, None, None, None) == _lib.BZ_ERR_ARG
+    assert lib.bz_seg_bin_check_f32(ctypes.byref(p), seg0, 3, None, 0.1, None, None, None, None, None, 0.5, 3.0,
+                                    None, None, 0, None, None) == _lib.BZ_ERR_ARG
+    # in-place resampling with a scratch set of another geometry: refused on the host
+    fake = ctypes.c_void_p(256)  # never dereferenced: the call returns before any launch
+    cnt = ctypes.c_void_p(512)
+
+    def seg(nseg, half):
+        s = _lib.Segments()
+        s.x = s.vx = s.vy = s.vz = s.w = fake
+        s.counts = cnt
+        s.nseg, s.half = nseg, half
+        return s
+
+    app = _lib.Particles(fake, fake, fake, fake, fake)
+    q = _lib.BzParams()
+    q.n_nodes = 17
+    q.flags = _lib.RESAMPLE_IN_PLACE
+    rc = lib.bz_seg_resample_f32(ctypes.byref(q), seg(4, 64), app, 100, seg(8, 64), 3, fake, fake, 0.1, 0.5, 3.0,
+                                 0.6, fake, fake, fake, fake, None, None, None, fake, 1 << 30, None, fake, None)
+    assert rc == _lib.BZ_ERR_ARG
+    # workspace queries
+    n = 1025
+    assert lib.bz_seg_push_workspace_nodes(n) >= lib.bz_seg_push_workspace() + 8 * n
+    assert lib.bz_push_workspace_fast_f32(1 << 20, n) >= 40 * (1 << 20)
+    assert lib.bz_push_workspace_fast_f64(1 << 20, n) >= 80 * (1 << 20)
+    assert lib.bz_seg_place_workspace(1000) >= lib.bz_seg_repack_workspace(1000)
