@@ -1127,8 +1127,9 @@ int dense_push_segmented(const bz_params &p, SoA<T> in, const int32_t *n_in, int
                          int32_t *counts, const T *E, const double *R, const double *gas, double *moments, void *ws,
                          size_t ws_bytes, uint32_t *status, cudaStream_t st) {
     const DenseWs L(in_cap, p.n_nodes, sizeof(T));
-    if (ws_bytes < L.total) return BZ_ERR_WORKSPACE;  // the caller runs the look-back push instead
-    if (int64_t(L.nseg) * 2 * DENSE_HALF > int64_t(UINT32_MAX) || cap > int64_t(INT32_MAX)) return BZ_ERR_TOO_LARGE;
+    // without the room, or beyond 32-bit slots and counts: the caller runs the look-back push
+    if (ws_bytes < L.total) return BZ_ERR_WORKSPACE;
+    if (int64_t(L.nseg) * 2 * DENSE_HALF > int64_t(UINT32_MAX) || cap > int64_t(INT32_MAX)) return BZ_ERR_WORKSPACE;
     unsigned char *b = static_cast<unsigned char *>(ws);
     int32_t *cin = reinterpret_cast<int32_t *>(b + L.cin);
     int32_t *cout = reinterpret_cast<int32_t *>(b + L.cout);
