@@ -558,6 +558,7 @@ static int seg_bin_entry(const bz_params *pp, S s, int nb, const double *edges, 
                          uint32_t *status, void *stream, const BinCheck *chk = nullptr) {
     if (!pp || !perm || !offsets || !counts || !hw_counts || !ws || !status) return BZ_ERR_ARG;
     if (!s.x || !s.vx || !s.vy || !s.vz || !s.w || !s.counts || s.nseg <= 0 || s.half <= 0) return BZ_ERR_ARG;
+    if (chk && (!chk->targets || !(chk->merge_at > chk->split_below))) return BZ_ERR_ARG;
     const bz_params &p = *pp;
     if (nb < 1 || nb > 16 || (nb > 1 && !edges) || p.n_nodes < 1 || (p.advect == BZ_ADVECT_1D && p.dx <= 0)) return BZ_ERR_ARG;
     const int nkeys = p.n_nodes * nb;
@@ -581,7 +582,6 @@ static int seg_bin_entry(const bz_params *pp, S s, int nb, const double *edges, 
     k_seg_totals<<<int(std::min<int64_t>(ceil_div(s.nseg, 256), 4096)), 256, 0, st>>>(s.counts, s.nseg, s.half, tot);
     k_key_offsets<<<1, 1024, 0, st>>>(tot, s.nseg, pre);
     const int32_t *n = pre + s.nseg;  // live total on the device
-    if (chk && (!chk->targets || !(chk->merge_at > chk->split_below))) return BZ_ERR_ARG;
     size_t smem = sizeof(uint32_t) * 2 * size_t(nkeys);
     auto kk = k_seg_bin_keys<T>;
     if (smem > 48 * 1024 &&

@@ -102,6 +102,12 @@ def test_new_entry_points_validate_without_gpu(lib):
     rc = lib.bz_seg_resample_f32(ctypes.byref(q), seg(4, 64), app, 100, seg(8, 64), 3, fake, fake, 0.1, 0.5, 3.0,
                                  0.6, fake, fake, fake, fake, None, None, None, fake, 1 << 30, None, fake, None)
     assert rc == _lib.BZ_ERR_ARG
+    # the checked binning without targets: refused before anything runs
+    q2 = _lib.BzParams()
+    q2.n_nodes = 17
+    rc = lib.bz_seg_bin_check_f32(ctypes.byref(q2), seg(4, 64), 3, fake, 0.1, fake, fake, fake, fake, None, 0.5, 3.0,
+                                  None, fake, 1 << 30, fake, None)
+    assert rc == _lib.BZ_ERR_ARG
     # workspace queries
     n = 1025
     assert lib.bz_seg_push_workspace_nodes(n) >= lib.bz_seg_push_workspace() + 8 * n
