@@ -103,7 +103,14 @@ class SegmentSet:
                         self.half)
 
     def n(self):
+        """Occupied slots (run 0 and run 1 of every segment)."""
         return int(self.counts.sum().item())
+
+    def n_live(self):
+        """Particles (w != 0) among the occupied slots: after an in-place resampling the runs
+        may hold slots its merges emptied until the next push drops them."""
+        idx = torch.as_tensor(self.slots("segments"), device=self.device)
+        return int((self.w[idx] != 0).sum().item()) if idx.numel() else 0
 
     def load(self, x, vx, vy, vz, w, ws=None, status=None):
         """Spread a dense particle list evenly over the segments (on the device)."""

@@ -275,7 +275,9 @@ class SwarmEnsemble:
         self.steps_acc = 0
 
     def n(self):
-        return self.A.n()
+        """Particles in all swarms (the step ends with the resampling, whose merges may leave
+        emptied slots until the next push: those are not counted)."""
+        return self.A.n_live()
 
     def counts(self):
         """Weight (particle count at weight 1) per swarm after the last step."""

@@ -138,3 +138,18 @@ def test_omp_step_matches_serial_oracle():
         np.testing.assert_allclose(mom2[j], mom1[j], rtol=1e-10, atol=1e-9)
     # the guard: a sample larger than half its buffer is refused, nothing written
     assert O.lib().orc_step_omp(ctypes.byref(p), n, n, d2, t2, dt_, tt_, np.ascontiguousarray(E), mom2, 2) == -1
+
+
+def test_segment_set_counts_live_particles_apart_from_slots():
+    """SegmentSet.n() counts occupied slots, n_live() the particles among them (slots with
+    w = 0, which an in-place resampling leaves, are not particles)."""
+    import torch
+    from boltzmann_gb300 import kernels as K
+    s = K.SegmentSet(3, 8, torch.float32, device="cpu")
+    s.counts.copy_(torch.tensor([3, 1, 0, 2, 8, 0], dtype=torch.int32))
+    s.w.fill_(1.0)
+    s.w[1] = 0.0            # segment 0, run 0, slot 1
+    s.w[2 * 8 + 8 + 1] = 0.0  # segment 1, run 1, slot 1
+    s.w[2 * 8 + 3] = 0.0    # segment 1, run 0, slot 3: not occupied, not counted either way
+    assert s.n() == 14
+    assert s.n_live() == 12
