@@ -324,43 +324,53 @@ static int radix_grid(int64_t cap, bool scatter) {
 
 // offsets[k] = exclusive scan of counts[0..nkeys), offsets[nkeys] = live total.
 __global__ void __launch_bounds__(1024) k_key_offsets(const int32_t *counts, int nkeys, int32_t *offsets) {
-    __shared__ int32_t part[1024];
-    const int per = (nkeys + 1023) / 1024;
-    const int lo = threadIdx.x * per, hi = min(nkeys, lo + per);
-    // each thread's span is read in batches of eight independent loads (the sums and the
-    // running offsets only depend on the values, not on the loads' order)
-    int32_t s = 0;
-    int k = lo;
-    for (; k + 8 <= hi; k += 8) {
-        int32_t v[8];
+    // chunks of 1024 x 8 consecutive entries: each thread loads its eight at once (neighbouring
+    // threads' spans are adjacent, so a warp reads 1 KB in one sweep), a warp-shuffle scan
+    // and one over the 32 warps' sums give the offsets, a carry links the chunks
+    constexpr int PER = 8, CHUNK = 1024 * PER;
+    __shared__ int32_t wsum[32];
+    __shared__ int32_t chunk_total;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    int32_t carry = 0;
+    for (int base = 0; base < nkeys; base += CHUNK) {
+        const int k0 = base + t * PER;
+        int32_t v[PER], local = 0;
 #pragma unroll
-        for (int u = 0; u < 8; ++u) v[u] = counts[k + u];
+        for (int u = 0; u < PER; ++u) {
+            v[u] = k0 + u < nkeys ? counts[k0 + u] : 0;
+            local += v[u];
+        }
+        int32_t incl = local;
 #pragma unroll
-        for (int u = 0; u < 8; ++u) s += v[u];
-    }
-    for (; k < hi; ++k) s += counts[k];
-    part[threadIdx.x] = s;
-    __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {
-        int32_t t = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t x = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += x;
+        }
+        if (lane == 31) wsum[warp] = incl;
         __syncthreads();
-        part[threadIdx.x] += t;
+        if (warp == 0) {
+            const int32_t ws = wsum[lane];
+            int32_t wi = ws;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int32_t x = __shfl_up_sync(0xffffffffu, wi, o);
+                if (lane >= o) wi += x;
+            }
+            wsum[lane] = wi - ws;  // the warps before this one
+        }
         __syncthreads();
-    }
-    int32_t run = part[threadIdx.x] - s;
-    k = lo;
-    for (; k + 8 <= hi; k += 8) {
-        int32_t v[8];
+        int32_t run = carry + wsum[warp] + incl - local;
 #pragma unroll
-        for (int u = 0; u < 8; ++u) v[u] = counts[k + u];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            offsets[k + u] = run;
+        for (int u = 0; u < PER; ++u) {
+            if (k0 + u < nkeys) offsets[k0 + u] = run;
             run += v[u];
         }
+        if (t == 1023) chunk_total = run;  // carry + the whole chunk
+        __syncthreads();
+        carry = chunk_total;
+        __syncthreads();  // wsum and chunk_total are rewritten by the next chunk
     }
-    for (; k < hi; ++k) { offsets[k] = run; run += counts[k]; }
-    if (threadIdx.x == 1023) offsets[nkeys] = part[1023];
+    if (t == 0) offsets[nkeys] = carry;
 }
 
 struct BinWs {

@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(1024) k_rs_decide(const int32_t *counts, const
                                                     double merge_at, double merge_keep, int flags, int32_t *act,
                                                     int32_t *app_off, int32_t *draw_off, int32_t *misc,
                                                     int32_t *need_out) {
-    __shared__ int64_t pa[1024], pd[1024];
+    __shared__ int64_t pa[65], pd[65];  // per-warp sums, then the warps' offsets, then the totals
     __shared__ int s_need_last, s_need_any;
     const int nkeys = n_nodes * nb;
     if (threadIdx.x == 0) { s_need_last = 0; s_need_any = 0; }
@@ -76,20 +76,45 @@ __global__ void __launch_bounds__(1024) k_rs_decide(const int32_t *counts, const
     }
     if (need_last) atomicOr(&s_need_last, 1);
     if (need_any) atomicOr(&s_need_any, 1);
-    pa[threadIdx.x] = sa;
-    pd[threadIdx.x] = sd;
-    __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {
-        int64_t ta = threadIdx.x >= o ? pa[threadIdx.x - o] : 0;
-        int64_t td = threadIdx.x >= o ? pd[threadIdx.x - o] : 0;
-        __syncthreads();
-        pa[threadIdx.x] += ta;
-        pd[threadIdx.x] += td;
-        __syncthreads();
+    // exclusive scans of the appended and drawn counts over the 1024 threads' spans: within
+    // each warp by shuffles, then over the 32 warp sums
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int64_t ia = sa, id = sd;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int64_t xa = __shfl_up_sync(0xffffffffu, ia, o), xd = __shfl_up_sync(0xffffffffu, id, o);
+        if (lane >= o) {
+            ia += xa;
+            id += xd;
+        }
     }
+    if (lane == 31) {
+        pa[warp] = ia;
+        pd[warp] = id;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const int64_t wa = pa[lane], wd = pd[lane];
+        int64_t xa = wa, xd = wd;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int64_t ya = __shfl_up_sync(0xffffffffu, xa, o), yd = __shfl_up_sync(0xffffffffu, xd, o);
+            if (lane >= o) {
+                xa += ya;
+                xd += yd;
+            }
+        }
+        pa[32 + lane] = xa - wa;  // the warps before this one
+        pd[32 + lane] = xd - wd;
+        if (lane == 31) {
+            pa[64] = xa;  // the totals
+            pd[64] = xd;
+        }
+    }
+    __syncthreads();
     // the reference decides with its last max test only (boltzmann.py:913-916)
     const int need = (flags & BZ_QUIRK_TRIGGER_LAST) ? s_need_last : s_need_any;
-    int64_t ra = pa[threadIdx.x] - sa, rd = pd[threadIdx.x] - sd;
+    int64_t ra = pa[32 + warp] + ia - sa, rd = pd[32 + warp] + id - sd;
     for (int k = lo; k < hi; ++k) {
         if (!need) act[k] = ACT_NONE;
         int a = act[k];
@@ -104,7 +129,7 @@ __global__ void __launch_bounds__(1024) k_rs_decide(const int32_t *counts, const
         }
     }
     if (threadIdx.x == 1023) {
-        misc[0] = need ? int32_t(pa[1023]) : 0;
+        misc[0] = need ? int32_t(pa[64]) : 0;
         misc[1] = need;
         if (need_out) need_out[0] = need;
     }
